@@ -1,0 +1,192 @@
+/*
+ * miniamr_gb300.h -- C ABI of the GB300 (sm_103a) back end for miniAMR's
+ * per-timestep hot path: face ghost exchange, the 7/27-point averaging
+ * stencil, block split/consolidate data movement and the per-variable
+ * checksum.
+ *
+ * The reference keeps these as four C translation units that walk a
+ * host-side `double ****array` per block.  A drop-in replacement of those
+ * units (miniamr_gb300/dropin/) keeps every symbol the reference's driver,
+ * init and refine code call, and forwards the cell-data work here.  The
+ * host keeps all octree metadata; this library keeps the cell data resident
+ * in device memory as one strided pool indexed by block slot.
+ *
+ * Conventions
+ *   - Plain C types only; every call returns MAMR_OK (0) or a negative
+ *     MAMR_E* status and never exits the process.  mamr_last_error() gives
+ *     a one-line description of the most recent failure on this thread.
+ *   - One context = one pool on the current CUDA device, one CUDA stream.
+ *     A context is not re-entrant; one host thread drives it, as the
+ *     reference's single-threaded driver does.
+ *   - Cell layout in host buffers (upload/download): per block, per
+ *     variable, a dense (nx+2)*(ny+2)*(nz+2) array of doubles indexed
+ *     [i][j][k] with k fastest and one ghost layer on each side -- the
+ *     same indexing as the reference's blocks[n].array[var][i][j][k]
+ *     (ref/block.h:52, allocated ref/main.c:429-450).
+ *
+ * The same ABI is implemented on the CPU by the oracle
+ * (oracle/amr_oracle.c), which the tests use as the checker.
+ */
+#ifndef MINIAMR_GB300_H
+#define MINIAMR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MAMR_ABI_VERSION 1
+
+/* Storage / arithmetic precision of the cell pool. */
+enum {
+   MAMR_FP64 = 0,   /* bit-exact with the reference */
+   MAMR_FP32 = 1    /* FP32 cells; FP64-or-better checksum and coarsening */
+};
+
+/* Status codes. */
+enum {
+   MAMR_OK      =  0,
+   MAMR_EINVAL  = -1,  /* bad argument (size, index, null pointer) */
+   MAMR_ENOMEM  = -2,  /* device or host allocation failed */
+   MAMR_ECUDA   = -3,  /* CUDA runtime error */
+   MAMR_EMESH   = -4,  /* misconnected mesh (ref/comm.c:198-201) */
+   MAMR_EUNSUP  = -5,  /* configuration this back end does not run */
+   MAMR_EDEVICE = -6   /* a device-side check set the context error word */
+};
+
+typedef struct mamr_ctx mamr_ctx;
+
+/* Problem shape.  Field meanings follow the reference's globals
+ * (ref/block.h:79-146, defaults ref/param.h). */
+typedef struct {
+   int32_t nx, ny, nz;   /* x/y/z_block_size: cells per block, even */
+   int32_t num_vars;     /* num_vars */
+   int32_t max_blocks;   /* max_num_blocks: pool capacity in block slots */
+   int32_t stencil;      /* 7 or 27 (stencil 0 is not run here) */
+   int32_t code;         /* ghost-exchange variant; only 0 is run here */
+   int32_t permute;      /* --permute: direction order cycles with stage */
+   int32_t dtype;        /* MAMR_FP64 or MAMR_FP32 */
+   int32_t reserved[7];  /* must be zero */
+} mamr_config;
+
+/* One active block as the hot path sees it: a projection of the
+ * reference's `block` struct (ref/block.h:36-53).  An array of these in
+ * sorted_list order (level ascending, block number descending within a
+ * level; ref/block.c:610-625) describes the mesh. */
+typedef struct {
+   int32_t slot;          /* index into blocks[] == pool slot */
+   int32_t level;         /* refinement level */
+   int32_t nei_level[6];  /* W,E,S,N,D,U neighbour level; -2 = boundary */
+   int32_t nei[6][2][2];  /* neighbour slots; [l][0][0] for a same-level or
+                             coarser neighbour, all four for finer ones */
+} mamr_block;
+
+/* split_blocks(): parent slot -> 8 child slots, child[o] for octant
+ * o = i1 + 2*j1 + 4*k1 (ref/block.c:128-173). */
+typedef struct {
+   int32_t parent;
+   int32_t child[8];
+} mamr_split_job;
+
+/* consolidate_blocks(): 8 child slots (by octant) -> the slot of the
+ * re-formed block (ref/block.c:370-431). */
+typedef struct {
+   int32_t child[8];
+   int32_t target;
+} mamr_consolidate_job;
+
+/* Flags for mamr_run_timesteps(). */
+enum {
+   MAMR_RUN_PLAIN   = 0,  /* per-call path: comm, then stencil/check_sum per
+                             variable, exactly the driver's call sequence */
+   MAMR_RUN_BATCHED = 1,  /* one fused ghost+stencil(+checksum) launch per
+                             stage over every block and variable */
+   MAMR_RUN_GRAPH   = 2   /* with BATCHED: replay the stages as a CUDA graph */
+};
+
+/* ---- lifetime --------------------------------------------------------- */
+
+/* Allocates the zero-filled cell pool for cfg->max_blocks slots on the
+ * current CUDA device (replaces the per-block mallocs of
+ * ref/main.c:429-450; zero fill matches the fresh-heap contents the
+ * reference starts from).  The pool is never cleared afterwards. */
+int mamr_create(const mamr_config *cfg, mamr_ctx **out);
+int mamr_destroy(mamr_ctx *ctx);
+const char *mamr_last_error(void);
+/* The context's CUDA stream (a cudaStream_t) for callers that time it. */
+int mamr_stream(mamr_ctx *ctx, void **stream);
+/* Waits for all work queued on the context and reports device-side
+ * error words. */
+int mamr_sync(mamr_ctx *ctx);
+
+/* ---- cell data in and out -------------------------------------------- */
+
+/* Copies n blocks from a host buffer laid out [n][num_vars][nx+2][ny+2]
+ * [nz+2] (doubles) into pool slots slots[0..n).  FP32 pools round to
+ * nearest.  Used once after the reference's init() has filled its host
+ * arrays (ref/init.c:484-495). */
+int mamr_upload_blocks(mamr_ctx *ctx, const int32_t *slots, int32_t n,
+                       const double *host);
+/* The reverse copy, for verification and dumps. */
+int mamr_download_blocks(mamr_ctx *ctx, const int32_t *slots, int32_t n,
+                         double *host);
+
+/* ---- mesh ---------------------------------------------------------------- */
+
+/* Replaces the active mesh: n blocks in sorted_list order.  Checks the
+ * connectivity the exchange relies on and returns MAMR_EMESH where the
+ * reference would print "misconnected block" (ref/comm.c:198-201). */
+int mamr_set_mesh(mamr_ctx *ctx, const mamr_block *blocks, int32_t n);
+
+/* ---- the hot path (reference entry point each one replaces) ----------- */
+
+/* comm(start, num_comm, stage): ref/comm.c:42-242 on one rank --
+ * on_proc_comm (ref/comm.c:1465-1580), on_proc_comm_diff
+ * (ref/comm.c:1585-1908) and apply_bc (ref/comm.c:1911-1965) for
+ * variables [start, start+num_comm), directions x, y, z in order (or
+ * permuted by stage when cfg.permute). */
+int mamr_comm(mamr_ctx *ctx, int32_t start, int32_t num_comm, int32_t stage);
+
+/* stencil_driver(var, calc_stage) -> stencil_calc(var, stencil):
+ * ref/stencil.c:43-145. */
+int mamr_stencil(mamr_ctx *ctx, int32_t var, int32_t calc_stage);
+
+/* check_sum(var): ref/check_sum.c:36-65.  FP64 pools sum each block's
+ * interior serially (k fastest) and the block sums in sorted_list order,
+ * the reference's exact order.  FP32 pools accumulate every cell exactly
+ * in 128-bit fixed point (2^-52 units) and convert once. */
+int mamr_check_sum(mamr_ctx *ctx, int32_t var, double *sum);
+
+/* split_blocks() cell data: ref/block.c:158-173.  Jobs run in the given
+ * (reference) order semantics: a child may reuse a slot freed by an
+ * earlier parent in the same call. */
+int mamr_split(mamr_ctx *ctx, const mamr_split_job *jobs, int32_t n);
+
+/* consolidate_blocks() cell data: ref/block.c:411-431, same ordering
+ * semantics (a later target may be an earlier job's freed child, and a
+ * later job may read an earlier job's target). */
+int mamr_consolidate(mamr_ctx *ctx, const mamr_consolidate_job *jobs,
+                     int32_t n);
+
+/* The stage loop of ref/driver.c:73-108 for num_ts timesteps of
+ * stages_per_ts stages, comm over all variables at once (comm_vars = 0).
+ * comm_stage/calc_stage of the first stage is first_stage.  When
+ * checksum_freq > 0, stages with (stage % checksum_freq == 0) produce
+ * num_vars checksums, appended to sums (host memory, may be NULL) in
+ * stage order; *n_sums receives how many stages produced them.  The
+ * tolerance check of ref/driver.c:96-101 is left to the caller. */
+int mamr_run_timesteps(mamr_ctx *ctx, int32_t num_ts, int32_t stages_per_ts,
+                       int32_t checksum_freq, int32_t first_stage,
+                       int32_t flags, double *sums, int32_t *n_sums);
+
+/* Number of kernels this context has launched since creation (for the
+ * launch counts the benchmark reports). */
+int mamr_launch_count(mamr_ctx *ctx, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MINIAMR_GB300_H */

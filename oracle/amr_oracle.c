@@ -1,0 +1,671 @@
+/*
+ * amr_oracle.c -- CPU restatement of miniAMR's per-timestep hot path behind
+ * the mamr_* C ABI (include/miniamr_gb300.h).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker the GPU library is
+ * compared against; it is never linked into or called by the product path.
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
+ * it.  Parity of this restatement with the reference itself is pinned by
+ * running the reference's own driver over these functions
+ * (oracle/_ref/miniamr_hybrid_oracle vs oracle/_ref/miniamr_ref, see
+ * tests/test_oracle_vs_reference.py) and by the committed golden logs.
+ *
+ * Every routine is a sequential restatement of the reference code it cites
+ * (paths are inside the miniAMR repository).  Cells are held as doubles in
+ * a dense [slot][var][nx+2][ny+2][nz+2] array.  In FP32 mode every stored
+ * value is a float and every arithmetic result is rounded to float right
+ * after the double operation (RF below); double rounding is exact for
+ * +, -, *, / of floats because 53 >= 2*24+2.
+ */
+#include <math.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "miniamr_gb300.h"
+
+struct mamr_ctx {
+   mamr_config cfg;
+   int X, Y, Z;            /* nx+2, ny+2, nz+2 */
+   size_t bv;              /* cells per block-variable */
+   int fp32;
+   double *pool;           /* max_blocks * num_vars * bv */
+   mamr_block *mesh;
+   int32_t n_mesh;
+   int32_t *slot_pos;      /* slot -> position in mesh, -1 if inactive */
+   int64_t launches;       /* stays 0: the oracle launches nothing */
+};
+
+static __thread char err_buf[256];
+
+static int fail(int code, const char *fmt, ...)
+{
+   va_list ap;
+   va_start(ap, fmt);
+   vsnprintf(err_buf, sizeof(err_buf), fmt, ap);
+   va_end(ap);
+   return code;
+}
+
+const char *mamr_last_error(void) { return err_buf; }
+
+/* Round to the pool's precision. */
+static inline double RF(const mamr_ctx *c, double x)
+{
+   return c->fp32 ? (double) (float) x : x;
+}
+
+static inline double *blk(const mamr_ctx *c, int slot, int var)
+{
+   return c->pool + ((size_t) slot * c->cfg.num_vars + var) * c->bv;
+}
+
+#define AT(p, i, j, k) (p)[((size_t) (i) * c->Y + (j)) * c->Z + (k)]
+
+int mamr_create(const mamr_config *cfg, mamr_ctx **out)
+{
+   mamr_ctx *c;
+   int r;
+   if (!cfg || !out)
+      return fail(MAMR_EINVAL, "null argument");
+   if (cfg->nx < 2 || cfg->ny < 2 || cfg->nz < 2 || cfg->nx % 2 ||
+       cfg->ny % 2 || cfg->nz % 2)
+      return fail(MAMR_EINVAL, "block sizes must be even and >= 2");
+   if (cfg->num_vars < 1 || cfg->max_blocks < 1)
+      return fail(MAMR_EINVAL, "num_vars and max_blocks must be >= 1");
+   if (cfg->stencil != 7 && cfg->stencil != 27)
+      return fail(MAMR_EUNSUP, "stencil %d not supported", cfg->stencil);
+   if (cfg->code != 0)
+      return fail(MAMR_EUNSUP, "code %d not supported", cfg->code);
+   if (cfg->dtype != MAMR_FP64 && cfg->dtype != MAMR_FP32)
+      return fail(MAMR_EINVAL, "bad dtype");
+   for (r = 0; r < 7; r++)
+      if (cfg->reserved[r])
+         return fail(MAMR_EINVAL, "reserved fields must be zero");
+   c = (mamr_ctx *) calloc(1, sizeof(*c));
+   if (!c)
+      return fail(MAMR_ENOMEM, "host allocation");
+   c->cfg = *cfg;
+   c->X = cfg->nx + 2;
+   c->Y = cfg->ny + 2;
+   c->Z = cfg->nz + 2;
+   c->bv = (size_t) c->X * c->Y * c->Z;
+   c->fp32 = cfg->dtype == MAMR_FP32;
+   /* zero-filled, never cleared: ref/main.c:429-450 fresh heap */
+   c->pool = (double *) calloc((size_t) cfg->max_blocks * cfg->num_vars *
+                               c->bv, sizeof(double));
+   if (!c->pool) {
+      free(c);
+      return fail(MAMR_ENOMEM, "host pool allocation");
+   }
+   *out = c;
+   return MAMR_OK;
+}
+
+int mamr_destroy(mamr_ctx *c)
+{
+   if (!c)
+      return MAMR_OK;
+   free(c->pool);
+   free(c->mesh);
+   free(c->slot_pos);
+   free(c);
+   return MAMR_OK;
+}
+
+int mamr_stream(mamr_ctx *c, void **stream)
+{
+   if (!c || !stream)
+      return fail(MAMR_EINVAL, "null argument");
+   *stream = NULL;
+   return MAMR_OK;
+}
+
+int mamr_sync(mamr_ctx *c)
+{
+   return c ? MAMR_OK : fail(MAMR_EINVAL, "null context");
+}
+
+int mamr_launch_count(mamr_ctx *c, int64_t *count)
+{
+   if (!c || !count)
+      return fail(MAMR_EINVAL, "null argument");
+   *count = c->launches;
+   return MAMR_OK;
+}
+
+static int check_slot(const mamr_ctx *c, int32_t s)
+{
+   return s >= 0 && s < c->cfg.max_blocks;
+}
+
+int mamr_upload_blocks(mamr_ctx *c, const int32_t *slots, int32_t n,
+                       const double *host)
+{
+   int32_t b;
+   int v;
+   size_t q;
+   if (!c || (n && (!slots || !host)) || n < 0)
+      return fail(MAMR_EINVAL, "bad upload arguments");
+   for (b = 0; b < n; b++)
+      if (!check_slot(c, slots[b]))
+         return fail(MAMR_EINVAL, "slot %d out of range", slots[b]);
+   for (b = 0; b < n; b++)
+      for (v = 0; v < c->cfg.num_vars; v++) {
+         double *d = blk(c, slots[b], v);
+         const double *s = host + ((size_t) b * c->cfg.num_vars + v) * c->bv;
+         for (q = 0; q < c->bv; q++)
+            d[q] = RF(c, s[q]);
+      }
+   return MAMR_OK;
+}
+
+int mamr_download_blocks(mamr_ctx *c, const int32_t *slots, int32_t n,
+                         double *host)
+{
+   int32_t b;
+   int v;
+   if (!c || (n && (!slots || !host)) || n < 0)
+      return fail(MAMR_EINVAL, "bad download arguments");
+   for (b = 0; b < n; b++)
+      if (!check_slot(c, slots[b]))
+         return fail(MAMR_EINVAL, "slot %d out of range", slots[b]);
+   for (b = 0; b < n; b++)
+      for (v = 0; v < c->cfg.num_vars; v++)
+         memcpy(host + ((size_t) b * c->cfg.num_vars + v) * c->bv,
+                blk(c, slots[b], v), c->bv * sizeof(double));
+   return MAMR_OK;
+}
+
+int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks, int32_t n)
+{
+   int32_t b;
+   int l, i, j;
+   mamr_block *m;
+   if (!c || n < 0 || (n && !blocks))
+      return fail(MAMR_EINVAL, "bad mesh arguments");
+   for (b = 0; b < n; b++) {
+      const mamr_block *bp = &blocks[b];
+      if (!check_slot(c, bp->slot))
+         return fail(MAMR_EINVAL, "block %d: slot %d out of range", b,
+                     bp->slot);
+      for (l = 0; l < 6; l++) {
+         int nl = bp->nei_level[l];
+         if (nl == -2)
+            continue;
+         if (nl != bp->level && nl != bp->level + 1 && nl != bp->level - 1)
+            return fail(MAMR_EMESH, "misconnected block (slot %d face %d)",
+                        bp->slot, l);
+         for (i = 0; i < 2; i++)
+            for (j = 0; j < 2; j++)
+               if ((nl == bp->level + 1 || (i == 0 && j == 0)) &&
+                   !check_slot(c, bp->nei[l][i][j]))
+                  return fail(MAMR_EMESH,
+                              "misconnected block (slot %d face %d nei %d)",
+                              bp->slot, l, bp->nei[l][i][j]);
+      }
+   }
+   m = (mamr_block *) malloc(sizeof(mamr_block) * (n ? n : 1));
+   if (!m)
+      return fail(MAMR_ENOMEM, "host allocation");
+   if (!c->slot_pos) {
+      c->slot_pos = (int32_t *) malloc(sizeof(int32_t) * c->cfg.max_blocks);
+      if (!c->slot_pos) {
+         free(m);
+         return fail(MAMR_ENOMEM, "host allocation");
+      }
+   }
+   memcpy(m, blocks, sizeof(mamr_block) * n);
+   free(c->mesh);
+   c->mesh = m;
+   c->n_mesh = n;
+   for (b = 0; b < c->cfg.max_blocks; b++)
+      c->slot_pos[b] = -1;
+   for (b = 0; b < n; b++)
+      c->slot_pos[m[b].slot] = b;
+   return MAMR_OK;
+}
+
+/* ref/comm.c:1465-1534 (code 0): same-level exchange across face l between
+ * blocks n and n1, variables [start, start+num). */
+static void on_proc_comm(mamr_ctx *c, int n, int n1, int l, int start,
+                         int num)
+{
+   int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz, m, i, j, k;
+   int is, ie, js, je, lo, hi;
+   /* l even: bp = n, bp1 = n1; l odd: swapped */
+   lo = (l % 2 == 0) ? n : n1;   /* bp  */
+   hi = (l % 2 == 0) ? n1 : n;   /* bp1 */
+   for (m = start; m < start + num; m++) {
+      double *bp = blk(c, lo, m), *bp1 = blk(c, hi, m);
+      if (l / 2 == 0) {
+         for (j = 1; j <= ny; j++)
+            for (k = 1; k <= nz; k++) {
+               AT(bp1, nx + 1, j, k) = AT(bp, 1, j, k);
+               AT(bp, 0, j, k) = AT(bp1, nx, j, k);
+            }
+      } else if (l / 2 == 1) {
+         if (c->cfg.stencil == 7) { is = 1; ie = nx; }
+         else { is = 0; ie = nx + 1; }
+         for (i = is; i <= ie; i++)
+            for (k = 1; k <= nz; k++) {
+               AT(bp1, i, ny + 1, k) = AT(bp, i, 1, k);
+               AT(bp, i, 0, k) = AT(bp1, i, ny, k);
+            }
+      } else {
+         if (c->cfg.stencil == 7) { is = 1; ie = nx; js = 1; je = ny; }
+         else { is = 0; ie = nx + 1; js = 0; je = ny + 1; }
+         for (i = is; i <= ie; i++)
+            for (j = js; j <= je; j++) {
+               AT(bp1, i, j, nz + 1) = AT(bp, i, j, 1);
+               AT(bp, i, j, 0) = AT(bp1, i, j, nz);
+            }
+      }
+   }
+}
+
+/* ref/comm.c:1585-1688 (code 0): block n (coarse) and n1 (fine) across
+ * face l of n, quarter (iq, jq) of n's face.  Fine ghosts get coarse/4,
+ * the coarse ghost gets the left-to-right sum of the 2x2 fine cells. */
+static void on_proc_comm_diff(mamr_ctx *c, int n, int n1, int l, int iq,
+                              int jq, int start, int num)
+{
+   int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz;
+   int xh = nx / 2, yh = ny / 2, zh = nz / 2, m, i, j, k;
+   int a0, a1, a2, a3, o1, o2;
+   for (m = start; m < start + num; m++) {
+      double *bp = blk(c, n, m), *bp1 = blk(c, n1, m);
+      if (l / 2 == 0) {
+         if (l == 0) { a0 = 0; a1 = 1; a2 = nx + 1; a3 = nx; }
+         else { a0 = nx + 1; a1 = nx; a2 = 0; a3 = 1; }
+         o1 = jq * yh;   /* j offset */
+         o2 = iq * zh;   /* k offset */
+         for (j = 1; j <= yh; j++)
+            for (k = 1; k <= zh; k++) {
+               double q = RF(c, AT(bp, a1, j + o1, k + o2) / 4.0);
+               AT(bp1, a2, 2*j - 1, 2*k - 1) = q;
+               AT(bp1, a2, 2*j - 1, 2*k) = q;
+               AT(bp1, a2, 2*j, 2*k - 1) = q;
+               AT(bp1, a2, 2*j, 2*k) = q;
+               AT(bp, a0, j + o1, k + o2) =
+                  RF(c, RF(c, RF(c, AT(bp1, a3, 2*j - 1, 2*k - 1) +
+                                    AT(bp1, a3, 2*j - 1, 2*k)) +
+                             AT(bp1, a3, 2*j, 2*k - 1)) +
+                        AT(bp1, a3, 2*j, 2*k));
+            }
+      } else if (l / 2 == 1) {
+         if (l == 2) { a0 = 0; a1 = 1; a2 = ny + 1; a3 = ny; }
+         else { a0 = ny + 1; a1 = ny; a2 = 0; a3 = 1; }
+         o1 = jq * xh;   /* i offset */
+         o2 = iq * zh;   /* k offset */
+         for (i = 1; i <= xh; i++)
+            for (k = 1; k <= zh; k++) {
+               double q = RF(c, AT(bp, i + o1, a1, k + o2) / 4.0);
+               AT(bp1, 2*i - 1, a2, 2*k - 1) = q;
+               AT(bp1, 2*i - 1, a2, 2*k) = q;
+               AT(bp1, 2*i, a2, 2*k - 1) = q;
+               AT(bp1, 2*i, a2, 2*k) = q;
+               AT(bp, i + o1, a0, k + o2) =
+                  RF(c, RF(c, RF(c, AT(bp1, 2*i - 1, a3, 2*k - 1) +
+                                    AT(bp1, 2*i - 1, a3, 2*k)) +
+                             AT(bp1, 2*i, a3, 2*k - 1)) +
+                        AT(bp1, 2*i, a3, 2*k));
+            }
+      } else {
+         if (l == 4) { a0 = 0; a1 = 1; a2 = nz + 1; a3 = nz; }
+         else { a0 = nz + 1; a1 = nz; a2 = 0; a3 = 1; }
+         o1 = jq * xh;   /* i offset */
+         o2 = iq * yh;   /* j offset */
+         for (i = 1; i <= xh; i++)
+            for (j = 1; j <= yh; j++) {
+               double q = RF(c, AT(bp, i + o1, j + o2, a1) / 4.0);
+               AT(bp1, 2*i - 1, 2*j - 1, a2) = q;
+               AT(bp1, 2*i - 1, 2*j, a2) = q;
+               AT(bp1, 2*i, 2*j - 1, a2) = q;
+               AT(bp1, 2*i, 2*j, a2) = q;
+               AT(bp, i + o1, j + o2, a0) =
+                  RF(c, RF(c, RF(c, AT(bp1, 2*i - 1, 2*j - 1, a3) +
+                                    AT(bp1, 2*i - 1, 2*j, a3)) +
+                             AT(bp1, 2*i, 2*j - 1, a3)) +
+                        AT(bp1, 2*i, 2*j, a3));
+            }
+      }
+   }
+}
+
+/* ref/comm.c:1911-1965: reflective copy of the plane next to face l into
+ * its ghost plane; interior tangential range when code==0 && stencil==7,
+ * full 0..n+1 otherwise. */
+static void apply_bc(mamr_ctx *c, int l, int n, int start, int num)
+{
+   int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz, var, i, j, k, t, f;
+   int full = !(c->cfg.stencil == 7);
+   int lo0 = full ? 0 : 1;
+   for (var = start; var < start + num; var++) {
+      double *bp = blk(c, n, var);
+      if (l / 2 == 0) {
+         t = (l == 1) ? nx + 1 : 0;
+         f = (l == 1) ? nx : 1;
+         for (j = lo0; j <= (full ? ny + 1 : ny); j++)
+            for (k = lo0; k <= (full ? nz + 1 : nz); k++)
+               AT(bp, t, j, k) = AT(bp, f, j, k);
+      } else if (l / 2 == 1) {
+         t = (l == 3) ? ny + 1 : 0;
+         f = (l == 3) ? ny : 1;
+         for (i = lo0; i <= (full ? nx + 1 : nx); i++)
+            for (k = lo0; k <= (full ? nz + 1 : nz); k++)
+               AT(bp, i, t, k) = AT(bp, i, f, k);
+      } else {
+         t = (l == 5) ? nz + 1 : 0;
+         f = (l == 5) ? nz : 1;
+         for (i = lo0; i <= (full ? nx + 1 : nx); i++)
+            for (j = lo0; j <= (full ? ny + 1 : ny); j++)
+               AT(bp, i, j, t) = AT(bp, i, j, f);
+      }
+   }
+}
+
+static const int permutations[6][3] = { {0, 1, 2}, {1, 2, 0}, {2, 0, 1},
+                                        {0, 2, 1}, {1, 0, 2}, {2, 1, 0} };
+
+/* ref/comm.c:42-56,162-203: the on-rank part of comm() on one rank. */
+int mamr_comm(mamr_ctx *c, int32_t start, int32_t num, int32_t stage)
+{
+   int o, dir, in, l, i, j, k, m, n;
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   if (start < 0 || num < 0 || start + num > c->cfg.num_vars)
+      return fail(MAMR_EINVAL, "variable range out of bounds");
+   for (o = 0; o < 3; o++) {
+      dir = c->cfg.permute ? permutations[stage % 6][o] : o;
+      for (in = 0; in < c->n_mesh; in++) {
+         const mamr_block *bp = &c->mesh[in];
+         n = bp->slot;
+         for (l = dir * 2; l < dir * 2 + 2; l++) {
+            if (bp->nei_level[l] == bp->level) {
+               if ((m = bp->nei[l][0][0]) > n)
+                  on_proc_comm(c, n, m, l, start, num);
+            } else if (bp->nei_level[l] == bp->level + 1) {
+               for (i = 0; i < 2; i++)
+                  for (j = 0; j < 2; j++)
+                     if ((m = bp->nei[l][i][j]) > n)
+                        on_proc_comm_diff(c, n, m, l, i, j, start, num);
+            } else if (bp->nei_level[l] == bp->level - 1) {
+               if ((m = bp->nei[l][0][0]) > n) {
+                  /* blocks[m]: the coarse neighbour's record */
+                  const mamr_block *mb = c->slot_pos[m] >= 0 ?
+                                         &c->mesh[c->slot_pos[m]] : NULL;
+                  if (!mb)
+                     return fail(MAMR_EMESH, "neighbour slot %d not active",
+                                 m);
+                  k = dir * 2 + 1 - l % 2;
+                  for (i = 0; i < 2; i++)
+                     for (j = 0; j < 2; j++)
+                        if (mb->nei[k][i][j] == n)
+                           on_proc_comm_diff(c, m, n, k, i, j, start, num);
+               }
+            } else if (bp->nei_level[l] == -2) {
+               apply_bc(c, l, n, start, num);
+            } else {
+               return fail(MAMR_EMESH, "misconnected block");
+            }
+         }
+      }
+   }
+   return MAMR_OK;
+}
+
+/* ref/stencil.c:76-145 (stencil_calc), Jacobi update of every active
+ * block's interior for one variable. */
+int mamr_stencil(mamr_ctx *c, int32_t var, int32_t calc_stage)
+{
+   int nx = c ? c->cfg.nx : 0, ny = c ? c->cfg.ny : 0, nz = c ? c->cfg.nz : 0;
+   int in, i, j, k;
+   double *work;
+   (void) calc_stage;
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   if (var < 0 || var >= c->cfg.num_vars)
+      return fail(MAMR_EINVAL, "variable out of range");
+   work = (double *) malloc(sizeof(double) * c->bv);
+   if (!work)
+      return fail(MAMR_ENOMEM, "host allocation");
+   for (in = 0; in < c->n_mesh; in++) {
+      double *a = blk(c, c->mesh[in].slot, var);
+      for (i = 1; i <= nx; i++)
+         for (j = 1; j <= ny; j++)
+            for (k = 1; k <= nz; k++) {
+               double w;
+               if (c->cfg.stencil == 7) {
+                  w = RF(c, AT(a, i - 1, j, k) + AT(a, i, j - 1, k));
+                  w = RF(c, w + AT(a, i, j, k - 1));
+                  w = RF(c, w + AT(a, i, j, k));
+                  w = RF(c, w + AT(a, i, j, k + 1));
+                  w = RF(c, w + AT(a, i, j + 1, k));
+                  w = RF(c, w + AT(a, i + 1, j, k));
+                  w = RF(c, w / 7.0);
+               } else {
+                  double s[3];
+                  int p, jj, kk;
+                  for (p = 0; p < 3; p++) {
+                     double t = 0.0;
+                     int first = 1;
+                     for (jj = j - 1; jj <= j + 1; jj++)
+                        for (kk = k - 1; kk <= k + 1; kk++) {
+                           if (first) {
+                              t = AT(a, i - 1 + p, jj, kk);
+                              first = 0;
+                           } else
+                              t = RF(c, t + AT(a, i - 1 + p, jj, kk));
+                        }
+                     s[p] = t;
+                  }
+                  w = RF(c, RF(c, RF(c, s[0] + s[1]) + s[2]) / 27.0);
+               }
+               AT(work, i, j, k) = w;
+            }
+      for (i = 1; i <= nx; i++)
+         for (j = 1; j <= ny; j++)
+            for (k = 1; k <= nz; k++)
+               AT(a, i, j, k) = AT(work, i, j, k);
+   }
+   free(work);
+   return MAMR_OK;
+}
+
+/* FP32 checksum unit: each cell truncated toward zero to a multiple of
+ * 2^-52, accumulated exactly in 128 bits.  Returns 0 on success, -1 when a
+ * cell is not finite or |v| >= 2^10 (outside the fixed-point range). */
+static int fixed_cell(double v, int64_t *out)
+{
+   if (!(fabs(v) < 1024.0))
+      return -1;
+   *out = (int64_t) (v * 0x1p52);
+   return 0;
+}
+
+static double fixed128_to_double(__int128 acc)
+{
+   return (double) acc * 0x1p-52;
+}
+
+/* ref/check_sum.c:36-65. */
+int mamr_check_sum(mamr_ctx *c, int32_t var, double *sum)
+{
+   int in, i, j, k;
+   if (!c || !sum)
+      return fail(MAMR_EINVAL, "null argument");
+   if (var < 0 || var >= c->cfg.num_vars)
+      return fail(MAMR_EINVAL, "variable out of range");
+   if (!c->fp32) {
+      double s = 0.0, block_sum;
+      for (in = 0; in < c->n_mesh; in++) {
+         const double *a = blk(c, c->mesh[in].slot, var);
+         block_sum = 0.0;
+         for (i = 1; i <= c->cfg.nx; i++)
+            for (j = 1; j <= c->cfg.ny; j++)
+               for (k = 1; k <= c->cfg.nz; k++)
+                  block_sum += AT(a, i, j, k);
+         s += block_sum;
+      }
+      *sum = s;
+   } else {
+      __int128 acc = 0;
+      for (in = 0; in < c->n_mesh; in++) {
+         const double *a = blk(c, c->mesh[in].slot, var);
+         for (i = 1; i <= c->cfg.nx; i++)
+            for (j = 1; j <= c->cfg.ny; j++)
+               for (k = 1; k <= c->cfg.nz; k++) {
+                  int64_t q;
+                  if (fixed_cell(AT(a, i, j, k), &q))
+                     return fail(MAMR_EDEVICE,
+                                 "cell outside the fixed-point range");
+                  acc += q;
+               }
+      }
+      *sum = fixed128_to_double(acc);
+   }
+   return MAMR_OK;
+}
+
+/* ref/block.c:158-173: each child octant's interior is its parent's
+ * matching half-block, each parent cell replicated 2x2x2 and divided by 8
+ * (exact).  Child ghost cells keep the slot's previous contents. */
+int mamr_split(mamr_ctx *c, const mamr_split_job *jobs, int32_t n)
+{
+   int32_t t;
+   int o, v, i, j, k, i2, j2, k2;
+   if (!c || n < 0 || (n && !jobs))
+      return fail(MAMR_EINVAL, "bad split arguments");
+   for (t = 0; t < n; t++) {
+      if (!check_slot(c, jobs[t].parent))
+         return fail(MAMR_EINVAL, "split parent slot out of range");
+      for (o = 0; o < 8; o++)
+         if (!check_slot(c, jobs[t].child[o]))
+            return fail(MAMR_EINVAL, "split child slot out of range");
+   }
+   for (t = 0; t < n; t++)
+      for (o = 0; o < 8; o++) {
+         int i1 = (o % 2) * (c->cfg.nx / 2), j1 = ((o / 2) % 2) * (c->cfg.ny / 2),
+             k1 = (o / 4) * (c->cfg.nz / 2);
+         for (v = 0; v < c->cfg.num_vars; v++) {
+            const double *p = blk(c, jobs[t].parent, v);
+            double *ch = blk(c, jobs[t].child[o], v);
+            for (i2 = i = 1; i <= c->cfg.nx / 2; i++, i2 += 2)
+               for (j2 = j = 1; j <= c->cfg.ny / 2; j++, j2 += 2)
+                  for (k2 = k = 1; k <= c->cfg.nz / 2; k++, k2 += 2) {
+                     double q = RF(c, AT(p, i + i1, j + j1, k + k1) / 8.0);
+                     AT(ch, i2, j2, k2) = q;
+                     AT(ch, i2 + 1, j2, k2) = q;
+                     AT(ch, i2, j2 + 1, k2) = q;
+                     AT(ch, i2 + 1, j2 + 1, k2) = q;
+                     AT(ch, i2, j2, k2 + 1) = q;
+                     AT(ch, i2 + 1, j2, k2 + 1) = q;
+                     AT(ch, i2, j2 + 1, k2 + 1) = q;
+                     AT(ch, i2 + 1, j2 + 1, k2 + 1) = q;
+                  }
+         }
+      }
+   return MAMR_OK;
+}
+
+/* Neumaier-compensated FP64 sum of the 8 children of one coarse cell, in
+ * the reference's term order; used for FP32 pools. */
+static double sum8_compensated(const double *t)
+{
+   double s = t[0], comp = 0.0;
+   int q;
+   for (q = 1; q < 8; q++) {
+      double u = s + t[q];
+      if (fabs(s) >= fabs(t[q]))
+         comp += (s - u) + t[q];
+      else
+         comp += (t[q] - u) + s;
+      s = u;
+   }
+   return s + comp;
+}
+
+/* ref/block.c:411-431: each coarse interior cell is the left-to-right sum
+ * of its 8 children (no division: cell values are extensive).  The target's
+ * ghost cells keep the slot's previous contents. */
+int mamr_consolidate(mamr_ctx *c, const mamr_consolidate_job *jobs,
+                     int32_t n)
+{
+   int32_t t;
+   int o, v, i, j, k, i2, j2, k2;
+   if (!c || n < 0 || (n && !jobs))
+      return fail(MAMR_EINVAL, "bad consolidate arguments");
+   for (t = 0; t < n; t++) {
+      if (!check_slot(c, jobs[t].target))
+         return fail(MAMR_EINVAL, "consolidate target slot out of range");
+      for (o = 0; o < 8; o++)
+         if (!check_slot(c, jobs[t].child[o]))
+            return fail(MAMR_EINVAL, "consolidate child slot out of range");
+   }
+   for (t = 0; t < n; t++)
+      for (o = 0; o < 8; o++) {
+         int i1 = (o % 2) * (c->cfg.nx / 2), j1 = ((o / 2) % 2) * (c->cfg.ny / 2),
+             k1 = (o / 4) * (c->cfg.nz / 2);
+         for (v = 0; v < c->cfg.num_vars; v++) {
+            double *p = blk(c, jobs[t].target, v);
+            const double *ch = blk(c, jobs[t].child[o], v);
+            for (i2 = i = 1; i <= c->cfg.nx / 2; i++, i2 += 2)
+               for (j2 = j = 1; j <= c->cfg.ny / 2; j++, j2 += 2)
+                  for (k2 = k = 1; k <= c->cfg.nz / 2; k++, k2 += 2) {
+                     double t8[8] = {
+                        AT(ch, i2, j2, k2), AT(ch, i2 + 1, j2, k2),
+                        AT(ch, i2, j2 + 1, k2), AT(ch, i2 + 1, j2 + 1, k2),
+                        AT(ch, i2, j2, k2 + 1), AT(ch, i2 + 1, j2, k2 + 1),
+                        AT(ch, i2, j2 + 1, k2 + 1),
+                        AT(ch, i2 + 1, j2 + 1, k2 + 1) };
+                     double s;
+                     if (c->fp32)
+                        s = (double) (float) sum8_compensated(t8);
+                     else {
+                        int q;
+                        s = t8[0];
+                        for (q = 1; q < 8; q++)
+                           s += t8[q];
+                     }
+                     AT(p, i + i1, j + j1, k + k1) = s;
+                  }
+         }
+      }
+   return MAMR_OK;
+}
+
+/* ref/driver.c:73-108 with comm_vars = num_vars (one comm per stage). */
+int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts, int32_t stages_per_ts,
+                       int32_t checksum_freq, int32_t first_stage,
+                       int32_t flags, double *sums, int32_t *n_sums)
+{
+   int ts, stage, var, r, cnt = 0, gstage = first_stage;
+   (void) flags;
+   if (!c || num_ts < 0 || stages_per_ts < 1 || checksum_freq < 0)
+      return fail(MAMR_EINVAL, "bad run arguments");
+   for (ts = 0; ts < num_ts; ts++)
+      for (stage = 0; stage < stages_per_ts; stage++, gstage++) {
+         int do_cs = checksum_freq && !(stage % checksum_freq);
+         if ((r = mamr_comm(c, 0, c->cfg.num_vars, gstage)))
+            return r;
+         for (var = 0; var < c->cfg.num_vars; var++) {
+            if ((r = mamr_stencil(c, var, gstage)))
+               return r;
+            if (do_cs) {
+               double s;
+               if ((r = mamr_check_sum(c, var, &s)))
+                  return r;
+               if (sums)
+                  sums[(size_t) cnt * c->cfg.num_vars + var] = s;
+            }
+         }
+         if (do_cs)
+            cnt++;
+      }
+   if (n_sums)
+      *n_sums = cnt;
+   return MAMR_OK;
+}

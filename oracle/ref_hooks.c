@@ -1,0 +1,155 @@
+/*
+ * Link-time hooks for the reference build (oracle/_ref/miniamr_ref) and the
+ * drop-in hybrid build (oracle/_ref/miniamr_hybrid_oracle).
+ *
+ * Test infrastructure only.  Linked with -Wl,--wrap=check_sum,--wrap=refine
+ * so that the reference's own code runs unchanged and this file only
+ * observes it.  When the environment variable MAMR_REF_LOG names a file,
+ * every check_sum() call (ref/check_sum.c:36, called from ref/driver.c:91
+ * and ref/init.c:682) appends one line
+ *
+ *     cs <call#> <var> <checksum as 16 hex digits> <cell hash, 16 hex>
+ *
+ * where the cell hash is FNV-1a-64 over the bit patterns of every cell
+ * (ghosts included) of that variable in every active block, visited in
+ * sorted_list order (ref/block.h:72-77), each block prefixed by its
+ * number.  Every refine() call (ref/refine.c:38) appends one line
+ *
+ *     mesh <ts> <n_active> <hash of (slot,number,level,nei_level,nei,cen)>
+ *
+ * plus, when MAMR_REF_MESH_DUMP is set, the per-block records themselves.
+ * The hybrid build holds its cell data behind the mamr_* C ABI; there the
+ * drop-in's mamr_dropin_fetch() (a weak reference here) supplies the cells.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <stdint.h>
+#include <string.h>
+#include <mpi.h>
+
+#include "block.h"
+#include "comm.h"
+#include "proto.h"
+
+double __real_check_sum(int var);
+void __real_refine(int ts);
+
+/* Provided by the drop-in check_sum.c replacement in the hybrid build. */
+extern int mamr_dropin_fetch(int slot, int var, double *out)
+   __attribute__((weak));
+
+static FILE *log_fp;
+static int log_checked;
+static long cs_calls;
+
+static FILE *hook_log(void)
+{
+   if (!log_checked) {
+      const char *p = getenv("MAMR_REF_LOG");
+      log_checked = 1;
+      if (p && *p) {
+         log_fp = fopen(p, "w");
+         if (!log_fp) {
+            fprintf(stderr, "ref_hooks: cannot open %s\n", p);
+            exit(-1);
+         }
+      }
+   }
+   return log_fp;
+}
+
+static uint64_t fnv_bytes(uint64_t h, const void *p, size_t n)
+{
+   const unsigned char *c = (const unsigned char *) p;
+   size_t i;
+   for (i = 0; i < n; i++) {
+      h ^= c[i];
+      h *= 1099511628211ULL;
+   }
+   return h;
+}
+
+static uint64_t var_cell_hash(int var)
+{
+   int in, i, j, k, nx2 = x_block_size + 2, ny2 = y_block_size + 2,
+       nz2 = z_block_size + 2;
+   uint64_t h = 1469598103934665603ULL;
+   double *buf = NULL;
+
+   if (mamr_dropin_fetch)
+      buf = (double *) malloc(sizeof(double) * nx2 * ny2 * nz2);
+   for (in = 0; in < sorted_index[num_refine+1]; in++) {
+      int n = sorted_list[in].n;
+      long long number = (long long) blocks[n].number;
+      h = fnv_bytes(h, &number, sizeof(number));
+      if (buf) {
+         if (mamr_dropin_fetch(n, var, buf)) {
+            fprintf(stderr, "ref_hooks: fetch failed\n");
+            exit(-1);
+         }
+         h = fnv_bytes(h, buf, sizeof(double) * nx2 * ny2 * nz2);
+      } else {
+         for (i = 0; i < nx2; i++)
+            for (j = 0; j < ny2; j++)
+               for (k = 0; k < nz2; k++)
+                  h = fnv_bytes(h, &blocks[n].array[var][i][j][k],
+                                sizeof(double));
+      }
+   }
+   free(buf);
+   return h;
+}
+
+double __wrap_check_sum(int var)
+{
+   double s = __real_check_sum(var);
+   FILE *fp = hook_log();
+   if (fp) {
+      uint64_t bits;
+      memcpy(&bits, &s, sizeof(bits));
+      fprintf(fp, "cs %ld %d %016llx %016llx\n", cs_calls, var,
+              (unsigned long long) bits,
+              (unsigned long long) var_cell_hash(var));
+   }
+   cs_calls++;
+   return s;
+}
+
+void __wrap_refine(int ts)
+{
+   FILE *fp;
+   __real_refine(ts);
+   fp = hook_log();
+   if (fp) {
+      int in, l, a, b, dump = getenv("MAMR_REF_MESH_DUMP") != NULL;
+      uint64_t h = 1469598103934665603ULL;
+      for (in = 0; in < sorted_index[num_refine+1]; in++) {
+         int n = sorted_list[in].n;
+         block *bp = &blocks[n];
+         int rec[1 + 1 + 6 + 24 + 3];
+         long long number = (long long) bp->number;
+         rec[0] = n;
+         rec[1] = bp->level;
+         for (l = 0; l < 6; l++) {
+            rec[2 + l] = bp->nei_level[l];
+            for (a = 0; a < 2; a++)
+               for (b = 0; b < 2; b++)
+                  rec[8 + l*4 + a*2 + b] = bp->nei[l][a][b];
+         }
+         rec[32] = bp->cen[0];
+         rec[33] = bp->cen[1];
+         rec[34] = bp->cen[2];
+         h = fnv_bytes(h, &number, sizeof(number));
+         h = fnv_bytes(h, rec, sizeof(rec));
+         if (dump) {
+            fprintf(fp, "blk %lld", number);
+            for (l = 0; l < 35; l++)
+               fprintf(fp, " %d", rec[l]);
+            fprintf(fp, "\n");
+         }
+      }
+      fprintf(fp, "mesh %d %d %016llx\n", ts, sorted_index[num_refine+1],
+              (unsigned long long) h);
+      fflush(fp);
+   }
+}
