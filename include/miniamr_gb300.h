@@ -185,6 +185,18 @@ int mamr_run_timesteps(mamr_ctx *ctx, int32_t num_ts, int32_t stages_per_ts,
  * launch counts the benchmark reports). */
 int mamr_launch_count(mamr_ctx *ctx, int64_t *count);
 
+/* ---- host-side helper (no device work) --------------------------------- */
+
+/* The cell values the reference's init() gives its first n_blocks blocks
+ * on one rank (ref/init.c:484-495): per block in lattice order, per
+ * variable, every cell (ghosts included) zero, then the interior filled
+ * with rand()/RAND_MAX in i, j, k order (k fastest), from the C library's
+ * unseeded rand() stream (seed 1).  A private random_r state is used, so
+ * the caller's rand() state is untouched.  out: [n_blocks][num_vars]
+ * [nx+2][ny+2][nz+2] doubles.  Uses cfg's nx, ny, nz and num_vars. */
+int mamr_initial_values(const mamr_config *cfg, int32_t n_blocks,
+                        double *out);
+
 #ifdef __cplusplus
 }
 #endif

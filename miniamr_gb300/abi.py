@@ -1,0 +1,232 @@
+"""ctypes binding of the mamr_* C ABI declared in include/miniamr_gb300.h.
+
+The same ABI is exported by the GB300 library (the product) and by the CPU
+oracle used in tests; :class:`Library` binds either one, given its path.
+Array arguments are numpy arrays with the record dtypes below, which match
+the C structs field for field (all int32, no padding).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+FP64 = 0
+FP32 = 1
+
+RUN_PLAIN = 0
+RUN_BATCHED = 1
+RUN_GRAPH = 2
+
+STATUS = {
+    0: "MAMR_OK",
+    -1: "MAMR_EINVAL",
+    -2: "MAMR_ENOMEM",
+    -3: "MAMR_ECUDA",
+    -4: "MAMR_EMESH",
+    -5: "MAMR_EUNSUP",
+    -6: "MAMR_EDEVICE",
+}
+
+# struct mamr_block
+BLOCK_DTYPE = np.dtype([
+    ("slot", "<i4"),
+    ("level", "<i4"),
+    ("nei_level", "<i4", (6,)),
+    ("nei", "<i4", (6, 2, 2)),
+])
+# struct mamr_split_job
+SPLIT_DTYPE = np.dtype([("parent", "<i4"), ("child", "<i4", (8,))])
+# struct mamr_consolidate_job
+CONSOLIDATE_DTYPE = np.dtype([("child", "<i4", (8,)), ("target", "<i4")])
+
+
+class MamrError(RuntimeError):
+    """A mamr_* call returned a negative status."""
+
+    def __init__(self, status: int, where: str, message: str):
+        self.status = status
+        super().__init__(f"{where}: {STATUS.get(status, status)}: {message}")
+
+
+class Config(C.Structure):
+    """struct mamr_config."""
+
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+        ("num_vars", C.c_int32), ("max_blocks", C.c_int32),
+        ("stencil", C.c_int32), ("code", C.c_int32), ("permute", C.c_int32),
+        ("dtype", C.c_int32), ("reserved", C.c_int32 * 7),
+    ]
+
+    @classmethod
+    def make(cls, nx, ny, nz, num_vars, max_blocks, stencil=7, dtype=FP64,
+             permute=0, code=0) -> "Config":
+        return cls(nx, ny, nz, num_vars, max_blocks, stencil, code, permute,
+                   dtype)
+
+
+_I32P = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_F64P = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+class Library:
+    """One loaded implementation of the ABI (GPU library or oracle)."""
+
+    def __init__(self, path: str):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.path = path
+        self.lib = C.CDLL(path)
+        L = self.lib
+        vp = C.c_void_p
+        i32 = C.c_int32
+        sig = {
+            "mamr_create": [C.POINTER(Config), C.POINTER(vp)],
+            "mamr_destroy": [vp],
+            "mamr_stream": [vp, C.POINTER(vp)],
+            "mamr_sync": [vp],
+            "mamr_upload_blocks": [vp, vp, i32, vp],
+            "mamr_download_blocks": [vp, vp, i32, vp],
+            "mamr_set_mesh": [vp, vp, i32],
+            "mamr_comm": [vp, i32, i32, i32],
+            "mamr_stencil": [vp, i32, i32],
+            "mamr_check_sum": [vp, i32, C.POINTER(C.c_double)],
+            "mamr_split": [vp, vp, i32],
+            "mamr_consolidate": [vp, vp, i32],
+            "mamr_run_timesteps": [vp, i32, i32, i32, i32, i32, vp,
+                                   C.POINTER(i32)],
+            "mamr_launch_count": [vp, C.POINTER(C.c_int64)],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        L.mamr_last_error.argtypes = []
+        L.mamr_last_error.restype = C.c_char_p
+        L.mamr_initial_values.argtypes = [C.POINTER(Config), i32, vp]
+        L.mamr_initial_values.restype = C.c_int
+
+    def check(self, status: int, where: str) -> None:
+        if status != 0:
+            msg = self.lib.mamr_last_error() or b""
+            raise MamrError(status, where, msg.decode(errors="replace"))
+
+    def context(self, cfg: Config) -> "Context":
+        return Context(self, cfg)
+
+    def initial_values(self, cfg: Config, n_blocks: int) -> np.ndarray:
+        """The reference's init() values for its first n_blocks blocks,
+        [n][num_vars][nx+2][ny+2][nz+2] (mamr_initial_values)."""
+        out = np.empty((n_blocks, cfg.num_vars, cfg.nx + 2, cfg.ny + 2,
+                        cfg.nz + 2), dtype=np.float64)
+        self.check(self.lib.mamr_initial_values(C.byref(cfg), n_blocks,
+                                                _ptr(out)),
+                   "mamr_initial_values")
+        return out
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """A mamr_ctx: one cell pool plus its mesh, driven call by call.
+
+    Method names follow the reference entry points each call replaces
+    (comm, stencil_driver, check_sum, split_blocks, consolidate_blocks).
+    """
+
+    def __init__(self, lib: Library, cfg: Config):
+        self.lib = lib
+        self.cfg = cfg
+        self.h = C.c_void_p()
+        lib.check(lib.lib.mamr_create(C.byref(cfg), C.byref(self.h)),
+                  "mamr_create")
+        self.shape = (cfg.num_vars, cfg.nx + 2, cfg.ny + 2, cfg.nz + 2)
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.lib.mamr_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _call(self, name, *args):
+        self.lib.check(getattr(self.lib.lib, name)(self.h, *args), name)
+
+    # ---- data ------------------------------------------------------------
+    def upload(self, slots, data: np.ndarray) -> None:
+        slots = np.ascontiguousarray(slots, dtype=np.int32)
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        if data.shape != (len(slots),) + self.shape:
+            raise ValueError(f"data shape {data.shape} != "
+                             f"{(len(slots),) + self.shape}")
+        self._call("mamr_upload_blocks", _ptr(slots), len(slots), _ptr(data))
+
+    def download(self, slots) -> np.ndarray:
+        slots = np.ascontiguousarray(slots, dtype=np.int32)
+        out = np.empty((len(slots),) + self.shape, dtype=np.float64)
+        self._call("mamr_download_blocks", _ptr(slots), len(slots), _ptr(out))
+        return out
+
+    def set_mesh(self, blocks: np.ndarray) -> None:
+        blocks = np.ascontiguousarray(blocks, dtype=BLOCK_DTYPE)
+        self._call("mamr_set_mesh", _ptr(blocks), len(blocks))
+
+    # ---- hot path --------------------------------------------------------
+    def comm(self, start: int, num_comm: int, stage: int) -> None:
+        self._call("mamr_comm", start, num_comm, stage)
+
+    def stencil_driver(self, var: int, calc_stage: int = 0) -> None:
+        self._call("mamr_stencil", var, calc_stage)
+
+    def check_sum(self, var: int) -> float:
+        out = C.c_double()
+        self._call("mamr_check_sum", var, C.byref(out))
+        return out.value
+
+    def split(self, jobs: np.ndarray) -> None:
+        jobs = np.ascontiguousarray(jobs, dtype=SPLIT_DTYPE)
+        self._call("mamr_split", _ptr(jobs), len(jobs))
+
+    def consolidate(self, jobs: np.ndarray) -> None:
+        jobs = np.ascontiguousarray(jobs, dtype=CONSOLIDATE_DTYPE)
+        self._call("mamr_consolidate", _ptr(jobs), len(jobs))
+
+    def run_timesteps(self, num_ts: int, stages_per_ts: int,
+                      checksum_freq: int, first_stage: int = 0,
+                      flags: int = RUN_PLAIN, want_sums: bool = True):
+        per_ts = sum(1 for st in range(stages_per_ts)
+                     if checksum_freq and st % checksum_freq == 0)
+        n = per_ts * num_ts
+        sums = np.zeros((max(n, 1), self.cfg.num_vars), dtype=np.float64)
+        cnt = C.c_int32()
+        self._call("mamr_run_timesteps", num_ts, stages_per_ts,
+                   checksum_freq, first_stage, flags,
+                   _ptr(sums) if want_sums else None, C.byref(cnt))
+        return sums[:cnt.value]
+
+    def sync(self) -> None:
+        self._call("mamr_sync")
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._call("mamr_stream", C.byref(s))
+        return s.value or 0
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._call("mamr_launch_count", C.byref(n))
+        return n.value

@@ -1,0 +1,737 @@
+// Host side of the GB300 library: the mamr_* C ABI (include/miniamr_gb300.h).
+//
+// A context owns one zero-filled cell pool on the current device, a CUDA
+// stream, the per-direction exchange task lists derived from the mesh, and
+// small device buffers for checksum results.  Every entry point validates
+// its arguments on the host, queues kernels on the context's stream and
+// returns a status; nothing here exits the process.
+#include <algorithm>
+#include <array>
+#include <new>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "mamr_internal.h"
+#include "batched.h"
+
+using namespace mamr;
+
+static thread_local char g_err[512];
+
+static int fail(int code, const char *fmt, ...)
+{
+   va_list ap;
+   va_start(ap, fmt);
+   vsnprintf(g_err, sizeof(g_err), fmt, ap);
+   va_end(ap);
+   return code;
+}
+
+extern "C" const char *mamr_last_error(void) { return g_err; }
+
+#define CUDA_TRY(x)                                                         \
+   do {                                                                     \
+      cudaError_t e_ = (x);                                                 \
+      if (e_ != cudaSuccess)                                                \
+         return fail(MAMR_ECUDA, "%s: %s", #x, cudaGetErrorString(e_));     \
+   } while (0)
+
+#define LAUNCH_TRY(ctx, x)                                                  \
+   do {                                                                     \
+      int n_ = (x);                                                         \
+      if (n_ < 0)                                                           \
+         return fail(MAMR_ECUDA, "launch %s: %s", #x,                      \
+                     cudaGetErrorString(cudaGetLastError()));               \
+      (ctx)->launches += n_;                                                \
+   } while (0)
+
+namespace {
+
+// Growable device buffer.
+struct DevBuf {
+   void *p = nullptr;
+   size_t cap = 0;
+   cudaError_t ensure(size_t bytes)
+   {
+      if (bytes <= cap)
+         return cudaSuccess;
+      if (p)
+         cudaFree(p);
+      p = nullptr;
+      cap = 0;
+      size_t want = bytes + bytes / 4 + 256;
+      cudaError_t e = cudaMalloc(&p, want);
+      if (e == cudaSuccess)
+         cap = want;
+      return e;
+   }
+   void release()
+   {
+      if (p)
+         cudaFree(p);
+      p = nullptr;
+      cap = 0;
+   }
+};
+
+const int kPerm[6][3] = { {0, 1, 2}, {1, 2, 0}, {2, 0, 1},
+                          {0, 2, 1}, {1, 0, 2}, {2, 1, 0} };
+
+}  // namespace
+
+struct mamr_ctx {
+   mamr_config cfg;
+   Geom g;
+   bool fp32;
+   int device;
+   cudaStream_t stream;
+   void *pool;             // current pool
+   size_t pool_bytes;
+   void *pool_alt;         // second pool for the batched ping-pong (lazy)
+   std::vector<mamr_block> mesh;
+   std::vector<int32_t> slot_pos;   // slot -> index in mesh or -1
+   DevBuf d_slots;                  // sorted slots
+   DevBuf d_tasks[3];
+   DirTasks tasks[3];
+   DevBuf d_partials, d_jobs, d_stage, d_stage_slots, d_sums;
+   unsigned long long *d_acc;       // 2 words: fixed-point accumulator
+   double *d_sum;                   // FP64 checksum result
+   unsigned *d_err;                 // device error word
+   void *h_pinned;                  // 64 bytes of pinned host memory
+   long long launches;
+   mamr::BatchedState *batched;
+};
+
+static size_t elem_size(const mamr_ctx *c) { return c->fp32 ? 4 : 8; }
+
+static int check_error_word(mamr_ctx *c)
+{
+   unsigned h = 0;
+   CUDA_TRY(cudaMemcpyAsync(&h, c->d_err, sizeof(h), cudaMemcpyDeviceToHost,
+                            c->stream));
+   CUDA_TRY(cudaStreamSynchronize(c->stream));
+   if (h) {
+      CUDA_TRY(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
+      if (h & ERR_FIXED_RANGE)
+         return fail(MAMR_EDEVICE, "a cell is outside the FP32 checksum's "
+                     "fixed-point range (|v| < 1024, finite)");
+      return fail(MAMR_EDEVICE, "device error word 0x%x", h);
+   }
+   return MAMR_OK;
+}
+
+extern "C" int mamr_create(const mamr_config *cfg, mamr_ctx **out)
+{
+   if (!cfg || !out)
+      return fail(MAMR_EINVAL, "null argument");
+   *out = nullptr;
+   if (cfg->nx < 2 || cfg->ny < 2 || cfg->nz < 2 || cfg->nx % 2 ||
+       cfg->ny % 2 || cfg->nz % 2)
+      return fail(MAMR_EINVAL, "block sizes must be even and >= 2");
+   if (cfg->num_vars < 1 || cfg->num_vars > 65535 || cfg->max_blocks < 1)
+      return fail(MAMR_EINVAL, "num_vars must be in 1..65535 and "
+                  "max_blocks >= 1");
+   if (cfg->stencil != 7 && cfg->stencil != 27)
+      return fail(MAMR_EUNSUP, "stencil %d not supported", cfg->stencil);
+   if (cfg->code != 0)
+      return fail(MAMR_EUNSUP, "code %d not supported", cfg->code);
+   if (cfg->dtype != MAMR_FP64 && cfg->dtype != MAMR_FP32)
+      return fail(MAMR_EINVAL, "bad dtype");
+   for (int r = 0; r < 7; r++)
+      if (cfg->reserved[r])
+         return fail(MAMR_EINVAL, "reserved fields must be zero");
+
+   mamr_ctx *c = new (std::nothrow) mamr_ctx();
+   if (!c)
+      return fail(MAMR_ENOMEM, "host allocation");
+   c->cfg = *cfg;
+   c->fp32 = cfg->dtype == MAMR_FP32;
+   Geom &g = c->g;
+   g.nx = cfg->nx; g.ny = cfg->ny; g.nz = cfg->nz; g.V = cfg->num_vars;
+   g.X = g.nx + 2; g.Y = g.ny + 2; g.Z = g.nz + 2;
+   const int eps = 32 / (int) elem_size(c);      // elements per sector
+   g.koff = eps - 1;
+   g.Zp = ((g.koff + g.Z + eps - 1) / eps) * eps;
+   g.bv = (long long) g.X * g.Y * g.Zp;
+   size_t tile = (size_t) g.X * g.Y * g.Z * elem_size(c);
+   if (tile > 200 * 1024) {
+      delete c;
+      return fail(MAMR_EUNSUP, "block of %zu bytes does not fit the on-chip "
+                  "stencil tile (200 KiB)", tile);
+   }
+   int dev = 0;
+   cudaError_t e = cudaGetDevice(&dev);
+   if (e == cudaSuccess)
+      e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+   c->device = dev;
+   c->pool_bytes = (size_t) cfg->max_blocks * g.V * g.bv * elem_size(c);
+   if (e == cudaSuccess)
+      e = cudaMalloc(&c->pool, c->pool_bytes);
+   if (e == cudaSuccess)
+      e = cudaMemsetAsync(c->pool, 0, c->pool_bytes, c->stream);
+   if (e == cudaSuccess)
+      e = cudaMalloc((void **) &c->d_acc, 64);
+   if (e == cudaSuccess)
+      e = cudaMalloc((void **) &c->d_sum, 64);
+   if (e == cudaSuccess)
+      e = cudaMalloc((void **) &c->d_err, 64);
+   if (e == cudaSuccess)
+      e = cudaMemsetAsync(c->d_err, 0, 64, c->stream);
+   if (e == cudaSuccess)
+      e = cudaMallocHost(&c->h_pinned, 64);
+   if (e == cudaSuccess)
+      e = cudaStreamSynchronize(c->stream);
+   if (e != cudaSuccess) {
+      int code = (e == cudaErrorMemoryAllocation) ? MAMR_ENOMEM : MAMR_ECUDA;
+      mamr_destroy(c);
+      cudaGetLastError();
+      return fail(code, "mamr_create: %s", cudaGetErrorString(e));
+   }
+   c->slot_pos.assign(cfg->max_blocks, -1);
+   *out = c;
+   return MAMR_OK;
+}
+
+extern "C" int mamr_destroy(mamr_ctx *c)
+{
+   if (!c)
+      return MAMR_OK;
+   if (c->stream)
+      cudaStreamSynchronize(c->stream);
+   mamr::batched_destroy(c->batched);
+   if (c->pool) cudaFree(c->pool);
+   if (c->pool_alt) cudaFree(c->pool_alt);
+   for (auto &b : c->d_tasks) b.release();
+   c->d_slots.release(); c->d_partials.release(); c->d_jobs.release();
+   c->d_stage.release(); c->d_stage_slots.release(); c->d_sums.release();
+   if (c->d_acc) cudaFree(c->d_acc);
+   if (c->d_sum) cudaFree(c->d_sum);
+   if (c->d_err) cudaFree(c->d_err);
+   if (c->h_pinned) cudaFreeHost(c->h_pinned);
+   if (c->stream) cudaStreamDestroy(c->stream);
+   delete c;
+   return MAMR_OK;
+}
+
+extern "C" int mamr_stream(mamr_ctx *c, void **stream)
+{
+   if (!c || !stream)
+      return fail(MAMR_EINVAL, "null argument");
+   *stream = (void *) c->stream;
+   return MAMR_OK;
+}
+
+extern "C" int mamr_sync(mamr_ctx *c)
+{
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   CUDA_TRY(cudaStreamSynchronize(c->stream));
+   return check_error_word(c);
+}
+
+extern "C" int mamr_launch_count(mamr_ctx *c, int64_t *count)
+{
+   if (!c || !count)
+      return fail(MAMR_EINVAL, "null argument");
+   *count = c->launches;
+   return MAMR_OK;
+}
+
+static bool slot_ok(const mamr_ctx *c, int32_t s)
+{
+   return s >= 0 && s < c->cfg.max_blocks;
+}
+
+// Host buffers move through a bounded device staging area.
+static const size_t kStageBytes = 256u << 20;
+
+static int transfer(mamr_ctx *c, const int32_t *slots, int32_t n,
+                    double *host, bool up)
+{
+   if (n < 0 || (n && (!slots || !host)))
+      return fail(MAMR_EINVAL, "bad transfer arguments");
+   for (int32_t b = 0; b < n; b++)
+      if (!slot_ok(c, slots[b]))
+         return fail(MAMR_EINVAL, "slot %d out of range", slots[b]);
+   const Geom &g = c->g;
+   const size_t per_block = (size_t) g.V * g.X * g.Y * g.Z;
+   int32_t chunk = (int32_t) std::max<size_t>(1, kStageBytes /
+                                              (per_block * sizeof(double)));
+   CUDA_TRY(c->d_stage.ensure(std::min<size_t>(n, chunk) * per_block *
+                              sizeof(double)));
+   CUDA_TRY(c->d_stage_slots.ensure(sizeof(int32_t) * std::max(1, chunk)));
+   for (int32_t b0 = 0; b0 < n; b0 += chunk) {
+      int32_t m = std::min(chunk, n - b0);
+      double *h = host + (size_t) b0 * per_block;
+      CUDA_TRY(cudaMemcpyAsync(c->d_stage_slots.p, slots + b0,
+                               sizeof(int32_t) * m, cudaMemcpyHostToDevice,
+                               c->stream));
+      if (up) {
+         CUDA_TRY(cudaMemcpyAsync(c->d_stage.p, h,
+                                  sizeof(double) * per_block * m,
+                                  cudaMemcpyHostToDevice, c->stream));
+         if (c->fp32)
+            LAUNCH_TRY(c, launch_upload((float *) c->pool, g,
+                                        (const int32_t *) c->d_stage_slots.p,
+                                        m, (const double *) c->d_stage.p,
+                                        c->stream));
+         else
+            LAUNCH_TRY(c, launch_upload((double *) c->pool, g,
+                                        (const int32_t *) c->d_stage_slots.p,
+                                        m, (const double *) c->d_stage.p,
+                                        c->stream));
+      } else {
+         if (c->fp32)
+            LAUNCH_TRY(c, launch_download((const float *) c->pool, g,
+                                          (const int32_t *) c->d_stage_slots.p,
+                                          m, (double *) c->d_stage.p,
+                                          c->stream));
+         else
+            LAUNCH_TRY(c, launch_download((const double *) c->pool, g,
+                                          (const int32_t *) c->d_stage_slots.p,
+                                          m, (double *) c->d_stage.p,
+                                          c->stream));
+         CUDA_TRY(cudaMemcpyAsync(h, c->d_stage.p,
+                                  sizeof(double) * per_block * m,
+                                  cudaMemcpyDeviceToHost, c->stream));
+      }
+      CUDA_TRY(cudaStreamSynchronize(c->stream));
+   }
+   return MAMR_OK;
+}
+
+extern "C" int mamr_upload_blocks(mamr_ctx *c, const int32_t *slots,
+                                  int32_t n, const double *host)
+{
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   return transfer(c, slots, n, const_cast<double *>(host), true);
+}
+
+extern "C" int mamr_download_blocks(mamr_ctx *c, const int32_t *slots,
+                                    int32_t n, double *host)
+{
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   return transfer(c, slots, n, host, false);
+}
+
+// ref/comm.c:162-203 turned into per-direction task lists: the same faces,
+// in the same pairing, that the reference's on-rank loop visits.
+extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
+                             int32_t n)
+{
+   if (!c || n < 0 || (n && !blocks))
+      return fail(MAMR_EINVAL, "bad mesh arguments");
+   if (n > c->cfg.max_blocks)
+      return fail(MAMR_EINVAL, "%d blocks exceed max_blocks", n);
+   std::vector<int32_t> pos(c->cfg.max_blocks, -1);
+   for (int32_t b = 0; b < n; b++) {
+      const mamr_block &bp = blocks[b];
+      if (!slot_ok(c, bp.slot))
+         return fail(MAMR_EINVAL, "block %d: slot %d out of range", b,
+                     bp.slot);
+      if (pos[bp.slot] >= 0)
+         return fail(MAMR_EINVAL, "slot %d listed twice", bp.slot);
+      pos[bp.slot] = b;
+      for (int l = 0; l < 6; l++) {
+         int nl = bp.nei_level[l];
+         if (nl == -2)
+            continue;
+         if (nl != bp.level && nl != bp.level + 1 && nl != bp.level - 1)
+            return fail(MAMR_EMESH, "misconnected block (slot %d face %d)",
+                        bp.slot, l);
+         for (int i = 0; i < 2; i++)
+            for (int j = 0; j < 2; j++)
+               if ((nl == bp.level + 1 || (i == 0 && j == 0)) &&
+                   !slot_ok(c, bp.nei[l][i][j]))
+                  return fail(MAMR_EMESH, "misconnected block (slot %d face "
+                              "%d nei %d)", bp.slot, l, bp.nei[l][i][j]);
+      }
+   }
+   std::vector<SameTask> same[3];
+   std::vector<DiffTask> diff[3];
+   std::vector<BcTask> bc[3];
+   for (int32_t in = 0; in < n; in++) {
+      const mamr_block &bp = blocks[in];
+      const int s = bp.slot;
+      for (int l = 0; l < 6; l++) {
+         const int dir = l / 2;
+         if (bp.nei_level[l] == bp.level) {
+            int m = bp.nei[l][0][0];
+            if (m > s) {
+               if (pos[m] < 0)
+                  return fail(MAMR_EMESH, "neighbour slot %d not active", m);
+               // l even: the neighbour is on the low side
+               same[dir].push_back(l % 2 == 0 ? SameTask{m, s}
+                                              : SameTask{s, m});
+            }
+         } else if (bp.nei_level[l] == bp.level + 1) {
+            for (int i = 0; i < 2; i++)
+               for (int j = 0; j < 2; j++) {
+                  int m = bp.nei[l][i][j];
+                  if (m > s) {
+                     if (pos[m] < 0)
+                        return fail(MAMR_EMESH,
+                                    "neighbour slot %d not active", m);
+                     diff[dir].push_back(DiffTask{s, m, l, i, j});
+                  }
+               }
+         } else if (bp.nei_level[l] == bp.level - 1) {
+            int m = bp.nei[l][0][0];
+            if (m > s) {
+               if (pos[m] < 0)
+                  return fail(MAMR_EMESH, "neighbour slot %d not active", m);
+               const mamr_block &mb = blocks[pos[m]];
+               int k = dir * 2 + 1 - l % 2;
+               for (int i = 0; i < 2; i++)
+                  for (int j = 0; j < 2; j++)
+                     if (mb.nei[k][i][j] == s)
+                        diff[dir].push_back(DiffTask{m, s, k, i, j});
+            }
+         } else if (bp.nei_level[l] == -2) {
+            bc[dir].push_back(BcTask{s, l});
+         }
+      }
+   }
+   // Upload: sorted slots, then per direction same | diff | bc.
+   std::vector<int32_t> sorted(n);
+   for (int32_t b = 0; b < n; b++)
+      sorted[b] = blocks[b].slot;
+   CUDA_TRY(c->d_slots.ensure(sizeof(int32_t) * std::max(1, n)));
+   if (n)
+      CUDA_TRY(cudaMemcpyAsync(c->d_slots.p, sorted.data(),
+                               sizeof(int32_t) * n, cudaMemcpyHostToDevice,
+                               c->stream));
+   for (int d = 0; d < 3; d++) {
+      size_t b_same = same[d].size() * sizeof(SameTask);
+      size_t b_diff = diff[d].size() * sizeof(DiffTask);
+      size_t b_bc = bc[d].size() * sizeof(BcTask);
+      size_t o_diff = (b_same + 15) & ~(size_t) 15;
+      size_t o_bc = (o_diff + b_diff + 15) & ~(size_t) 15;
+      std::vector<unsigned char> blob(o_bc + b_bc + 16);
+      memcpy(blob.data(), same[d].data(), b_same);
+      memcpy(blob.data() + o_diff, diff[d].data(), b_diff);
+      memcpy(blob.data() + o_bc, bc[d].data(), b_bc);
+      CUDA_TRY(c->d_tasks[d].ensure(blob.size()));
+      CUDA_TRY(cudaMemcpyAsync(c->d_tasks[d].p, blob.data(), blob.size(),
+                               cudaMemcpyHostToDevice, c->stream));
+      unsigned char *base = (unsigned char *) c->d_tasks[d].p;
+      c->tasks[d].same = (const SameTask *) base;
+      c->tasks[d].n_same = (int) same[d].size();
+      c->tasks[d].diff = (const DiffTask *) (base + o_diff);
+      c->tasks[d].n_diff = (int) diff[d].size();
+      c->tasks[d].bc = (const BcTask *) (base + o_bc);
+      c->tasks[d].n_bc = (int) bc[d].size();
+   }
+   CUDA_TRY(c->d_partials.ensure(sizeof(double) * std::max(1, n)));
+   CUDA_TRY(cudaStreamSynchronize(c->stream));
+   c->mesh.assign(blocks, blocks + n);
+   c->slot_pos.swap(pos);
+   mamr::batched_mesh_changed(c->batched);
+   return MAMR_OK;
+}
+
+static int comm_impl(mamr_ctx *c, int32_t start, int32_t num, int32_t stage)
+{
+   for (int o = 0; o < 3; o++) {
+      int dir = c->cfg.permute ? kPerm[((stage % 6) + 6) % 6][o] : o;
+      if (c->fp32)
+         LAUNCH_TRY(c, launch_comm_dir((float *) c->pool, c->g, dir,
+                                       c->cfg.stencil, c->tasks[dir], start,
+                                       num, c->stream));
+      else
+         LAUNCH_TRY(c, launch_comm_dir((double *) c->pool, c->g, dir,
+                                       c->cfg.stencil, c->tasks[dir], start,
+                                       num, c->stream));
+   }
+   return MAMR_OK;
+}
+
+extern "C" int mamr_comm(mamr_ctx *c, int32_t start, int32_t num,
+                         int32_t stage)
+{
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   if (start < 0 || num < 0 || start + num > c->cfg.num_vars)
+      return fail(MAMR_EINVAL, "variable range [%d, %d) out of bounds",
+                  start, start + num);
+   return comm_impl(c, start, num, stage);
+}
+
+static int stencil_impl(mamr_ctx *c, int32_t var)
+{
+   const int n = (int) c->mesh.size();
+   if (c->fp32)
+      LAUNCH_TRY(c, launch_stencil((float *) c->pool, c->g, c->cfg.stencil,
+                                   (const int32_t *) c->d_slots.p, n, var,
+                                   c->stream));
+   else
+      LAUNCH_TRY(c, launch_stencil((double *) c->pool, c->g, c->cfg.stencil,
+                                   (const int32_t *) c->d_slots.p, n, var,
+                                   c->stream));
+   return MAMR_OK;
+}
+
+extern "C" int mamr_stencil(mamr_ctx *c, int32_t var, int32_t calc_stage)
+{
+   (void) calc_stage;
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   if (var < 0 || var >= c->cfg.num_vars)
+      return fail(MAMR_EINVAL, "variable %d out of range", var);
+   return stencil_impl(c, var);
+}
+
+// Converts a 128-bit fixed-point accumulator (units of 2^-52) to double
+// with one correct rounding.
+static double fixed_to_double(unsigned long long lo, unsigned long long hi)
+{
+   __int128 v = (__int128) (((unsigned __int128) hi << 64) |
+                            (unsigned __int128) lo);
+   return (double) v * 0x1p-52;
+}
+
+// Queues the checksum of var; FP64 into *d_out, FP32 into acc[2].
+static int checksum_queue(mamr_ctx *c, int32_t var, double *d_out,
+                          unsigned long long *acc)
+{
+   const int n = (int) c->mesh.size();
+   if (c->fp32) {
+      CUDA_TRY(cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long),
+                               c->stream));
+      LAUNCH_TRY(c, launch_checksum_fp32((const float *) c->pool, c->g,
+                                         (const int32_t *) c->d_slots.p, n,
+                                         var, acc, c->d_err, c->stream));
+   } else {
+      LAUNCH_TRY(c, launch_checksum_fp64((const double *) c->pool, c->g,
+                                         (const int32_t *) c->d_slots.p, n,
+                                         var, (double *) c->d_partials.p,
+                                         d_out, c->stream));
+   }
+   return MAMR_OK;
+}
+
+extern "C" int mamr_check_sum(mamr_ctx *c, int32_t var, double *sum)
+{
+   if (!c || !sum)
+      return fail(MAMR_EINVAL, "null argument");
+   if (var < 0 || var >= c->cfg.num_vars)
+      return fail(MAMR_EINVAL, "variable %d out of range", var);
+   int r = checksum_queue(c, var, c->d_sum, c->d_acc);
+   if (r)
+      return r;
+   if (c->fp32) {
+      unsigned long long *h = (unsigned long long *) c->h_pinned;
+      CUDA_TRY(cudaMemcpyAsync(h, c->d_acc, 2 * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, c->stream));
+      if ((r = check_error_word(c)))
+         return r;
+      *sum = fixed_to_double(h[0], h[1]);
+   } else {
+      double *h = (double *) c->h_pinned;
+      CUDA_TRY(cudaMemcpyAsync(h, c->d_sum, sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
+      if ((r = check_error_word(c)))
+         return r;
+      *sum = *h;
+   }
+   return MAMR_OK;
+}
+
+// Orders data-movement jobs into waves so that jobs of one wave touch
+// disjoint slots except for shared reads: a job waits for every earlier job
+// that reads a slot it writes or writes a slot it reads or writes.  This
+// keeps the reference's sequential semantics, where a later child (split)
+// or target (consolidate) may land in a slot an earlier job just freed, and
+// a later consolidation may read an earlier one's target.
+template <int NR, int NW>
+static void schedule_waves(const std::vector<std::array<int32_t, NR>> &reads,
+                           const std::vector<std::array<int32_t, NW>> &writes,
+                           int max_slots, std::vector<int> &wave)
+{
+   std::vector<int> last_r(max_slots, -1), last_w(max_slots, -1);
+   const size_t n = reads.size();
+   wave.assign(n, 0);
+   for (size_t t = 0; t < n; t++) {
+      int w = 0;
+      for (int32_t s : reads[t])
+         w = std::max(w, last_w[s] + 1);
+      for (int32_t s : writes[t])
+         w = std::max(w, std::max(last_r[s], last_w[s]) + 1);
+      wave[t] = w;
+      for (int32_t s : reads[t])
+         last_r[s] = std::max(last_r[s], w);
+      for (int32_t s : writes[t])
+         last_w[s] = w;
+   }
+}
+
+template <typename Job, typename Launch>
+static int run_waves(mamr_ctx *c, const Job *jobs, const std::vector<int> &wave,
+                     Launch launch)
+{
+   const size_t n = wave.size();
+   int n_waves = 0;
+   for (int w : wave)
+      n_waves = std::max(n_waves, w + 1);
+   std::vector<Job> ordered;
+   ordered.reserve(n);
+   std::vector<size_t> start(n_waves + 1, 0);
+   for (int w = 0; w < n_waves; w++) {
+      start[w] = ordered.size();
+      for (size_t t = 0; t < n; t++)
+         if (wave[t] == w)
+            ordered.push_back(jobs[t]);
+   }
+   start[n_waves] = ordered.size();
+   CUDA_TRY(c->d_jobs.ensure(sizeof(Job) * std::max<size_t>(1, n)));
+   CUDA_TRY(cudaMemcpyAsync(c->d_jobs.p, ordered.data(), sizeof(Job) * n,
+                            cudaMemcpyHostToDevice, c->stream));
+   for (int w = 0; w < n_waves; w++) {
+      const Job *dj = (const Job *) c->d_jobs.p + start[w];
+      LAUNCH_TRY(c, launch(dj, (int) (start[w + 1] - start[w])));
+   }
+   CUDA_TRY(cudaStreamSynchronize(c->stream));
+   return MAMR_OK;
+}
+
+extern "C" int mamr_split(mamr_ctx *c, const mamr_split_job *jobs, int32_t n)
+{
+   if (!c || n < 0 || (n && !jobs))
+      return fail(MAMR_EINVAL, "bad split arguments");
+   std::vector<std::array<int32_t, 1>> rd(n);
+   std::vector<std::array<int32_t, 8>> wr(n);
+   for (int32_t t = 0; t < n; t++) {
+      if (!slot_ok(c, jobs[t].parent))
+         return fail(MAMR_EINVAL, "split parent slot %d out of range",
+                     jobs[t].parent);
+      rd[t][0] = jobs[t].parent;
+      for (int o = 0; o < 8; o++) {
+         if (!slot_ok(c, jobs[t].child[o]))
+            return fail(MAMR_EINVAL, "split child slot %d out of range",
+                        jobs[t].child[o]);
+         wr[t][o] = jobs[t].child[o];
+      }
+   }
+   if (n == 0)
+      return MAMR_OK;
+   std::vector<int> wave;
+   schedule_waves<1, 8>(rd, wr, c->cfg.max_blocks, wave);
+   return run_waves(c, jobs, wave, [&](const mamr_split_job *dj, int m) {
+      return c->fp32 ? launch_split((float *) c->pool, c->g, dj, m, c->stream)
+                     : launch_split((double *) c->pool, c->g, dj, m,
+                                    c->stream);
+   });
+}
+
+extern "C" int mamr_consolidate(mamr_ctx *c, const mamr_consolidate_job *jobs,
+                                int32_t n)
+{
+   if (!c || n < 0 || (n && !jobs))
+      return fail(MAMR_EINVAL, "bad consolidate arguments");
+   std::vector<std::array<int32_t, 8>> rd(n);
+   std::vector<std::array<int32_t, 1>> wr(n);
+   for (int32_t t = 0; t < n; t++) {
+      if (!slot_ok(c, jobs[t].target))
+         return fail(MAMR_EINVAL, "consolidate target slot %d out of range",
+                     jobs[t].target);
+      wr[t][0] = jobs[t].target;
+      for (int o = 0; o < 8; o++) {
+         if (!slot_ok(c, jobs[t].child[o]))
+            return fail(MAMR_EINVAL, "consolidate child slot %d out of range",
+                        jobs[t].child[o]);
+         rd[t][o] = jobs[t].child[o];
+      }
+   }
+   if (n == 0)
+      return MAMR_OK;
+   std::vector<int> wave;
+   schedule_waves<8, 1>(rd, wr, c->cfg.max_blocks, wave);
+   return run_waves(c, jobs, wave, [&](const mamr_consolidate_job *dj, int m) {
+      return c->fp32 ? launch_consolidate((float *) c->pool, c->g, dj, m,
+                                          c->stream)
+                     : launch_consolidate((double *) c->pool, c->g, dj, m,
+                                          c->stream);
+   });
+}
+
+// Plain stage loop: the driver's call sequence queued without host syncs;
+// checksums land in a device array and come back once at the end.
+static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
+                     int32_t first_stage, double *sums, int32_t *n_sums)
+{
+   const int V = c->cfg.num_vars;
+   int per_ts = 0;
+   if (freq)
+      for (int st = 0; st < spt; st++)
+         per_ts += !(st % freq);
+   const size_t n_cs = (size_t) per_ts * num_ts;
+   const size_t slot_bytes = c->fp32 ? 2 * sizeof(unsigned long long)
+                                     : sizeof(double);
+   CUDA_TRY(c->d_sums.ensure(std::max<size_t>(1, n_cs * V) * slot_bytes));
+   int cnt = 0, gstage = first_stage, r;
+   for (int ts = 0; ts < num_ts; ts++)
+      for (int st = 0; st < spt; st++, gstage++) {
+         const bool do_cs = freq && !(st % freq);
+         if ((r = comm_impl(c, 0, V, gstage)))
+            return r;
+         for (int var = 0; var < V; var++) {
+            if ((r = stencil_impl(c, var)))
+               return r;
+            if (do_cs) {
+               size_t idx = (size_t) cnt * V + var;
+               if (c->fp32)
+                  r = checksum_queue(c, var, nullptr,
+                                     (unsigned long long *) c->d_sums.p +
+                                        2 * idx);
+               else
+                  r = checksum_queue(c, var, (double *) c->d_sums.p + idx,
+                                     nullptr);
+               if (r)
+                  return r;
+            }
+         }
+         if (do_cs)
+            cnt++;
+      }
+   if ((r = mamr_sync(c)))
+      return r;
+   if (sums && cnt) {
+      if (c->fp32) {
+         std::vector<unsigned long long> h((size_t) cnt * V * 2);
+         CUDA_TRY(cudaMemcpy(h.data(), c->d_sums.p, h.size() * 8,
+                             cudaMemcpyDeviceToHost));
+         for (size_t q = 0; q < (size_t) cnt * V; q++)
+            sums[q] = fixed_to_double(h[2 * q], h[2 * q + 1]);
+      } else {
+         CUDA_TRY(cudaMemcpy(sums, c->d_sums.p, sizeof(double) * cnt * V,
+                             cudaMemcpyDeviceToHost));
+      }
+   }
+   if (n_sums)
+      *n_sums = cnt;
+   return MAMR_OK;
+}
+
+extern "C" int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts,
+                                  int32_t stages_per_ts,
+                                  int32_t checksum_freq, int32_t first_stage,
+                                  int32_t flags, double *sums,
+                                  int32_t *n_sums)
+{
+   if (!c || num_ts < 0 || stages_per_ts < 1 || checksum_freq < 0)
+      return fail(MAMR_EINVAL, "bad run arguments");
+   if (flags & ~(MAMR_RUN_BATCHED | MAMR_RUN_GRAPH))
+      return fail(MAMR_EINVAL, "unknown run flags 0x%x", flags);
+   if (!(flags & MAMR_RUN_BATCHED)) {
+      if (flags & MAMR_RUN_GRAPH)
+         return fail(MAMR_EINVAL, "MAMR_RUN_GRAPH needs MAMR_RUN_BATCHED");
+      return run_plain(c, num_ts, stages_per_ts, checksum_freq, first_stage,
+                       sums, n_sums);
+   }
+   return fail(MAMR_EUNSUP, "batched path not available");
+}

@@ -1,0 +1,176 @@
+// Arithmetic building blocks shared by the plain and batched kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace mamr {
+
+// ---- correctly rounded division by the stencil constants -----------------
+//
+// FP64: x / 7 and x / 27 as the reference computes them (IEEE division,
+// round to nearest), in three FP64 operations instead of a full divide.
+// Method: Markstein (1990), correction of a quotient by its exact
+// remainder.  With y = RN(1/c): q0 = RN(x*y); r = fma(-q0, c, x), exact
+// whenever q0 is a faithful rounding of x/c; then RN(q0 + r*y) = RN(x/c)
+// (Markstein's theorem; Muller et al., Handbook of Floating-Point
+// Arithmetic, section on division with a known reciprocal).  q0 is faithful
+// here because |y*c - 1| = 2^-54 for both constants (checked with exact
+// rational arithmetic), so |x*y - x/c| < ulp(x/c)/2.  The argument needs x,
+// q0 and r away from underflow and overflow, so x outside biased exponents
+// (100, 2000) -- zero, tiny, huge, inf, nan -- takes the IEEE division.
+// tests/test_gpu_arith.py compares against IEEE division on the GPU.
+template <int C>
+__device__ __forceinline__ double div_const(double x);
+
+template <>
+__device__ __forceinline__ double div_const<7>(double x)
+{
+   const double y = 0x1.2492492492492p-3;   // RN(1/7)
+   const int e = (__double2hiint(x) >> 20) & 0x7ff;
+   if (e > 100 && e < 2000) {
+      double q0 = __dmul_rn(x, y);
+      double r = __fma_rn(-q0, 7.0, x);
+      return __fma_rn(r, y, q0);
+   }
+   return __ddiv_rn(x, 7.0);
+}
+
+template <>
+__device__ __forceinline__ double div_const<27>(double x)
+{
+   const double y = 0x1.2f684bda12f68p-5;   // RN(1/27)
+   const int e = (__double2hiint(x) >> 20) & 0x7ff;
+   if (e > 100 && e < 2000) {
+      double q0 = __dmul_rn(x, y);
+      double r = __fma_rn(-q0, 27.0, x);
+      return __fma_rn(r, y, q0);
+   }
+   return __ddiv_rn(x, 27.0);
+}
+
+__device__ __forceinline__ double div7(double x) { return div_const<7>(x); }
+__device__ __forceinline__ double div27(double x) { return div_const<27>(x); }
+// FP32: RN(1/7f) misses the faithfulness bound above (|y*7 - 1| =
+// 1.5 * 2^-25), so FP32 keeps the IEEE division (cheap on the FP32 pipes).
+__device__ __forceinline__ float div7(float x) { return __fdiv_rn(x, 7.0f); }
+__device__ __forceinline__ float div27(float x) { return __fdiv_rn(x, 27.0f); }
+
+// Exact scalings: x/4 and x/8 equal x*0.25 and x*0.125 in IEEE arithmetic.
+__device__ __forceinline__ double quarter(double x) { return x * 0.25; }
+__device__ __forceinline__ float quarter(float x) { return x * 0.25f; }
+__device__ __forceinline__ double eighth(double x) { return x * 0.125; }
+__device__ __forceinline__ float eighth(float x) { return x * 0.125f; }
+
+// ---- coarsening sum of 8 children ----------------------------------------
+// FP64: left to right, as ref/block.c:419-426.
+__device__ __forceinline__ double sum8(const double *t)
+{
+   double s = t[0] + t[1];
+   s = s + t[2];
+   s = s + t[3];
+   s = s + t[4];
+   s = s + t[5];
+   s = s + t[6];
+   s = s + t[7];
+   return s;
+}
+
+// FP32 pools: Neumaier-compensated FP64 sum in the same term order, rounded
+// once to FP32.
+__device__ __forceinline__ float sum8(const float *t)
+{
+   double s = (double) t[0], comp = 0.0;
+#pragma unroll
+   for (int q = 1; q < 8; q++) {
+      double v = (double) t[q];
+      double u = s + v;
+      if (fabs(s) >= fabs(v))
+         comp = comp + ((s - u) + v);
+      else
+         comp = comp + ((v - u) + s);
+      s = u;
+   }
+   return (float) (s + comp);
+}
+
+// ---- exact fixed-point checksum of FP32 cells ------------------------------
+// A cell v becomes trunc(v * 2^52) (toward zero), using integer operations
+// only.  Returns false (and q = 0) for |v| >= 2^10, inf or nan.
+__device__ __forceinline__ bool fixed52(float v, long long &q)
+{
+   const unsigned u = __float_as_uint(v);
+   const unsigned e = (u >> 23) & 0xffu;
+   if (e >= 137u) {            // |v| >= 1024, inf, nan
+      q = 0;
+      return false;
+   }
+   unsigned long long m = u & 0x7fffffu;
+   int sh;
+   if (e == 0)
+      sh = -149 + 52;          // subnormal: v = m * 2^-149
+   else {
+      m |= 0x800000u;
+      sh = (int) e - 150 + 52; // v = m * 2^(e-150)
+   }
+   unsigned long long mag = sh >= 0 ? (m << sh)
+                                    : (sh > -64 ? (m >> (-sh)) : 0ull);
+   q = (u >> 31) ? -(long long) mag : (long long) mag;
+   return true;
+}
+
+// 128-bit two's complement accumulator held as (lo, hi).
+__device__ __forceinline__ void acc128_add(unsigned long long &lo,
+                                           unsigned long long &hi,
+                                           long long q)
+{
+   unsigned long long x = (unsigned long long) q;
+   unsigned long long n = lo + x;
+   hi += (n < lo ? 1ull : 0ull) + (q < 0 ? ~0ull : 0ull);
+   lo = n;
+}
+
+__device__ __forceinline__ void acc128_merge(unsigned long long &lo,
+                                             unsigned long long &hi,
+                                             unsigned long long lo2,
+                                             unsigned long long hi2)
+{
+   unsigned long long n = lo + lo2;
+   hi = hi + hi2 + (n < lo ? 1ull : 0ull);
+   lo = n;
+}
+
+// Adds the CTA's accumulators into the global 128-bit acc[0..1].  Two
+// atomics per CTA: the low word, then the high word plus the carry the low
+// add produced.  The carries and the high words add up to the exact 128-bit
+// total whatever order the CTAs arrive in.  blockDim.x must be a multiple
+// of 32 and at most 1024.
+__device__ __forceinline__ void block_acc128_flush(unsigned long long lo,
+                                                   unsigned long long hi,
+                                                   unsigned long long *acc)
+{
+   __shared__ unsigned long long s_lo[32], s_hi[32];
+#pragma unroll
+   for (int off = 16; off; off >>= 1) {
+      unsigned long long l2 = __shfl_down_sync(0xffffffffu, lo, off);
+      unsigned long long h2 = __shfl_down_sync(0xffffffffu, hi, off);
+      acc128_merge(lo, hi, l2, h2);
+   }
+   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   if (lane == 0) {
+      s_lo[w] = lo;
+      s_hi[w] = hi;
+   }
+   __syncthreads();
+   if (threadIdx.x == 0) {
+      unsigned long long L = 0, H = 0;
+      for (int q = 0; q < (int) (blockDim.x >> 5); q++)
+         acc128_merge(L, H, s_lo[q], s_hi[q]);
+      unsigned long long old = atomicAdd(acc, L);
+      unsigned long long hadd = H + ((old + L < old) ? 1ull : 0ull);
+      if (hadd)
+         atomicAdd(acc + 1, hadd);
+   }
+   __syncthreads();
+}
+
+}  // namespace mamr

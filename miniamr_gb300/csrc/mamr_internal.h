@@ -1,0 +1,89 @@
+// Internal declarations shared by the host side (api.cu) and the kernels
+// (plain_kernels.cu, batched_kernels.cu) of the GB300 library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+
+#include "miniamr_gb300.h"
+
+namespace mamr {
+
+// Pool geometry.  One block-variable is X*Y rows of Zp elements; cell
+// (i, j, k), 0 <= i < X etc., sits at row i*Y + j, column koff + k.  koff
+// puts k = 1 on a 32-byte sector boundary so that every interior row
+// (k = 1..nz) starts a sector, and Zp keeps that true for every row.
+struct Geom {
+   int nx, ny, nz, V;
+   int X, Y, Z;       // nx+2, ny+2, nz+2
+   int Zp, koff;      // padded row length, column of k = 0
+   long long bv;      // elements per block-variable: X*Y*Zp
+};
+
+__host__ __device__ inline long long bv_offset(const Geom &g, int slot,
+                                               int var)
+{
+   return ((long long) slot * g.V + var) * g.bv;
+}
+
+__host__ __device__ inline long long cell_offset(const Geom &g, int i, int j,
+                                                 int k)
+{
+   return ((long long) i * g.Y + j) * g.Zp + g.koff + k;
+}
+
+// Same-level exchange across one face: lo is the block on the low side
+// (west / south / down), hi the one on the high side.
+struct SameTask { int32_t lo, hi; };
+// Coarse/fine exchange: face l of the coarse block, quarter (iq, jq) of it.
+struct DiffTask { int32_t coarse, fine, l, iq, jq; };
+// Reflective boundary on face l of a block.
+struct BcTask { int32_t slot, l; };
+
+struct DirTasks {
+   const SameTask *same; int n_same;
+   const DiffTask *diff; int n_diff;
+   const BcTask *bc; int n_bc;
+};
+
+// Error word bits written by kernels (context error word).
+enum : unsigned {
+   ERR_FIXED_RANGE = 1u,   // a cell outside the fixed-point checksum range
+   ERR_TASK = 2u           // a task that does not fit the geometry
+};
+
+// Kernel launchers (plain path).  All return the launch count they issued
+// (>= 0) or -1 after a launch error (cudaGetLastError is left set).
+template <typename T>
+int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil,
+                    const DirTasks &t, int var0, int nvar, cudaStream_t s);
+template <typename T>
+int launch_stencil(T *pool, const Geom &g, int stencil, const int32_t *slots,
+                   int n, int var, cudaStream_t s);
+// FP64: serial per-block sums in exact reference order, then a serial sum
+// over blocks; result in *d_out.
+int launch_checksum_fp64(const double *pool, const Geom &g,
+                         const int32_t *slots, int n, int var,
+                         double *d_partials, double *d_out, cudaStream_t s);
+// FP32: exact 128-bit fixed-point accumulation into acc[2] (lo, hi),
+// which must be zeroed first.
+int launch_checksum_fp32(const float *pool, const Geom &g,
+                         const int32_t *slots, int n, int var,
+                         unsigned long long *acc, unsigned *err,
+                         cudaStream_t s);
+template <typename T>
+int launch_split(T *pool, const Geom &g, const mamr_split_job *jobs, int n,
+                 cudaStream_t s);
+template <typename T>
+int launch_consolidate(T *pool, const Geom &g,
+                       const mamr_consolidate_job *jobs, int n,
+                       cudaStream_t s);
+template <typename T>
+int launch_upload(T *pool, const Geom &g, const int32_t *slots, int n,
+                  const double *dense, cudaStream_t s);
+template <typename T>
+int launch_download(const T *pool, const Geom &g, const int32_t *slots,
+                    int n, double *dense, cudaStream_t s);
+
+}  // namespace mamr

@@ -1,0 +1,441 @@
+// Plain-path kernels: the reference's call sequence, one launch per call,
+// every cell bit-identical to the reference in FP64 (compiled with
+// -fmad=false; sums in the reference's order; divisions correctly rounded).
+#include "mamr_internal.h"
+#include "arith.cuh"
+
+namespace mamr {
+
+// (normal coordinate nc, tangential a, b) -> (i, j, k) for a face normal to
+// dir.  a/b are (j, k) for x faces, (i, k) for y faces, (i, j) for z faces,
+// the loop order of ref/comm.c:1473-1534.
+__device__ __forceinline__ long long face_cell(const Geom &g, int dir, int nc,
+                                               int a, int b)
+{
+   if (dir == 0) return cell_offset(g, nc, a, b);
+   if (dir == 1) return cell_offset(g, a, nc, b);
+   return cell_offset(g, a, b, nc);
+}
+
+// One CTA per (task, variable).  Tasks of one direction are independent:
+// each ghost cell is written by exactly one task and every read is of a
+// plane that this direction does not write (ref/comm.c:162-203).
+template <typename T>
+__global__ void __launch_bounds__(128)
+comm_dir_kernel(T *__restrict__ pool, Geom g, int dir, int stencil,
+                DirTasks t, int var0)
+{
+   int task = blockIdx.x, var = var0 + blockIdx.y;
+   const int n = dir == 0 ? g.nx : (dir == 1 ? g.ny : g.nz);
+   const int na = dir == 0 ? g.ny : g.nx;
+   const int nb = dir == 2 ? g.ny : g.nz;
+
+   if (task < t.n_same) {
+      // ref/comm.c:1473-1534 (code 0)
+      SameTask st = t.same[task];
+      T *lo = pool + bv_offset(g, st.lo, var);
+      T *hi = pool + bv_offset(g, st.hi, var);
+      int a0 = 1, a1 = na, b0 = 1, b1 = nb;
+      if (stencil != 7) {
+         if (dir >= 1) { a0 = 0; a1 = na + 1; }
+         if (dir == 2) { b0 = 0; b1 = nb + 1; }
+      }
+      const int cb = b1 - b0 + 1, cnt = (a1 - a0 + 1) * cb;
+      for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+         int a = a0 + e / cb, b = b0 + e % cb;
+         lo[face_cell(g, dir, n + 1, a, b)] = hi[face_cell(g, dir, 1, a, b)];
+         hi[face_cell(g, dir, 0, a, b)] = lo[face_cell(g, dir, n, a, b)];
+      }
+      return;
+   }
+   task -= t.n_same;
+   if (task < t.n_diff) {
+      // ref/comm.c:1597-1688 (code 0)
+      DiffTask dt = t.diff[task];
+      T *C = pool + bv_offset(g, dt.coarse, var);
+      T *F = pool + bv_offset(g, dt.fine, var);
+      const bool low = (dt.l % 2) == 0;
+      const int c0 = low ? 0 : n + 1, c1 = low ? 1 : n;
+      const int f2 = low ? n + 1 : 0, f3 = low ? n : 1;
+      const int ha = na / 2, hb = nb / 2;
+      const int oa = dt.jq * ha, ob = dt.iq * hb;
+      for (int e = threadIdx.x; e < ha * hb; e += blockDim.x) {
+         int a = 1 + e / hb, b = 1 + e % hb;
+         T q = quarter(C[face_cell(g, dir, c1, a + oa, b + ob)]);
+         F[face_cell(g, dir, f2, 2*a - 1, 2*b - 1)] = q;
+         F[face_cell(g, dir, f2, 2*a - 1, 2*b)] = q;
+         F[face_cell(g, dir, f2, 2*a, 2*b - 1)] = q;
+         F[face_cell(g, dir, f2, 2*a, 2*b)] = q;
+         T s = F[face_cell(g, dir, f3, 2*a - 1, 2*b - 1)] +
+               F[face_cell(g, dir, f3, 2*a - 1, 2*b)];
+         s = s + F[face_cell(g, dir, f3, 2*a, 2*b - 1)];
+         s = s + F[face_cell(g, dir, f3, 2*a, 2*b)];
+         C[face_cell(g, dir, c0, a + oa, b + ob)] = s;
+      }
+      return;
+   }
+   task -= t.n_diff;
+   if (task < t.n_bc) {
+      // ref/comm.c:1911-1965
+      BcTask bt = t.bc[task];
+      T *B = pool + bv_offset(g, bt.slot, var);
+      const bool hiside = (bt.l % 2) == 1;
+      const int tp = hiside ? n + 1 : 0, fp = hiside ? n : 1;
+      const bool full = stencil != 7;
+      const int a0 = full ? 0 : 1, a1 = full ? na + 1 : na;
+      const int b0 = full ? 0 : 1, b1 = full ? nb + 1 : nb;
+      const int cb = b1 - b0 + 1, cnt = (a1 - a0 + 1) * cb;
+      for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+         int a = a0 + e / cb, b = b0 + e % cb;
+         B[face_cell(g, dir, tp, a, b)] = B[face_cell(g, dir, fp, a, b)];
+      }
+   }
+}
+
+template <typename T>
+int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil,
+                    const DirTasks &t, int var0, int nvar, cudaStream_t s)
+{
+   int n = t.n_same + t.n_diff + t.n_bc;
+   if (n == 0 || nvar == 0)
+      return 0;
+   comm_dir_kernel<T><<<dim3(n, nvar), 128, 0, s>>>(pool, g, dir, stencil, t,
+                                                    var0);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+// ---------------------------------------------------------------------------
+// Stencil: one CTA per active block, the whole block-variable (ghosts
+// included) staged in shared memory, each thread sweeping one (j, k) column
+// along i.  Results are written straight back to the pool: every read comes
+// from the staged copy, so the in-place update is the reference's
+// work-array Jacobi update (ref/stencil.c:82-99, 103-141).
+template <typename T, int ST>
+__global__ void __launch_bounds__(256)
+stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
+               int var)
+{
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   T *tile = reinterpret_cast<T *>(smem_raw);
+   const int X = g.X, Y = g.Y, Z = g.Z;
+   T *base = pool + bv_offset(g, slots[blockIdx.x], var);
+   for (int e = threadIdx.x; e < X * Y * Z; e += blockDim.x) {
+      int row = e / Z, k = e - row * Z;
+      tile[e] = base[(long long) row * g.Zp + g.koff + k];
+   }
+   __syncthreads();
+#define TL(i, j, k) tile[((i) * Y + (j)) * Z + (k)]
+   for (int col = threadIdx.x; col < g.ny * g.nz; col += blockDim.x) {
+      const int j = col / g.nz + 1, k = col % g.nz + 1;
+      if (ST == 7) {
+         for (int i = 1; i <= g.nx; i++) {
+            T w = TL(i - 1, j, k) + TL(i, j - 1, k);
+            w = w + TL(i, j, k - 1);
+            w = w + TL(i, j, k);
+            w = w + TL(i, j, k + 1);
+            w = w + TL(i, j + 1, k);
+            w = w + TL(i + 1, j, k);
+            base[cell_offset(g, i, j, k)] = div7(w);
+         }
+      } else {
+         // S(p) = the 9-point left-to-right sum on plane p around (j, k):
+         // sb, sm and sf of cell i are S(i-1), S(i), S(i+1), so each S is
+         // formed once and reused by three cells -- same operations, same
+         // order, a third of the adds.
+         auto S = [&](int p) -> T {
+            T s = TL(p, j - 1, k - 1) + TL(p, j - 1, k);
+            s = s + TL(p, j - 1, k + 1);
+            s = s + TL(p, j, k - 1);
+            s = s + TL(p, j, k);
+            s = s + TL(p, j, k + 1);
+            s = s + TL(p, j + 1, k - 1);
+            s = s + TL(p, j + 1, k);
+            s = s + TL(p, j + 1, k + 1);
+            return s;
+         };
+         T s0 = S(0), s1 = S(1);
+         for (int i = 1; i <= g.nx; i++) {
+            T s2 = S(i + 1);
+            base[cell_offset(g, i, j, k)] = div27((s0 + s1) + s2);
+            s0 = s1;
+            s1 = s2;
+         }
+      }
+   }
+#undef TL
+}
+
+template <typename T>
+int launch_stencil(T *pool, const Geom &g, int stencil, const int32_t *slots,
+                   int n, int var, cudaStream_t s)
+{
+   if (n == 0)
+      return 0;
+   size_t smem = (size_t) g.X * g.Y * g.Z * sizeof(T);
+   int threads = g.ny * g.nz;
+   threads = threads > 256 ? 256 : ((threads + 31) / 32) * 32;
+   if (stencil == 7) {
+      cudaFuncSetAttribute(stencil_kernel<T, 7>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int) smem);
+      stencil_kernel<T, 7><<<n, threads, smem, s>>>(pool, g, slots, var);
+   } else {
+      cudaFuncSetAttribute(stencil_kernel<T, 27>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int) smem);
+      stencil_kernel<T, 27><<<n, threads, smem, s>>>(pool, g, slots, var);
+   }
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+// ---------------------------------------------------------------------------
+// Checksum, FP64: ref/check_sum.c:44-53 in exactly its order -- each block's
+// interior summed serially with k fastest, then the block sums serially in
+// sorted_list order.  One thread per block for the first pass.
+__global__ void __launch_bounds__(128)
+block_sums_fp64(const double *__restrict__ pool, Geom g,
+                const int32_t *__restrict__ slots, int n, int var,
+                double *__restrict__ partials)
+{
+   int b = blockIdx.x * blockDim.x + threadIdx.x;
+   if (b >= n)
+      return;
+   const double *base = pool + bv_offset(g, slots[b], var);
+   double s = 0.0;
+   for (int i = 1; i <= g.nx; i++)
+      for (int j = 1; j <= g.ny; j++) {
+         const double *row = base + cell_offset(g, i, j, 1);
+#pragma unroll 8
+         for (int k = 0; k < g.nz; k++)
+            s = s + row[k];
+      }
+   partials[b] = s;
+}
+
+__global__ void __launch_bounds__(256)
+total_sum_fp64(const double *__restrict__ partials, int n,
+               double *__restrict__ out)
+{
+   __shared__ double buf[2048];
+   double s = 0.0;
+   for (int base = 0; base < n; base += 2048) {
+      int m = n - base < 2048 ? n - base : 2048;
+      for (int e = threadIdx.x; e < m; e += blockDim.x)
+         buf[e] = partials[base + e];
+      __syncthreads();
+      if (threadIdx.x == 0)
+         for (int e = 0; e < m; e++)
+            s = s + buf[e];
+      __syncthreads();
+   }
+   if (threadIdx.x == 0)
+      *out = s;
+}
+
+int launch_checksum_fp64(const double *pool, const Geom &g,
+                         const int32_t *slots, int n, int var,
+                         double *d_partials, double *d_out, cudaStream_t s)
+{
+   int launches = 0;
+   if (n > 0) {
+      block_sums_fp64<<<(n + 127) / 128, 128, 0, s>>>(pool, g, slots, n, var,
+                                                       d_partials);
+      launches++;
+   }
+   total_sum_fp64<<<1, 256, 0, s>>>(d_partials, n, d_out);
+   launches++;
+   return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
+}
+
+// Checksum, FP32: every interior cell as a multiple of 2^-52 (truncated
+// toward zero), summed exactly in 128-bit two's complement.  Integer
+// addition is associative, so the result does not depend on the order in
+// which CTAs finish.
+__global__ void __launch_bounds__(256)
+checksum_fp32_kernel(const float *__restrict__ pool, Geom g,
+                     const int32_t *__restrict__ slots, int var,
+                     unsigned long long *__restrict__ acc,
+                     unsigned *__restrict__ err)
+{
+   const float *base = pool + bv_offset(g, slots[blockIdx.x], var);
+   unsigned long long lo = 0, hi = 0;
+   bool ok = true;
+   const int cells = g.nx * g.ny * g.nz;
+   for (int e = threadIdx.x; e < cells; e += blockDim.x) {
+      int i = e / (g.ny * g.nz) + 1, r = e % (g.ny * g.nz);
+      int j = r / g.nz + 1, k = r % g.nz + 1;
+      long long q;
+      ok &= fixed52(base[cell_offset(g, i, j, k)], q);
+      acc128_add(lo, hi, q);
+   }
+   if (!ok)
+      atomicOr(err, ERR_FIXED_RANGE);
+   block_acc128_flush(lo, hi, acc);
+}
+
+int launch_checksum_fp32(const float *pool, const Geom &g,
+                         const int32_t *slots, int n, int var,
+                         unsigned long long *acc, unsigned *err,
+                         cudaStream_t s)
+{
+   if (n == 0)
+      return 0;
+   checksum_fp32_kernel<<<n, 256, 0, s>>>(pool, g, slots, var, acc, err);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+// ---------------------------------------------------------------------------
+// split_blocks() data (ref/block.c:158-173): one CTA per (job, octant,
+// variable).  A child cell (ci, cj, ck) takes parent cell
+// ((ci+1)/2 + i1, ...) / 8 -- exact in binary floating point.
+template <typename T>
+__global__ void __launch_bounds__(256)
+split_kernel(T *__restrict__ pool, Geom g,
+             const mamr_split_job *__restrict__ jobs)
+{
+   const int job = blockIdx.x >> 3, o = blockIdx.x & 7, var = blockIdx.y;
+   const T *P = pool + bv_offset(g, jobs[job].parent, var);
+   T *C = pool + bv_offset(g, jobs[job].child[o], var);
+   const int i1 = (o & 1) * (g.nx / 2), j1 = ((o >> 1) & 1) * (g.ny / 2),
+             k1 = (o >> 2) * (g.nz / 2);
+   const int cells = g.nx * g.ny * g.nz;
+   for (int e = threadIdx.x; e < cells; e += blockDim.x) {
+      int ci = e / (g.ny * g.nz) + 1, r = e % (g.ny * g.nz);
+      int cj = r / g.nz + 1, ck = r % g.nz + 1;
+      C[cell_offset(g, ci, cj, ck)] =
+         eighth(P[cell_offset(g, (ci + 1) / 2 + i1, (cj + 1) / 2 + j1,
+                              (ck + 1) / 2 + k1)]);
+   }
+}
+
+template <typename T>
+int launch_split(T *pool, const Geom &g, const mamr_split_job *jobs, int n,
+                 cudaStream_t s)
+{
+   if (n == 0)
+      return 0;
+   split_kernel<T><<<dim3(n * 8, g.V), 256, 0, s>>>(pool, g, jobs);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+// consolidate_blocks() data (ref/block.c:411-431): one CTA per (job,
+// octant, variable); each coarse cell is the sum of its 8 children in the
+// reference's term order (left to right in FP64; compensated FP64 rounded
+// once to FP32 for FP32 pools).
+template <typename T>
+__global__ void __launch_bounds__(256)
+consolidate_kernel(T *__restrict__ pool, Geom g,
+                   const mamr_consolidate_job *__restrict__ jobs)
+{
+   const int job = blockIdx.x >> 3, o = blockIdx.x & 7, var = blockIdx.y;
+   T *P = pool + bv_offset(g, jobs[job].target, var);
+   const T *C = pool + bv_offset(g, jobs[job].child[o], var);
+   const int xh = g.nx / 2, yh = g.ny / 2, zh = g.nz / 2;
+   const int i1 = (o & 1) * xh, j1 = ((o >> 1) & 1) * yh, k1 = (o >> 2) * zh;
+   for (int e = threadIdx.x; e < xh * yh * zh; e += blockDim.x) {
+      int i = e / (yh * zh) + 1, r = e % (yh * zh);
+      int j = r / zh + 1, k = r % zh + 1;
+      int i2 = 2 * i - 1, j2 = 2 * j - 1, k2 = 2 * k - 1;
+      T t[8] = { C[cell_offset(g, i2, j2, k2)],
+                 C[cell_offset(g, i2 + 1, j2, k2)],
+                 C[cell_offset(g, i2, j2 + 1, k2)],
+                 C[cell_offset(g, i2 + 1, j2 + 1, k2)],
+                 C[cell_offset(g, i2, j2, k2 + 1)],
+                 C[cell_offset(g, i2 + 1, j2, k2 + 1)],
+                 C[cell_offset(g, i2, j2 + 1, k2 + 1)],
+                 C[cell_offset(g, i2 + 1, j2 + 1, k2 + 1)] };
+      P[cell_offset(g, i + i1, j + j1, k + k1)] = sum8(t);
+   }
+}
+
+template <typename T>
+int launch_consolidate(T *pool, const Geom &g,
+                       const mamr_consolidate_job *jobs, int n,
+                       cudaStream_t s)
+{
+   if (n == 0)
+      return 0;
+   consolidate_kernel<T><<<dim3(n * 8, g.V), 256, 0, s>>>(pool, g, jobs);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+// ---------------------------------------------------------------------------
+// Host layout [n][V][X][Y][Z] doubles <-> pool slots.
+template <typename T>
+__global__ void upload_kernel(T *__restrict__ pool, Geom g,
+                              const int32_t *__restrict__ slots, long long total,
+                              const double *__restrict__ dense)
+{
+   for (long long e = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+        e < total; e += (long long) gridDim.x * blockDim.x) {
+      long long row = e / g.Z;
+      int k = (int) (e - row * g.Z);
+      long long bvi = row / (g.X * g.Y);
+      int r = (int) (row - bvi * (g.X * g.Y));
+      int b = (int) (bvi / g.V), var = (int) (bvi - (long long) b * g.V);
+      pool[bv_offset(g, slots[b], var) + (long long) r * g.Zp + g.koff + k] =
+         (T) dense[e];
+   }
+}
+
+template <typename T>
+__global__ void download_kernel(const T *__restrict__ pool, Geom g,
+                                const int32_t *__restrict__ slots,
+                                long long total, double *__restrict__ dense)
+{
+   for (long long e = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+        e < total; e += (long long) gridDim.x * blockDim.x) {
+      long long row = e / g.Z;
+      int k = (int) (e - row * g.Z);
+      long long bvi = row / (g.X * g.Y);
+      int r = (int) (row - bvi * (g.X * g.Y));
+      int b = (int) (bvi / g.V), var = (int) (bvi - (long long) b * g.V);
+      dense[e] = (double) pool[bv_offset(g, slots[b], var) +
+                               (long long) r * g.Zp + g.koff + k];
+   }
+}
+
+template <typename T>
+int launch_upload(T *pool, const Geom &g, const int32_t *slots, int n,
+                  const double *dense, cudaStream_t s)
+{
+   long long total = (long long) n * g.V * g.X * g.Y * g.Z;
+   if (total == 0)
+      return 0;
+   long long blocks = (total + 255) / 256;
+   upload_kernel<T><<<(int) (blocks < 152 * 64 ? blocks : 152 * 64), 256, 0,
+                      s>>>(pool, g, slots, total, dense);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+template <typename T>
+int launch_download(const T *pool, const Geom &g, const int32_t *slots,
+                    int n, double *dense, cudaStream_t s)
+{
+   long long total = (long long) n * g.V * g.X * g.Y * g.Z;
+   if (total == 0)
+      return 0;
+   long long blocks = (total + 255) / 256;
+   download_kernel<T><<<(int) (blocks < 152 * 64 ? blocks : 152 * 64), 256,
+                        0, s>>>(pool, g, slots, total, dense);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+#define INSTANTIATE(T)                                                        \
+   template int launch_comm_dir<T>(T *, const Geom &, int, int,               \
+                                   const DirTasks &, int, int, cudaStream_t); \
+   template int launch_stencil<T>(T *, const Geom &, int, const int32_t *,    \
+                                  int, int, cudaStream_t);                    \
+   template int launch_split<T>(T *, const Geom &, const mamr_split_job *,    \
+                                int, cudaStream_t);                           \
+   template int launch_consolidate<T>(T *, const Geom &,                      \
+                                      const mamr_consolidate_job *, int,      \
+                                      cudaStream_t);                          \
+   template int launch_upload<T>(T *, const Geom &, const int32_t *, int,     \
+                                 const double *, cudaStream_t);               \
+   template int launch_download<T>(const T *, const Geom &, const int32_t *,  \
+                                   int, double *, cudaStream_t);
+INSTANTIATE(double)
+INSTANTIATE(float)
+
+}  // namespace mamr

@@ -66,7 +66,7 @@ void split_blocks(void)
    block *bp, *bp1;
    parent *pp;
 
-   mamr_dropin_sync_state();
+   mamr_dropin_sync_data();
    for (m = level = 0; level <= cur_max_level; level++) {
       /* slot order, not the sorted list: this routine edits the list */
       for (n = 0; n < max_active_block; n++) {
@@ -253,7 +253,7 @@ void consolidate_blocks(void)
    block *bp, *bp1;
    parent *pp;
 
-   mamr_dropin_sync_state();
+   mamr_dropin_sync_data();
    for (level = cur_max_level; level >= 0; level--)
       for (p = 0; p < max_active_parent; p++) {
          pp = &parents[p];

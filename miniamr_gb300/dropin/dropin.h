@@ -23,6 +23,10 @@ mamr_ctx *mamr_dropin_ctx(void);
  * blocks' connectivity changed since the last call. */
 void mamr_dropin_sync_state(void);
 
+/* Creates the context and uploads init()'s host arrays (once), without
+ * touching the mesh: what split/consolidate need. */
+void mamr_dropin_sync_data(void);
+
 /* Marks the mesh as changed (split/consolidate). */
 void mamr_dropin_mesh_changed(void);
 

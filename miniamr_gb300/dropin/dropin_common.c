@@ -125,13 +125,19 @@ static void build_desc(void)
    n_desc = nact;
 }
 
-void mamr_dropin_sync_state(void)
+void mamr_dropin_sync_data(void)
 {
    mamr_dropin_ctx();
    if (!uploaded) {
       upload_initial();
       uploaded = 1;
    }
+   generation++;
+}
+
+void mamr_dropin_sync_state(void)
+{
+   mamr_dropin_sync_data();
    build_desc();
    if (mesh_dirty || n_desc != n_sent ||
        memcmp(desc, sent, sizeof(mamr_block) * n_desc)) {

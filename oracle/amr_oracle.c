@@ -669,3 +669,38 @@ int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts, int32_t stages_per_ts,
       *n_sums = cnt;
    return MAMR_OK;
 }
+
+/* ref/init.c:484-495 on one rank: zero every cell, then the interior from
+ * the unseeded rand() stream (seed 1), reproduced with a private random_r
+ * state. */
+int mamr_initial_values(const mamr_config *cfg, int32_t n_blocks, double *out)
+{
+   char state[128];
+   struct random_data rd;
+   int32_t b;
+   int v, i, j, k, X, Y, Z;
+   size_t bv;
+   if (!cfg || n_blocks < 0 || (n_blocks && !out) || cfg->nx < 1 ||
+       cfg->ny < 1 || cfg->nz < 1 || cfg->num_vars < 1)
+      return fail(MAMR_EINVAL, "bad initial-value arguments");
+   memset(&rd, 0, sizeof(rd));
+   memset(state, 0, sizeof(state));
+   if (initstate_r(1u, state, sizeof(state), &rd))
+      return fail(MAMR_EINVAL, "initstate_r failed");
+   X = cfg->nx + 2; Y = cfg->ny + 2; Z = cfg->nz + 2;
+   bv = (size_t) X * Y * Z;
+   for (b = 0; b < n_blocks; b++)
+      for (v = 0; v < cfg->num_vars; v++) {
+         double *a = out + ((size_t) b * cfg->num_vars + v) * bv;
+         memset(a, 0, sizeof(double) * bv);
+         for (i = 1; i <= cfg->nx; i++)
+            for (j = 1; j <= cfg->ny; j++)
+               for (k = 1; k <= cfg->nz; k++) {
+                  int32_t r;
+                  random_r(&rd, &r);
+                  a[((size_t) i * Y + j) * Z + k] =
+                     ((double) r) / ((double) RAND_MAX);
+               }
+      }
+   return MAMR_OK;
+}

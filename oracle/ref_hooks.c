@@ -10,10 +10,9 @@
  *
  *     cs <call#> <var> <checksum as 16 hex digits> <cell hash, 16 hex>
  *
- * where the cell hash is FNV-1a-64 over the bit patterns of every cell
- * (ghosts included) of that variable in every active block, visited in
- * sorted_list order (ref/block.h:72-77), each block prefixed by its
- * number.  Every refine() call (ref/refine.c:38) appends one line
+ * where the cell hash (var_cell_hash below) covers the bit pattern of
+ * every cell, ghosts included, of that variable in every active block, in
+ * sorted_list order (ref/block.h:72-77), and each block's number.  Every refine() call (ref/refine.c:38) appends one line
  *
  *     mesh <ts> <n_active> <hash of (slot,number,level,nei_level,nei,cen)>
  *
@@ -69,32 +68,44 @@ static uint64_t fnv_bytes(uint64_t h, const void *p, size_t n)
    return h;
 }
 
+/* splitmix64 finaliser: position weights of the cell hash. */
+static uint64_t mix64(uint64_t z)
+{
+   z += 0x9E3779B97F4A7C15ULL;
+   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+   z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+   return z ^ (z >> 31);
+}
+
+/* Cell hash of one variable: sum over active blocks (position p in
+ * sorted_list) of number * w(p, 2^32-1) plus, over every cell c of the
+ * block-variable (ghosts included, [i][j][k] order), bits(cell) * w(p, c),
+ * all mod 2^64, with w(p, c) = mix64(p << 32 | c) | 1. */
 static uint64_t var_cell_hash(int var)
 {
    int in, i, j, k, nx2 = x_block_size + 2, ny2 = y_block_size + 2,
        nz2 = z_block_size + 2;
-   uint64_t h = 1469598103934665603ULL;
+   uint64_t h = 0;
    double *buf = NULL;
 
    if (mamr_dropin_fetch)
       buf = (double *) malloc(sizeof(double) * nx2 * ny2 * nz2);
    for (in = 0; in < sorted_index[num_refine+1]; in++) {
       int n = sorted_list[in].n;
-      long long number = (long long) blocks[n].number;
-      h = fnv_bytes(h, &number, sizeof(number));
-      if (buf) {
-         if (mamr_dropin_fetch(n, var, buf)) {
-            fprintf(stderr, "ref_hooks: fetch failed\n");
-            exit(-1);
-         }
-         h = fnv_bytes(h, buf, sizeof(double) * nx2 * ny2 * nz2);
-      } else {
-         for (i = 0; i < nx2; i++)
-            for (j = 0; j < ny2; j++)
-               for (k = 0; k < nz2; k++)
-                  h = fnv_bytes(h, &blocks[n].array[var][i][j][k],
-                                sizeof(double));
+      uint64_t c = 0, base = (uint64_t) in << 32;
+      h += (uint64_t) (long long) blocks[n].number * (mix64(base | 0xFFFFFFFFULL) | 1);
+      if (buf && mamr_dropin_fetch(n, var, buf)) {
+         fprintf(stderr, "ref_hooks: fetch failed\n");
+         exit(-1);
       }
+      for (i = 0; i < nx2; i++)
+         for (j = 0; j < ny2; j++)
+            for (k = 0; k < nz2; k++, c++) {
+               double v = buf ? buf[c] : blocks[n].array[var][i][j][k];
+               uint64_t bits;
+               memcpy(&bits, &v, sizeof(bits));
+               h += bits * (mix64(base | c) | 1);
+            }
    }
    free(buf);
    return h;

@@ -1,0 +1,124 @@
+"""Generates the golden fixtures in tests/golden/ from the miniAMR reference.
+
+Needs the reference sources (default /root/reference/ref, or
+MAMR_REFERENCE_SRC) and runs only where they exist; the fixtures it writes
+are committed so that the tests need no reference at run time.
+
+For every case in CASES it
+  1. runs the unmodified reference (oracle/_ref/miniamr_ref) with its
+     check_sum/refine hooks, producing <name>.reflog.xz: every checksum the
+     reference computed (exact bits) with a hash of every cell of that
+     variable, and a hash of the mesh after each refine();
+  2. runs the reference's driver over the drop-in translation units and the
+     CPU oracle (oracle/_ref/miniamr_hybrid_trace), which must produce the
+     identical log, and records every mamr_* call it made as
+     <name>.trace.xz.
+cases.json lists each case's command line.
+
+    python tests/golden/make_golden.py [case ...]
+"""
+from __future__ import annotations
+
+import json
+import lzma
+import os
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF_BIN = os.path.join(REPO, "oracle", "_ref", "miniamr_ref")
+HYB_BIN = os.path.join(REPO, "oracle", "_ref", "miniamr_hybrid_trace")
+
+SPHERE = ["--num_objects", "1", "--object", "2", "1", "0.25", "0.25", "0.25",
+          "0.03", "0.03", "0.03", "0.15", "0.15", "0.15", "0", "0", "0"]
+
+
+def small(stencil, extra=()):
+    return (["--init_x", "2", "--init_y", "2", "--init_z", "2", "--nx", "8",
+             "--ny", "8", "--nz", "8", "--num_vars", "4", "--stencil",
+             str(stencil), "--num_refine", "3", "--refine_freq", "2",
+             "--num_tsteps", "16", "--stages_per_ts", "2", "--checksum_freq",
+             "1", "--error_tol", "0", "--max_blocks", "4000"] + SPHERE +
+            list(extra))
+
+
+CASES = {
+    # the reference's own CPU case: 2^3 blocks of 8^3, 40 vars, 7-point,
+    # no refinement, 20 timesteps x 1 stage, checksum every stage
+    "config1": ["--init_x", "2", "--init_y", "2", "--init_z", "2", "--nx",
+                "8", "--ny", "8", "--nz", "8", "--num_vars", "40",
+                "--stencil", "7", "--num_refine", "0", "--num_tsteps", "20",
+                "--stages_per_ts", "1", "--checksum_freq", "1"],
+    # moving sphere, refine + coarsen every 2 timesteps, up to 3 levels
+    "amr27": small(27),
+    "amr7": small(7),
+    "amr27_permute": small(27, ["--permute"]) [:],
+    # uniform refinement, non-cubic blocks, 27-point
+    "uniform27": ["--init_x", "2", "--init_y", "1", "--init_z", "3", "--nx",
+                  "4", "--ny", "6", "--nz", "8", "--num_vars", "3",
+                  "--stencil", "27", "--num_refine", "2", "--uniform_refine",
+                  "1", "--num_tsteps", "5", "--stages_per_ts", "2",
+                  "--checksum_freq", "1", "--error_tol", "0", "--max_blocks",
+                  "4000"],
+    # two objects, volume + surface refinement, 7-point, 4 levels, default
+    # checksum cadence (every 5th stage of 3)
+    "amr7_objects": ["--init_x", "2", "--init_y", "2", "--init_z", "2",
+                     "--nx", "6", "--ny", "6", "--nz", "6", "--num_vars", "3",
+                     "--stencil", "7", "--num_refine", "4", "--refine_freq",
+                     "1", "--num_tsteps", "12", "--stages_per_ts", "3",
+                     "--max_blocks", "20000",
+                     "--num_objects", "2",
+                     "--object", "3", "1", "0.3", "0.6", "0.5", "0.04",
+                     "-0.03", "0.0", "0.12", "0.12", "0.12", "0", "0", "0",
+                     "--object", "2", "1", "0.7", "0.3", "0.4", "-0.03",
+                     "0.04", "0.02", "0.1", "0.1", "0.1", "0", "0", "0"],
+}
+
+
+def run_case(name, args):
+    with tempfile.TemporaryDirectory() as td:
+        rlog = os.path.join(td, "r.log")
+        hlog = os.path.join(td, "h.log")
+        trc = os.path.join(td, "t.trc")
+        env = dict(os.environ, MAMR_REF_LOG=rlog)
+        r = subprocess.run([REF_BIN] + args, cwd=td, env=env,
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"{name}: reference failed\n{r.stdout[-2000:]}")
+        env = dict(os.environ, MAMR_REF_LOG=hlog, MAMR_TRACE=trc)
+        h = subprocess.run([HYB_BIN] + args, cwd=td, env=env,
+                           capture_output=True, text=True)
+        if h.returncode != 0:
+            raise RuntimeError(f"{name}: hybrid failed\n{h.stdout[-2000:]}")
+        ref_log = open(rlog, "rb").read()
+        if open(hlog, "rb").read() != ref_log:
+            raise RuntimeError(f"{name}: drop-in hybrid differs from the "
+                               "reference")
+        with lzma.open(os.path.join(HERE, name + ".reflog.xz"), "wb",
+                       preset=9) as f:
+            f.write(ref_log)
+        with lzma.open(os.path.join(HERE, name + ".trace.xz"), "wb",
+                       preset=9) as f:
+            f.write(open(trc, "rb").read())
+        summary = [l for l in r.stdout.splitlines() if l.startswith("Summary")]
+        return summary[-1] if summary else ""
+
+
+def main(argv):
+    if not os.path.exists(REF_BIN) or not os.path.exists(HYB_BIN):
+        subprocess.run(["make", "-s", "-j8", "-C",
+                        os.path.join(REPO, "oracle"), "all"], check=True)
+    names = argv or list(CASES)
+    meta_path = os.path.join(HERE, "cases.json")
+    meta = json.load(open(meta_path)) if os.path.exists(meta_path) else {}
+    for n in names:
+        s = run_case(n, CASES[n])
+        meta[n] = {"args": CASES[n], "reference_summary": s}
+        print(n, s)
+    json.dump(meta, open(meta_path, "w"), indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

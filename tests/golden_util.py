@@ -1,0 +1,38 @@
+"""Access to the committed golden fixtures (tests/golden/, made by
+tests/golden/make_golden.py from the reference itself)."""
+import json
+import lzma
+import os
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def cases():
+    return json.load(open(os.path.join(GOLDEN, "cases.json")))
+
+
+def reflog(name):
+    """(checksums, cell_hashes, meshes) from the reference's hook log:
+    checksums[i] = (var, value) of the i-th check_sum call, cell_hashes[i]
+    the hash of that variable's cells, meshes = [(ts, n_active, hash)]."""
+    sums, hashes, meshes = [], [], []
+    with lzma.open(os.path.join(GOLDEN, name + ".reflog.xz"), "rt") as f:
+        for line in f:
+            p = line.split()
+            if p[0] == "cs":
+                v = int(p[3], 16)
+                sums.append((int(p[2]),
+                             __import__("struct").unpack(
+                                 "<d", v.to_bytes(8, "little"))[0]))
+                hashes.append(int(p[4], 16))
+            elif p[0] == "mesh":
+                meshes.append((int(p[1]), int(p[2]), p[3]))
+    return sums, hashes, meshes
+
+
+def trace_path(name):
+    return os.path.join(GOLDEN, name + ".trace.xz")
+
+
+def arg(args, flag, default=None):
+    return args[args.index(flag) + 1] if flag in args else default

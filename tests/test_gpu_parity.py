@@ -1,0 +1,138 @@
+"""GPU library parity: bit-exact against the reference's golden vectors and
+the CPU oracle, through the C ABI."""
+import numpy as np
+import pytest
+
+from golden_util import cases, reflog, trace_path
+from miniamr_gb300 import mesh as meshmod
+from miniamr_gb300.abi import FP32, FP64, MamrError, Config
+from miniamr_gb300.trace import read_trace, replay
+
+pytestmark = pytest.mark.gpu
+CASES = sorted(cases())
+
+
+def bits(a):
+    return np.ascontiguousarray(a, dtype=np.float64).view(np.uint64)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_trace_fp64_bit_exact_vs_reference(gpu_lib, name):
+    """The reference's own call sequence replayed on the GPU: every
+    checksum bit-identical to the reference's, and every cell (ghosts
+    included) at the first, middle and last checksum stage."""
+    sums, hashes, _ = reflog(name)
+    recs = read_trace(trace_path(name))
+    V = next(r.args[0].num_vars for r in recs if r.op == 1)
+    n_st = len(sums) // V
+    want = {0, n_st // 2, n_st - 1}
+    res = replay(gpu_lib, recs, hash_stages=want)
+    got = [(v, s) for v, s, _ in res.checksums]
+    assert got == sums
+    for st, hs in res.hashes:
+        assert hs == hashes[st * V:(st + 1) * V], f"cells differ, stage {st}"
+    res.ctx.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_trace_fp32_vs_oracle_and_reference(gpu_lib, oracle_lib, name):
+    """FP32 pools: bit-identical to the FP32 oracle (same operation order,
+    correctly rounded FP32 division, exact fixed-point checksum) and within
+    1e-6 relative of the reference's FP64 checksums."""
+    sums, _, _ = reflog(name)
+    recs = read_trace(trace_path(name))
+    g = replay(gpu_lib, recs, dtype=FP32)
+    o = replay(oracle_lib, recs, dtype=FP32)
+    assert [s for _, s, _ in g.checksums] == [s for _, s, _ in o.checksums]
+    slots = g.mesh["slot"]
+    assert np.array_equal(bits(g.ctx.download(slots)),
+                          bits(o.ctx.download(slots)))
+    rel = [abs(s - r) / abs(r) for (_, s, _), (_, r) in zip(g.checksums, sums)
+           if r != 0.0]
+    assert max(rel) <= 1e-6, max(rel)
+    g.ctx.close()
+    o.ctx.close()
+
+
+UNIFORM = [
+    # (lattice, block, vars, stencil, refine passes, permute)
+    ((2, 2, 2), (8, 8, 8), 4, 7, 0, 0),
+    ((2, 2, 2), (8, 8, 8), 4, 27, 1, 0),
+    ((3, 1, 2), (4, 6, 8), 3, 27, 1, 1),
+    ((2, 2, 1), (16, 16, 16), 2, 7, 1, 1),
+    ((1, 2, 2), (16, 16, 16), 2, 27, 1, 0),
+]
+
+
+@pytest.mark.parametrize("dtype", [FP64, FP32])
+@pytest.mark.parametrize("case", UNIFORM)
+def test_uniform_run_vs_oracle(gpu_lib, oracle_lib, case, dtype):
+    (ix, iy, iz), (nx, ny, nz), V, st, passes, perm = case
+    n0 = ix * iy * iz
+    cap = n0 * (1 + 8 ** passes) + 8
+    cfg = Config.make(nx, ny, nz, V, cap, stencil=st, dtype=dtype,
+                      permute=perm)
+    init = gpu_lib.initial_values(cfg, n0)
+    outs = []
+    for lib in (gpu_lib, oracle_lib):
+        m = meshmod.initial_mesh(ix, iy, iz, passes, cap)
+        ctx = lib.context(cfg)
+        ctx.upload(np.arange(n0), init)
+        for _ in range(passes):
+            ctx.split(m.split_all())
+        ctx.set_mesh(m.blocks())
+        sums = ctx.run_timesteps(3, 2, 1)
+        outs.append((sums, ctx.download(m.sorted_slots())))
+        ctx.close()
+    assert np.array_equal(bits(outs[0][0]), bits(outs[1][0]))
+    assert np.array_equal(bits(outs[0][1]), bits(outs[1][1]))
+
+
+def test_division_edge_values(gpu_lib, oracle_lib):
+    """Stencil averages over cells spanning the whole FP64 range (tiny,
+    huge, negative, zero) -- both division paths -- match the oracle's IEEE
+    division bit for bit."""
+    rng = np.random.default_rng(7)
+    for st in (7, 27):
+        cfg = Config.make(8, 8, 8, 2, 8, stencil=st, dtype=FP64)
+        vals = np.zeros((8, 2, 10, 10, 10))
+        mant = rng.uniform(-2, 2, size=(8, 2, 8, 8, 8))
+        expo = rng.integers(-1070, 1015, size=(8, 2, 8, 8, 8))
+        vals[:, :, 1:9, 1:9, 1:9] = np.ldexp(mant, expo) / 64.0
+        vals[0, 0, 1:9, 1:9, 1:9] = np.ldexp(mant[0, 0], -930)
+        m = meshmod.initial_mesh(2, 2, 2, 0, 8)
+        outs = []
+        for lib in (gpu_lib, oracle_lib):
+            with lib.context(cfg) as ctx:
+                ctx.upload(np.arange(8), vals)
+                ctx.set_mesh(m.blocks())
+                for s in range(2):
+                    ctx.comm(0, 2, s)
+                    ctx.stencil_driver(0, s)
+                    ctx.stencil_driver(1, s)
+                outs.append(ctx.download(np.arange(8)))
+        assert np.array_equal(bits(outs[0]), bits(outs[1]))
+
+
+def test_errors_are_reported_and_context_survives(gpu_lib):
+    cfg = Config.make(8, 8, 8, 2, 16, stencil=7, dtype=FP32)
+    m = meshmod.initial_mesh(2, 2, 2, 0, 16)
+    with gpu_lib.context(cfg) as ctx:
+        with pytest.raises(MamrError) as e:
+            ctx.upload([99], np.zeros((1, 2, 10, 10, 10)))
+        assert e.value.status == -1
+        bad = m.blocks()
+        bad["nei_level"][0, 1] = 5
+        with pytest.raises(MamrError) as e:
+            ctx.set_mesh(bad)
+        assert e.value.status == -4
+        ctx.set_mesh(m.blocks())
+        v = np.zeros((8, 2, 10, 10, 10))
+        v[3, 1, 4, 4, 4] = 5000.0      # outside the FP32 checksum range
+        ctx.upload(np.arange(8), v)
+        with pytest.raises(MamrError) as e:
+            ctx.check_sum(1)
+        assert e.value.status == -6
+        assert ctx.check_sum(0) == 0.0   # context still usable
+        with pytest.raises(MamrError):
+            ctx.comm(1, 5, 0)
