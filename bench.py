@@ -1,0 +1,360 @@
+#!/usr/bin/env python3
+"""miniAMR hot path on GB300: cell-variable updates/s and HBM roofline.
+
+Workload (the precision variant of the uniform 4096-block mesh): 8x8x8
+initial blocks of 16^3 cells uniformly refined once -> 4096 blocks, 40
+variables, 27-point stencil, 4 stages per timestep, checksum every 5th
+stage (the reference's default cadence), initial values from the
+reference's init().  One step = one timestep (4 stages of comm + stencil
+over every block and variable, checksums on stage 0).
+
+Headline `value`: the batched FP32 path (one fused ghost+stencil+checksum
+launch per stage, CUDA graph) with the pool resident in HBM (3.4 GB of
+interior FP32 cells -- far larger than L2, so no flush is needed).  `e2e`:
+the same run through the C ABI from pinned host buffers -- the initial
+blocks uploaded, refined on the device, stepped, checksums read back every
+step.  Also reported: the plain FP64 path (bit-exact with the reference),
+the batched FP64 path, and the max / RMS relative error of every FP32
+checksum against the FP64 (reference-exact) checksums of the same run.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference algorithm on the host cores (the CPU
+oracle, OpenMP over blocks, FP64) on a bounded sample of the workload.
+Under torchrun each rank runs an independent replica ("replicas only":
+the hot path has no exchange between GPUs on one logical rank).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = ("cell-var updates/s + %HBM roofline: FP32-batched vs FP64 GPU at "
+          "1e-6 rel chksum")
+UNIT = "cell-var updates/s"
+INIT = (8, 8, 8)
+N = 16
+V = 40
+STENCIL = 27
+SPT = 4
+FREQ = 5
+N0 = INIT[0] * INIT[1] * INIT[2]
+N_BLOCKS = N0 * 8
+CAP = N0 + N_BLOCKS + 8
+UPD_PER_STAGE = N_BLOCKS * N ** 3 * V
+# reference arm / CPU baseline sample: the same blocks and stencil on a
+# 4x4x4-initial mesh (512 blocks), one timestep per step
+SAMPLE_INIT = (4, 4, 4)
+WORKLOAD = {
+    "workload": "uniform mesh 4096 blocks of 16^3 (8x8x8 initial, uniform "
+                "refine 1), 40 vars, 27-point, 4 stages/ts, checksum every "
+                "5th stage",
+    "blocks": N_BLOCKS, "cells_per_block": N ** 3, "num_vars": V,
+    "stencil": STENCIL, "stages_per_ts": SPT, "checksum_freq": FREQ,
+    "path": "batched FP32 (fused ghost+stencil+checksum, CUDA graph)",
+    "l2": "inputs larger than L2 (3.4 GB FP32 interiors per pool)",
+}
+
+
+def updates(steps):
+    return steps * SPT * UPD_PER_STAGE
+
+
+def build_mesh(lib, dtype, init=INIT, cap=CAP, ctx=None, host=None):
+    from miniamr_gb300 import mesh as meshmod
+    from miniamr_gb300.abi import Config
+    n0 = init[0] * init[1] * init[2]
+    cfg = Config.make(N, N, N, V, cap, stencil=STENCIL, dtype=dtype)
+    if ctx is None:
+        ctx = lib.context(cfg)
+    if host is None:
+        host = lib.initial_values(cfg, n0)
+    m = meshmod.initial_mesh(*init, 1, cap)
+    ctx.upload(np.arange(n0), host)
+    ctx.split(m.split_all())
+    ctx.set_mesh(m.blocks())
+    return ctx, m
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a run."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.p:
+            time.sleep(0.15)
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out, _ = self.p.communicate()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        p = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the stage kernel from the committed ncu
+    summary (profiles/batched_stage_fp32_27pt_4096blk.json), if present."""
+    p = os.path.join(REPO, "profiles", "batched_stage_fp32_27pt_4096blk.json")
+    try:
+        return json.load(open(p)).get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def oracle_rate(steps, threads=None):
+    """The reference algorithm on the host cores: CPU oracle, FP64, OpenMP
+    over blocks, on the 512-block sample; returns (updates/s, threads)."""
+    from miniamr_gb300 import build
+    from miniamr_gb300.abi import FP64, Library
+    threads = threads or os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    lib = Library(build.build_oracle())
+    n0 = SAMPLE_INIT[0] * SAMPLE_INIT[1] * SAMPLE_INIT[2]
+    ctx, _ = build_mesh(lib, FP64, init=SAMPLE_INIT, cap=n0 * 9 + 8)
+    ctx.run_timesteps(1, SPT, FREQ)           # warm-up
+    t0 = time.perf_counter()
+    ctx.run_timesteps(steps, SPT, FREQ)
+    dt = time.perf_counter() - t0
+    ctx.close()
+    return steps * SPT * n0 * 8 * N ** 3 * V / dt, threads, dt
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    return world, rank, local, pg
+
+
+def reference_arm(args, world, rank, pg):
+    if rank != 0:
+        return 0
+    steps = max(1, args.steps)
+    for _ in range(max(0, args.warmup)):
+        pass
+    rate, threads, dt = oracle_rate(steps)
+    line = {
+        "metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference",
+        "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: the reference's init() values (rand(), seed 1)",
+        "config": dict(WORKLOAD, path="reference algorithm on host cores"),
+        "cpu_baseline": {
+            "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "512 blocks of 16^3 (4x4x4 initial, refine 1), 40 "
+                      "vars, 27-point, FP64; one timestep (4 stages) per "
+                      "step; CPU oracle (restatement of ref/stencil.c, "
+                      "ref/comm.c, ref/check_sum.c), OpenMP over blocks"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-steps", type=int, default=None,
+                    help="timesteps of the FP64 comparison runs")
+    args = ap.parse_args()
+    world, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        return reference_arm(args, world, rank, pg)
+
+    import torch
+    from miniamr_gb300 import build, load
+    from miniamr_gb300.abi import FP32, FP64, RUN_BATCHED, RUN_GRAPH, RUN_PLAIN
+
+    torch.cuda.set_device(local)
+    build.build_library()
+    lib = load()
+    K, W = args.steps, max(3, args.warmup)
+    flags = RUN_BATCHED | RUN_GRAPH
+
+    # ---- headline: FP32 batched, pool resident -----------------------
+    ctx, _ = build_mesh(lib, FP32)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ctx.run_timesteps(W, SPT, FREQ, flags=flags)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    l0 = ctx.launch_count()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        sums32 = ctx.run_timesteps(K, SPT, FREQ, first_stage=W * SPT,
+                                   flags=flags)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = ctx.launch_count() - l0
+    ms = ev0.elapsed_time(ev1)
+    if pg:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    value = updates(K) * world / (ms / 1e3)
+    n_stage_launches = K * SPT
+    per_launch_s = ms / 1e3 / n_stage_launches
+    alg_bytes = UPD_PER_STAGE * 2 * 4
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / per_launch_s / 1e9
+    traffic = ncu_traffic()
+    ctx.close()
+
+    # ---- e2e through the C ABI from pinned host buffers -----------------
+    from miniamr_gb300.abi import Config
+    cfg = Config.make(N, N, N, V, CAP, stencil=STENCIL, dtype=FP32)
+    pinned = torch.empty((N0, V, N + 2, N + 2, N + 2), dtype=torch.float64,
+                         pin_memory=True)
+    host = pinned.numpy()
+    host[...] = lib.initial_values(cfg, N0)
+    ctx = lib.context(cfg)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    build_mesh(lib, FP32, ctx=ctx, host=host)
+    e2e_sums = ctx.run_timesteps(K, SPT, FREQ, flags=flags)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if pg:
+        t = torch.tensor([e2e_s], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    ctx.close()
+    h2d = host.nbytes
+    d2h = e2e_sums.nbytes
+
+    # ---- FP64 paths and the FP32 checksum error ------------------------
+    K64 = args.fp64_steps if args.fp64_steps is not None else K
+    ctx64, _ = build_mesh(lib, FP64)
+    s64 = ctx64.run_timesteps(W + K64, SPT, FREQ, flags=flags)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx64.run_timesteps(2, SPT, FREQ, first_stage=(W + K64) * SPT,
+                        flags=flags)
+    fp64_batched = updates(2) / (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    ctx64.run_timesteps(1, SPT, FREQ, flags=RUN_PLAIN)
+    fp64_plain = updates(1) / (time.perf_counter() - t0)
+    ctx64.close()
+    ref = s64[W:W + min(K, K64)]
+    got = sums32[:len(ref)]
+    rel = np.abs(got - ref) / np.abs(ref)
+    err = {"checksums": int(rel.size), "max_rel": float(rel.max()),
+           "rms_rel": float(np.sqrt(np.mean(rel ** 2))),
+           "fp64_reference": "batched FP64 path (bit-exact with the "
+                             "reference's checksums)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": K, "warmup": W, "ms_per_step": ms / K,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic: the reference's init() values "
+                                "(rand(), seed 1), uniform mesh",
+        "config": WORKLOAD,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "batched_stage_kernel<float,27>",
+                     "alg_bytes_per_launch": alg_bytes},
+        "e2e": {"value": updates(K) * world / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
+                "seconds": e2e_s},
+        "gpu_launches": launches,
+        "paths": {"fp32_batched": value / world,
+                  "fp64_batched": fp64_batched, "fp64_plain": fp64_plain,
+                  "fp32_batched_over_fp64_plain": value / world / fp64_plain},
+        "fp32_checksum_error": err,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, threads, dt = oracle_rate(3)
+        line["cpu_baseline"] = {
+            "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "512 blocks of 16^3, 40 vars, 27-point, FP64, 3 "
+                      "timesteps; CPU oracle with OpenMP over blocks "
+                      f"({dt:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

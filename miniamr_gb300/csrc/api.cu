@@ -82,6 +82,29 @@ const int kPerm[6][3] = { {0, 1, 2}, {1, 2, 0}, {2, 0, 1},
 
 }  // namespace
 
+namespace mamr {
+struct BatchedState {
+   DevBuf items, partials, sums, acc;
+   int n = 0;
+   bool valid = false;
+   bool single_level = false;
+   int grid = 0;
+};
+void batched_destroy(BatchedState *b)
+{
+   if (!b)
+      return;
+   b->items.release(); b->partials.release(); b->sums.release();
+   b->acc.release();
+   delete b;
+}
+void batched_mesh_changed(BatchedState *b)
+{
+   if (b)
+      b->valid = false;
+}
+}  // namespace mamr
+
 struct mamr_ctx {
    mamr_config cfg;
    Geom g;
@@ -102,6 +125,7 @@ struct mamr_ctx {
    unsigned *d_err;                 // device error word
    void *h_pinned;                  // 64 bytes of pinned host memory
    long long launches;
+   int hw_slots;                    // 1 + highest slot ever holding data
    mamr::BatchedState *batched;
 };
 
@@ -256,6 +280,9 @@ static int transfer(mamr_ctx *c, const int32_t *slots, int32_t n,
    for (int32_t b = 0; b < n; b++)
       if (!slot_ok(c, slots[b]))
          return fail(MAMR_EINVAL, "slot %d out of range", slots[b]);
+   if (up)
+      for (int32_t b = 0; b < n; b++)
+         c->hw_slots = std::max(c->hw_slots, slots[b] + 1);
    const Geom &g = c->g;
    const size_t per_block = (size_t) g.V * g.X * g.Y * g.Z;
    int32_t chunk = (int32_t) std::max<size_t>(1, kStageBytes /
@@ -431,6 +458,8 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
    CUDA_TRY(cudaStreamSynchronize(c->stream));
    c->mesh.assign(blocks, blocks + n);
    c->slot_pos.swap(pos);
+   for (int32_t b = 0; b < n; b++)
+      c->hw_slots = std::max(c->hw_slots, blocks[b].slot + 1);
    mamr::batched_mesh_changed(c->batched);
    return MAMR_OK;
 }
@@ -615,6 +644,7 @@ extern "C" int mamr_split(mamr_ctx *c, const mamr_split_job *jobs, int32_t n)
             return fail(MAMR_EINVAL, "split child slot %d out of range",
                         jobs[t].child[o]);
          wr[t][o] = jobs[t].child[o];
+         c->hw_slots = std::max(c->hw_slots, jobs[t].child[o] + 1);
       }
    }
    if (n == 0)
@@ -640,6 +670,7 @@ extern "C" int mamr_consolidate(mamr_ctx *c, const mamr_consolidate_job *jobs,
          return fail(MAMR_EINVAL, "consolidate target slot %d out of range",
                      jobs[t].target);
       wr[t][0] = jobs[t].target;
+      c->hw_slots = std::max(c->hw_slots, jobs[t].target + 1);
       for (int o = 0; o < 8; o++) {
          if (!slot_ok(c, jobs[t].child[o]))
             return fail(MAMR_EINVAL, "consolidate child slot %d out of range",
@@ -717,6 +748,215 @@ static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
    return MAMR_OK;
 }
 
+
+// Per-block descriptors for the batched stage kernel, from the mesh.
+static int build_items(mamr_ctx *c)
+{
+   BatchedState *B = c->batched;
+   const int n = (int) c->mesh.size();
+   std::vector<BItem> items(std::max(1, n));
+   bool single = true;
+   const int lev0 = n ? c->mesh[0].level : 0;
+   for (int q = 0; q < n; q++) {
+      const mamr_block &bp = c->mesh[q];
+      BItem &it = items[q];
+      memset(&it, 0, sizeof(it));
+      it.slot = bp.slot;
+      if (bp.level != lev0)
+         single = false;
+      for (int l = 0; l < 6; l++) {
+         BFace &f = it.f[l];
+         const int nl = bp.nei_level[l];
+         if (nl == -2) {
+            f.type = FACE_BC;
+            it.bmask |= 1 << l;
+         } else if (nl == bp.level) {
+            f.type = FACE_SAME;
+            f.nb[0] = bp.nei[l][0][0];
+         } else if (nl == bp.level + 1) {
+            f.type = FACE_FINE;
+            for (int iq = 0; iq < 2; iq++)
+               for (int jq = 0; jq < 2; jq++)
+                  f.nb[iq * 2 + jq] = bp.nei[l][iq][jq];
+         } else {
+            f.type = FACE_COARSE;
+            const int m = bp.nei[l][0][0];
+            const int pm = c->slot_pos[m];
+            if (pm < 0)
+               return fail(MAMR_EMESH, "neighbour slot %d not active", m);
+            bool found = false;
+            for (int iq = 0; iq < 2 && !found; iq++)
+               for (int jq = 0; jq < 2 && !found; jq++)
+                  if (c->mesh[pm].nei[l ^ 1][iq][jq] == bp.slot) {
+                     f.nb[0] = m;
+                     f.iq = iq;
+                     f.jq = jq;
+                     found = true;
+                  }
+            if (!found)
+               return fail(MAMR_EMESH, "slot %d is not a child face of its "
+                           "coarser neighbour %d", bp.slot, m);
+         }
+      }
+      // neighbours across edges and corners: hop x, then y, then z
+      for (int dz = -1; dz <= 1; dz++)
+         for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++) {
+               int cur = bp.slot;
+               const int d[3] = {dx, dy, dz};
+               for (int ax = 0; ax < 3 && cur >= 0; ax++) {
+                  if (!d[ax])
+                     continue;
+                  const mamr_block &cb = c->mesh[c->slot_pos[cur]];
+                  const int l = 2 * ax + (d[ax] > 0);
+                  cur = (cb.nei_level[l] == cb.level) ? cb.nei[l][0][0] : -1;
+                  if (cur >= 0 && c->slot_pos[cur] < 0)
+                     cur = -1;
+               }
+               it.nb27[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)] =
+                  cur >= 0 ? cur : bp.slot;
+            }
+   }
+   CUDA_TRY(B->items.ensure(sizeof(BItem) * items.size()));
+   CUDA_TRY(cudaMemcpyAsync(B->items.p, items.data(),
+                            sizeof(BItem) * items.size(),
+                            cudaMemcpyHostToDevice, c->stream));
+   CUDA_TRY(cudaStreamSynchronize(c->stream));
+   B->n = n;
+   B->single_level = single;
+   B->valid = true;
+   return MAMR_OK;
+}
+
+// The stage loop of ref/driver.c:73-108 as one fused launch per stage.
+static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
+                       int32_t freq, bool graph, double *sums,
+                       int32_t *n_sums)
+{
+   int r;
+   if (!c->batched) {
+      c->batched = new (std::nothrow) BatchedState();
+      if (!c->batched)
+         return fail(MAMR_ENOMEM, "host allocation");
+   }
+   BatchedState *B = c->batched;
+   if (!B->valid && (r = build_items(c)))
+      return r;
+   if (c->cfg.stencil == 27 && !B->single_level)
+      return fail(MAMR_EUNSUP, "batched 27-point stencil needs a "
+                  "single-level mesh (edge/corner ghosts at level jumps "
+                  "follow the per-call exchange only)");
+   const int V = c->cfg.num_vars, nb = B->n;
+   int per_ts = 0;
+   if (freq)
+      for (int st = 0; st < spt; st++)
+         per_ts += !(st % freq);
+   const size_t n_cs = (size_t) per_ts * num_ts;
+   const size_t es = elem_size(c);
+   if (!c->pool_alt) {
+      CUDA_TRY(cudaMalloc(&c->pool_alt, c->pool_bytes));
+      CUDA_TRY(cudaMemsetAsync(c->pool_alt, 0, c->pool_bytes, c->stream));
+   }
+   // both pools start identical, so cells no stage writes (stale ghosts,
+   // free slots) read the same whichever pool ends up current
+   const size_t used = (size_t) c->hw_slots * c->g.V * c->g.bv * es;
+   if (used)
+      CUDA_TRY(cudaMemcpyAsync(c->pool_alt, c->pool, used,
+                               cudaMemcpyDeviceToDevice, c->stream));
+   if (c->fp32) {
+      CUDA_TRY(B->acc.ensure(std::max<size_t>(1, n_cs * V) * 16));
+      CUDA_TRY(cudaMemsetAsync(B->acc.p, 0, std::max<size_t>(1, n_cs * V) * 16,
+                               c->stream));
+   } else {
+      CUDA_TRY(B->partials.ensure(sizeof(double) * std::max(1, nb) * V));
+      CUDA_TRY(B->sums.ensure(sizeof(double) * std::max<size_t>(1, n_cs * V)));
+   }
+   const int grid = c->fp32 ? batched_grid<float>(c->g, c->cfg.stencil, nb * V)
+                            : batched_grid<double>(c->g, c->cfg.stencil, nb * V);
+   CUDA_TRY(cudaGetLastError());
+
+   cudaGraph_t g_graph = nullptr;
+   if (graph)
+      CUDA_TRY(cudaStreamBeginCapture(c->stream,
+                                      cudaStreamCaptureModeThreadLocal));
+   void *cur = c->pool, *oth = c->pool_alt;
+   long long launches = 0;
+   int cnt = 0, status = MAMR_OK;
+   const int total = num_ts * spt;
+   for (int ts = 0, q = 0; ts < num_ts && status == MAMR_OK; ts++)
+      for (int st = 0; st < spt; st++, q++) {
+         const bool do_cs = freq && !(st % freq);
+         const int last = (q == total - 1);
+         int k;
+         if (c->fp32)
+            k = launch_batched_stage((const float *) cur, (float *) oth, c->g,
+                                     c->cfg.stencil,
+                                     (const BItem *) B->items.p, nb, grid,
+                                     last, do_cs, nullptr, nullptr,
+                                     (unsigned long long *) B->acc.p +
+                                        (size_t) cnt * V * 2,
+                                     c->d_err, c->stream);
+         else
+            k = launch_batched_stage((const double *) cur, (double *) oth,
+                                     c->g, c->cfg.stencil,
+                                     (const BItem *) B->items.p, nb, grid,
+                                     last, do_cs, (double *) B->partials.p,
+                                     (double *) B->sums.p + (size_t) cnt * V,
+                                     nullptr, c->d_err, c->stream);
+         if (k < 0) {
+            status = fail(MAMR_ECUDA, "batched stage launch: %s",
+                          cudaGetErrorString(cudaGetLastError()));
+            break;
+         }
+         launches += k;
+         if (do_cs)
+            cnt++;
+         std::swap(cur, oth);
+      }
+   if (graph) {
+      cudaError_t e = cudaStreamEndCapture(c->stream, &g_graph);
+      if (status != MAMR_OK) {
+         if (g_graph)
+            cudaGraphDestroy(g_graph);
+         return status;
+      }
+      if (e != cudaSuccess)
+         return fail(MAMR_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+      cudaGraphExec_t exec = nullptr;
+      e = cudaGraphInstantiate(&exec, g_graph, 0);
+      if (e == cudaSuccess)
+         e = cudaGraphLaunch(exec, c->stream);
+      if (exec)
+         cudaGraphExecDestroy(exec);
+      cudaGraphDestroy(g_graph);
+      if (e != cudaSuccess)
+         return fail(MAMR_ECUDA, "graph launch: %s", cudaGetErrorString(e));
+   } else if (status != MAMR_OK) {
+      return status;
+   }
+   c->launches += launches;
+   if (cur != c->pool) {
+      std::swap(c->pool, c->pool_alt);
+   }
+   if ((r = mamr_sync(c)))
+      return r;
+   if (sums && cnt) {
+      if (c->fp32) {
+         std::vector<unsigned long long> h((size_t) cnt * V * 2);
+         CUDA_TRY(cudaMemcpy(h.data(), B->acc.p, h.size() * 8,
+                             cudaMemcpyDeviceToHost));
+         for (size_t q = 0; q < (size_t) cnt * V; q++)
+            sums[q] = fixed_to_double(h[2 * q], h[2 * q + 1]);
+      } else {
+         CUDA_TRY(cudaMemcpy(sums, B->sums.p, sizeof(double) * cnt * V,
+                             cudaMemcpyDeviceToHost));
+      }
+   }
+   if (n_sums)
+      *n_sums = cnt;
+   return MAMR_OK;
+}
+
 extern "C" int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts,
                                   int32_t stages_per_ts,
                                   int32_t checksum_freq, int32_t first_stage,
@@ -733,5 +973,6 @@ extern "C" int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts,
       return run_plain(c, num_ts, stages_per_ts, checksum_freq, first_stage,
                        sums, n_sums);
    }
-   return fail(MAMR_EUNSUP, "batched path not available");
+   return run_batched(c, num_ts, stages_per_ts, checksum_freq,
+                      (flags & MAMR_RUN_GRAPH) != 0, sums, n_sums);
 }

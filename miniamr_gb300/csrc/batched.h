@@ -1,13 +1,53 @@
-// Batched (fused ghost + stencil + checksum) path: per-context state.
+// Batched path: one fused launch per stage over every (block, variable) --
+// ghost gather from the neighbours' interiors, stencil, checksum -- reading
+// one pool and writing the other (ping-pong), so that no grid-wide barrier
+// separates the exchange from the update.
 #pragma once
 
 #include "mamr_internal.h"
 
 namespace mamr {
 
+// How one face of a block gets its ghost layer in the batched path.
+enum : int32_t {
+   FACE_SAME = 0,    // same-level neighbour nb[0]
+   FACE_BC = 1,      // domain boundary: reflect the block's own plane
+   FACE_COARSE = 2,  // coarser neighbour nb[0]; this block is quarter
+                     // (iq, jq) of the neighbour's face
+   FACE_FINE = 3     // four finer neighbours nb[iq*2 + jq]
+};
+
+struct BFace {
+   int32_t type;
+   int32_t nb[4];
+   int32_t iq, jq;
+};
+
+// Per active block, in sorted_list order.
+struct BItem {
+   int32_t slot;
+   int32_t bmask;      // bit l: face l is a domain boundary
+   BFace f[6];
+   int32_t nb27[27];   // neighbour at offset (dx,dy,dz), index
+                       // (dx+1) + 3(dy+1) + 9(dz+1); single-level meshes
+};
+
 struct BatchedState;
 
 void batched_destroy(BatchedState *b);
 void batched_mesh_changed(BatchedState *b);
+
+// Launches one fused stage: src -> dst for every block and variable.
+// FP64 checksums: per-block serial sums into partials[var][block], then
+// finalize into sums[var]; FP32: exact fixed-point into acc[var][2].
+template <typename T>
+int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
+                         const BItem *items, int n_blocks, int grid,
+                         int write_ghosts, int do_cs, double *partials,
+                         double *sums, unsigned long long *acc,
+                         unsigned *err, cudaStream_t s);
+// Persistent grid size for the stage kernel (CTAs resident at once).
+template <typename T>
+int batched_grid(const Geom &g, int stencil, int n_items);
 
 }  // namespace mamr

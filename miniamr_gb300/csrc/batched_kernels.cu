@@ -1,12 +1,363 @@
+// Batched stage kernel: one persistent launch per stage covering every
+// (block, variable) item.  Each item stages its block-variable in shared
+// memory with a ghost layer gathered straight from the neighbours'
+// interiors in the source pool -- the values comm() would have written
+// (same-level copy, coarse/4 prolongation, 4-cell restriction sum,
+// reflection; ref/comm.c:1465-1965) -- applies the stencil in the
+// reference's operation order (ref/stencil.c:82-144), writes the interior
+// to the destination pool and folds the checksum of the result
+// (ref/check_sum.c:44-53) into the same pass.
+//
+// Exactness: face ghosts are exact for every mesh.  27-point edge and
+// corner ghosts are resolved axis by axis (neighbour across each
+// out-of-range axis, reflection where that axis is a domain boundary),
+// which is what comm()'s x, y, z sweeps compose to when all blocks share
+// one level; the host only selects this path for 27-point stencils on such
+// meshes.
 #include "batched.h"
+#include "arith.cuh"
 
 namespace mamr {
 
-struct BatchedState {
-   int dummy;
-};
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; };
+template <> struct Vec16<double> { using type = double2; };
 
-void batched_destroy(BatchedState *b) { delete b; }
-void batched_mesh_changed(BatchedState *b) { (void) b; }
+// Shared-memory row length: column KO holds k = 0 so that k = 1 starts a
+// 16-byte vector.
+__host__ __device__ inline int tile_zs(int nz, int vw)
+{
+   return ((vw - 1 + nz + 2 + vw - 1) / vw) * vw;
+}
+
+template <typename T>
+__host__ __device__ inline size_t tile_bytes(const Geom &g)
+{
+   const int vw = 16 / (int) sizeof(T);
+   return (size_t) g.X * g.Y * tile_zs(g.nz, vw) * sizeof(T);
+}
+
+__device__ __forceinline__ long long fcell(const Geom &g, int dir, int nc,
+                                           int a, int b)
+{
+   if (dir == 0) return cell_offset(g, nc, a, b);
+   if (dir == 1) return cell_offset(g, a, nc, b);
+   return cell_offset(g, a, b, nc);
+}
+
+template <typename T, int ST>
+__global__ void __launch_bounds__(256)
+batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
+                     const BItem *__restrict__ items, int nb,
+                     int write_ghosts, int do_cs,
+                     double *__restrict__ partials,
+                     unsigned long long *__restrict__ acc,
+                     unsigned *__restrict__ err)
+{
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   __shared__ BItem sI;
+   T *tile = reinterpret_cast<T *>(smem_raw);
+   constexpr int VW = 16 / (int) sizeof(T), KO = VW - 1;
+   const int nx = g.nx, ny = g.ny, nz = g.nz, Y = g.Y;
+   const int Zs = tile_zs(nz, VW);
+#define TS(i, j, k) tile[((i) * Y + (j)) * Zs + KO + (k)]
+   const int n_items = nb * g.V;
+   const int nvec = nz / VW;
+   const bool vec = (nz % VW) == 0;
+
+   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+      const int var = it / nb, b = it - var * nb;
+      {
+         const int32_t *from = reinterpret_cast<const int32_t *>(items + b);
+         int32_t *to = reinterpret_cast<int32_t *>(&sI);
+         for (int q = threadIdx.x; q < (int) (sizeof(BItem) / 4);
+              q += blockDim.x)
+            to[q] = from[q];
+      }
+      __syncthreads();
+      const T *s = src + bv_offset(g, sI.slot, var);
+      T *d = dst + bv_offset(g, sI.slot, var);
+
+      // interior rows, 16-byte vectors (rows start on a sector boundary)
+      if (vec) {
+         using V = typename Vec16<T>::type;
+         for (int e = threadIdx.x; e < nx * ny * nvec; e += blockDim.x) {
+            int r = e / nvec, q = e - r * nvec;
+            int i = r / ny + 1, j = r - (i - 1) * ny + 1;
+            V v = __ldg(reinterpret_cast<const V *>(s + cell_offset(g, i, j, 1)) + q);
+            *reinterpret_cast<V *>(&TS(i, j, 1 + q * VW)) = v;
+         }
+      } else {
+         for (int e = threadIdx.x; e < nx * ny * nz; e += blockDim.x) {
+            int r = e / nz, k = e - r * nz + 1;
+            int i = r / ny + 1, j = r - (i - 1) * ny + 1;
+            TS(i, j, k) = s[cell_offset(g, i, j, k)];
+         }
+      }
+
+      // face ghosts (tangential interior), one face per pass
+      for (int l = 0; l < 6; l++) {
+         const int dir = l >> 1;
+         const bool low = !(l & 1);
+         const int n = dir == 0 ? nx : (dir == 1 ? ny : nz);
+         const int na = dir == 0 ? ny : nx;
+         const int nbb = dir == 2 ? ny : nz;
+         const int type = sI.f[l].type;
+         const int gn = low ? 0 : n + 1;
+         for (int e = threadIdx.x; e < na * nbb; e += blockDim.x) {
+            const int a = e / nbb + 1, bq = e - (a - 1) * nbb + 1;
+            T v;
+            if (type == FACE_SAME) {
+               v = src[bv_offset(g, sI.f[l].nb[0], var) +
+                       fcell(g, dir, low ? n : 1, a, bq)];
+            } else if (type == FACE_BC) {
+               v = s[fcell(g, dir, low ? 1 : n, a, bq)];
+            } else if (type == FACE_COARSE) {
+               const int ha = na / 2, hb = nbb / 2;
+               v = quarter(src[bv_offset(g, sI.f[l].nb[0], var) +
+                               fcell(g, dir, low ? n : 1,
+                                     (a + 1) / 2 + sI.f[l].jq * ha,
+                                     (bq + 1) / 2 + sI.f[l].iq * hb)]);
+            } else {
+               const int ha = na / 2, hb = nbb / 2;
+               const int jq = a > ha, iq = bq > hb;
+               const int a2 = a - jq * ha, b2 = bq - iq * hb;
+               const int p = low ? n : 1;
+               const T *f = src + bv_offset(g, sI.f[l].nb[iq * 2 + jq], var);
+               T t = f[fcell(g, dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
+                     f[fcell(g, dir, p, 2 * a2 - 1, 2 * b2)];
+               t = t + f[fcell(g, dir, p, 2 * a2, 2 * b2 - 1)];
+               t = t + f[fcell(g, dir, p, 2 * a2, 2 * b2)];
+               v = t;
+            }
+            int gi, gj, gk;
+            if (dir == 0) { gi = gn; gj = a; gk = bq; }
+            else if (dir == 1) { gi = a; gj = gn; gk = bq; }
+            else { gi = a; gj = bq; gk = gn; }
+            TS(gi, gj, gk) = v;
+            if (write_ghosts)
+               d[cell_offset(g, gi, gj, gk)] = v;
+         }
+      }
+
+      if (ST == 27) {
+         // 12 edges and 8 corners, resolved axis by axis
+         const int ne = 4 * (nx + ny + nz) + 8;
+         for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+            int gi, gj, gk;
+            if (e < 4 * nz) {
+               int q = e / nz;
+               gk = e - q * nz + 1;
+               gi = (q & 1) ? nx + 1 : 0;
+               gj = (q & 2) ? ny + 1 : 0;
+            } else if (e < 4 * (nz + ny)) {
+               int e2 = e - 4 * nz, q = e2 / ny;
+               gj = e2 - q * ny + 1;
+               gi = (q & 1) ? nx + 1 : 0;
+               gk = (q & 2) ? nz + 1 : 0;
+            } else if (e < 4 * (nz + ny + nx)) {
+               int e2 = e - 4 * (nz + ny), q = e2 / nx;
+               gi = e2 - q * nx + 1;
+               gj = (q & 1) ? ny + 1 : 0;
+               gk = (q & 2) ? nz + 1 : 0;
+            } else {
+               int q = e - 4 * (nx + ny + nz);
+               gi = (q & 1) ? nx + 1 : 0;
+               gj = (q & 2) ? ny + 1 : 0;
+               gk = (q & 4) ? nz + 1 : 0;
+            }
+            int dx = gi == 0 ? -1 : (gi == nx + 1 ? 1 : 0);
+            int dy = gj == 0 ? -1 : (gj == ny + 1 ? 1 : 0);
+            int dz = gk == 0 ? -1 : (gk == nz + 1 ? 1 : 0);
+            int si = gi, sj = gj, sk = gk;
+            if (dx) {
+               if (sI.bmask & (1 << (dx < 0 ? 0 : 1))) { si = dx < 0 ? 1 : nx; dx = 0; }
+               else si = dx < 0 ? nx : 1;
+            }
+            if (dy) {
+               if (sI.bmask & (1 << (dy < 0 ? 2 : 3))) { sj = dy < 0 ? 1 : ny; dy = 0; }
+               else sj = dy < 0 ? ny : 1;
+            }
+            if (dz) {
+               if (sI.bmask & (1 << (dz < 0 ? 4 : 5))) { sk = dz < 0 ? 1 : nz; dz = 0; }
+               else sk = dz < 0 ? nz : 1;
+            }
+            const int nbs = sI.nb27[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)];
+            const T v = src[bv_offset(g, nbs, var) + cell_offset(g, si, sj, sk)];
+            TS(gi, gj, gk) = v;
+            if (write_ghosts)
+               d[cell_offset(g, gi, gj, gk)] = v;
+         }
+      }
+      __syncthreads();
+
+      // stencil, one (j, k) column per thread sweeping i
+      unsigned long long lo = 0, hi = 0;
+      bool ok = true;
+      for (int col = threadIdx.x; col < ny * nz; col += blockDim.x) {
+         const int j = col / nz + 1, k = col - (j - 1) * nz + 1;
+         if (ST == 7) {
+            T am = TS(0, j, k), ac = TS(1, j, k);
+            for (int i = 1; i <= nx; i++) {
+               const T ap = TS(i + 1, j, k);
+               T w = am + TS(i, j - 1, k);
+               w = w + TS(i, j, k - 1);
+               w = w + ac;
+               w = w + TS(i, j, k + 1);
+               w = w + TS(i, j + 1, k);
+               w = w + ap;
+               const T out = div7(w);
+               d[cell_offset(g, i, j, k)] = out;
+               if (sizeof(T) == 4 && do_cs) {
+                  long long q;
+                  ok &= fixed52((float) out, q);
+                  acc128_add(lo, hi, q);
+               }
+               am = ac;
+               ac = ap;
+            }
+         } else {
+            auto S = [&](int p) -> T {
+               T t = TS(p, j - 1, k - 1) + TS(p, j - 1, k);
+               t = t + TS(p, j - 1, k + 1);
+               t = t + TS(p, j, k - 1);
+               t = t + TS(p, j, k);
+               t = t + TS(p, j, k + 1);
+               t = t + TS(p, j + 1, k - 1);
+               t = t + TS(p, j + 1, k);
+               t = t + TS(p, j + 1, k + 1);
+               return t;
+            };
+            T s0 = S(0), s1 = S(1);
+            for (int i = 1; i <= nx; i++) {
+               const T s2 = S(i + 1);
+               const T out = div27((s0 + s1) + s2);
+               d[cell_offset(g, i, j, k)] = out;
+               if (sizeof(T) == 4 && do_cs) {
+                  long long q;
+                  ok &= fixed52((float) out, q);
+                  acc128_add(lo, hi, q);
+               }
+               s0 = s1;
+               s1 = s2;
+            }
+         }
+      }
+      if (do_cs) {
+         if (sizeof(T) == 4) {
+            if (!ok)
+               atomicOr(err, ERR_FIXED_RANGE);
+            block_acc128_flush(lo, hi, acc + 2 * var);
+         } else {
+            // the reference's order: serial over i, j, k of this block
+            __syncthreads();
+            if (threadIdx.x == 0) {
+               double bs = 0.0;
+               for (int i = 1; i <= nx; i++)
+                  for (int j = 1; j <= ny; j++) {
+                     const T *row = d + cell_offset(g, i, j, 1);
+#pragma unroll 8
+                     for (int k = 0; k < nz; k++)
+                        bs = bs + (double) row[k];
+                  }
+               partials[(size_t) var * nb + b] = bs;
+            }
+         }
+      }
+      __syncthreads();
+   }
+#undef TS
+}
+
+// Sum over blocks in sorted_list order, one thread per variable.
+__global__ void finalize_fp64(const double *__restrict__ partials, int nb,
+                              int V, double *__restrict__ sums)
+{
+   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V;
+        v += gridDim.x * blockDim.x) {
+      const double *p = partials + (size_t) v * nb;
+      double s = 0.0;
+#pragma unroll 8
+      for (int b = 0; b < nb; b++)
+         s = s + p[b];
+      sums[v] = s;
+   }
+}
+
+template <typename T, int ST>
+static void set_smem(size_t bytes)
+{
+   cudaFuncSetAttribute(batched_stage_kernel<T, ST>,
+                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                        (int) bytes);
+}
+
+static int block_threads(const Geom &g)
+{
+   int t = g.ny * g.nz;
+   return t >= 256 ? 256 : ((t + 31) / 32) * 32;
+}
+
+template <typename T>
+int batched_grid(const Geom &g, int stencil, int n_items)
+{
+   const size_t smem = tile_bytes<T>(g);
+   int per_sm = 0, dev = 0, sms = 0;
+   const int thr = block_threads(g);
+   cudaGetDevice(&dev);
+   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+   if (stencil == 7) {
+      set_smem<T, 7>(smem);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+         &per_sm, batched_stage_kernel<T, 7>, thr, smem);
+   } else {
+      set_smem<T, 27>(smem);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+         &per_sm, batched_stage_kernel<T, 27>, thr, smem);
+   }
+   long long grid = (long long) (per_sm > 0 ? per_sm : 1) * sms;
+   return (int) (grid < n_items ? grid : (n_items > 0 ? n_items : 1));
+}
+
+template <typename T>
+int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
+                         const BItem *items, int n_blocks, int grid,
+                         int write_ghosts, int do_cs, double *partials,
+                         double *sums, unsigned long long *acc,
+                         unsigned *err, cudaStream_t s)
+{
+   if (n_blocks == 0)
+      return 0;
+   const size_t smem = tile_bytes<T>(g);
+   const int thr = block_threads(g);
+   if (stencil == 7)
+      batched_stage_kernel<T, 7><<<grid, thr, smem, s>>>(
+         src, dst, g, items, n_blocks, write_ghosts, do_cs, partials, acc,
+         err);
+   else
+      batched_stage_kernel<T, 27><<<grid, thr, smem, s>>>(
+         src, dst, g, items, n_blocks, write_ghosts, do_cs, partials, acc,
+         err);
+   int launches = 1;
+   if (do_cs && sizeof(T) == 8) {
+      finalize_fp64<<<(g.V + 127) / 128, 128, 0, s>>>(partials, n_blocks,
+                                                       g.V, sums);
+      launches++;
+   }
+   return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
+}
+
+template int batched_grid<float>(const Geom &, int, int);
+template int batched_grid<double>(const Geom &, int, int);
+template int launch_batched_stage<float>(const float *, float *, const Geom &,
+                                         int, const BItem *, int, int, int,
+                                         int, double *, double *,
+                                         unsigned long long *, unsigned *,
+                                         cudaStream_t);
+template int launch_batched_stage<double>(const double *, double *,
+                                          const Geom &, int, const BItem *,
+                                          int, int, int, int, double *,
+                                          double *, unsigned long long *,
+                                          unsigned *, cudaStream_t);
 
 }  // namespace mamr

@@ -370,108 +370,132 @@ static void apply_bc(mamr_ctx *c, int l, int n, int start, int num)
 static const int permutations[6][3] = { {0, 1, 2}, {1, 2, 0}, {2, 0, 1},
                                         {0, 2, 1}, {1, 0, 2}, {2, 1, 0} };
 
-/* ref/comm.c:42-56,162-203: the on-rank part of comm() on one rank. */
+/* ref/comm.c:42-56,162-203: the on-rank part of comm() on one rank.
+ * Within one direction every ghost cell is written by exactly one face
+ * exchange and only planes that direction does not write are read, so the
+ * blocks of a direction may be visited in any order or concurrently
+ * (the reference's OpenMP variant threads this loop, openmp/comm.c:166). */
+static int comm_block(mamr_ctx *c, int in, int dir, int start, int num)
+{
+   const mamr_block *bp = &c->mesh[in];
+   int n = bp->slot, l, i, j, k, m;
+   for (l = dir * 2; l < dir * 2 + 2; l++) {
+      if (bp->nei_level[l] == bp->level) {
+         if ((m = bp->nei[l][0][0]) > n)
+            on_proc_comm(c, n, m, l, start, num);
+      } else if (bp->nei_level[l] == bp->level + 1) {
+         for (i = 0; i < 2; i++)
+            for (j = 0; j < 2; j++)
+               if ((m = bp->nei[l][i][j]) > n)
+                  on_proc_comm_diff(c, n, m, l, i, j, start, num);
+      } else if (bp->nei_level[l] == bp->level - 1) {
+         if ((m = bp->nei[l][0][0]) > n) {
+            /* blocks[m]: the coarse neighbour's record */
+            const mamr_block *mb = c->slot_pos[m] >= 0 ?
+                                   &c->mesh[c->slot_pos[m]] : NULL;
+            if (!mb)
+               return MAMR_EMESH;
+            k = dir * 2 + 1 - l % 2;
+            for (i = 0; i < 2; i++)
+               for (j = 0; j < 2; j++)
+                  if (mb->nei[k][i][j] == n)
+                     on_proc_comm_diff(c, m, n, k, i, j, start, num);
+         }
+      } else if (bp->nei_level[l] == -2) {
+         apply_bc(c, l, n, start, num);
+      } else {
+         return MAMR_EMESH;
+      }
+   }
+   return MAMR_OK;
+}
+
 int mamr_comm(mamr_ctx *c, int32_t start, int32_t num, int32_t stage)
 {
-   int o, dir, in, l, i, j, k, m, n;
+   int o, dir, in, bad = 0;
    if (!c)
       return fail(MAMR_EINVAL, "null context");
    if (start < 0 || num < 0 || start + num > c->cfg.num_vars)
       return fail(MAMR_EINVAL, "variable range out of bounds");
    for (o = 0; o < 3; o++) {
       dir = c->cfg.permute ? permutations[stage % 6][o] : o;
-      for (in = 0; in < c->n_mesh; in++) {
-         const mamr_block *bp = &c->mesh[in];
-         n = bp->slot;
-         for (l = dir * 2; l < dir * 2 + 2; l++) {
-            if (bp->nei_level[l] == bp->level) {
-               if ((m = bp->nei[l][0][0]) > n)
-                  on_proc_comm(c, n, m, l, start, num);
-            } else if (bp->nei_level[l] == bp->level + 1) {
-               for (i = 0; i < 2; i++)
-                  for (j = 0; j < 2; j++)
-                     if ((m = bp->nei[l][i][j]) > n)
-                        on_proc_comm_diff(c, n, m, l, i, j, start, num);
-            } else if (bp->nei_level[l] == bp->level - 1) {
-               if ((m = bp->nei[l][0][0]) > n) {
-                  /* blocks[m]: the coarse neighbour's record */
-                  const mamr_block *mb = c->slot_pos[m] >= 0 ?
-                                         &c->mesh[c->slot_pos[m]] : NULL;
-                  if (!mb)
-                     return fail(MAMR_EMESH, "neighbour slot %d not active",
-                                 m);
-                  k = dir * 2 + 1 - l % 2;
-                  for (i = 0; i < 2; i++)
-                     for (j = 0; j < 2; j++)
-                        if (mb->nei[k][i][j] == n)
-                           on_proc_comm_diff(c, m, n, k, i, j, start, num);
-               }
-            } else if (bp->nei_level[l] == -2) {
-               apply_bc(c, l, n, start, num);
-            } else {
-               return fail(MAMR_EMESH, "misconnected block");
-            }
-         }
-      }
+#pragma omp parallel for schedule(dynamic, 4) reduction(|:bad)
+      for (in = 0; in < c->n_mesh; in++)
+         bad |= comm_block(c, in, dir, start, num) != MAMR_OK;
+      if (bad)
+         return fail(MAMR_EMESH, "misconnected block");
    }
    return MAMR_OK;
 }
 
 /* ref/stencil.c:76-145 (stencil_calc), Jacobi update of every active
  * block's interior for one variable. */
+static void stencil_block(mamr_ctx *c, double *a, double *work)
+{
+   int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz, i, j, k;
+   for (i = 1; i <= nx; i++)
+      for (j = 1; j <= ny; j++)
+         for (k = 1; k <= nz; k++) {
+            double w;
+            if (c->cfg.stencil == 7) {
+               w = RF(c, AT(a, i - 1, j, k) + AT(a, i, j - 1, k));
+               w = RF(c, w + AT(a, i, j, k - 1));
+               w = RF(c, w + AT(a, i, j, k));
+               w = RF(c, w + AT(a, i, j, k + 1));
+               w = RF(c, w + AT(a, i, j + 1, k));
+               w = RF(c, w + AT(a, i + 1, j, k));
+               w = RF(c, w / 7.0);
+            } else {
+               double s[3];
+               int p, jj, kk;
+               for (p = 0; p < 3; p++) {
+                  double t = 0.0;
+                  int first = 1;
+                  for (jj = j - 1; jj <= j + 1; jj++)
+                     for (kk = k - 1; kk <= k + 1; kk++) {
+                        if (first) {
+                           t = AT(a, i - 1 + p, jj, kk);
+                           first = 0;
+                        } else
+                           t = RF(c, t + AT(a, i - 1 + p, jj, kk));
+                     }
+                  s[p] = t;
+               }
+               w = RF(c, RF(c, RF(c, s[0] + s[1]) + s[2]) / 27.0);
+            }
+            AT(work, i, j, k) = w;
+         }
+   for (i = 1; i <= nx; i++)
+      for (j = 1; j <= ny; j++)
+         for (k = 1; k <= nz; k++)
+            AT(a, i, j, k) = AT(work, i, j, k);
+}
+
+/* ref/stencil.c:76-145 (stencil_calc), Jacobi update of every active
+ * block's interior for one variable; blocks are independent (threaded over
+ * blocks as in openmp/stencil.c:84,107). */
 int mamr_stencil(mamr_ctx *c, int32_t var, int32_t calc_stage)
 {
-   int nx = c ? c->cfg.nx : 0, ny = c ? c->cfg.ny : 0, nz = c ? c->cfg.nz : 0;
-   int in, i, j, k;
-   double *work;
+   int bad = 0;
    (void) calc_stage;
    if (!c)
       return fail(MAMR_EINVAL, "null context");
    if (var < 0 || var >= c->cfg.num_vars)
       return fail(MAMR_EINVAL, "variable out of range");
-   work = (double *) malloc(sizeof(double) * c->bv);
-   if (!work)
-      return fail(MAMR_ENOMEM, "host allocation");
-   for (in = 0; in < c->n_mesh; in++) {
-      double *a = blk(c, c->mesh[in].slot, var);
-      for (i = 1; i <= nx; i++)
-         for (j = 1; j <= ny; j++)
-            for (k = 1; k <= nz; k++) {
-               double w;
-               if (c->cfg.stencil == 7) {
-                  w = RF(c, AT(a, i - 1, j, k) + AT(a, i, j - 1, k));
-                  w = RF(c, w + AT(a, i, j, k - 1));
-                  w = RF(c, w + AT(a, i, j, k));
-                  w = RF(c, w + AT(a, i, j, k + 1));
-                  w = RF(c, w + AT(a, i, j + 1, k));
-                  w = RF(c, w + AT(a, i + 1, j, k));
-                  w = RF(c, w / 7.0);
-               } else {
-                  double s[3];
-                  int p, jj, kk;
-                  for (p = 0; p < 3; p++) {
-                     double t = 0.0;
-                     int first = 1;
-                     for (jj = j - 1; jj <= j + 1; jj++)
-                        for (kk = k - 1; kk <= k + 1; kk++) {
-                           if (first) {
-                              t = AT(a, i - 1 + p, jj, kk);
-                              first = 0;
-                           } else
-                              t = RF(c, t + AT(a, i - 1 + p, jj, kk));
-                        }
-                     s[p] = t;
-                  }
-                  w = RF(c, RF(c, RF(c, s[0] + s[1]) + s[2]) / 27.0);
-               }
-               AT(work, i, j, k) = w;
-            }
-      for (i = 1; i <= nx; i++)
-         for (j = 1; j <= ny; j++)
-            for (k = 1; k <= nz; k++)
-               AT(a, i, j, k) = AT(work, i, j, k);
+#pragma omp parallel reduction(|:bad)
+   {
+      double *work = (double *) malloc(sizeof(double) * c->bv);
+      int in;
+      if (!work)
+         bad = 1;
+#pragma omp for schedule(dynamic, 4)
+      for (in = 0; in < c->n_mesh; in++)
+         if (work)
+            stencil_block(c, blk(c, c->mesh[in].slot, var), work);
+      free(work);
    }
-   free(work);
+   if (bad)
+      return fail(MAMR_ENOMEM, "host allocation");
    return MAMR_OK;
 }
 
@@ -480,8 +504,10 @@ int mamr_stencil(mamr_ctx *c, int32_t var, int32_t calc_stage)
  * cell is not finite or |v| >= 2^10 (outside the fixed-point range). */
 static int fixed_cell(double v, int64_t *out)
 {
-   if (!(fabs(v) < 1024.0))
+   if (!(fabs(v) < 1024.0)) {
+      *out = 0;
       return -1;
+   }
    *out = (int64_t) (v * 0x1p52);
    return 0;
 }
@@ -491,40 +517,60 @@ static double fixed128_to_double(__int128 acc)
    return (double) acc * 0x1p-52;
 }
 
-/* ref/check_sum.c:36-65. */
+/* ref/check_sum.c:36-65.  Block sums may be formed concurrently; they are
+ * added serially in sorted_list order. */
 int mamr_check_sum(mamr_ctx *c, int32_t var, double *sum)
 {
-   int in, i, j, k;
+   int in, bad = 0;
    if (!c || !sum)
       return fail(MAMR_EINVAL, "null argument");
    if (var < 0 || var >= c->cfg.num_vars)
       return fail(MAMR_EINVAL, "variable out of range");
    if (!c->fp32) {
-      double s = 0.0, block_sum;
+      double s = 0.0, *bs = (double *) malloc(sizeof(double) *
+                                              (c->n_mesh ? c->n_mesh : 1));
+      if (!bs)
+         return fail(MAMR_ENOMEM, "host allocation");
+#pragma omp parallel for schedule(dynamic, 8)
       for (in = 0; in < c->n_mesh; in++) {
          const double *a = blk(c, c->mesh[in].slot, var);
-         block_sum = 0.0;
+         double block_sum = 0.0;
+         int i, j, k;
          for (i = 1; i <= c->cfg.nx; i++)
             for (j = 1; j <= c->cfg.ny; j++)
                for (k = 1; k <= c->cfg.nz; k++)
                   block_sum += AT(a, i, j, k);
-         s += block_sum;
+         bs[in] = block_sum;
       }
+      for (in = 0; in < c->n_mesh; in++)
+         s += bs[in];
+      free(bs);
       *sum = s;
    } else {
-      __int128 acc = 0;
+      __int128 acc = 0, *bs = (__int128 *) malloc(sizeof(__int128) *
+                                                 (c->n_mesh ? c->n_mesh : 1));
+      if (!bs)
+         return fail(MAMR_ENOMEM, "host allocation");
+#pragma omp parallel for schedule(dynamic, 8) reduction(|:bad)
       for (in = 0; in < c->n_mesh; in++) {
          const double *a = blk(c, c->mesh[in].slot, var);
+         __int128 t = 0;
+         int i, j, k;
          for (i = 1; i <= c->cfg.nx; i++)
             for (j = 1; j <= c->cfg.ny; j++)
                for (k = 1; k <= c->cfg.nz; k++) {
                   int64_t q;
                   if (fixed_cell(AT(a, i, j, k), &q))
-                     return fail(MAMR_EDEVICE,
-                                 "cell outside the fixed-point range");
-                  acc += q;
+                     bad = 1;
+                  t += q;
                }
+         bs[in] = t;
       }
+      for (in = 0; in < c->n_mesh; in++)
+         acc += bs[in];
+      free(bs);
+      if (bad)
+         return fail(MAMR_EDEVICE, "cell outside the fixed-point range");
       *sum = fixed128_to_double(acc);
    }
    return MAMR_OK;

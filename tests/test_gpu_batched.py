@@ -1,0 +1,79 @@
+"""The batched path (one fused ghost+stencil+checksum launch per stage,
+ping-pong pools, optional CUDA graph) against the plain per-call path:
+every cell and every checksum bit-identical."""
+import numpy as np
+import pytest
+
+from golden_util import trace_path
+from miniamr_gb300 import mesh as meshmod
+from miniamr_gb300.abi import (FP32, FP64, RUN_BATCHED, RUN_GRAPH, Config,
+                               MamrError)
+from miniamr_gb300.trace import read_trace, replay
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, dtype=np.float64).view(np.uint64)
+
+
+UNIFORM = [
+    ((2, 2, 2), (8, 8, 8), 3, 7, 1),
+    ((2, 2, 2), (8, 8, 8), 3, 27, 1),
+    ((2, 1, 2), (16, 16, 16), 2, 7, 1),
+    ((1, 2, 2), (16, 16, 16), 2, 27, 1),
+    ((3, 1, 2), (4, 6, 8), 2, 27, 1),
+    ((2, 2, 1), (6, 6, 6), 2, 7, 0),
+]
+
+
+@pytest.mark.parametrize("flags", [RUN_BATCHED, RUN_BATCHED | RUN_GRAPH])
+@pytest.mark.parametrize("dtype", [FP64, FP32])
+@pytest.mark.parametrize("case", UNIFORM)
+def test_batched_equals_plain_uniform(gpu_lib, case, dtype, flags):
+    (ix, iy, iz), (nx, ny, nz), V, st, passes = case
+    n0 = ix * iy * iz
+    cap = n0 * (1 + 8 ** passes) + 8
+    cfg = Config.make(nx, ny, nz, V, cap, stencil=st, dtype=dtype)
+    init = gpu_lib.initial_values(cfg, n0)
+    outs = []
+    for fl in (0, flags):
+        m = meshmod.initial_mesh(ix, iy, iz, passes, cap)
+        with gpu_lib.context(cfg) as ctx:
+            ctx.upload(np.arange(n0), init)
+            for _ in range(passes):
+                ctx.split(m.split_all())
+            ctx.set_mesh(m.blocks())
+            s1 = ctx.run_timesteps(2, 3, 2, flags=fl)
+            s2 = ctx.run_timesteps(1, 3, 1, first_stage=6, flags=fl)
+            outs.append((s1, s2, ctx.download(np.arange(cap))))
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(bits(a), bits(b))
+
+
+@pytest.mark.parametrize("name", ["amr7", "amr7_objects"])
+@pytest.mark.parametrize("dtype", [FP64, FP32])
+def test_batched_equals_plain_amr7(gpu_lib, name, dtype):
+    """7-point stencil on the reference's own multi-level meshes (states
+    reached by replaying its recorded runs): face ghosts across level jumps
+    (coarse/4 and 4-cell sums) gathered inside the fused kernel."""
+    recs = read_trace(trace_path(name))
+    outs = []
+    for fl in (0, RUN_BATCHED | RUN_GRAPH):
+        res = replay(gpu_lib, recs, dtype=dtype)
+        assert len(np.unique(res.mesh["level"])) > 1
+        s = res.ctx.run_timesteps(2, 2, 1, flags=fl)
+        cap = res.ctx.cfg.max_blocks
+        outs.append((s, res.ctx.download(np.arange(cap))))
+        res.ctx.close()
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(bits(a), bits(b))
+
+
+def test_batched_27_multilevel_is_refused(gpu_lib):
+    recs = read_trace(trace_path("amr27"))
+    res = replay(gpu_lib, recs)
+    with pytest.raises(MamrError) as e:
+        res.ctx.run_timesteps(1, 1, 1, flags=RUN_BATCHED)
+    assert e.value.status == -5
+    res.ctx.close()
