@@ -197,6 +197,38 @@ int mamr_launch_count(mamr_ctx *ctx, int64_t *count);
 int mamr_initial_values(const mamr_config *cfg, int32_t n_blocks,
                         double *out);
 
+/* ---- allocation-free checksum ------------------------------------------ */
+
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory -- e.g. code whose device memory is all reserved up front by
+ * another allocator (a framework's caching allocator, a serving process
+ * with a fixed arena), or a latency-critical path that must not risk the
+ * device-wide synchronisation an allocation can bring.  It computes the same
+ * FP64 checksum as mamr_check_sum() (the reference's summation order, bit
+ * for bit) over blocks the caller already holds on the device, and
+ * allocates nothing: its only scratch, one partial sum per block, is a
+ * file-scope device array of MAMR_STATIC_MAX_BLOCKS doubles (512 KiB) that
+ * every GPU loading this library keeps until the process exits.
+ *
+ *   blocks   device pointer: FP64 cells in the dense layout of the host
+ *            buffers above, [slot][num_vars][nx+2][ny+2][nz+2]
+ *   cfg      nx, ny, nz and num_vars of that layout (other fields unused)
+ *   slots    device pointer: n_blocks slots in sorted_list order
+ *   sum      device pointer that receives the checksum of variable var
+ *   stream   cudaStream_t the two kernels are queued on (NULL: default)
+ *
+ * n_blocks above MAMR_STATIC_MAX_BLOCKS is rejected with MAMR_EINVAL.  The
+ * first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls on a device share the one array:
+ * calls that overlap on the GPU (other streams, other host threads) race
+ * and give wrong sums, so keep them ordered.  Every partial is written
+ * before it is read, so no clearing is needed between calls. */
+#define MAMR_STATIC_MAX_BLOCKS 65536
+int mamr_check_sum_fp64_noalloc(const double *blocks, const mamr_config *cfg,
+                                const int32_t *slots, int32_t n_blocks,
+                                int32_t var, double *sum, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,6 +32,15 @@ static int fail(int code, const char *fmt, ...)
 
 extern "C" const char *mamr_last_error(void) { return g_err; }
 
+int mamr::report_error(int code, const char *fmt, ...)
+{
+   va_list ap;
+   va_start(ap, fmt);
+   vsnprintf(g_err, sizeof(g_err), fmt, ap);
+   va_end(ap);
+   return code;
+}
+
 #define CUDA_TRY(x)                                                         \
    do {                                                                     \
       cudaError_t e_ = (x);                                                 \

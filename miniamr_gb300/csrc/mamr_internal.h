@@ -53,6 +53,9 @@ enum : unsigned {
    ERR_TASK = 2u           // a task that does not fit the geometry
 };
 
+// Records a failure for mamr_last_error() and returns code.
+int report_error(int code, const char *fmt, ...);
+
 // Kernel launchers (plain path).  All return the launch count they issued
 // (>= 0) or -1 after a launch error (cudaGetLastError is left set).
 template <typename T>
