@@ -181,6 +181,30 @@ def oracle_rate(steps, threads=None):
     return steps * SPT * n0 * 8 * N ** 3 * V / dt, threads, dt
 
 
+def profile_case(name):
+    """Small batched run for ncu captures: 4096 blocks of 16^3, 4 vars
+    (268 MB of FP32 interior cells per pool, twice the L2), four stages
+    launched one by one."""
+    global V, UPD_PER_STAGE
+    import torch
+    from miniamr_gb300 import build, load
+    from miniamr_gb300.abi import FP32, FP64, RUN_BATCHED
+    global STENCIL
+    dtype = FP32 if name.startswith("fp32") else FP64
+    STENCIL = 27 if name.endswith("27") else 7
+    V = 4
+    UPD_PER_STAGE = N_BLOCKS * N ** 3 * V
+    build.build_library()
+    lib = load()
+    ctx, _ = build_mesh(lib, dtype)
+    ctx.run_timesteps(1, 2, 1, flags=RUN_BATCHED)
+    ctx.run_timesteps(1, 2, 1, first_stage=2, flags=RUN_BATCHED)
+    torch.cuda.synchronize()
+    ctx.close()
+    print(f"profile case {name}: 4 batched stages, {V} vars")
+    return 0
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -229,7 +253,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=None,
                     help="timesteps of the FP64 comparison runs")
+    ap.add_argument("--profile-case", default=None,
+                    choices=["fp32_27", "fp32_7", "fp64_27", "fp64_7"],
+                    help="a small case for ncu: the 4096-block mesh with 4 "
+                         "variables, 2 warm-up + 2 profiled batched stages "
+                         "launched without a graph")
     args = ap.parse_args()
+    if args.profile_case:
+        return profile_case(args.profile_case)
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":
         return reference_arm(args, world, rank, pg)
