@@ -197,6 +197,16 @@ int mamr_launch_count(mamr_ctx *ctx, int64_t *count);
 int mamr_initial_values(const mamr_config *cfg, int32_t n_blocks,
                         double *out);
 
+/* ---- diagnostics --------------------------------------------------------- */
+
+/* Device self-test of the division routines (no counterpart in the
+ * reference): mismatches[0..1] count floats in [1, 2) where a three-step
+ * remainder-corrected x/7 and x/27 differ from IEEE FP32 division;
+ * mismatches[2..3] count, over n_fp64 hashed doubles (all exponent
+ * classes), where the FP64 kernels' x/7 and x/27 differ from IEEE FP64
+ * division.  Runs on the current device. */
+int mamr_selftest_division(int64_t n_fp64, int64_t *mismatches);
+
 /* ---- allocation-free checksum ------------------------------------------ */
 
 /* No counterpart in the reference.  For callers that cannot allocate device

@@ -93,18 +93,19 @@ const int kPerm[6][3] = { {0, 1, 2}, {1, 2, 0}, {2, 0, 1},
 
 namespace mamr {
 struct BatchedState {
-   DevBuf items, partials, sums, acc;
+   DevBuf items, partials, sums, acc, chain, pencils;
    int n = 0;
    bool valid = false;
    bool single_level = false;
    int grid = 0;
+   int n_pencils = 0;     // > 0: the pencil kernel applies
 };
 void batched_destroy(BatchedState *b)
 {
    if (!b)
       return;
    b->items.release(); b->partials.release(); b->sums.release();
-   b->acc.release();
+   b->acc.release(); b->chain.release(); b->pencils.release();
    delete b;
 }
 void batched_mesh_changed(BatchedState *b)
@@ -826,6 +827,49 @@ static int build_items(mamr_ctx *c)
                   cur >= 0 ? cur : bp.slot;
             }
    }
+   // Pencils: chains of blocks along z from a lower z boundary to an upper
+   // one, for single-level meshes of 16^3 blocks; every block must lie on
+   // exactly one chain.
+   std::vector<int32_t> chain;
+   std::vector<int2> pencils;
+   B->n_pencils = 0;
+   if (single && n > 0 && c->g.nx == 16 && c->g.ny == 16 && c->g.nz == 16) {
+      std::vector<char> seen(n, 0);
+      bool ok = true;
+      for (int q = 0; q < n && ok; q++) {
+         if (!(items[q].bmask & (1 << 4)))
+            continue;
+         int2 pc;
+         pc.x = (int) chain.size();
+         int cur = q;
+         while (ok) {
+            if (seen[cur]) { ok = false; break; }
+            seen[cur] = 1;
+            chain.push_back(cur);
+            if (items[cur].bmask & (1 << 5))
+               break;
+            const int up = items[cur].f[5].nb[0];
+            cur = c->slot_pos[up];
+            if (cur < 0)
+               ok = false;
+         }
+         pc.y = (int) chain.size() - pc.x;
+         pencils.push_back(pc);
+      }
+      for (int q = 0; q < n && ok; q++)
+         ok = seen[q] != 0;
+      if (ok) {
+         CUDA_TRY(B->chain.ensure(sizeof(int32_t) * chain.size()));
+         CUDA_TRY(B->pencils.ensure(sizeof(int2) * pencils.size()));
+         CUDA_TRY(cudaMemcpyAsync(B->chain.p, chain.data(),
+                                  sizeof(int32_t) * chain.size(),
+                                  cudaMemcpyHostToDevice, c->stream));
+         CUDA_TRY(cudaMemcpyAsync(B->pencils.p, pencils.data(),
+                                  sizeof(int2) * pencils.size(),
+                                  cudaMemcpyHostToDevice, c->stream));
+         B->n_pencils = (int) pencils.size();
+      }
+   }
    CUDA_TRY(B->items.ensure(sizeof(BItem) * items.size()));
    CUDA_TRY(cudaMemcpyAsync(B->items.p, items.data(),
                             sizeof(BItem) * items.size(),
@@ -880,8 +924,13 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       CUDA_TRY(B->partials.ensure(sizeof(double) * std::max(1, nb) * V));
       CUDA_TRY(B->sums.ensure(sizeof(double) * std::max<size_t>(1, n_cs * V)));
    }
-   const int grid = c->fp32 ? batched_grid<float>(c->g, c->cfg.stencil, nb * V)
-                            : batched_grid<double>(c->g, c->cfg.stencil, nb * V);
+   const bool pencil = B->n_pencils > 0;
+   const int np = B->n_pencils;
+   const int grid =
+      pencil ? (c->fp32 ? pencil_grid<float>(c->cfg.stencil, np * V)
+                        : pencil_grid<double>(c->cfg.stencil, np * V))
+             : (c->fp32 ? batched_grid<float>(c->g, c->cfg.stencil, nb * V)
+                        : batched_grid<double>(c->g, c->cfg.stencil, nb * V));
    CUDA_TRY(cudaGetLastError());
 
    cudaGraph_t g_graph = nullptr;
@@ -897,7 +946,26 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
          const bool do_cs = freq && !(st % freq);
          const int last = (q == total - 1);
          int k;
-         if (c->fp32)
+         if (pencil && c->fp32)
+            k = launch_pencil_stage((const float *) cur, (float *) oth, c->g,
+                                    c->cfg.stencil,
+                                    (const BItem *) B->items.p, nb,
+                                    (const int32_t *) B->chain.p,
+                                    (const int2 *) B->pencils.p, np, grid,
+                                    last, do_cs, nullptr, nullptr,
+                                    (unsigned long long *) B->acc.p +
+                                       (size_t) cnt * V * 2,
+                                    c->d_err, c->stream);
+         else if (pencil)
+            k = launch_pencil_stage((const double *) cur, (double *) oth,
+                                    c->g, c->cfg.stencil,
+                                    (const BItem *) B->items.p, nb,
+                                    (const int32_t *) B->chain.p,
+                                    (const int2 *) B->pencils.p, np, grid,
+                                    last, do_cs, (double *) B->partials.p,
+                                    (double *) B->sums.p + (size_t) cnt * V,
+                                    nullptr, c->d_err, c->stream);
+         else if (c->fp32)
             k = launch_batched_stage((const float *) cur, (float *) oth, c->g,
                                      c->cfg.stencil,
                                      (const BItem *) B->items.p, nb, grid,

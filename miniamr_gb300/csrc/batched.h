@@ -50,4 +50,19 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
 template <typename T>
 int batched_grid(const Geom &g, int stencil, int n_items);
 
+// Pencil variant for single-level meshes of 16^3 blocks: CTAs walk chains
+// of blocks along z (chain[pencils[p].x .. +pencils[p].y) are indices into
+// items, bottom to top).  FP32 checksums are fused (acc); FP64 checksums
+// run as a separate all-variable pass into partials and sums.
+template <typename T>
+int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
+                        const BItem *items, int n_blocks,
+                        const int32_t *chain, const int2 *pencils,
+                        int n_pencils, int grid, int write_ghosts, int do_cs,
+                        double *partials, double *sums,
+                        unsigned long long *acc, unsigned *err,
+                        cudaStream_t s);
+template <typename T>
+int pencil_grid(int stencil, int n_work);
+
 }  // namespace mamr

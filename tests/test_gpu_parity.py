@@ -136,3 +136,18 @@ def test_errors_are_reported_and_context_survives(gpu_lib):
         assert ctx.check_sum(0) == 0.0   # context still usable
         with pytest.raises(MamrError):
             ctx.comm(1, 5, 0)
+
+
+def test_division_selftest(gpu_lib):
+    """The FP64 kernels' correctly rounded x/7 and x/27 equal IEEE division
+    on 2^26 hashed doubles of every exponent class (the FP32 column reports
+    whether the remainder-corrected FP32 quotient is exact on a full
+    binade; the FP32 kernels use IEEE division either way)."""
+    import ctypes as C
+    f = gpu_lib.lib.mamr_selftest_division
+    f.argtypes = [C.c_int64, C.POINTER(C.c_int64)]
+    f.restype = C.c_int
+    out = (C.c_int64 * 4)()
+    assert f(1 << 26, out) == 0
+    print("fp32 rc-division mismatches (7, 27):", out[0], out[1])
+    assert out[2] == 0 and out[3] == 0
