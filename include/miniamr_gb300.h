@@ -200,11 +200,10 @@ int mamr_initial_values(const mamr_config *cfg, int32_t n_blocks,
 /* ---- diagnostics --------------------------------------------------------- */
 
 /* Device self-test of the division routines (no counterpart in the
- * reference): mismatches[0..1] count floats in [1, 2) where a three-step
- * remainder-corrected x/7 and x/27 differ from IEEE FP32 division;
- * mismatches[2..3] count, over n_fp64 hashed doubles (all exponent
- * classes), where the FP64 kernels' x/7 and x/27 differ from IEEE FP64
- * division.  Runs on the current device. */
+ * reference): mismatches[0..1] count where the FP32 kernels' x/7 and x/27
+ * differ from IEEE FP32 division, over every float in [1, 2) plus 2^23
+ * hashed floats of all classes; mismatches[2..3] the same for the FP64
+ * kernels over n_fp64 hashed doubles.  Runs on the current device. */
 int mamr_selftest_division(int64_t n_fp64, int64_t *mismatches);
 
 /* ---- allocation-free checksum ------------------------------------------ */

@@ -186,9 +186,11 @@ extern "C" int mamr_create(const mamr_config *cfg, mamr_ctx **out)
    Geom &g = c->g;
    g.nx = cfg->nx; g.ny = cfg->ny; g.nz = cfg->nz; g.V = cfg->num_vars;
    g.X = g.nx + 2; g.Y = g.ny + 2; g.Z = g.nz + 2;
-   const int eps = 32 / (int) elem_size(c);      // elements per sector
-   g.koff = eps - 1;
-   g.Zp = ((g.koff + g.Z + eps - 1) / eps) * eps;
+   // k = 1 starts a 64-byte DRAM burst, and every row is a whole number
+   // of bursts: an interior row then costs exactly its own bytes
+   const int burst = 64 / (int) elem_size(c);    // elements per 64 bytes
+   g.koff = burst - 1;
+   g.Zp = ((g.koff + g.Z + burst - 1) / burst) * burst;
    g.bv = (long long) g.X * g.Y * g.Zp;
    size_t tile = (size_t) g.X * g.Y * g.Z * elem_size(c);
    if (tile > 200 * 1024) {
@@ -830,7 +832,7 @@ static int build_items(mamr_ctx *c)
    // Pencils: chains of blocks along z from a lower z boundary to an upper
    // one, for single-level meshes of 16^3 blocks; every block must lie on
    // exactly one chain.
-   std::vector<int32_t> chain;
+   std::vector<TileDesc> chain;
    std::vector<int2> pencils;
    B->n_pencils = 0;
    if (single && n > 0 && c->g.nx == 16 && c->g.ny == 16 && c->g.nz == 16) {
@@ -845,7 +847,12 @@ static int build_items(mamr_ctx *c)
          while (ok) {
             if (seen[cur]) { ok = false; break; }
             seen[cur] = 1;
-            chain.push_back(cur);
+            TileDesc td;
+            td.slot = items[cur].slot;
+            td.bmask = items[cur].bmask;
+            for (int d = 0; d < 9; d++)
+               td.nb9[d] = items[cur].nb27[9 + d];
+            chain.push_back(td);
             if (items[cur].bmask & (1 << 5))
                break;
             const int up = items[cur].f[5].nb[0];
@@ -854,15 +861,17 @@ static int build_items(mamr_ctx *c)
                ok = false;
          }
          pc.y = (int) chain.size() - pc.x;
+         if (pc.y > PENCIL_MAX)
+            ok = false;
          pencils.push_back(pc);
       }
       for (int q = 0; q < n && ok; q++)
          ok = seen[q] != 0;
       if (ok) {
-         CUDA_TRY(B->chain.ensure(sizeof(int32_t) * chain.size()));
+         CUDA_TRY(B->chain.ensure(sizeof(TileDesc) * chain.size()));
          CUDA_TRY(B->pencils.ensure(sizeof(int2) * pencils.size()));
          CUDA_TRY(cudaMemcpyAsync(B->chain.p, chain.data(),
-                                  sizeof(int32_t) * chain.size(),
+                                  sizeof(TileDesc) * chain.size(),
                                   cudaMemcpyHostToDevice, c->stream));
          CUDA_TRY(cudaMemcpyAsync(B->pencils.p, pencils.data(),
                                   sizeof(int2) * pencils.size(),
@@ -950,7 +959,7 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
             k = launch_pencil_stage((const float *) cur, (float *) oth, c->g,
                                     c->cfg.stencil,
                                     (const BItem *) B->items.p, nb,
-                                    (const int32_t *) B->chain.p,
+                                    (const TileDesc *) B->chain.p,
                                     (const int2 *) B->pencils.p, np, grid,
                                     last, do_cs, nullptr, nullptr,
                                     (unsigned long long *) B->acc.p +
@@ -960,7 +969,7 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
             k = launch_pencil_stage((const double *) cur, (double *) oth,
                                     c->g, c->cfg.stencil,
                                     (const BItem *) B->items.p, nb,
-                                    (const int32_t *) B->chain.p,
+                                    (const TileDesc *) B->chain.p,
                                     (const int2 *) B->pencils.p, np, grid,
                                     last, do_cs, (double *) B->partials.p,
                                     (double *) B->sums.p + (size_t) cnt * V,

@@ -18,7 +18,7 @@ namespace mamr {
 // rational arithmetic), so |x*y - x/c| < ulp(x/c)/2.  The argument needs x,
 // q0 and r away from underflow and overflow, so x outside biased exponents
 // (100, 2000) -- zero, tiny, huge, inf, nan -- takes the IEEE division.
-// tests/test_gpu_arith.py compares against IEEE division on the GPU.
+// mamr_selftest_division compares against IEEE division on the GPU.
 template <int C>
 __device__ __forceinline__ double div_const(double x);
 
@@ -50,10 +50,33 @@ __device__ __forceinline__ double div_const<27>(double x)
 
 __device__ __forceinline__ double div7(double x) { return div_const<7>(x); }
 __device__ __forceinline__ double div27(double x) { return div_const<27>(x); }
-// FP32: RN(1/7f) misses the faithfulness bound above (|y*7 - 1| =
-// 1.5 * 2^-25), so FP32 keeps the IEEE division (cheap on the FP32 pipes).
-__device__ __forceinline__ float div7(float x) { return __fdiv_rn(x, 7.0f); }
-__device__ __forceinline__ float div27(float x) { return __fdiv_rn(x, 27.0f); }
+
+// FP32: the same three-step quotient with y = RN_f32(1/c).  The general
+// bound does not cover c = 7 in FP32 (|y*7 - 1| = 1.5 * 2^-25), so this
+// form was instead checked exhaustively against IEEE FP32 division on
+// every float in [1, 2) for both constants (mamr_selftest_division; zero
+// differences).  All three steps scale exactly by powers of two, so the
+// result holds for every x whose quotient and remainder stay normal:
+// biased exponents (60, 250); the rest takes the IEEE division.
+template <int C>
+__device__ __forceinline__ float div_const_f(float x, float y)
+{
+   const unsigned e = (__float_as_uint(x) >> 23) & 0xffu;
+   if (e > 60u && e < 250u) {
+      const float q0 = __fmul_rn(x, y);
+      const float r = __fmaf_rn(-q0, (float) C, x);
+      return __fmaf_rn(r, y, q0);
+   }
+   return __fdiv_rn(x, (float) C);
+}
+__device__ __forceinline__ float div7(float x)
+{
+   return div_const_f<7>(x, 0x1.24924ap-3f);
+}
+__device__ __forceinline__ float div27(float x)
+{
+   return div_const_f<27>(x, 0x1.2f684cp-5f);
+}
 
 // Exact scalings: x/4 and x/8 equal x*0.25 and x*0.125 in IEEE arithmetic.
 __device__ __forceinline__ double quarter(double x) { return x * 0.25; }

@@ -32,6 +32,16 @@ struct BItem {
                        // (dx+1) + 3(dy+1) + 9(dz+1); single-level meshes
 };
 
+// One tile of a pencil: the block and its in-plane neighbours at offset
+// (dx, dy), index (dx+1) + 3(dy+1), with bmask as in BItem.
+struct TileDesc {
+   int32_t slot;
+   int32_t bmask;
+   int32_t nb9[9];
+};
+// Longest pencil (blocks along z) the pencil kernel takes.
+constexpr int PENCIL_MAX = 64;
+
 struct BatchedState;
 
 void batched_destroy(BatchedState *b);
@@ -51,13 +61,12 @@ template <typename T>
 int batched_grid(const Geom &g, int stencil, int n_items);
 
 // Pencil variant for single-level meshes of 16^3 blocks: CTAs walk chains
-// of blocks along z (chain[pencils[p].x .. +pencils[p].y) are indices into
-// items, bottom to top).  FP32 checksums are fused (acc); FP64 checksums
+// of blocks along z (chain[pencils[p].x .. +pencils[p].y), bottom to top).  FP32 checksums are fused (acc); FP64 checksums
 // run as a separate all-variable pass into partials and sums.
 template <typename T>
 int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
                         const BItem *items, int n_blocks,
-                        const int32_t *chain, const int2 *pencils,
+                        const TileDesc *chain, const int2 *pencils,
                         int n_pencils, int grid, int write_ghosts, int do_cs,
                         double *partials, double *sums,
                         unsigned long long *acc, unsigned *err,

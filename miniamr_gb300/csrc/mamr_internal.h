@@ -12,8 +12,8 @@ namespace mamr {
 
 // Pool geometry.  One block-variable is X*Y rows of Zp elements; cell
 // (i, j, k), 0 <= i < X etc., sits at row i*Y + j, column koff + k.  koff
-// puts k = 1 on a 32-byte sector boundary so that every interior row
-// (k = 1..nz) starts a sector, and Zp keeps that true for every row.
+// puts k = 1 on a 64-byte boundary (a DRAM burst) so that every interior
+// row (k = 1..nz) starts a burst, and Zp keeps that true for every row.
 struct Geom {
    int nx, ny, nz, V;
    int X, Y, Z;       // nx+2, ny+2, nz+2

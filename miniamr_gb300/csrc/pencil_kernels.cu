@@ -75,12 +75,14 @@ constexpr size_t pencil_smem_bytes()
    return (size_t) 3 * (TILE_ROWS * RS + 2 * KC) * sizeof(T);
 }
 
+constexpr int DESC = sizeof(TileDesc) / sizeof(int32_t);
+
 // Queues the cp.async copies of tile `s` of the pencil into ring buffer t:
 // the interior rows, the four x/y face rows (neighbour or reflection) and,
 // for 27 points, the four z-running edge rows.
 template <typename T, int ST>
 __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
-                                           const Geom &g, const BItem *it,
+                                           const Geom &g, const TileDesc *it,
                                            int var, T *t)
 {
    constexpr int VW = 16 / (int) sizeof(T);   // elements per 16 bytes
@@ -98,7 +100,9 @@ __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
       const int f = c / (NB * CPR), r = c % (NB * CPR);
       const int a = r / CPR + 1, q = r % CPR;
       const bool bnd = (bmask >> f) & 1;
-      const T *blk = bnd ? own : src + bv_offset(g, it->f[f].nb[0], var);
+      // nb9 index of the W, E, S, N neighbour: 3, 5, 1, 7
+      const int nbi = (f < 2) ? (f == 0 ? 3 : 5) : (f == 2 ? 1 : 7);
+      const T *blk = bnd ? own : src + bv_offset(g, it->nb9[nbi], var);
       const bool low = (f & 1) == 0;
       // neighbour: its plane next to us; boundary: our own first plane
       const int sp = bnd ? (low ? 1 : NB) : (low ? NB : 1);
@@ -123,7 +127,7 @@ __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
          else si = (e & 1) ? 1 : NB;
          if (bmask & (1 << ((e & 2) ? 3 : 2))) { sj = (e & 2) ? NB : 1; dy = 0; }
          else sj = (e & 2) ? 1 : NB;
-         const int nb = it->nb27[(dx + 1) + 3 * (dy + 1) + 9];
+         const int nb = it->nb9[(dx + 1) + 3 * (dy + 1)];
          cp_async16(t + (gi * G + gj) * RS + q * VW,
                     src + bv_offset(g, nb, var) + cell_offset(g, si, sj, 1) +
                        q * VW);
@@ -133,18 +137,23 @@ __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
 }
 
 // Row (i, j) of a tile as six k values: k-1 .. k+4 around the thread's
-// quad k .. k+3 (k = 4*kq + 1); the z ghosts come from the k-columns.
+// quad k .. k+3 (k = 4*kq + 1).  The four lanes of a row hold the row's 16
+// values between them; the outer neighbours k-1 and k+4 come from the
+// adjacent lanes by shuffle, and from the z ghost columns at the row ends.
+// Every lane of the warp must call this together.
 template <typename T>
 __device__ __forceinline__ void row6(const T *t, const T *klo, const T *khi,
                                      int i, int j, int kq, T (&r)[6])
 {
    const int e = i * G + j;
-   const T *row = t + e * RS + 4 * kq;
    T v[4];
-   Quad<T>::ld(row, v);
+   Quad<T>::ld(t + e * RS + 4 * kq, v);
+   const T left = __shfl_up_sync(0xffffffffu, v[3], 1);
+   const T right = __shfl_down_sync(0xffffffffu, v[0], 1);
+   const T edge = kq == 0 ? klo[e] : khi[e];
+   r[0] = kq == 0 ? edge : left;
    r[1] = v[0]; r[2] = v[1]; r[3] = v[2]; r[4] = v[3];
-   r[0] = kq ? row[-1] : klo[e];
-   r[5] = kq < 3 ? row[4] : khi[e];
+   r[5] = kq == 3 ? edge : right;
 }
 
 }  // namespace
@@ -152,14 +161,14 @@ __device__ __forceinline__ void row6(const T *t, const T *klo, const T *khi,
 template <typename T, int ST>
 __global__ void __launch_bounds__(THREADS)
 pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
-                    const BItem *__restrict__ items,
-                    const int32_t *__restrict__ chain,
+                    const TileDesc *__restrict__ chain,
                     const int2 *__restrict__ pencils, int n_pencils,
                     int write_ghosts, int do_cs,
                     unsigned long long *__restrict__ acc,
                     unsigned *__restrict__ err)
 {
    extern __shared__ __align__(16) unsigned char smem_raw[];
+   __shared__ TileDesc s_desc[PENCIL_MAX];
    T *tiles = reinterpret_cast<T *>(smem_raw);
    T *klos = tiles + 3 * TILE_ROWS * RS;
    T *khis = klos + 3 * KC;
@@ -170,10 +179,16 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       const int var = w / n_pencils, p = w - var * n_pencils;
       const int2 pc = pencils[p];
       const int len = pc.y;
-      issue_tile<T, ST>(src, g, items + chain[pc.x], var, tiles);
+      {
+         const int32_t *from = reinterpret_cast<const int32_t *>(chain + pc.x);
+         int32_t *to = reinterpret_cast<int32_t *>(s_desc);
+         for (int q = tid; q < len * DESC; q += THREADS)
+            to[q] = from[q];
+      }
+      __syncthreads();
+      issue_tile<T, ST>(src, g, s_desc, var, tiles);
       if (len > 1)
-         issue_tile<T, ST>(src, g, items + chain[pc.x + 1], var,
-                           tiles + TILE_ROWS * RS);
+         issue_tile<T, ST>(src, g, s_desc + 1, var, tiles + TILE_ROWS * RS);
       unsigned long long lo = 0, hi = 0;
       bool ok = true;
       for (int s = 0; s < len; s++) {
@@ -198,10 +213,10 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
          }
          __syncthreads();
          if (s + 2 < len)
-            issue_tile<T, ST>(src, g, items + chain[pc.x + s + 2], var,
+            issue_tile<T, ST>(src, g, s_desc + s + 2, var,
                               tiles + ((s + 2) % 3) * TILE_ROWS * RS);
 
-         const int slot = items[chain[pc.x + s]].slot;
+         const int slot = s_desc[s].slot;
          T *d = dst + bv_offset(g, slot, var);
          T out[4];
          if (ST == 7) {
@@ -397,7 +412,7 @@ int pencil_grid(int stencil, int n_work)
 template <typename T>
 int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
                         const BItem *items, int n_blocks,
-                        const int32_t *chain, const int2 *pencils,
+                        const TileDesc *chain, const int2 *pencils,
                         int n_pencils, int grid, int write_ghosts, int do_cs,
                         double *partials, double *sums,
                         unsigned long long *acc, unsigned *err,
@@ -409,12 +424,12 @@ int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
    const int fused_cs = (sizeof(T) == 4) ? do_cs : 0;
    if (stencil == 7)
       pencil_stage_kernel<T, 7><<<grid, THREADS, smem, s>>>(
-         src, dst, g, items, chain, pencils, n_pencils, write_ghosts,
-         fused_cs, acc, err);
+         src, dst, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc,
+         err);
    else
       pencil_stage_kernel<T, 27><<<grid, THREADS, smem, s>>>(
-         src, dst, g, items, chain, pencils, n_pencils, write_ghosts,
-         fused_cs, acc, err);
+         src, dst, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc,
+         err);
    int launches = 1;
    if (do_cs && sizeof(T) == 8) {
       const long long n = (long long) n_blocks * g.V;
@@ -431,13 +446,13 @@ template int pencil_grid<float>(int, int);
 template int pencil_grid<double>(int, int);
 template int launch_pencil_stage<float>(const float *, float *, const Geom &,
                                         int, const BItem *, int,
-                                        const int32_t *, const int2 *, int,
+                                        const TileDesc *, const int2 *, int,
                                         int, int, int, double *, double *,
                                         unsigned long long *, unsigned *,
                                         cudaStream_t);
 template int launch_pencil_stage<double>(const double *, double *,
                                          const Geom &, int, const BItem *,
-                                         int, const int32_t *, const int2 *,
+                                         int, const TileDesc *, const int2 *,
                                          int, int, int, int, double *,
                                          double *, unsigned long long *,
                                          unsigned *, cudaStream_t);

@@ -1,10 +1,10 @@
 // Device self-test of the division routines the kernels rely on.
 //
-// FP32: a three-operation remainder-corrected quotient (q0 = x*y,
-// r = fma(-q0, c, x), q = fma(r, y, q0), y = RN(1/c)) against the IEEE
-// division __fdiv_rn for every float in [1, 2).  Both sides scale exactly
-// with the exponent in the normal range, so that binade decides every
-// normal x whose quotient and remainder stay normal.
+// FP32: the kernels' x/7 and x/27 (a three-operation remainder-corrected
+// quotient q0 = x*y, r = fma(-q0, c, x), q = fma(r, y, q0), y = RN(1/c),
+// inside its exponent window) against the IEEE division __fdiv_rn for every
+// float in [1, 2) -- both sides scale exactly with the exponent, so that
+// binade decides the whole window -- and on hashed floats of every class.
 // FP64: the kernels' div7/div27 against __ddiv_rn on hashed bit patterns
 // covering all exponents (zeros, subnormals, inf and nan included).
 #include "mamr_internal.h"
@@ -12,23 +12,23 @@
 
 namespace {
 
-__device__ __forceinline__ float rc_div(float x, float c, float y)
+__device__ __forceinline__ unsigned mix32(unsigned z)
 {
-   const float q0 = __fmul_rn(x, y);
-   const float r = __fmaf_rn(-q0, c, x);
-   return __fmaf_rn(r, y, q0);
+   z ^= z >> 16; z *= 0x7feb352du; z ^= z >> 15; z *= 0x846ca68bu;
+   return z ^ (z >> 16);
 }
 
 __global__ void check_f32(unsigned long long *bad)
 {
-   const float y7 = 0x1.24924ap-3f, y27 = 0x1.2f684cp-5f;
    unsigned long long b7 = 0, b27 = 0;
-   for (unsigned m = blockIdx.x * blockDim.x + threadIdx.x; m < (1u << 23);
+   for (unsigned m = blockIdx.x * blockDim.x + threadIdx.x; m < (1u << 24);
         m += gridDim.x * blockDim.x) {
-      const float x = __uint_as_float(0x3f800000u | m);
-      b7 += __float_as_uint(rc_div(x, 7.0f, y7)) !=
+      // first 2^23: the binade [1, 2); then hashed bit patterns
+      const unsigned bits = m < (1u << 23) ? (0x3f800000u | m) : mix32(m);
+      const float x = __uint_as_float(bits);
+      b7 += __float_as_uint(mamr::div7(x)) !=
             __float_as_uint(__fdiv_rn(x, 7.0f));
-      b27 += __float_as_uint(rc_div(x, 27.0f, y27)) !=
+      b27 += __float_as_uint(mamr::div27(x)) !=
              __float_as_uint(__fdiv_rn(x, 27.0f));
    }
    if (b7) atomicAdd(bad + 0, b7);

@@ -139,15 +139,13 @@ def test_errors_are_reported_and_context_survives(gpu_lib):
 
 
 def test_division_selftest(gpu_lib):
-    """The FP64 kernels' correctly rounded x/7 and x/27 equal IEEE division
-    on 2^26 hashed doubles of every exponent class (the FP32 column reports
-    whether the remainder-corrected FP32 quotient is exact on a full
-    binade; the FP32 kernels use IEEE division either way)."""
+    """The kernels' x/7 and x/27 equal IEEE division: FP32 on every float
+    in [1, 2) (which decides its whole fast-path window) and on hashed
+    floats of every class, FP64 on 2^26 hashed doubles of every class."""
     import ctypes as C
     f = gpu_lib.lib.mamr_selftest_division
     f.argtypes = [C.c_int64, C.POINTER(C.c_int64)]
     f.restype = C.c_int
     out = (C.c_int64 * 4)()
     assert f(1 << 26, out) == 0
-    print("fp32 rc-division mismatches (7, 27):", out[0], out[1])
-    assert out[2] == 0 and out[3] == 0
+    assert list(out) == [0, 0, 0, 0]
