@@ -186,12 +186,13 @@ extern "C" int mamr_create(const mamr_config *cfg, mamr_ctx **out)
    Geom &g = c->g;
    g.nx = cfg->nx; g.ny = cfg->ny; g.nz = cfg->nz; g.V = cfg->num_vars;
    g.X = g.nx + 2; g.Y = g.ny + 2; g.Z = g.nz + 2;
-   // k = 1 starts a 64-byte DRAM burst, and every row is a whole number
-   // of bursts: an interior row then costs exactly its own bytes
-   const int burst = 64 / (int) elem_size(c);    // elements per 64 bytes
-   g.koff = burst - 1;
-   g.Zp = ((g.koff + g.Z + burst - 1) / burst) * burst;
-   g.bv = (long long) g.X * g.Y * g.Zp;
+   // split layout: dense interior rows, then the two k-ghost planes; each
+   // block-variable starts a 128-byte line
+   const int line = 128 / (int) elem_size(c);
+   g.Zp = g.Z;
+   g.koff = 0;
+   g.kplane = (long long) g.X * g.Y * g.nz;
+   g.bv = ((g.kplane + 2LL * g.X * g.Y + line - 1) / line) * line;
    size_t tile = (size_t) g.X * g.Y * g.Z * elem_size(c);
    if (tile > 200 * 1024) {
       delete c;

@@ -10,15 +10,21 @@
 
 namespace mamr {
 
-// Pool geometry.  One block-variable is X*Y rows of Zp elements; cell
-// (i, j, k), 0 <= i < X etc., sits at row i*Y + j, column koff + k.  koff
-// puts k = 1 on a 64-byte boundary (a DRAM burst) so that every interior
-// row (k = 1..nz) starts a burst, and Zp keeps that true for every row.
+// Pool geometry.  Two layouts of one block-variable:
+//  - split (kplane >= 0; the device pool): the X*Y rows hold only the
+//    interior k = 1..nz, back to back (row i*Y + j at (i*Y + j)*nz), so the
+//    128-byte lines DRAM delivers carry nothing but interior cells; the
+//    ghost values k = 0 and k = nz+1 of row (i, j) sit in two planes after
+//    the rows, at kplane + i*Y + j and kplane + X*Y + i*Y + j.  bv is
+//    rounded up to whole 128-byte lines.
+//  - inline (kplane < 0; host buffers): rows of Zp elements holding
+//    k = 0..nz+1 at columns koff .. koff+nz+1.
 struct Geom {
    int nx, ny, nz, V;
    int X, Y, Z;       // nx+2, ny+2, nz+2
-   int Zp, koff;      // padded row length, column of k = 0
-   long long bv;      // elements per block-variable: X*Y*Zp
+   int Zp, koff;      // inline layout: row length, column of k = 0
+   long long kplane;  // split layout: offset of the k = 0 plane, else -1
+   long long bv;      // elements per block-variable
 };
 
 __host__ __device__ inline long long bv_offset(const Geom &g, int slot,
@@ -30,7 +36,18 @@ __host__ __device__ inline long long bv_offset(const Geom &g, int slot,
 __host__ __device__ inline long long cell_offset(const Geom &g, int i, int j,
                                                  int k)
 {
-   return ((long long) i * g.Y + j) * g.Zp + g.koff + k;
+   const long long row = (long long) i * g.Y + j;
+   if (g.kplane < 0)
+      return row * g.Zp + g.koff + k;
+   if (k >= 1 && k <= g.nz)
+      return row * g.nz + (k - 1);
+   return g.kplane + (k == 0 ? 0 : (long long) g.X * g.Y) + row;
+}
+
+// Offset of interior row (i, j), k = 1, in the split layout.
+__host__ __device__ inline long long row_offset(const Geom &g, int i, int j)
+{
+   return ((long long) i * g.Y + j) * g.nz;
 }
 
 // Same-level exchange across one face: lo is the block on the low side

@@ -121,7 +121,8 @@ stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
    T *base = pool + bv_offset(g, slots[blockIdx.x], var);
    for (int e = threadIdx.x; e < X * Y * Z; e += blockDim.x) {
       int row = e / Z, k = e - row * Z;
-      tile[e] = base[(long long) row * g.Zp + g.koff + k];
+      int i = row / Y, j = row - i * Y;
+      tile[e] = base[cell_offset(g, i, j, k)];
    }
    __syncthreads();
 #define TL(i, j, k) tile[((i) * Y + (j)) * Z + (k)]
@@ -373,7 +374,8 @@ __global__ void upload_kernel(T *__restrict__ pool, Geom g,
       long long bvi = row / (g.X * g.Y);
       int r = (int) (row - bvi * (g.X * g.Y));
       int b = (int) (bvi / g.V), var = (int) (bvi - (long long) b * g.V);
-      pool[bv_offset(g, slots[b], var) + (long long) r * g.Zp + g.koff + k] =
+      int i = r / g.Y, j = r - i * g.Y;
+      pool[bv_offset(g, slots[b], var) + cell_offset(g, i, j, k)] =
          (T) dense[e];
    }
 }
@@ -390,8 +392,9 @@ __global__ void download_kernel(const T *__restrict__ pool, Geom g,
       long long bvi = row / (g.X * g.Y);
       int r = (int) (row - bvi * (g.X * g.Y));
       int b = (int) (bvi / g.V), var = (int) (bvi - (long long) b * g.V);
+      int i = r / g.Y, j = r - i * g.Y;
       dense[e] = (double) pool[bv_offset(g, slots[b], var) +
-                               (long long) r * g.Zp + g.koff + k];
+                               cell_offset(g, i, j, k)];
    }
 }
 
