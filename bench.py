@@ -183,8 +183,9 @@ def oracle_rate(steps, threads=None):
 
 def profile_case(name):
     """Small batched run for ncu captures: 4096 blocks of 16^3, 4 vars
-    (268 MB of FP32 interior cells per pool, twice the L2), four stages
-    launched one by one."""
+    (268 MB of FP32 interior cells per pool, twice the L2), two timesteps
+    of four stages launched one by one (checksums on each timestep's first
+    stage, as in the benchmark)."""
     global V, UPD_PER_STAGE
     import torch
     from miniamr_gb300 import build, load
@@ -197,11 +198,12 @@ def profile_case(name):
     build.build_library()
     lib = load()
     ctx, _ = build_mesh(lib, dtype)
-    ctx.run_timesteps(1, 2, 1, flags=RUN_BATCHED)
-    ctx.run_timesteps(1, 2, 1, first_stage=2, flags=RUN_BATCHED)
+    # the benchmark's cadence: 4 stages per timestep, checksum on stage 0
+    ctx.run_timesteps(1, SPT, FREQ, flags=RUN_BATCHED)
+    ctx.run_timesteps(1, SPT, FREQ, first_stage=SPT, flags=RUN_BATCHED)
     torch.cuda.synchronize()
     ctx.close()
-    print(f"profile case {name}: 4 batched stages, {V} vars")
+    print(f"profile case {name}: {2 * SPT} batched stages, {V} vars")
     return 0
 
 

@@ -26,8 +26,8 @@ template <>
 __device__ __forceinline__ double div_const<7>(double x)
 {
    const double y = 0x1.2492492492492p-3;   // RN(1/7)
-   const int e = (__double2hiint(x) >> 20) & 0x7ff;
-   if (e > 100 && e < 2000) {
+   const unsigned e = ((unsigned) __double2hiint(x) >> 20) & 0x7ffu;
+   if (e - 101u < 1899u) {                    // 100 < e < 2000
       double q0 = __dmul_rn(x, y);
       double r = __fma_rn(-q0, 7.0, x);
       return __fma_rn(r, y, q0);
@@ -39,8 +39,8 @@ template <>
 __device__ __forceinline__ double div_const<27>(double x)
 {
    const double y = 0x1.2f684bda12f68p-5;   // RN(1/27)
-   const int e = (__double2hiint(x) >> 20) & 0x7ff;
-   if (e > 100 && e < 2000) {
+   const unsigned e = ((unsigned) __double2hiint(x) >> 20) & 0x7ffu;
+   if (e - 101u < 1899u) {                    // 100 < e < 2000
       double q0 = __dmul_rn(x, y);
       double r = __fma_rn(-q0, 27.0, x);
       return __fma_rn(r, y, q0);
@@ -62,7 +62,7 @@ template <int C>
 __device__ __forceinline__ float div_const_f(float x, float y)
 {
    const unsigned e = (__float_as_uint(x) >> 23) & 0xffu;
-   if (e > 60u && e < 250u) {
+   if (e - 61u < 189u) {                      // 60 < e < 250
       const float q0 = __fmul_rn(x, y);
       const float r = __fmaf_rn(-q0, (float) C, x);
       return __fmaf_rn(r, y, q0);

@@ -94,7 +94,7 @@ __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
       const int q = c % CPR, r = c / CPR;
       const int j = r % NB + 1, i = r / NB + 1;
       cp_async16(t + (i * G + j) * RS + q * VW,
-                 own + cell_offset(g, i, j, 1) + q * VW);
+                 own + row_offset(g, i, j) + q * VW);
    }
    for (int c = tid; c < 4 * NB * CPR; c += THREADS) {
       const int f = c / (NB * CPR), r = c % (NB * CPR);
@@ -110,10 +110,10 @@ __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
       const T *from;
       T *to;
       if (f < 2) {
-         from = blk + cell_offset(g, sp, a, 1);
+         from = blk + row_offset(g, sp, a);
          to = t + (gp * G + a) * RS;
       } else {
-         from = blk + cell_offset(g, a, sp, 1);
+         from = blk + row_offset(g, a, sp);
          to = t + (a * G + gp) * RS;
       }
       cp_async16(to + q * VW, from + q * VW);
@@ -129,7 +129,7 @@ __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
          else sj = (e & 2) ? 1 : NB;
          const int nb = it->nb9[(dx + 1) + 3 * (dy + 1)];
          cp_async16(t + (gi * G + gj) * RS + q * VW,
-                    src + bv_offset(g, nb, var) + cell_offset(g, si, sj, 1) +
+                    src + bv_offset(g, nb, var) + row_offset(g, si, sj) +
                        q * VW);
       }
    }
@@ -159,7 +159,7 @@ __device__ __forceinline__ void row6(const T *t, const T *klo, const T *khi,
 }  // namespace
 
 template <typename T, int ST>
-__global__ void __launch_bounds__(THREADS)
+__global__ void __launch_bounds__(THREADS, sizeof(T) == 4 ? 3 : 1)
 pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                     const TileDesc *__restrict__ chain,
                     const int2 *__restrict__ pencils, int n_pencils,
@@ -240,7 +240,7 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                   v = v + c[m + 1];
                   out[m] = div7(v);
                }
-               Quad<T>::st(d + cell_offset(g, i, j, 4 * kq + 1), out);
+               Quad<T>::st(d + row_offset(g, i, j) + 4 * kq, out);
                if (sizeof(T) == 4 && do_cs)
 #pragma unroll
                   for (int m = 0; m < 4; m++) {
@@ -286,7 +286,7 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
 #pragma unroll
                for (int m = 0; m < 4; m++)
                   out[m] = div27((s0[m] + s1[m]) + s2[m]);
-               Quad<T>::st(d + cell_offset(g, i, j, 4 * kq + 1), out);
+               Quad<T>::st(d + row_offset(g, i, j) + 4 * kq, out);
                if (sizeof(T) == 4 && do_cs)
 #pragma unroll
                   for (int m = 0; m < 4; m++) {
