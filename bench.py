@@ -207,6 +207,16 @@ def profile_case(name):
     return 0
 
 
+def max_over_ranks(x, dist=None, device="cpu"):
+    """The slowest rank's value (the job's time); x itself on one rank."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -294,11 +304,7 @@ def main():
         ev1.record(stream)
         torch.cuda.synchronize()
     launches = ctx.launch_count() - l0
-    ms = ev0.elapsed_time(ev1)
-    if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), pg, "cuda")
     value = updates(K) * world / (ms / 1e3)
     n_stage_launches = K * SPT
     per_launch_s = ms / 1e3 / n_stage_launches
@@ -323,11 +329,7 @@ def main():
     build_mesh(lib, FP32, ctx=ctx, host=host)
     e2e_sums = ctx.run_timesteps(K, SPT, FREQ, flags=flags)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if pg:
-        t = torch.tensor([e2e_s], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, pg, "cuda")
     ctx.close()
     h2d = host.nbytes
     d2h = e2e_sums.nbytes
@@ -363,7 +365,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "batched_stage_kernel<float,27>",
+                     "kernel": "pencil_stage_kernel<float,27>",
                      "alg_bytes_per_launch": alg_bytes},
         "e2e": {"value": updates(K) * world / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,

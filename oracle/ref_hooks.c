@@ -12,7 +12,8 @@
  *
  * where the cell hash (var_cell_hash below) covers the bit pattern of
  * every cell, ghosts included, of that variable in every active block, in
- * sorted_list order (ref/block.h:72-77), and each block's number.  Every refine() call (ref/refine.c:38) appends one line
+ * sorted_list order (ref/block.h:72-77), and each block's number
+ * (0 where MAMR_REF_HASH_STRIDE skips it).  Every refine() call (ref/refine.c:38) appends one line
  *
  *     mesh <ts> <n_active> <hash of (slot,number,level,nei_level,nei,cen)>
  *
@@ -111,16 +112,29 @@ static uint64_t var_cell_hash(int var)
    return h;
 }
 
+/* MAMR_REF_HASH_STRIDE=n: cell hashes only for every n-th group of
+ * num_vars check_sum calls (the others log hash 0), for long runs. */
+static long hash_stride(void)
+{
+   static long stride = -1;
+   if (stride < 0) {
+      const char *p = getenv("MAMR_REF_HASH_STRIDE");
+      stride = (p && atol(p) > 0) ? atol(p) : 1;
+   }
+   return stride;
+}
+
 double __wrap_check_sum(int var)
 {
    double s = __real_check_sum(var);
    FILE *fp = hook_log();
    if (fp) {
-      uint64_t bits;
+      uint64_t bits, h = 0;
       memcpy(&bits, &s, sizeof(bits));
+      if ((cs_calls / num_vars) % hash_stride() == 0)
+         h = var_cell_hash(var);
       fprintf(fp, "cs %ld %d %016llx %016llx\n", cs_calls, var,
-              (unsigned long long) bits,
-              (unsigned long long) var_cell_hash(var));
+              (unsigned long long) bits, (unsigned long long) h);
    }
    cs_calls++;
    return s;

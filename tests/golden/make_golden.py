@@ -62,6 +62,20 @@ CASES = {
                   "1", "--num_tsteps", "5", "--stages_per_ts", "2",
                   "--checksum_freq", "1", "--error_tol", "0", "--max_blocks",
                   "4000"],
+    # the AMR configuration at full size: 4^3 blocks of 16^3, 40 vars,
+    # 27-point, up to 4 levels around a surface sphere (r 0.15) moving at
+    # 0.01/step and bouncing inside the cube, refine every 5 steps, 100
+    # steps; the 27-point stencil does not conserve the sum under
+    # refinement, so the run needs --error_tol 0.  Cell hashes every 10th
+    # checksum stage.
+    "config2": ["--init_x", "4", "--init_y", "4", "--init_z", "4", "--nx",
+                "16", "--ny", "16", "--nz", "16", "--num_vars", "40",
+                "--stencil", "27", "--num_refine", "4", "--refine_freq", "5",
+                "--num_tsteps", "100", "--stages_per_ts", "1",
+                "--checksum_freq", "1", "--error_tol", "0", "--max_blocks",
+                "8000", "--num_objects", "1", "--object", "2", "1", "0.25",
+                "0.25", "0.25", "0.01", "0.01", "0.01", "0.15", "0.15", "0.15",
+                "0", "0", "0"],
     # two objects, volume + surface refinement, 7-point, 4 levels, default
     # checksum cadence (every 5th stage of 3)
     "amr7_objects": ["--init_x", "2", "--init_y", "2", "--init_z", "2",
@@ -77,17 +91,22 @@ CASES = {
 }
 
 
+HASH_STRIDE = {"config2": 10}
+
+
 def run_case(name, args):
     with tempfile.TemporaryDirectory() as td:
         rlog = os.path.join(td, "r.log")
         hlog = os.path.join(td, "h.log")
         trc = os.path.join(td, "t.trc")
-        env = dict(os.environ, MAMR_REF_LOG=rlog)
+        base_env = dict(os.environ,
+                        MAMR_REF_HASH_STRIDE=str(HASH_STRIDE.get(name, 1)))
+        env = dict(base_env, MAMR_REF_LOG=rlog)
         r = subprocess.run([REF_BIN] + args, cwd=td, env=env,
                            capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"{name}: reference failed\n{r.stdout[-2000:]}")
-        env = dict(os.environ, MAMR_REF_LOG=hlog, MAMR_TRACE=trc)
+        env = dict(base_env, MAMR_REF_LOG=hlog, MAMR_TRACE=trc)
         h = subprocess.run([HYB_BIN] + args, cwd=td, env=env,
                            capture_output=True, text=True)
         if h.returncode != 0:

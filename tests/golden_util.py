@@ -36,3 +36,16 @@ def trace_path(name):
 
 def arg(args, flag, default=None):
     return args[args.index(flag) + 1] if flag in args else default
+
+
+# Cases too large to replay through the CPU oracle inside the CPU suite;
+# they are pinned by make_golden.py (hybrid == reference) and replayed on
+# the GPU.
+HEAVY = {"config2"}
+
+
+def hashed_stages(hashes, V):
+    """Checksum stages whose cell hashes the log carries (0 = not taken);
+    returns first, middle and last of them."""
+    st = [s for s in range(len(hashes) // V) if hashes[s * V] != 0]
+    return {st[0], st[len(st) // 2], st[-1]} if st else set()

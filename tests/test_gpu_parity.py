@@ -3,7 +3,7 @@ the CPU oracle, through the C ABI."""
 import numpy as np
 import pytest
 
-from golden_util import cases, reflog, trace_path
+from golden_util import cases, hashed_stages, reflog, trace_path
 from miniamr_gb300 import mesh as meshmod
 from miniamr_gb300.abi import FP32, FP64, MamrError, Config
 from miniamr_gb300.trace import read_trace, replay
@@ -24,11 +24,11 @@ def test_trace_fp64_bit_exact_vs_reference(gpu_lib, name):
     sums, hashes, _ = reflog(name)
     recs = read_trace(trace_path(name))
     V = next(r.args[0].num_vars for r in recs if r.op == 1)
-    n_st = len(sums) // V
-    want = {0, n_st // 2, n_st - 1}
+    want = hashed_stages(hashes, V)
     res = replay(gpu_lib, recs, hash_stages=want)
     got = [(v, s) for v, s, _ in res.checksums]
     assert got == sums
+    assert len(res.hashes) == len(want)
     for st, hs in res.hashes:
         assert hs == hashes[st * V:(st + 1) * V], f"cells differ, stage {st}"
     res.ctx.close()

@@ -1,0 +1,116 @@
+"""Host-side checks that need no GPU: the GPU library loads and exports the
+whole ABI, the replica reduction of the benchmark across ranks, argument
+validation in the oracle, and the drop-in against the reference on a case
+outside the committed fixtures (where the reference sources exist)."""
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "miniamr_gb300.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(mamr_\w+)\s*\(",
+                                 src, re.M)))
+
+
+def test_gpu_library_exports_every_abi_function():
+    from miniamr_gb300 import build
+    lib = build.build_library()
+    out = subprocess.run(["nm", "-D", "--defined-only", lib],
+                         capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\sT\s(mamr_\w+)$", out, re.M))
+    missing = [f for f in header_functions() if f not in exported]
+    assert not missing, missing
+    import ctypes
+    ctypes.CDLL(lib)                     # loads without a GPU
+
+
+def test_oracle_exports_the_hot_path_abi(oracle_lib):
+    for f in header_functions():
+        if f in ("mamr_check_sum_fp64_noalloc", "mamr_selftest_division"):
+            continue                     # device-only entry points
+        assert hasattr(oracle_lib.lib, f), f
+
+
+def test_oracle_rejects_bad_arguments(oracle_lib):
+    from miniamr_gb300.abi import Config, MamrError
+    with pytest.raises(MamrError) as e:
+        oracle_lib.context(Config.make(7, 8, 8, 2, 4))     # odd block size
+    assert e.value.status == -1
+    with pytest.raises(MamrError) as e:
+        oracle_lib.context(Config.make(8, 8, 8, 2, 4, stencil=0))
+    assert e.value.status == -5
+    with oracle_lib.context(Config.make(8, 8, 8, 2, 4)) as ctx:
+        with pytest.raises(MamrError):
+            ctx.check_sum(2)
+        with pytest.raises(MamrError):
+            ctx.upload([4], np.zeros((1, 2, 10, 10, 10)))
+        ctx.set_mesh(np.zeros(0, dtype=__import__(
+            "miniamr_gb300.abi", fromlist=["BLOCK_DTYPE"]).BLOCK_DTYPE))
+        assert ctx.check_sum(0) == 0.0   # empty mesh
+
+
+def _rank(rank, world, port, q):
+    import torch.distributed as dist
+    sys.path.insert(0, REPO)
+    import bench
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}",
+                            rank=rank, world_size=world)
+    q.put((rank, bench.max_over_ranks(10.0 + rank, dist)))
+    dist.destroy_process_group()
+
+
+def test_replica_time_is_max_over_ranks_gloo():
+    """bench.py under torchrun: each rank times its own replica and the job
+    time is the slowest rank's (world size 2, gloo on CPU)."""
+    import multiprocessing as mp
+    import socket
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    for p in ps:
+        p.join(120)
+    got = sorted(q.get(timeout=5) for _ in range(2))
+    assert got == [(0, 11.0), (1, 11.0)]
+
+
+REF = os.environ.get("MAMR_REFERENCE_SRC", "/root/reference/ref")
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources absent")
+def test_dropin_matches_reference_on_fresh_case(tmp_path):
+    """The reference's driver over the drop-in units and the oracle equals
+    the unmodified reference on a case the fixtures do not contain
+    (cylinder object, 7-point, block_change 2, checksum every 2nd stage)."""
+    from miniamr_gb300 import build
+    assert build.build_reference_binaries()
+    args = ["--init_x", "1", "--init_y", "2", "--init_z", "2", "--nx", "6",
+            "--ny", "4", "--nz", "6", "--num_vars", "2", "--stencil", "7",
+            "--num_refine", "3", "--block_change", "2", "--refine_freq", "1",
+            "--num_tsteps", "6", "--stages_per_ts", "4", "--checksum_freq",
+            "2", "--max_blocks", "6000", "--num_objects", "1", "--object",
+            "20", "1", "0.5", "0.4", "0.5", "0.02", "0.03", "0.0", "0.15",
+            "0.15", "0.6", "0", "0", "0"]
+    logs = []
+    for binary in ("miniamr_ref", "miniamr_hybrid_oracle"):
+        log = tmp_path / (binary + ".log")
+        r = subprocess.run([os.path.join(REPO, "oracle", "_ref", binary)] +
+                           args, cwd=tmp_path, capture_output=True, text=True,
+                           env=dict(os.environ, MAMR_REF_LOG=str(log)))
+        assert r.returncode == 0, r.stdout[-500:]
+        logs.append(log.read_text())
+    assert len(logs[0]) > 0 and logs[0] == logs[1]
+    assert "mesh" in logs[0]
