@@ -77,82 +77,61 @@ constexpr size_t pencil_smem_bytes()
 
 constexpr int DESC = sizeof(TileDesc) / sizeof(int32_t);
 
-template <int BYTES>
-__device__ __forceinline__ void cp_async_small(void *smem, const void *gmem)
-{
-   unsigned s = (unsigned) __cvta_generic_to_shared(smem);
-   asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s),
-                "l"(gmem), "n"(BYTES));
-}
-
-// Global source of row e = (i, j) of a tile (i, j in 0..G-1): the tile's
-// own interior rows, or -- for ghost rows -- the neighbour across each
-// out-of-range axis (its adjacent row), or the block's own first/last row
-// where that axis is a domain boundary (reflection).  Axis by axis, as
-// comm()'s sweeps compose on a single-level mesh.
-template <typename T>
-__device__ __forceinline__ const T *row_source(const T *__restrict__ src,
-                                               const Geom &g,
-                                               const TileDesc *d, int var,
-                                               int i, int j)
-{
-   int dx = i == 0 ? -1 : (i == G - 1 ? 1 : 0);
-   int dy = j == 0 ? -1 : (j == G - 1 ? 1 : 0);
-   int si = i, sj = j;
-   if (dx) {
-      if (d->bmask & (1 << (dx < 0 ? 0 : 1))) { si = dx < 0 ? 1 : NB; dx = 0; }
-      else si = dx < 0 ? NB : 1;
-   }
-   if (dy) {
-      if (d->bmask & (1 << (dy < 0 ? 2 : 3))) { sj = dy < 0 ? 1 : NB; dy = 0; }
-      else sj = dy < 0 ? NB : 1;
-   }
-   return src + bv_offset(g, d->nb9[(dx + 1) + 3 * (dy + 1)], var) +
-          row_offset(g, si, sj);
-}
-
-// Queues the cp.async copies for tile s of a pencil (descriptors ds[0..len)):
-//  - every row of the tile into ring buffer t (the 27-point stencil needs
-//    all G*G rows; the 7-point one skips the four z-running edge rows);
-//  - its lower z-ghost column klo: tile s-1's k = NB values of the same
-//    rows (k = 1 of its own rows at the bottom boundary: reflection);
-//  - the upper z-ghost column of tile s-1 (khi_prev): this tile's k = 1
-//    values; and its own khi, k = NB of its rows, at the top boundary.
+// Queues the cp.async copies of tile `s` of the pencil into ring buffer t:
+// the interior rows, the four x/y face rows (neighbour or reflection) and,
+// for 27 points, the four z-running edge rows.
 template <typename T, int ST>
 __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
-                                           const Geom &g,
-                                           const TileDesc *ds, int s,
-                                           int len, int var, T *t, T *klo,
-                                           T *khi, T *khi_prev)
+                                           const Geom &g, const TileDesc *it,
+                                           int var, T *t)
 {
    constexpr int VW = 16 / (int) sizeof(T);   // elements per 16 bytes
    constexpr int CPR = NB / VW;               // 16-byte chunks per row
    const int tid = threadIdx.x;
-   const TileDesc *d = ds + s;
-   for (int c = tid; c < G * G * CPR; c += THREADS) {
-      const int e = c / CPR, q = c % CPR;
-      const int i = e / G, j = e % G;
-      if (ST == 7 && (i == 0 || i == G - 1) && (j == 0 || j == G - 1))
-         continue;
-      cp_async16(t + e * RS + q * VW,
-                 row_source(src, g, d, var, i, j) + q * VW);
+   const int slot = it->slot, bmask = it->bmask;
+   const T *own = src + bv_offset(g, slot, var);
+   for (int c = tid; c < NB * NB * CPR; c += THREADS) {
+      const int q = c % CPR, r = c / CPR;
+      const int j = r % NB + 1, i = r / NB + 1;
+      cp_async16(t + (i * G + j) * RS + q * VW,
+                 own + row_offset(g, i, j) + q * VW);
    }
-   for (int e = tid; e < G * G; e += THREADS) {
-      const int i = e / G, j = e % G;
-      const bool ghost_row = i == 0 || i == G - 1 || j == 0 || j == G - 1;
-      if (ST == 7 && ghost_row)
-         continue;                   // 7 points read k-ghosts of interior rows only
-      const T *own = row_source(src, g, d, var, i, j);
-      if (s == 0)
-         cp_async_small<sizeof(T)>(klo + e, own);
-      else {
-         cp_async_small<sizeof(T)>(klo + e,
-                                   row_source(src, g, d - 1, var, i, j) +
-                                      NB - 1);
-         cp_async_small<sizeof(T)>(khi_prev + e, own);
+   for (int c = tid; c < 4 * NB * CPR; c += THREADS) {
+      const int f = c / (NB * CPR), r = c % (NB * CPR);
+      const int a = r / CPR + 1, q = r % CPR;
+      const bool bnd = (bmask >> f) & 1;
+      // nb9 index of the W, E, S, N neighbour: 3, 5, 1, 7
+      const int nbi = (f < 2) ? (f == 0 ? 3 : 5) : (f == 2 ? 1 : 7);
+      const T *blk = bnd ? own : src + bv_offset(g, it->nb9[nbi], var);
+      const bool low = (f & 1) == 0;
+      // neighbour: its plane next to us; boundary: our own first plane
+      const int sp = bnd ? (low ? 1 : NB) : (low ? NB : 1);
+      const int gp = low ? 0 : G - 1;
+      const T *from;
+      T *to;
+      if (f < 2) {
+         from = blk + row_offset(g, sp, a);
+         to = t + (gp * G + a) * RS;
+      } else {
+         from = blk + row_offset(g, a, sp);
+         to = t + (a * G + gp) * RS;
       }
-      if (s == len - 1)
-         cp_async_small<sizeof(T)>(khi + e, own + NB - 1);
+      cp_async16(to + q * VW, from + q * VW);
+   }
+   if (ST == 27) {
+      for (int c = tid; c < 4 * CPR; c += THREADS) {
+         const int e = c / CPR, q = c % CPR;
+         const int gi = (e & 1) ? G - 1 : 0, gj = (e & 2) ? G - 1 : 0;
+         int dx = (e & 1) ? 1 : -1, dy = (e & 2) ? 1 : -1, si, sj;
+         if (bmask & (1 << ((e & 1) ? 1 : 0))) { si = (e & 1) ? NB : 1; dx = 0; }
+         else si = (e & 1) ? 1 : NB;
+         if (bmask & (1 << ((e & 2) ? 3 : 2))) { sj = (e & 2) ? NB : 1; dy = 0; }
+         else sj = (e & 2) ? 1 : NB;
+         const int nb = it->nb9[(dx + 1) + 3 * (dy + 1)];
+         cp_async16(t + (gi * G + gj) * RS + q * VW,
+                    src + bv_offset(g, nb, var) + row_offset(g, si, sj) +
+                       q * VW);
+      }
    }
    cp_async_commit();
 }
@@ -207,26 +186,35 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
             to[q] = from[q];
       }
       __syncthreads();
-      issue_tile<T, ST>(src, g, s_desc, 0, len, var, tiles, klos, khis,
-                        nullptr);
+      issue_tile<T, ST>(src, g, s_desc, var, tiles);
       if (len > 1)
-         issue_tile<T, ST>(src, g, s_desc, 1, len, var,
-                           tiles + TILE_ROWS * RS, klos + KC, khis + KC,
-                           khis);
+         issue_tile<T, ST>(src, g, s_desc + 1, var, tiles + TILE_ROWS * RS);
       unsigned long long lo = 0, hi = 0;
       bool ok = true;
       for (int s = 0; s < len; s++) {
-         const int b = s % 3;
+         const int b = s % 3, bn = (s + 1) % 3;
          T *t = tiles + b * TILE_ROWS * RS;
          T *klo = klos + b * KC, *khi = khis + b * KC;
          cp_async_wait_all();
          __syncthreads();
-         if (s + 2 < len) {
-            const int b2 = (s + 2) % 3, b1 = (s + 1) % 3;
-            issue_tile<T, ST>(src, g, s_desc, s + 2, len, var,
-                              tiles + b2 * TILE_ROWS * RS, klos + b2 * KC,
-                              khis + b2 * KC, khis + b1 * KC);
+         // z ghost columns: tile s+1's k=1 (or our own k=16 at the top
+         // boundary); tile s+1's lower column is our k=16; the bottom tile
+         // reflects its own k=1
+         for (int e = tid; e < KC; e += THREADS) {
+            const T *tn = tiles + bn * TILE_ROWS * RS;
+            if (s + 1 < len) {
+               khi[e] = tn[e * RS];
+               klos[bn * KC + e] = t[e * RS + NB - 1];
+            } else {
+               khi[e] = t[e * RS + NB - 1];
+            }
+            if (s == 0)
+               klo[e] = t[e * RS];
          }
+         __syncthreads();
+         if (s + 2 < len)
+            issue_tile<T, ST>(src, g, s_desc + s + 2, var,
+                              tiles + ((s + 2) % 3) * TILE_ROWS * RS);
 
          const int slot = s_desc[s].slot;
          T *d = dst + bv_offset(g, slot, var);
