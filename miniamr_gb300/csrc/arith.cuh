@@ -19,37 +19,29 @@ namespace mamr {
 // q0 and r away from underflow and overflow, so x outside biased exponents
 // (100, 2000) -- zero, tiny, huge, inf, nan -- takes the IEEE division.
 // mamr_selftest_division compares against IEEE division on the GPU.
+// The fast quotient is computed for every argument; arguments outside the
+// window take the IEEE division in a separate, rarely entered branch so
+// that the long IEEE sequence is never if-converted into the common path.
+__device__ __forceinline__ bool div_window(double x)
+{
+   const unsigned e = ((unsigned) __double2hiint(x) >> 20) & 0x7ffu;
+   return e - 101u < 1899u;                   // 100 < e < 2000
+}
+__device__ __forceinline__ bool div_window(float x)
+{
+   const unsigned e = (__float_as_uint(x) >> 23) & 0xffu;
+   return e - 61u < 189u;                     // 60 < e < 250
+}
+
 template <int C>
-__device__ __forceinline__ double div_const(double x);
-
-template <>
-__device__ __forceinline__ double div_const<7>(double x)
+__device__ __forceinline__ double div_fast(double x)
 {
-   const double y = 0x1.2492492492492p-3;   // RN(1/7)
-   const unsigned e = ((unsigned) __double2hiint(x) >> 20) & 0x7ffu;
-   if (e - 101u < 1899u) {                    // 100 < e < 2000
-      double q0 = __dmul_rn(x, y);
-      double r = __fma_rn(-q0, 7.0, x);
-      return __fma_rn(r, y, q0);
-   }
-   return __ddiv_rn(x, 7.0);
+   const double y = C == 7 ? 0x1.2492492492492p-3    // RN(1/7)
+                           : 0x1.2f684bda12f68p-5;   // RN(1/27)
+   const double q0 = __dmul_rn(x, y);
+   const double r = __fma_rn(-q0, (double) C, x);
+   return __fma_rn(r, y, q0);
 }
-
-template <>
-__device__ __forceinline__ double div_const<27>(double x)
-{
-   const double y = 0x1.2f684bda12f68p-5;   // RN(1/27)
-   const unsigned e = ((unsigned) __double2hiint(x) >> 20) & 0x7ffu;
-   if (e - 101u < 1899u) {                    // 100 < e < 2000
-      double q0 = __dmul_rn(x, y);
-      double r = __fma_rn(-q0, 27.0, x);
-      return __fma_rn(r, y, q0);
-   }
-   return __ddiv_rn(x, 27.0);
-}
-
-__device__ __forceinline__ double div7(double x) { return div_const<7>(x); }
-__device__ __forceinline__ double div27(double x) { return div_const<27>(x); }
 
 // FP32: the same three-step quotient with y = RN_f32(1/c).  The general
 // bound does not cover c = 7 in FP32 (|y*7 - 1| = 1.5 * 2^-25), so this
@@ -59,24 +51,54 @@ __device__ __forceinline__ double div27(double x) { return div_const<27>(x); }
 // result holds for every x whose quotient and remainder stay normal:
 // biased exponents (60, 250); the rest takes the IEEE division.
 template <int C>
-__device__ __forceinline__ float div_const_f(float x, float y)
+__device__ __forceinline__ float div_fast(float x)
 {
-   const unsigned e = (__float_as_uint(x) >> 23) & 0xffu;
-   if (e - 61u < 189u) {                      // 60 < e < 250
-      const float q0 = __fmul_rn(x, y);
-      const float r = __fmaf_rn(-q0, (float) C, x);
-      return __fmaf_rn(r, y, q0);
+   const float y = C == 7 ? 0x1.24924ap-3f : 0x1.2f684cp-5f;
+   const float q0 = __fmul_rn(x, y);
+   const float r = __fmaf_rn(-q0, (float) C, x);
+   return __fmaf_rn(r, y, q0);
+}
+
+static __device__ __noinline__ double div_ieee(double x, double c)
+{
+   return __ddiv_rn(x, c);
+}
+static __device__ __noinline__ float div_ieee(float x, float c)
+{
+   return __fdiv_rn(x, c);
+}
+
+template <int C, typename T>
+__device__ __forceinline__ T div_const(T x)
+{
+   T q = div_fast<C>(x);
+   if (__builtin_expect(!div_window(x), 0))
+      q = div_ieee(x, (T) C);
+   return q;
+}
+
+// Four quotients at once: one test for the rare slow path.
+template <int C, typename T>
+__device__ __forceinline__ void div_const4(const T (&x)[4], T (&q)[4])
+{
+   bool slow = false;
+#pragma unroll
+   for (int m = 0; m < 4; m++) {
+      q[m] = div_fast<C>(x[m]);
+      slow |= !div_window(x[m]);
    }
-   return __fdiv_rn(x, (float) C);
+   if (__builtin_expect(slow, 0)) {
+#pragma unroll
+      for (int m = 0; m < 4; m++)
+         if (!div_window(x[m]))
+            q[m] = div_ieee(x[m], (T) C);
+   }
 }
-__device__ __forceinline__ float div7(float x)
-{
-   return div_const_f<7>(x, 0x1.24924ap-3f);
-}
-__device__ __forceinline__ float div27(float x)
-{
-   return div_const_f<27>(x, 0x1.2f684cp-5f);
-}
+
+__device__ __forceinline__ double div7(double x) { return div_const<7>(x); }
+__device__ __forceinline__ double div27(double x) { return div_const<27>(x); }
+__device__ __forceinline__ float div7(float x) { return div_const<7>(x); }
+__device__ __forceinline__ float div27(float x) { return div_const<27>(x); }
 
 // Exact scalings: x/4 and x/8 equal x*0.25 and x*0.125 in IEEE arithmetic.
 __device__ __forceinline__ double quarter(double x) { return x * 0.25; }

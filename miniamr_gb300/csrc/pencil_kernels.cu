@@ -230,6 +230,7 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                Quad<T>::ld(t + (i * G + j - 1) * RS + 4 * kq, sm);
                Quad<T>::ld(t + (i * G + j + 1) * RS + 4 * kq, sp);
                row6(t, klo, khi, i + 1, j, kq, c);
+               T w[4];
 #pragma unroll
                for (int m = 0; m < 4; m++) {
                   T v = am[m] + sm[m];
@@ -238,8 +239,9 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                   v = v + r[m + 2];
                   v = v + sp[m];
                   v = v + c[m + 1];
-                  out[m] = div7(v);
+                  w[m] = v;
                }
+               div_const4<7>(w, out);
                Quad<T>::st(d + row_offset(g, i, j) + 4 * kq, out);
                if (sizeof(T) == 4 && do_cs)
 #pragma unroll
@@ -283,9 +285,11 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
             for (int ii = 1; ii <= 4; ii++) {
                const int i = 4 * ih + ii;
                S4(i + 1, s2);
+               T w[4];
 #pragma unroll
                for (int m = 0; m < 4; m++)
-                  out[m] = div27((s0[m] + s1[m]) + s2[m]);
+                  w[m] = (s0[m] + s1[m]) + s2[m];
+               div_const4<27>(w, out);
                Quad<T>::st(d + row_offset(g, i, j) + 4 * kq, out);
                if (sizeof(T) == 4 && do_cs)
 #pragma unroll
