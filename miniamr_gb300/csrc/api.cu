@@ -193,7 +193,6 @@ extern "C" int mamr_create(const mamr_config *cfg, mamr_ctx **out)
    g.koff = 0;
    g.kplane = (long long) g.X * g.Y * g.nz;
    g.bv = ((g.kplane + 2LL * g.X * g.Y + line - 1) / line) * line;
-   g.kil = c->fp32 ? 1 : 0;
    size_t tile = (size_t) g.X * g.Y * g.Z * elem_size(c);
    if (tile > 200 * 1024) {
       delete c;

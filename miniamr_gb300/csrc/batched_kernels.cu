@@ -78,8 +78,8 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       const T *s = src + bv_offset(g, sI.slot, var);
       T *d = dst + bv_offset(g, sI.slot, var);
 
-      // interior rows, 16-byte vectors when they hold k in order
-      if (vec && !g.kil) {
+      // interior rows, 16-byte vectors (rows start on a sector boundary)
+      if (vec) {
          using V = typename Vec16<T>::type;
          for (int e = threadIdx.x; e < nx * ny * nvec; e += blockDim.x) {
             int r = e / nvec, q = e - r * nvec;

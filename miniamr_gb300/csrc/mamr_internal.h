@@ -17,9 +17,6 @@ namespace mamr {
 //    ghost values k = 0 and k = nz+1 of row (i, j) sit in two planes after
 //    the rows, at kplane + i*Y + j and kplane + X*Y + i*Y + j.  bv is
 //    rounded up to whole 128-byte lines.
-//    With kil set (FP32 pools) a row stores its interior k-interleaved:
-//    k = 1, 1+nz/2, 2, 2+nz/2, ..., so that the pairs (k, k+nz/2) a thread
-//    updates together with packed two-wide FP32 arithmetic sit side by side.
 //  - inline (kplane < 0; host buffers): rows of Zp elements holding
 //    k = 0..nz+1 at columns koff .. koff+nz+1.
 struct Geom {
@@ -28,7 +25,6 @@ struct Geom {
    int Zp, koff;      // inline layout: row length, column of k = 0
    long long kplane;  // split layout: offset of the k = 0 plane, else -1
    long long bv;      // elements per block-variable
-   int kil;           // split layout: interior rows k-interleaved
 };
 
 __host__ __device__ inline long long bv_offset(const Geom &g, int slot,
@@ -43,19 +39,12 @@ __host__ __device__ inline long long cell_offset(const Geom &g, int i, int j,
    const long long row = (long long) i * g.Y + j;
    if (g.kplane < 0)
       return row * g.Zp + g.koff + k;
-   if (k >= 1 && k <= g.nz) {
-      int kk = k - 1;
-      if (g.kil) {
-         const int h = g.nz >> 1;
-         kk = kk < h ? 2 * kk : 2 * (kk - h) + 1;
-      }
-      return row * g.nz + kk;
-   }
+   if (k >= 1 && k <= g.nz)
+      return row * g.nz + (k - 1);
    return g.kplane + (k == 0 ? 0 : (long long) g.X * g.Y) + row;
 }
 
-// Offset of interior row (i, j) in the split layout (its first element;
-// k = 1 unless the rows are interleaved).
+// Offset of interior row (i, j), k = 1, in the split layout.
 __host__ __device__ inline long long row_offset(const Geom &g, int i, int j)
 {
    return ((long long) i * g.Y + j) * g.nz;

@@ -80,7 +80,7 @@ constexpr int DESC = sizeof(TileDesc) / sizeof(int32_t);
 // Queues the cp.async copies of tile `s` of the pencil into ring buffer t:
 // the interior rows, the four x/y face rows (neighbour or reflection) and,
 // for 27 points, the four z-running edge rows.
-template <typename T, int ST, int ROW = RS>
+template <typename T, int ST>
 __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
                                            const Geom &g, const TileDesc *it,
                                            int var, T *t)
@@ -93,7 +93,7 @@ __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
    for (int c = tid; c < NB * NB * CPR; c += THREADS) {
       const int q = c % CPR, r = c / CPR;
       const int j = r % NB + 1, i = r / NB + 1;
-      cp_async16(t + (i * G + j) * ROW + q * VW,
+      cp_async16(t + (i * G + j) * RS + q * VW,
                  own + row_offset(g, i, j) + q * VW);
    }
    for (int c = tid; c < 4 * NB * CPR; c += THREADS) {
@@ -111,10 +111,10 @@ __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
       T *to;
       if (f < 2) {
          from = blk + row_offset(g, sp, a);
-         to = t + (gp * G + a) * ROW;
+         to = t + (gp * G + a) * RS;
       } else {
          from = blk + row_offset(g, a, sp);
-         to = t + (a * G + gp) * ROW;
+         to = t + (a * G + gp) * RS;
       }
       cp_async16(to + q * VW, from + q * VW);
    }
@@ -128,7 +128,7 @@ __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
          if (bmask & (1 << ((e & 2) ? 3 : 2))) { sj = (e & 2) ? NB : 1; dy = 0; }
          else sj = (e & 2) ? 1 : NB;
          const int nb = it->nb9[(dx + 1) + 3 * (dy + 1)];
-         cp_async16(t + (gi * G + gj) * ROW + q * VW,
+         cp_async16(t + (gi * G + gj) * RS + q * VW,
                     src + bv_offset(g, nb, var) + row_offset(g, si, sj) +
                        q * VW);
       }
@@ -349,225 +349,6 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
    }
 }
 
-// ---------------------------------------------------------------------------
-// FP32 pencil kernel on packed pairs.  FP32 pools store each interior row
-// k-interleaved (k = 1, 9, 2, 10, ..., 8, 16), so element pairs (k, k+8)
-// are adjacent and one two-wide FP32 instruction (__fadd2_rn etc.)
-// updates both: two independent IEEE round-to-nearest operations, bit for
-// bit what the scalar code computes, in half the instructions.  A shared
-// row holds the 8 interior pairs, then (k9, k17) and (k0, k8): the
-// neighbour pairs of the first and last interior pairs, filled once per
-// step from this tile and its z neighbours.  A thread owns interior pairs
-// 2kq and 2kq+1 of one (j) row for 4 planes and loads the pairs
-// 2kq-1 .. 2kq+2 it needs with aligned 8- and 16-byte loads.
-namespace {
-
-constexpr int RS2 = 20;        // floats per shared row
-constexpr int P_HI = 16;       // (k9, k17)
-constexpr int P_LO = 18;       // (k0, k8)
-
-__device__ __forceinline__ float2 ld2(const float *p)
-{
-   return *reinterpret_cast<const float2 *>(p);
-}
-__device__ __forceinline__ float2 add2(float2 a, float2 b)
-{
-   return __fadd2_rn(a, b);
-}
-
-// w / C for both lanes: the three-step quotient of div_fast, packed, with
-// the IEEE division for lanes outside its window (rare branch).
-template <int C>
-__device__ __forceinline__ float2 div2(float2 w)
-{
-   const float y = C == 7 ? 0x1.24924ap-3f : 0x1.2f684cp-5f;
-   const float2 yy = make_float2(y, y);
-   const float2 q0 = __fmul2_rn(w, yy);
-   const float2 r = __ffma2_rn(q0, make_float2(-(float) C, -(float) C), w);
-   float2 q = __ffma2_rn(r, yy, q0);
-   if (__builtin_expect(!div_window(w.x) || !div_window(w.y), 0)) {
-      if (!div_window(w.x)) q.x = div_ieee(w.x, (float) C);
-      if (!div_window(w.y)) q.y = div_ieee(w.y, (float) C);
-   }
-   return q;
-}
-
-}  // namespace
-
-template <int ST>
-__global__ void __launch_bounds__(THREADS, 2)
-pencil_f32x2_kernel(const float *__restrict__ src, float *__restrict__ dst,
-                    Geom g, const TileDesc *__restrict__ chain,
-                    const int2 *__restrict__ pencils, int n_pencils,
-                    int write_ghosts, int do_cs,
-                    unsigned long long *__restrict__ acc,
-                    unsigned *__restrict__ err)
-{
-   extern __shared__ __align__(16) unsigned char smem_raw[];
-   __shared__ TileDesc s_desc[PENCIL_MAX];
-   float *tiles = reinterpret_cast<float *>(smem_raw);
-   constexpr int TILE = TILE_ROWS * RS2;
-   const int tid = threadIdx.x;
-   const int kq = tid & 3, j = ((tid >> 2) & 15) + 1, ih = tid >> 6;
-   const int offA = kq == 0 ? P_LO : 4 * kq - 2;   // pair 2kq-1
-   const int offB = 4 * kq;                        // pairs 2kq, 2kq+1
-   const int offD = 4 * kq + 4;                    // pair 2kq+2
-
-   for (int w = blockIdx.x; w < n_pencils * g.V; w += gridDim.x) {
-      const int var = w / n_pencils, p = w - var * n_pencils;
-      const int2 pc = pencils[p];
-      const int len = pc.y;
-      {
-         const int32_t *from = reinterpret_cast<const int32_t *>(chain + pc.x);
-         int32_t *to = reinterpret_cast<int32_t *>(s_desc);
-         for (int q = tid; q < len * DESC; q += THREADS)
-            to[q] = from[q];
-      }
-      __syncthreads();
-      issue_tile<float, ST, RS2>(src, g, s_desc, var, tiles);
-      if (len > 1)
-         issue_tile<float, ST, RS2>(src, g, s_desc + 1, var, tiles + TILE);
-      unsigned long long lo = 0, hi = 0;
-      bool ok = true;
-      for (int s = 0; s < len; s++) {
-         float *t = tiles + (s % 3) * TILE;
-         const float *tn = tiles + ((s + 1) % 3) * TILE;
-         const float *tp = tiles + ((s + 2) % 3) * TILE;   // tile s-1
-         cp_async_wait_all();
-         __syncthreads();
-         // edge pairs: (k9, k17) and (k0, k8); k17 is tile s+1's k1 (or
-         // our k16 at the top boundary), k0 tile s-1's k16 (or our k1)
-         for (int e = tid; e < KC; e += THREADS) {
-            const int i = e / G, jj = e - (e / G) * G;
-            if (ST == 7 && (i == 0 || i == G - 1 || jj == 0 || jj == G - 1))
-               continue;
-            float *r = t + e * RS2;
-            r[P_HI] = r[1];
-            r[P_HI + 1] = s + 1 < len ? tn[e * RS2] : r[15];
-            r[P_LO] = s > 0 ? tp[e * RS2 + 15] : r[0];
-            r[P_LO + 1] = r[14];
-         }
-         __syncthreads();
-         if (s + 2 < len)
-            issue_tile<float, ST, RS2>(src, g, s_desc + s + 2, var,
-                                       tiles + ((s + 2) % 3) * TILE);
-
-         const int slot = s_desc[s].slot;
-         float *d = dst + bv_offset(g, slot, var);
-         if (ST == 7) {
-            const float *x = t + ((4 * ih + 1) * G + j) * RS2;
-            float2 mB = ld2(t + ((4 * ih) * G + j) * RS2 + offB);
-            float2 mC = ld2(t + ((4 * ih) * G + j) * RS2 + offB + 2);
-            float2 xA = ld2(x + offA), xB = ld2(x + offB),
-                   xC = ld2(x + offB + 2), xD = ld2(x + offD);
-#pragma unroll
-            for (int ii = 1; ii <= 4; ii++) {
-               const int i = 4 * ih + ii;
-               const float *jm = t + (i * G + j - 1) * RS2;
-               const float *jp = t + (i * G + j + 1) * RS2;
-               const float *xn = t + ((i + 1) * G + j) * RS2;
-               const float2 jmB = ld2(jm + offB), jmC = ld2(jm + offB + 2);
-               const float2 jpB = ld2(jp + offB), jpC = ld2(jp + offB + 2);
-               const float2 nA = ld2(xn + offA), nB = ld2(xn + offB),
-                            nC = ld2(xn + offB + 2), nD = ld2(xn + offD);
-               float2 wa = add2(add2(add2(add2(add2(add2(mB, jmB), xA), xB),
-                                          xC), jpB), nB);
-               float2 wb = add2(add2(add2(add2(add2(add2(mC, jmC), xB), xC),
-                                          xD), jpC), nC);
-               const float2 qa = div2<7>(wa), qb = div2<7>(wb);
-               *reinterpret_cast<float4 *>(d + row_offset(g, i, j) + offB) =
-                  make_float4(qa.x, qa.y, qb.x, qb.y);
-               if (do_cs) {
-                  long long q;
-                  ok &= fixed52(qa.x, q); acc128_add(lo, hi, q);
-                  ok &= fixed52(qa.y, q); acc128_add(lo, hi, q);
-                  ok &= fixed52(qb.x, q); acc128_add(lo, hi, q);
-                  ok &= fixed52(qb.y, q); acc128_add(lo, hi, q);
-               }
-               mB = xB; mC = xC;
-               xA = nA; xB = nB; xC = nC; xD = nD;
-            }
-         } else {
-            // the reference's 9-term plane sum for the thread's two pairs
-            auto S2 = [&](int pl, float2 &sa, float2 &sb) {
-               const float *r0 = t + (pl * G + j - 1) * RS2;
-               const float *r1 = r0 + RS2, *r2 = r1 + RS2;
-               const float2 a0 = ld2(r0 + offA), b0 = ld2(r0 + offB),
-                            c0 = ld2(r0 + offB + 2), d0 = ld2(r0 + offD);
-               const float2 a1 = ld2(r1 + offA), b1 = ld2(r1 + offB),
-                            c1 = ld2(r1 + offB + 2), d1 = ld2(r1 + offD);
-               const float2 a2 = ld2(r2 + offA), b2 = ld2(r2 + offB),
-                            c2 = ld2(r2 + offB + 2), d2 = ld2(r2 + offD);
-               sa = add2(add2(add2(add2(add2(add2(add2(add2(a0, b0), c0), a1),
-                                                b1), c1), a2), b2), c2);
-               sb = add2(add2(add2(add2(add2(add2(add2(add2(b0, c0), d0), b1),
-                                                c1), d1), b2), c2), d2);
-            };
-            float2 s0a, s0b, s1a, s1b;
-            S2(4 * ih, s0a, s0b);
-            S2(4 * ih + 1, s1a, s1b);
-#pragma unroll
-            for (int ii = 1; ii <= 4; ii++) {
-               const int i = 4 * ih + ii;
-               float2 s2a, s2b;
-               S2(i + 1, s2a, s2b);
-               const float2 qa = div2<27>(add2(add2(s0a, s1a), s2a));
-               const float2 qb = div2<27>(add2(add2(s0b, s1b), s2b));
-               *reinterpret_cast<float4 *>(d + row_offset(g, i, j) + offB) =
-                  make_float4(qa.x, qa.y, qb.x, qb.y);
-               if (do_cs) {
-                  long long q;
-                  ok &= fixed52(qa.x, q); acc128_add(lo, hi, q);
-                  ok &= fixed52(qa.y, q); acc128_add(lo, hi, q);
-                  ok &= fixed52(qb.x, q); acc128_add(lo, hi, q);
-                  ok &= fixed52(qb.y, q); acc128_add(lo, hi, q);
-               }
-               s0a = s1a; s0b = s1b;
-               s1a = s2a; s1b = s2b;
-            }
-         }
-         if (write_ghosts) {
-            const int n_shell = G * G * G - NB * NB * NB;
-            for (int e = tid; e < n_shell; e += THREADS) {
-               int gi, gj, gk;
-               if (e < 2 * G * G) {
-                  gi = e < G * G ? 0 : G - 1;
-                  const int r = e % (G * G);
-                  gj = r / G; gk = r % G;
-               } else if (e < 2 * G * G + 2 * NB * G) {
-                  const int r = e - 2 * G * G;
-                  gj = r < NB * G ? 0 : G - 1;
-                  const int r2 = r % (NB * G);
-                  gi = r2 / G + 1; gk = r2 % G;
-               } else {
-                  const int r = e - 2 * G * G - 2 * NB * G;
-                  gk = r < NB * NB ? 0 : G - 1;
-                  const int r2 = r % (NB * NB);
-                  gi = r2 / NB + 1; gj = r2 % NB + 1;
-               }
-               const int outside = (gi == 0 || gi == G - 1) +
-                                   (gj == 0 || gj == G - 1) +
-                                   (gk == 0 || gk == G - 1);
-               if (ST == 7 && outside != 1)
-                  continue;
-               const float *r = t + (gi * G + gj) * RS2;
-               int pos;
-               if (gk == 0) pos = P_LO;
-               else if (gk == G - 1) pos = P_HI + 1;
-               else pos = gk <= NB / 2 ? 2 * (gk - 1) : 2 * (gk - 1 - NB / 2) + 1;
-               d[cell_offset(g, gi, gj, gk)] = r[pos];
-            }
-         }
-      }
-      if (do_cs) {
-         if (!ok)
-            atomicOr(err, ERR_FIXED_RANGE);
-         block_acc128_flush(lo, hi, acc + 2 * var);
-      }
-      __syncthreads();
-   }
-}
-
 // FP64 checksum of every (block, variable) of the pool in the reference's
 // order: one thread per block-variable sums its interior serially.
 __global__ void __launch_bounds__(128)
@@ -613,33 +394,13 @@ static cudaError_t pencil_attr()
                                (int) pencil_smem_bytes<T>());
 }
 
-constexpr size_t f32x2_smem_bytes()
-{
-   return (size_t) 3 * TILE_ROWS * RS2 * sizeof(float);
-}
-
 template <typename T>
 int pencil_grid(int stencil, int n_work)
 {
    int per_sm = 0, dev = 0, sms = 0;
    cudaGetDevice(&dev);
    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-   if (sizeof(T) == 4) {
-      const size_t smem = f32x2_smem_bytes();
-      if (stencil == 7) {
-         cudaFuncSetAttribute(pencil_f32x2_kernel<7>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int) smem);
-         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, pencil_f32x2_kernel<7>, THREADS, smem);
-      } else {
-         cudaFuncSetAttribute(pencil_f32x2_kernel<27>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int) smem);
-         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, pencil_f32x2_kernel<27>, THREADS, smem);
-      }
-   } else if (stencil == 7) {
+   if (stencil == 7) {
       pencil_attr<T, 7>();
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
          &per_sm, pencil_stage_kernel<T, 7>, THREADS, pencil_smem_bytes<T>());
@@ -665,19 +426,7 @@ int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
       return 0;
    const size_t smem = pencil_smem_bytes<T>();
    const int fused_cs = (sizeof(T) == 4) ? do_cs : 0;
-   if (sizeof(T) == 4) {
-      // FP32 pools are k-interleaved: the packed kernel
-      const float *fs = reinterpret_cast<const float *>(src);
-      float *fd = reinterpret_cast<float *>(dst);
-      if (stencil == 7)
-         pencil_f32x2_kernel<7><<<grid, THREADS, f32x2_smem_bytes(), s>>>(
-            fs, fd, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc,
-            err);
-      else
-         pencil_f32x2_kernel<27><<<grid, THREADS, f32x2_smem_bytes(), s>>>(
-            fs, fd, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc,
-            err);
-   } else if (stencil == 7)
+   if (stencil == 7)
       pencil_stage_kernel<T, 7><<<grid, THREADS, smem, s>>>(
          src, dst, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc,
          err);

@@ -75,7 +75,6 @@ extern "C" int mamr_check_sum_fp64_noalloc(const double *blocks,
    g.Zp = g.Z;
    g.koff = 0;
    g.kplane = -1;
-   g.kil = 0;
    g.bv = (long long) g.X * g.Y * g.Z;
    int n = mamr::launch_checksum_fp64(blocks, g, slots, n_blocks, var,
                                       partials, sum,
