@@ -279,7 +279,8 @@ def main():
 
     import torch
     from miniamr_gb300 import build, load
-    from miniamr_gb300.abi import FP32, FP64, RUN_BATCHED, RUN_GRAPH, RUN_PLAIN
+    from miniamr_gb300.abi import (FP32, FP64, RUN_BATCHED, RUN_GRAPH,
+                                   RUN_PER_BLOCK, RUN_PLAIN)
 
     torch.cuda.set_device(local)
     build.build_library()
@@ -346,6 +347,10 @@ def main():
     t0 = time.perf_counter()
     ctx64.run_timesteps(1, SPT, FREQ, flags=RUN_PLAIN)
     fp64_plain = updates(1) / (time.perf_counter() - t0)
+    # the naive port: one stencil launch per (block, variable), one stage
+    t0 = time.perf_counter()
+    ctx64.run_timesteps(1, 1, 0, flags=RUN_PLAIN | RUN_PER_BLOCK)
+    fp64_per_block = UPD_PER_STAGE / (time.perf_counter() - t0)
     ctx64.close()
     ref = s64[W:W + min(K, K64)]
     got = sums32[:len(ref)]
@@ -373,6 +378,7 @@ def main():
         "gpu_launches": launches,
         "paths": {"fp32_batched": value / world,
                   "fp64_batched": fp64_batched, "fp64_plain": fp64_plain,
+                  "fp64_one_launch_per_block_var": fp64_per_block,
                   "fp32_batched_over_fp64_plain": value / world / fp64_plain},
         "fp32_checksum_error": err,
         "clocks": clk.summary(),

@@ -103,7 +103,10 @@ enum {
                              variable, exactly the driver's call sequence */
    MAMR_RUN_BATCHED = 1,  /* one fused ghost+stencil(+checksum) launch per
                              stage over every block and variable */
-   MAMR_RUN_GRAPH   = 2   /* with BATCHED: replay the stages as a CUDA graph */
+   MAMR_RUN_GRAPH   = 2,  /* with BATCHED: replay the stages as a CUDA graph */
+   MAMR_RUN_PER_BLOCK = 4 /* with PLAIN: one stencil launch per (block,
+                             variable) -- the naive port, kept as a
+                             baseline to measure the batched path against */
 };
 
 /* ---- lifetime --------------------------------------------------------- */

@@ -18,6 +18,7 @@ FP32 = 1
 RUN_PLAIN = 0
 RUN_BATCHED = 1
 RUN_GRAPH = 2
+RUN_PER_BLOCK = 4
 
 STATUS = {
     0: "MAMR_OK",

@@ -504,9 +504,23 @@ extern "C" int mamr_comm(mamr_ctx *c, int32_t start, int32_t num,
    return comm_impl(c, start, num, stage);
 }
 
-static int stencil_impl(mamr_ctx *c, int32_t var)
+static int stencil_impl(mamr_ctx *c, int32_t var, bool per_block = false)
 {
    const int n = (int) c->mesh.size();
+   if (per_block) {
+      for (int b = 0; b < n; b++) {
+         const int32_t *one = (const int32_t *) c->d_slots.p + b;
+         if (c->fp32)
+            LAUNCH_TRY(c, launch_stencil((float *) c->pool, c->g,
+                                         c->cfg.stencil, one, 1, var,
+                                         c->stream));
+         else
+            LAUNCH_TRY(c, launch_stencil((double *) c->pool, c->g,
+                                         c->cfg.stencil, one, 1, var,
+                                         c->stream));
+      }
+      return MAMR_OK;
+   }
    if (c->fp32)
       LAUNCH_TRY(c, launch_stencil((float *) c->pool, c->g, c->cfg.stencil,
                                    (const int32_t *) c->d_slots.p, n, var,
@@ -706,7 +720,8 @@ extern "C" int mamr_consolidate(mamr_ctx *c, const mamr_consolidate_job *jobs,
 // Plain stage loop: the driver's call sequence queued without host syncs;
 // checksums land in a device array and come back once at the end.
 static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
-                     int32_t first_stage, double *sums, int32_t *n_sums)
+                     int32_t first_stage, bool per_block, double *sums,
+                     int32_t *n_sums)
 {
    const int V = c->cfg.num_vars;
    int per_ts = 0;
@@ -724,7 +739,7 @@ static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
          if ((r = comm_impl(c, 0, V, gstage)))
             return r;
          for (int var = 0; var < V; var++) {
-            if ((r = stencil_impl(c, var)))
+            if ((r = stencil_impl(c, var, per_block)))
                return r;
             if (do_cs) {
                size_t idx = (size_t) cnt * V + var;
@@ -1052,14 +1067,16 @@ extern "C" int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts,
 {
    if (!c || num_ts < 0 || stages_per_ts < 1 || checksum_freq < 0)
       return fail(MAMR_EINVAL, "bad run arguments");
-   if (flags & ~(MAMR_RUN_BATCHED | MAMR_RUN_GRAPH))
+   if (flags & ~(MAMR_RUN_BATCHED | MAMR_RUN_GRAPH | MAMR_RUN_PER_BLOCK))
       return fail(MAMR_EINVAL, "unknown run flags 0x%x", flags);
    if (!(flags & MAMR_RUN_BATCHED)) {
       if (flags & MAMR_RUN_GRAPH)
          return fail(MAMR_EINVAL, "MAMR_RUN_GRAPH needs MAMR_RUN_BATCHED");
       return run_plain(c, num_ts, stages_per_ts, checksum_freq, first_stage,
-                       sums, n_sums);
+                       (flags & MAMR_RUN_PER_BLOCK) != 0, sums, n_sums);
    }
+   if (flags & MAMR_RUN_PER_BLOCK)
+      return fail(MAMR_EINVAL, "MAMR_RUN_PER_BLOCK applies to the plain path");
    return run_batched(c, num_ts, stages_per_ts, checksum_freq,
                       (flags & MAMR_RUN_GRAPH) != 0, sums, n_sums);
 }

@@ -182,3 +182,86 @@ def replay(lib: Library, records: list[Record], dtype: int | None = None,
         elif r.op == OP_CONSOLIDATE:
             ctx.consolidate(r.args[0])
     return ReplayResult(sums, hashes, ctx, mesh, numbers)
+
+
+def replay_batched(lib: Library, records: list[Record], flags: int,
+                   dtype: int | None = None, num_vars: int | None = None):
+    """Replays a trace with every run of consecutive stages between mesh
+    changes executed as one mamr_run_timesteps call (flags: RUN_BATCHED,
+    RUN_GRAPH ...), one timestep of one stage per recorded stage.  Returns
+    (checksums [(var, replayed, recorded)], ReplayResult-like context),
+    plus per-call timings [(stages, seconds)] for throughput figures.
+
+    Checksum cadence must be uniform inside a run: stages are grouped by
+    whether they computed checksums.  num_vars overrides the recorded
+    variable count (the mesh sequence does not depend on it; the initial
+    values are then regenerated for the new count without the upload hash
+    check, and recorded checksums are not comparable)."""
+    import time
+    ctx = None
+    cfg = None
+    sums = []
+    timings = []
+    pending = []          # [(stage, with_checksums, recorded sums)]
+
+    def flush():
+        i = 0
+        while i < len(pending):
+            j = i
+            while (j + 1 < len(pending) and pending[j + 1][1] == pending[i][1]
+                   and pending[j + 1][0] == pending[j][0] + 1):
+                j += 1
+            n = j - i + 1
+            cs = pending[i][1]
+            t0 = time.perf_counter()
+            got = ctx.run_timesteps(n, 1, 1 if cs else 0, pending[i][0],
+                                    flags=flags)
+            timings.append((n, time.perf_counter() - t0))
+            if cs:
+                for q in range(n):
+                    for var, rec in pending[i + q][2]:
+                        if var < cfg.num_vars:
+                            sums.append((var, float(got[q][var]), rec))
+            i = j + 1
+        pending.clear()
+
+    stage = None
+    for r in records:
+        if r.op == OP_CREATE:
+            cfg = Config.from_buffer_copy(bytes(r.args[0]))
+            if dtype is not None:
+                cfg.dtype = dtype
+            rec_vars = cfg.num_vars
+            if num_vars is not None:
+                cfg.num_vars = num_vars
+            ctx = lib.context(cfg)
+        elif r.op == OP_UPLOAD:
+            slots, h = r.args
+            data = lib.initial_values(cfg, int(slots.max()) + 1)[slots]
+            if cfg.num_vars == rec_vars and upload_hash(data) != h:
+                raise AssertionError("regenerated initial values differ")
+            ctx.upload(slots, data)
+        elif r.op in (OP_SET_MESH, OP_SPLIT, OP_CONSOLIDATE):
+            flush()
+            if r.op == OP_SET_MESH:
+                ctx.set_mesh(r.args[0])
+            elif r.op == OP_SPLIT:
+                ctx.split(r.args[0])
+            else:
+                ctx.consolidate(r.args[0])
+        elif r.op == OP_COMM:
+            if r.args[0] != 0 or r.args[1] != rec_vars:
+                raise ValueError("batched replay needs comm over all vars")
+            stage = [r.args[2], False, []]
+            pending.append(stage)
+        elif r.op == OP_CHECK_SUM:
+            if stage is None:
+                # init()'s checksums, before any stage
+                if r.args[0] < cfg.num_vars:
+                    sums.append((r.args[0], ctx.check_sum(r.args[0]),
+                                 r.args[1]))
+            else:
+                stage[1] = True
+                stage[2].append(r.args)
+    flush()
+    return sums, ctx, timings

@@ -76,6 +76,26 @@ CASES = {
                 "8000", "--num_objects", "1", "--object", "2", "1", "0.25",
                 "0.25", "0.25", "0.01", "0.01", "0.01", "0.15", "0.15", "0.15",
                 "0", "0", "0"],
+    # the multi-level stress mesh, shortened: 4^3 blocks of 8^3, 5 levels,
+    # four moving objects (surface sphere r 0.06, solid sphere r 0.05,
+    # surface cylinder r 0.03, surface box of half-side 0.06; sizes tuned on
+    # the reference so the mesh holds ~21k-24k blocks), 7-point, refine every
+    # 2 steps, 20 steps x 2 stages, 4 variables (the block sequence does not
+    # depend on the variable count).  Cell hashes every 8th checksum stage.
+    "config5": ["--init_x", "4", "--init_y", "4", "--init_z", "4", "--nx",
+                "8", "--ny", "8", "--nz", "8", "--num_vars", "4",
+                "--stencil", "7", "--num_refine", "5", "--refine_freq", "2",
+                "--num_tsteps", "20", "--stages_per_ts", "2",
+                "--checksum_freq", "1", "--max_blocks", "40000",
+                "--num_objects", "4",
+                "--object", "2", "1", "0.3", "0.3", "0.3", "0.01", "0.007",
+                "0.005", "0.06", "0.06", "0.06", "0", "0", "0",
+                "--object", "3", "1", "0.7", "0.6", "0.4", "-0.008", "0.006",
+                "0.01", "0.05", "0.05", "0.05", "0", "0", "0",
+                "--object", "20", "1", "0.5", "0.5", "0.7", "0.006", "-0.01",
+                "0.004", "0.12", "0.03", "0.03", "0", "0", "0",
+                "--object", "0", "1", "0.3", "0.7", "0.7", "0.007", "-0.005",
+                "-0.009", "0.06", "0.06", "0.06", "0", "0", "0"],
     # two objects, volume + surface refinement, 7-point, 4 levels, default
     # checksum cadence (every 5th stage of 3)
     "amr7_objects": ["--init_x", "2", "--init_y", "2", "--init_z", "2",
@@ -91,7 +111,7 @@ CASES = {
 }
 
 
-HASH_STRIDE = {"config2": 10}
+HASH_STRIDE = {"config2": 10, "config5": 8}
 
 
 def run_case(name, args):

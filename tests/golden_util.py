@@ -41,7 +41,7 @@ def arg(args, flag, default=None):
 # Cases too large to replay through the CPU oracle inside the CPU suite;
 # they are pinned by make_golden.py (hybrid == reference) and replayed on
 # the GPU.
-HEAVY = {"config2"}
+HEAVY = {"config2", "config5"}
 
 
 def hashed_stages(hashes, V):

@@ -6,8 +6,8 @@ import pytest
 
 from golden_util import trace_path
 from miniamr_gb300 import mesh as meshmod
-from miniamr_gb300.abi import (FP32, FP64, RUN_BATCHED, RUN_GRAPH, Config,
-                               MamrError)
+from miniamr_gb300.abi import (FP32, FP64, RUN_BATCHED, RUN_GRAPH,
+                               RUN_PER_BLOCK, Config, MamrError)
 from miniamr_gb300.trace import read_trace, replay
 
 pytestmark = pytest.mark.gpu
@@ -27,7 +27,8 @@ UNIFORM = [
 ]
 
 
-@pytest.mark.parametrize("flags", [RUN_BATCHED, RUN_BATCHED | RUN_GRAPH])
+@pytest.mark.parametrize("flags", [RUN_BATCHED, RUN_BATCHED | RUN_GRAPH,
+                                   RUN_PER_BLOCK])
 @pytest.mark.parametrize("dtype", [FP64, FP32])
 @pytest.mark.parametrize("case", UNIFORM)
 def test_batched_equals_plain_uniform(gpu_lib, case, dtype, flags):
