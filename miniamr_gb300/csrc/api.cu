@@ -16,6 +16,7 @@
 
 #include "mamr_internal.h"
 #include "batched.h"
+#include "segments.h"
 
 using namespace mamr;
 
@@ -130,6 +131,7 @@ struct mamr_ctx {
    DevBuf d_tasks[3];
    DirTasks tasks[3];
    DevBuf d_partials, d_jobs, d_stage, d_stage_slots, d_sums;
+   DevBuf d_xfer, d_xfer_slots;      // staging copies for split/consolidate
    unsigned long long *d_acc;       // 2 words: fixed-point accumulator
    double *d_sum;                   // FP64 checksum result
    unsigned *d_err;                 // device error word
@@ -244,6 +246,7 @@ extern "C" int mamr_destroy(mamr_ctx *c)
    for (auto &b : c->d_tasks) b.release();
    c->d_slots.release(); c->d_partials.release(); c->d_jobs.release();
    c->d_stage.release(); c->d_stage_slots.release(); c->d_sums.release();
+   c->d_xfer.release(); c->d_xfer_slots.release();
    if (c->d_acc) cudaFree(c->d_acc);
    if (c->d_sum) cudaFree(c->d_sum);
    if (c->d_err) cudaFree(c->d_err);
@@ -598,58 +601,56 @@ extern "C" int mamr_check_sum(mamr_ctx *c, int32_t var, double *sum)
    return MAMR_OK;
 }
 
-// Orders data-movement jobs into waves so that jobs of one wave touch
-// disjoint slots except for shared reads: a job waits for every earlier job
-// that reads a slot it writes or writes a slot it reads or writes.  This
-// keeps the reference's sequential semantics, where a later child (split)
-// or target (consolidate) may land in a slot an earlier job just freed, and
-// a later consolidation may read an earlier one's target.
-template <int NR, int NW>
-static void schedule_waves(const std::vector<std::array<int32_t, NR>> &reads,
-                           const std::vector<std::array<int32_t, NW>> &writes,
-                           int max_slots, std::vector<int> &wave)
+template <int NR, int NW, typename Job, typename Reads, typename Writes,
+          typename Launch>
+static int run_segments(mamr_ctx *c, const Job *jobs_in, int32_t n,
+                        Reads reads, Writes writes, Launch launch)
 {
-   std::vector<int> last_r(max_slots, -1), last_w(max_slots, -1);
-   const size_t n = reads.size();
-   wave.assign(n, 0);
-   for (size_t t = 0; t < n; t++) {
-      int w = 0;
-      for (int32_t s : reads[t])
-         w = std::max(w, last_w[s] + 1);
-      for (int32_t s : writes[t])
-         w = std::max(w, std::max(last_r[s], last_w[s]) + 1);
-      wave[t] = w;
-      for (int32_t s : reads[t])
-         last_r[s] = std::max(last_r[s], w);
-      for (int32_t s : writes[t])
-         last_w[s] = w;
+   const size_t elem = c->fp32 ? sizeof(float) : sizeof(double);
+   const size_t block_bytes = (size_t) c->cfg.num_vars * c->g.bv * elem;
+   std::vector<Job> jobs;
+   std::vector<int32_t> staged;
+   std::vector<Segment> segs;
+   size_t max_stage = std::max<size_t>(8, (size_t(1) << 30) / block_bytes);
+   for (;;) {
+      jobs.assign(jobs_in, jobs_in + n);
+      plan_segments<NR, NW>(jobs, c->cfg.max_blocks, max_stage, reads,
+                            writes, staged, segs);
+      size_t most = 0;
+      for (const Segment &sg : segs)
+         most = std::max(most, sg.stage_end - sg.stage_begin);
+      cudaError_t e = c->d_xfer.ensure(std::max<size_t>(1, most) *
+                                       block_bytes);
+      if (e == cudaSuccess)
+         break;
+      cudaGetLastError();
+      if (max_stage == 8)
+         return fail(MAMR_ENOMEM, "no device memory for %zu staged blocks",
+                     most);
+      max_stage = 8;
    }
-}
-
-template <typename Job, typename Launch>
-static int run_waves(mamr_ctx *c, const Job *jobs, const std::vector<int> &wave,
-                     Launch launch)
-{
-   const size_t n = wave.size();
-   int n_waves = 0;
-   for (int w : wave)
-      n_waves = std::max(n_waves, w + 1);
-   std::vector<Job> ordered;
-   ordered.reserve(n);
-   std::vector<size_t> start(n_waves + 1, 0);
-   for (int w = 0; w < n_waves; w++) {
-      start[w] = ordered.size();
-      for (size_t t = 0; t < n; t++)
-         if (wave[t] == w)
-            ordered.push_back(jobs[t]);
-   }
-   start[n_waves] = ordered.size();
-   CUDA_TRY(c->d_jobs.ensure(sizeof(Job) * std::max<size_t>(1, n)));
-   CUDA_TRY(cudaMemcpyAsync(c->d_jobs.p, ordered.data(), sizeof(Job) * n,
+   CUDA_TRY(c->d_jobs.ensure(sizeof(Job) * jobs.size()));
+   CUDA_TRY(cudaMemcpyAsync(c->d_jobs.p, jobs.data(), sizeof(Job) * n,
                             cudaMemcpyHostToDevice, c->stream));
-   for (int w = 0; w < n_waves; w++) {
-      const Job *dj = (const Job *) c->d_jobs.p + start[w];
-      LAUNCH_TRY(c, launch(dj, (int) (start[w + 1] - start[w])));
+   CUDA_TRY(c->d_xfer_slots.ensure(sizeof(int32_t) *
+                                   std::max<size_t>(1, staged.size())));
+   if (!staged.empty())
+      CUDA_TRY(cudaMemcpyAsync(c->d_xfer_slots.p, staged.data(),
+                               sizeof(int32_t) * staged.size(),
+                               cudaMemcpyHostToDevice, c->stream));
+   for (const Segment &sg : segs) {
+      const int32_t *sl = (const int32_t *) c->d_xfer_slots.p + sg.stage_begin;
+      const int ns = (int) (sg.stage_end - sg.stage_begin);
+      if (c->fp32)
+         LAUNCH_TRY(c, launch_stage_blocks((float *) c->d_xfer.p,
+                                           (const float *) c->pool, c->g, sl,
+                                           ns, c->stream));
+      else
+         LAUNCH_TRY(c, launch_stage_blocks((double *) c->d_xfer.p,
+                                           (const double *) c->pool, c->g, sl,
+                                           ns, c->stream));
+      const Job *dj = (const Job *) c->d_jobs.p + sg.begin;
+      LAUNCH_TRY(c, launch(dj, (int) (sg.end - sg.begin)));
    }
    CUDA_TRY(cudaStreamSynchronize(c->stream));
    return MAMR_OK;
@@ -659,30 +660,37 @@ extern "C" int mamr_split(mamr_ctx *c, const mamr_split_job *jobs, int32_t n)
 {
    if (!c || n < 0 || (n && !jobs))
       return fail(MAMR_EINVAL, "bad split arguments");
-   std::vector<std::array<int32_t, 1>> rd(n);
-   std::vector<std::array<int32_t, 8>> wr(n);
    for (int32_t t = 0; t < n; t++) {
       if (!slot_ok(c, jobs[t].parent))
          return fail(MAMR_EINVAL, "split parent slot %d out of range",
                      jobs[t].parent);
-      rd[t][0] = jobs[t].parent;
       for (int o = 0; o < 8; o++) {
          if (!slot_ok(c, jobs[t].child[o]))
             return fail(MAMR_EINVAL, "split child slot %d out of range",
                         jobs[t].child[o]);
-         wr[t][o] = jobs[t].child[o];
          c->hw_slots = std::max(c->hw_slots, jobs[t].child[o] + 1);
       }
    }
    if (n == 0)
       return MAMR_OK;
-   std::vector<int> wave;
-   schedule_waves<1, 8>(rd, wr, c->cfg.max_blocks, wave);
-   return run_waves(c, jobs, wave, [&](const mamr_split_job *dj, int m) {
-      return c->fp32 ? launch_split((float *) c->pool, c->g, dj, m, c->stream)
-                     : launch_split((double *) c->pool, c->g, dj, m,
-                                    c->stream);
-   });
+   return run_segments<1, 8>(
+      c, jobs, n,
+      [](mamr_split_job &j) { return std::array<int32_t *, 1>{&j.parent}; },
+      [](mamr_split_job &j) {
+         std::array<int32_t *, 8> w;
+         for (int o = 0; o < 8; o++)
+            w[o] = &j.child[o];
+         return w;
+      },
+      [&](const mamr_split_job *dj, int m) {
+         return c->fp32
+                   ? launch_split((float *) c->pool,
+                                  (const float *) c->d_xfer.p, c->g, dj, m,
+                                  c->stream)
+                   : launch_split((double *) c->pool,
+                                  (const double *) c->d_xfer.p, c->g, dj, m,
+                                  c->stream);
+      });
 }
 
 extern "C" int mamr_consolidate(mamr_ctx *c, const mamr_consolidate_job *jobs,
@@ -690,31 +698,38 @@ extern "C" int mamr_consolidate(mamr_ctx *c, const mamr_consolidate_job *jobs,
 {
    if (!c || n < 0 || (n && !jobs))
       return fail(MAMR_EINVAL, "bad consolidate arguments");
-   std::vector<std::array<int32_t, 8>> rd(n);
-   std::vector<std::array<int32_t, 1>> wr(n);
    for (int32_t t = 0; t < n; t++) {
       if (!slot_ok(c, jobs[t].target))
          return fail(MAMR_EINVAL, "consolidate target slot %d out of range",
                      jobs[t].target);
-      wr[t][0] = jobs[t].target;
       c->hw_slots = std::max(c->hw_slots, jobs[t].target + 1);
-      for (int o = 0; o < 8; o++) {
+      for (int o = 0; o < 8; o++)
          if (!slot_ok(c, jobs[t].child[o]))
             return fail(MAMR_EINVAL, "consolidate child slot %d out of range",
                         jobs[t].child[o]);
-         rd[t][o] = jobs[t].child[o];
-      }
    }
    if (n == 0)
       return MAMR_OK;
-   std::vector<int> wave;
-   schedule_waves<8, 1>(rd, wr, c->cfg.max_blocks, wave);
-   return run_waves(c, jobs, wave, [&](const mamr_consolidate_job *dj, int m) {
-      return c->fp32 ? launch_consolidate((float *) c->pool, c->g, dj, m,
-                                          c->stream)
-                     : launch_consolidate((double *) c->pool, c->g, dj, m,
-                                          c->stream);
-   });
+   return run_segments<8, 1>(
+      c, jobs, n,
+      [](mamr_consolidate_job &j) {
+         std::array<int32_t *, 8> r;
+         for (int o = 0; o < 8; o++)
+            r[o] = &j.child[o];
+         return r;
+      },
+      [](mamr_consolidate_job &j) {
+         return std::array<int32_t *, 1>{&j.target};
+      },
+      [&](const mamr_consolidate_job *dj, int m) {
+         return c->fp32
+                   ? launch_consolidate((float *) c->pool,
+                                        (const float *) c->d_xfer.p, c->g, dj,
+                                        m, c->stream)
+                   : launch_consolidate((double *) c->pool,
+                                        (const double *) c->d_xfer.p, c->g,
+                                        dj, m, c->stream);
+      });
 }
 
 // Plain stage loop: the driver's call sequence queued without host syncs;

@@ -93,10 +93,14 @@ int launch_checksum_fp32(const float *pool, const Geom &g,
                          unsigned long long *acc, unsigned *err,
                          cudaStream_t s);
 template <typename T>
-int launch_split(T *pool, const Geom &g, const mamr_split_job *jobs, int n,
-                 cudaStream_t s);
+int launch_stage_blocks(T *stage, const T *pool, const Geom &g,
+                        const int32_t *slots, int n, cudaStream_t s);
+// Data-movement reads with a negative slot s come from staging entry -s-1.
 template <typename T>
-int launch_consolidate(T *pool, const Geom &g,
+int launch_split(T *pool, const T *stage, const Geom &g,
+                 const mamr_split_job *jobs, int n, cudaStream_t s);
+template <typename T>
+int launch_consolidate(T *pool, const T *stage, const Geom &g,
                        const mamr_consolidate_job *jobs, int n,
                        cudaStream_t s);
 template <typename T>

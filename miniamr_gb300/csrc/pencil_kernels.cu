@@ -10,6 +10,15 @@
 // from the neighbouring pencils, as 64-byte rows that those pencils' own
 // CTAs read at about the same time, so they hit in L2.
 //
+// Shared-memory traffic bounds the FP32 kernel, so the tile is laid out
+// and walked to keep it low: every thread of an FP32 CTA updates two
+// j-rows of four k values on four i-planes (four rows loaded per two
+// output rows).  Each i-plane of a tile is padded by 16 bytes, which puts
+// rows four planes apart in opposite halves of a 128-byte bank span; an
+// 8-lane phase of a warp pairs such rows, so the warp's 16-byte row loads
+// are free of bank conflicts while every address stays a per-thread base
+// plus a constant.
+//
 // Values and operation order are exactly those of the plain path: ghosts
 // as comm() leaves them on a single-level mesh (axis-by-axis neighbour or
 // reflection), the reference's summation order, correctly rounded
@@ -24,9 +33,29 @@ namespace {
 constexpr int NB = 16;              // cells per block edge
 constexpr int G = NB + 2;           // with ghosts
 constexpr int RS = NB;              // shared row: the 16 interior k values
-constexpr int KC = G * G;           // one k-column array (i, j incl. ghosts)
-constexpr int TILE_ROWS = G * G;
-constexpr int THREADS = 256;
+constexpr int KC = G * G;           // rows of a tile (i, j incl. ghosts)
+
+// Tile geometry in elements of T: row (i, j) starts at i * PW + j * RS.
+template <typename T> struct TileGeom {
+   static constexpr int PW = G * RS + 16 / (int) sizeof(T);   // plane
+   static constexpr int TILE = G * PW;
+};
+template <typename T>
+__device__ __forceinline__ int trow(int i, int j)
+{
+   return i * TileGeom<T>::PW + j * RS;
+}
+
+// Work split: JP j-rows per thread.  FP32 (bound by shared-memory
+// bandwidth): 2 rows, 128 threads, three CTAs per SM.  FP64 (bound by the
+// FP64 pipe): 1 row, 256 threads, one CTA per SM.
+template <typename T> struct Shape;
+template <> struct Shape<float> {
+   static constexpr int JP = 2, THREADS = 128, CTAS = 3;
+};
+template <> struct Shape<double> {
+   static constexpr int JP = 1, THREADS = 256, CTAS = 1;
+};
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
@@ -43,7 +72,8 @@ __device__ __forceinline__ void cp_async_wait_all()
    asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
-template <typename T> struct Quad;   // four consecutive k values
+// Four consecutive k values (16-byte aligned).
+template <typename T> struct Quad;
 template <> struct Quad<float> {
    __device__ static void ld(const float *p, float (&v)[4])
    {
@@ -69,36 +99,52 @@ template <> struct Quad<double> {
    }
 };
 
+// Ring of three tiles, two lower z-ghost columns (tiles s and s+1) and
+// one upper column, one element per row; the upper column sits an odd
+// number of words after the lower ones so that the two read in one
+// instruction use disjoint banks.  After a 128-byte alignment pad.
 template <typename T>
 constexpr size_t pencil_smem_bytes()
 {
-   return (size_t) 3 * (TILE_ROWS * RS + 2 * KC) * sizeof(T);
+   return (size_t) (3 * TileGeom<T>::TILE + 3 * KC + 1) * sizeof(T) + 128;
 }
 
 constexpr int DESC = sizeof(TileDesc) / sizeof(int32_t);
 
+// Global row (i, j) of a 16^3 block-variable (split layout: rows of the
+// 16 interior k values, ghost rows included).
+__device__ __forceinline__ int grow(int i, int j) { return (i * G + j) * NB; }
+
 // Queues the cp.async copies of tile `s` of the pencil into ring buffer t:
 // the interior rows, the four x/y face rows (neighbour or reflection) and,
-// for 27 points, the four z-running edge rows.
-template <typename T, int ST>
+// for 27 points, the four z-running edge rows.  A thread's chunks sit at
+// fixed (j, k) positions, so every address is a per-tile base plus a
+// constant.
+template <typename T, int ST, int THREADS>
 __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
                                            const Geom &g, const TileDesc *it,
                                            int var, T *t)
 {
    constexpr int VW = 16 / (int) sizeof(T);   // elements per 16 bytes
    constexpr int CPR = NB / VW;               // 16-byte chunks per row
+   constexpr int RPP = NB * CPR;              // chunks per 16-row plane
+   constexpr int PW = TileGeom<T>::PW;
+   constexpr int PSTEP = THREADS / RPP;       // planes per sweep
+   static_assert(THREADS % RPP == 0, "thread count vs plane chunks");
    const int tid = threadIdx.x;
+   const int q = tid % CPR, a = (tid / CPR) % NB + 1, p0 = tid / RPP;
    const int slot = it->slot, bmask = it->bmask;
    const T *own = src + bv_offset(g, slot, var);
-   for (int c = tid; c < NB * NB * CPR; c += THREADS) {
-      const int q = c % CPR, r = c / CPR;
-      const int j = r % NB + 1, i = r / NB + 1;
-      cp_async16(t + (i * G + j) * RS + q * VW,
-                 own + row_offset(g, i, j) + q * VW);
+   {
+      const T *from = own + grow(p0 + 1, a) + q * VW;
+      T *to = t + trow<T>(p0 + 1, a) + q * VW;
+#pragma unroll
+      for (int m = 0; m < NB / PSTEP; m++)
+         cp_async16(to + m * PSTEP * PW, from + m * PSTEP * grow(1, 0));
    }
-   for (int c = tid; c < 4 * NB * CPR; c += THREADS) {
-      const int f = c / (NB * CPR), r = c % (NB * CPR);
-      const int a = r / CPR + 1, q = r % CPR;
+#pragma unroll
+   for (int m = 0; m < 4 / PSTEP; m++) {
+      const int f = p0 + m * PSTEP;            // face W, E, S, N
       const bool bnd = (bmask >> f) & 1;
       // nb9 index of the W, E, S, N neighbour: 3, 5, 1, 7
       const int nbi = (f < 2) ? (f == 0 ? 3 : 5) : (f == 2 ? 1 : 7);
@@ -107,59 +153,226 @@ __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
       // neighbour: its plane next to us; boundary: our own first plane
       const int sp = bnd ? (low ? 1 : NB) : (low ? NB : 1);
       const int gp = low ? 0 : G - 1;
-      const T *from;
-      T *to;
-      if (f < 2) {
-         from = blk + row_offset(g, sp, a);
-         to = t + (gp * G + a) * RS;
-      } else {
-         from = blk + row_offset(g, a, sp);
-         to = t + (a * G + gp) * RS;
-      }
-      cp_async16(to + q * VW, from + q * VW);
+      const int from = f < 2 ? grow(sp, a) : grow(a, sp);
+      const int to = f < 2 ? trow<T>(gp, a) : trow<T>(a, gp);
+      cp_async16(t + to + q * VW, blk + from + q * VW);
    }
-   if (ST == 27) {
-      for (int c = tid; c < 4 * CPR; c += THREADS) {
-         const int e = c / CPR, q = c % CPR;
-         const int gi = (e & 1) ? G - 1 : 0, gj = (e & 2) ? G - 1 : 0;
-         int dx = (e & 1) ? 1 : -1, dy = (e & 2) ? 1 : -1, si, sj;
-         if (bmask & (1 << ((e & 1) ? 1 : 0))) { si = (e & 1) ? NB : 1; dx = 0; }
-         else si = (e & 1) ? 1 : NB;
-         if (bmask & (1 << ((e & 2) ? 3 : 2))) { sj = (e & 2) ? NB : 1; dy = 0; }
-         else sj = (e & 2) ? 1 : NB;
-         const int nb = it->nb9[(dx + 1) + 3 * (dy + 1)];
-         cp_async16(t + (gi * G + gj) * RS + q * VW,
-                    src + bv_offset(g, nb, var) + row_offset(g, si, sj) +
-                       q * VW);
-      }
+   if (ST == 27 && tid < 4 * CPR) {
+      const int e = tid / CPR;
+      const int gi = (e & 1) ? G - 1 : 0, gj = (e & 2) ? G - 1 : 0;
+      int dx = (e & 1) ? 1 : -1, dy = (e & 2) ? 1 : -1, si, sj;
+      if (bmask & (1 << ((e & 1) ? 1 : 0))) { si = (e & 1) ? NB : 1; dx = 0; }
+      else si = (e & 1) ? 1 : NB;
+      if (bmask & (1 << ((e & 2) ? 3 : 2))) { sj = (e & 2) ? NB : 1; dy = 0; }
+      else sj = (e & 2) ? 1 : NB;
+      const int nb = it->nb9[(dx + 1) + 3 * (dy + 1)];
+      cp_async16(t + trow<T>(gi, gj) + q * VW,
+                 src + bv_offset(g, nb, var) + grow(si, sj) + q * VW);
    }
    cp_async_commit();
 }
 
-// Row (i, j) of a tile as six k values: k-1 .. k+4 around the thread's
+// Row (i, j) of tile t as six k values: k-1 .. k+4 around the thread's
 // quad k .. k+3 (k = 4*kq + 1).  The four lanes of a row hold the row's 16
 // values between them; the outer neighbours k-1 and k+4 come from the
 // adjacent lanes by shuffle, and from the z ghost columns at the row ends.
 // Every lane of the warp must call this together.
+// `tq` is the thread's quad in tile t (row 0 of plane 0 plus 4*kq) and
+// `eg` its ghost column (the lower column for kq < 3, the upper for kq = 3).
 template <typename T>
-__device__ __forceinline__ void row6(const T *t, const T *klo, const T *khi,
-                                     int i, int j, int kq, T (&r)[6])
+__device__ __forceinline__ void row6(const T *tq, const T *eg, int i, int j,
+                                     int kq, T (&r)[6])
 {
-   const int e = i * G + j;
    T v[4];
-   Quad<T>::ld(t + e * RS + 4 * kq, v);
+   Quad<T>::ld(tq + trow<T>(i, j), v);
    const T left = __shfl_up_sync(0xffffffffu, v[3], 1);
    const T right = __shfl_down_sync(0xffffffffu, v[0], 1);
-   const T edge = kq == 0 ? klo[e] : khi[e];
+   const T edge = eg[i * G + j];
    r[0] = kq == 0 ? edge : left;
    r[1] = v[0]; r[2] = v[1]; r[3] = v[2]; r[4] = v[3];
    r[5] = kq == 3 ? edge : right;
 }
 
+template <typename T>
+__device__ __forceinline__ void checksum4(const T (&out)[4], bool &ok,
+                                          unsigned long long &lo,
+                                          unsigned long long &hi)
+{
+#pragma unroll
+   for (int m = 0; m < 4; m++) {
+      long long q;
+      ok &= fixed52((float) out[m], q);
+      acc128_add(lo, hi, q);
+   }
+}
+
+__device__ __forceinline__ float div_rn_inline(float x, float c)
+{
+   return __fdiv_rn(x, c);
+}
+__device__ __forceinline__ double div_rn_inline(double x, double c)
+{
+   return __ddiv_rn(x, c);
+}
+
+// Accumulators of a thread's pass over its outputs of a tile.
+struct PassState {
+   bool slow;                       // some sum fell outside div_window
+   bool ok;                         // every FP32 checksum term in range
+   unsigned long long lo, hi;       // FP32 fixed-point checksum
+};
+
+// Quotients of four sums, stored at p (global).  The fast pass stores the
+// three-step quotient and records whether any sum lay outside the window
+// where it is exact; the fix-up pass (run only then) stores the IEEE
+// quotient for those sums and moves their checksum terms accordingly.
+template <int C, bool FIX, typename T>
+__device__ __forceinline__ void emit4(const T (&w)[4], T *p, int do_cs,
+                                      PassState &st)
+{
+   if (!FIX) {
+      T q[4];
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+         q[m] = div_fast<C>(w[m]);
+         st.slow |= !div_window(w[m]);
+      }
+      Quad<T>::st(p, q);
+      if (sizeof(T) == 4 && do_cs)
+         checksum4(q, st.ok, st.lo, st.hi);
+   } else {
+#pragma unroll
+      for (int m = 0; m < 4; m++)
+         if (!div_window(w[m])) {
+            const T qf = div_fast<C>(w[m]);
+            const T qc = div_rn_inline(w[m], (T) C);
+            p[m] = qc;
+            if (sizeof(T) == 4 && do_cs) {
+               long long a, b;
+               st.ok &= fixed52((float) qc, a);
+               fixed52((float) qf, b);
+               acc128_add(st.lo, st.hi, a);
+               acc128_add(st.lo, st.hi, -b);
+            }
+         }
+   }
+}
+
+// One pass over the thread's outputs of a tile: JP rows (jrow ..) of four
+// k values on planes 4*ih+1 .. 4*ih+4.  `tq` is the thread's quad of row
+// (4*ih, jrow) in the tile, `eg` its ghost column from the same row, `d`
+// the matching global position.  Every lane of the warp runs it together.
+template <typename T, int ST, int JP, bool FIX>
+__device__ __forceinline__ void tile_pass(const T *tq, const T *eg, T *d,
+                                          int kq, int do_cs, PassState &st)
+{
+   if (ST == 7) {
+      // (i-1, j) quads and (i, j) rows of the thread's JP rows
+      T am[JP][4], r[JP][6];
+#pragma unroll
+      for (int jj = 0; jj < JP; jj++) {
+         Quad<T>::ld(tq + trow<T>(0, jj), am[jj]);
+         row6(tq, eg, 1, jj, kq, r[jj]);
+      }
+#pragma unroll
+      for (int ii = 1; ii <= 4; ii++) {
+         T qm[4], qp[4], c[JP][6];
+         Quad<T>::ld(tq + trow<T>(ii, -1), qm);
+         Quad<T>::ld(tq + trow<T>(ii, JP), qp);
+#pragma unroll
+         for (int jj = 0; jj < JP; jj++)
+            row6(tq, eg, ii + 1, jj, kq, c[jj]);
+#pragma unroll
+         for (int jj = 0; jj < JP; jj++) {
+            T w[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+               const T sm = jj == 0 ? qm[m] : r[jj > 0 ? jj - 1 : 0][m + 1];
+               const T sp = jj == JP - 1 ? qp[m]
+                                         : r[jj < JP - 1 ? jj + 1 : 0][m + 1];
+               T v = am[jj][m] + sm;
+               v = v + r[jj][m];
+               v = v + r[jj][m + 1];
+               v = v + r[jj][m + 2];
+               v = v + sp;
+               v = v + c[jj][m + 1];
+               w[m] = v;
+            }
+            emit4<7, FIX>(w, d + grow(ii, jj), do_cs, st);
+         }
+#pragma unroll
+         for (int jj = 0; jj < JP; jj++) {
+#pragma unroll
+            for (int m = 0; m < 4; m++)
+               am[jj][m] = r[jj][m + 1];
+#pragma unroll
+            for (int m = 0; m < 6; m++)
+               r[jj][m] = c[jj][m];
+         }
+      }
+   } else {
+      // S(p): the reference's 9-term sum on plane p, for the thread's JP
+      // rows and 4 k values
+      auto S = [&](int pl, T (&s4)[JP][4]) {
+         T rw[JP + 2][6];
+#pragma unroll
+         for (int dd = 0; dd < JP + 2; dd++)
+            row6(tq, eg, pl, dd - 1, kq, rw[dd]);
+#pragma unroll
+         for (int jj = 0; jj < JP; jj++)
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+               const T *a = rw[jj], *b = rw[jj + 1], *c = rw[jj + 2];
+               T v = a[m] + a[m + 1];
+               v = v + a[m + 2];
+               v = v + b[m];
+               v = v + b[m + 1];
+               v = v + b[m + 2];
+               v = v + c[m];
+               v = v + c[m + 1];
+               v = v + c[m + 2];
+               s4[jj][m] = v;
+            }
+      };
+      T s0[JP][4], s1[JP][4], s2[JP][4];
+      S(0, s0);
+      S(1, s1);
+#pragma unroll
+      for (int ii = 1; ii <= 4; ii++) {
+         S(ii + 1, s2);
+#pragma unroll
+         for (int jj = 0; jj < JP; jj++) {
+            T w[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++)
+               w[m] = (s0[jj][m] + s1[jj][m]) + s2[jj][m];
+            emit4<27, FIX>(w, d + grow(ii, jj), do_cs, st);
+         }
+#pragma unroll
+         for (int jj = 0; jj < JP; jj++)
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+               s0[jj][m] = s1[jj][m];
+               s1[jj][m] = s2[jj][m];
+            }
+      }
+   }
+}
+
+// The fix-up pass out of line, so that its registers do not weigh on the
+// fast pass; called only when a warp met a sum outside the window.
+template <typename T, int ST, int JP>
+__device__ __noinline__ PassState tile_fix(const T *tq, const T *eg, T *d,
+                                           int kq, int do_cs, PassState st)
+{
+   tile_pass<T, ST, JP, true>(tq, eg, d, kq, do_cs, st);
+   return st;
+}
+
 }  // namespace
 
 template <typename T, int ST>
-__global__ void __launch_bounds__(THREADS, sizeof(T) == 4 ? 3 : 1)
+__global__ void __launch_bounds__(Shape<T>::THREADS, Shape<T>::CTAS)
 pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                     const TileDesc *__restrict__ chain,
                     const int2 *__restrict__ pencils, int n_pencils,
@@ -167,13 +380,33 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                     unsigned long long *__restrict__ acc,
                     unsigned *__restrict__ err)
 {
+   constexpr int JP = Shape<T>::JP, THREADS = Shape<T>::THREADS;
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ TileDesc s_desc[PENCIL_MAX];
-   T *tiles = reinterpret_cast<T *>(smem_raw);
-   T *klos = tiles + 3 * TILE_ROWS * RS;
-   T *khis = klos + 3 * KC;
-   const int tid = threadIdx.x;
-   const int kq = tid & 3, j = ((tid >> 2) & 15) + 1, ih = tid >> 6;
+   T *tiles = reinterpret_cast<T *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t) 127);
+   constexpr int TILE = TileGeom<T>::TILE;
+   T *klos = tiles + 3 * TILE;          // lower columns of tiles s, s+1
+   T *khi = klos + 2 * KC + 1;          // upper column of tile s
+   const int tid = threadIdx.x, lane = tid & 31;
+   // Lanes: kq fastest.  For two rows per thread, lane bit 2 selects the
+   // i-plane group (4 planes apart) and bits 3-4 the row pair, so an
+   // 8-lane phase loads two rows in opposite halves of a bank span.
+   const int kq = lane & 3;
+   const int jrow = JP == 2
+      ? 2 * (((lane >> 3) & 3) + 4 * ((tid >> 5) & 1)) + 1
+      : ((tid >> 2) & 15) + 1;
+   const int ih = JP == 2 ? ((lane >> 2) & 1) + 2 * (tid >> 6) : tid >> 6;
+
+   // the ghost-column rows this thread copies each step, walked i fastest
+   // (fewer bank conflicts): (tile offset << 9) | column index
+   constexpr int NFILL = (KC + THREADS - 1) / THREADS;
+   int fill[NFILL];
+#pragma unroll
+   for (int m = 0; m < NFILL; m++) {
+      const int q = tid + m * THREADS, i = q % G, j = q / G;
+      fill[m] = q < KC ? (trow<T>(i, j) << 9) | (i * G + j) : -1;
+   }
 
    for (int w = blockIdx.x; w < n_pencils * g.V; w += gridDim.x) {
       const int var = w / n_pencils, p = w - var * n_pencils;
@@ -186,126 +419,49 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
             to[q] = from[q];
       }
       __syncthreads();
-      issue_tile<T, ST>(src, g, s_desc, var, tiles);
+      issue_tile<T, ST, THREADS>(src, g, s_desc, var, tiles);
       if (len > 1)
-         issue_tile<T, ST>(src, g, s_desc + 1, var, tiles + TILE_ROWS * RS);
-      unsigned long long lo = 0, hi = 0;
-      bool ok = true;
+         issue_tile<T, ST, THREADS>(src, g, s_desc + 1, var, tiles + TILE);
+      PassState st;
+      st.ok = true;
+      st.lo = st.hi = 0;
       for (int s = 0; s < len; s++) {
-         const int b = s % 3, bn = (s + 1) % 3;
-         T *t = tiles + b * TILE_ROWS * RS;
-         T *klo = klos + b * KC, *khi = khis + b * KC;
+         const T *t = tiles + (s % 3) * TILE;
+         const T *tn = tiles + ((s + 1) % 3) * TILE;
+         T *kcur = klos + (s & 1) * KC;
+         T *knext = klos + ((s + 1) & 1) * KC;
          cp_async_wait_all();
          __syncthreads();
-         // z ghost columns: tile s+1's k=1 (or our own k=16 at the top
-         // boundary); tile s+1's lower column is our k=16; the bottom tile
-         // reflects its own k=1
-         for (int e = tid; e < KC; e += THREADS) {
-            const T *tn = tiles + bn * TILE_ROWS * RS;
-            if (s + 1 < len) {
-               khi[e] = tn[e * RS];
-               klos[bn * KC + e] = t[e * RS + NB - 1];
-            } else {
-               khi[e] = t[e * RS + NB - 1];
-            }
+         // z ghost columns: upper of tile s = tile s+1's k = 1 (our own
+         // k = 16 at the top); lower of tile s+1 = our k = 16; the bottom
+         // tile reflects its own k = 1
+#pragma unroll
+         for (int m = 0; m < NFILL; m++) {
+            if (fill[m] < 0)
+               continue;
+            const int r = fill[m] >> 9, e = fill[m] & 511;
+            const T top = t[r + NB - 1];
+            khi[e] = s + 1 < len ? tn[r] : top;
+            if (s + 1 < len)
+               knext[e] = top;
             if (s == 0)
-               klo[e] = t[e * RS];
+               kcur[e] = t[r];
          }
          __syncthreads();
          if (s + 2 < len)
-            issue_tile<T, ST>(src, g, s_desc + s + 2, var,
-                              tiles + ((s + 2) % 3) * TILE_ROWS * RS);
-
+            issue_tile<T, ST, THREADS>(src, g, s_desc + s + 2, var,
+                                       tiles + ((s + 2) % 3) * TILE);
+         // the thread's quad of row (4*ih, jrow) and its ghost column
+         const T *tq = t + trow<T>(4 * ih, jrow) + 4 * kq;
+         const T *eg = (kq == 3 ? khi : kcur) + 4 * ih * G + jrow;
          const int slot = s_desc[s].slot;
-         T *d = dst + bv_offset(g, slot, var);
-         T out[4];
-         if (ST == 7) {
-            T am[4], r[6], c[6];
-            Quad<T>::ld(t + ((4 * ih) * G + j) * RS + 4 * kq, am);
-            row6(t, klo, khi, 4 * ih + 1, j, kq, r);
-#pragma unroll
-            for (int ii = 1; ii <= 4; ii++) {
-               const int i = 4 * ih + ii;
-               T sm[4], sp[4];
-               Quad<T>::ld(t + (i * G + j - 1) * RS + 4 * kq, sm);
-               Quad<T>::ld(t + (i * G + j + 1) * RS + 4 * kq, sp);
-               row6(t, klo, khi, i + 1, j, kq, c);
-               T w[4];
-#pragma unroll
-               for (int m = 0; m < 4; m++) {
-                  T v = am[m] + sm[m];
-                  v = v + r[m];
-                  v = v + r[m + 1];
-                  v = v + r[m + 2];
-                  v = v + sp[m];
-                  v = v + c[m + 1];
-                  w[m] = v;
-               }
-               div_const4<7>(w, out);
-               Quad<T>::st(d + row_offset(g, i, j) + 4 * kq, out);
-               if (sizeof(T) == 4 && do_cs)
-#pragma unroll
-                  for (int m = 0; m < 4; m++) {
-                     long long q;
-                     ok &= fixed52((float) out[m], q);
-                     acc128_add(lo, hi, q);
-                  }
-#pragma unroll
-               for (int m = 0; m < 4; m++) {
-                  am[m] = r[m + 1];
-               }
-#pragma unroll
-               for (int m = 0; m < 6; m++)
-                  r[m] = c[m];
-            }
-         } else {
-            // S(p): the reference's 9-term sum on plane p, for 4 k values
-            auto S4 = [&](int pl, T (&s4)[4]) {
-               T a[6], bb[6], cc[6];
-               row6(t, klo, khi, pl, j - 1, kq, a);
-               row6(t, klo, khi, pl, j, kq, bb);
-               row6(t, klo, khi, pl, j + 1, kq, cc);
-#pragma unroll
-               for (int m = 0; m < 4; m++) {
-                  T v = a[m] + a[m + 1];
-                  v = v + a[m + 2];
-                  v = v + bb[m];
-                  v = v + bb[m + 1];
-                  v = v + bb[m + 2];
-                  v = v + cc[m];
-                  v = v + cc[m + 1];
-                  v = v + cc[m + 2];
-                  s4[m] = v;
-               }
-            };
-            T s0[4], s1[4], s2[4];
-            S4(4 * ih, s0);
-            S4(4 * ih + 1, s1);
-#pragma unroll
-            for (int ii = 1; ii <= 4; ii++) {
-               const int i = 4 * ih + ii;
-               S4(i + 1, s2);
-               T w[4];
-#pragma unroll
-               for (int m = 0; m < 4; m++)
-                  w[m] = (s0[m] + s1[m]) + s2[m];
-               div_const4<27>(w, out);
-               Quad<T>::st(d + row_offset(g, i, j) + 4 * kq, out);
-               if (sizeof(T) == 4 && do_cs)
-#pragma unroll
-                  for (int m = 0; m < 4; m++) {
-                     long long q;
-                     ok &= fixed52((float) out[m], q);
-                     acc128_add(lo, hi, q);
-                  }
-#pragma unroll
-               for (int m = 0; m < 4; m++) {
-                  s0[m] = s1[m];
-                  s1[m] = s2[m];
-               }
-            }
-         }
+         T *d = dst + bv_offset(g, slot, var) + grow(4 * ih, jrow) + 4 * kq;
+         st.slow = false;
+         tile_pass<T, ST, JP, false>(tq, eg, d, kq, do_cs, st);
+         if (__any_sync(0xffffffffu, st.slow))
+            st = tile_fix<T, ST, JP>(tq, eg, d, kq, do_cs, st);
          if (write_ghosts) {
+            T *base = dst + bv_offset(g, slot, var);
             // the ghost cells comm() writes: face interiors for 7 points,
             // the whole shell for 27 points
             const int n_shell = G * G * G - NB * NB * NB;
@@ -334,16 +490,17 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                if (ST == 7 && outside != 1)
                   continue;
                const int ee = gi * G + gj;
-               const T v = gk == 0 ? klo[ee]
-                         : (gk == G - 1 ? khi[ee] : t[ee * RS + gk - 1]);
-               d[cell_offset(g, gi, gj, gk)] = v;
+               const T v = gk == 0 ? kcur[ee]
+                         : (gk == G - 1 ? khi[ee]
+                                        : t[trow<T>(gi, gj) + gk - 1]);
+               base[cell_offset(g, gi, gj, gk)] = v;
             }
          }
       }
       if (sizeof(T) == 4 && do_cs) {
-         if (!ok)
+         if (!st.ok)
             atomicOr(err, ERR_FIXED_RANGE);
-         block_acc128_flush(lo, hi, acc + 2 * var);
+         block_acc128_flush(st.lo, st.hi, acc + 2 * var);
       }
       __syncthreads();
    }
@@ -403,11 +560,13 @@ int pencil_grid(int stencil, int n_work)
    if (stencil == 7) {
       pencil_attr<T, 7>();
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &per_sm, pencil_stage_kernel<T, 7>, THREADS, pencil_smem_bytes<T>());
+         &per_sm, pencil_stage_kernel<T, 7>, Shape<T>::THREADS,
+         pencil_smem_bytes<T>());
    } else {
       pencil_attr<T, 27>();
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &per_sm, pencil_stage_kernel<T, 27>, THREADS, pencil_smem_bytes<T>());
+         &per_sm, pencil_stage_kernel<T, 27>, Shape<T>::THREADS,
+         pencil_smem_bytes<T>());
    }
    long long grid = (long long) (per_sm > 0 ? per_sm : 1) * sms;
    return (int) (grid < n_work ? grid : (n_work > 0 ? n_work : 1));
@@ -427,11 +586,11 @@ int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
    const size_t smem = pencil_smem_bytes<T>();
    const int fused_cs = (sizeof(T) == 4) ? do_cs : 0;
    if (stencil == 7)
-      pencil_stage_kernel<T, 7><<<grid, THREADS, smem, s>>>(
+      pencil_stage_kernel<T, 7><<<grid, Shape<T>::THREADS, smem, s>>>(
          src, dst, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc,
          err);
    else
-      pencil_stage_kernel<T, 27><<<grid, THREADS, smem, s>>>(
+      pencil_stage_kernel<T, 27><<<grid, Shape<T>::THREADS, smem, s>>>(
          src, dst, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc,
          err);
    int launches = 1;

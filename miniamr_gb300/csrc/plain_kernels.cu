@@ -1,6 +1,8 @@
 // Plain-path kernels: the reference's call sequence, one launch per call,
 // every cell bit-identical to the reference in FP64 (compiled with
 // -fmad=false; sums in the reference's order; divisions correctly rounded).
+#include <algorithm>
+
 #include "mamr_internal.h"
 #include "arith.cuh"
 
@@ -286,16 +288,61 @@ int launch_checksum_fp32(const float *pool, const Geom &g,
 }
 
 // ---------------------------------------------------------------------------
+// Source of a data-movement read: a pool slot, or (slot < 0) entry -slot-1
+// of the staging copy taken before a batch whose later jobs overwrite it.
+template <typename T>
+__device__ __forceinline__ const T *read_base(const T *pool, const T *stage,
+                                              const Geom &g, int slot, int var)
+{
+   return slot >= 0 ? pool + bv_offset(g, slot, var)
+                    : stage + bv_offset(g, -slot - 1, var);
+}
+
+// Copies whole blocks (all variables, ghosts included) from pool slots to
+// consecutive staging entries; one CTA row per block, 16-byte vectors when
+// the block size allows.
+template <typename T>
+__global__ void __launch_bounds__(256)
+stage_blocks_kernel(T *__restrict__ stage, const T *__restrict__ pool, Geom g,
+                    const int32_t *__restrict__ slots)
+{
+   const long long words = (long long) g.V * g.bv;
+   const T *src = pool + bv_offset(g, slots[blockIdx.y], 0);
+   T *dst = stage + bv_offset(g, blockIdx.y, 0);
+   const long long step = (long long) gridDim.x * blockDim.x;
+   const long long t0 = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if ((words * sizeof(T)) % 16 == 0) {
+      const long long vec = words * sizeof(T) / 16;
+      for (long long e = t0; e < vec; e += step)
+         ((uint4 *) dst)[e] = __ldg((const uint4 *) src + e);
+   } else {
+      for (long long e = t0; e < words; e += step)
+         dst[e] = src[e];
+   }
+}
+
+template <typename T>
+int launch_stage_blocks(T *stage, const T *pool, const Geom &g,
+                        const int32_t *slots, int n, cudaStream_t s)
+{
+   if (n == 0)
+      return 0;
+   long long vec = ((long long) g.V * g.bv * sizeof(T) + 15) / 16;
+   int gx = (int) std::min<long long>((vec + 255) / 256, 64);
+   stage_blocks_kernel<T><<<dim3(gx, n), 256, 0, s>>>(stage, pool, g, slots);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
 // split_blocks() data (ref/block.c:158-173): one CTA per (job, octant,
 // variable).  A child cell (ci, cj, ck) takes parent cell
 // ((ci+1)/2 + i1, ...) / 8 -- exact in binary floating point.
 template <typename T>
 __global__ void __launch_bounds__(256)
-split_kernel(T *__restrict__ pool, Geom g,
+split_kernel(T *__restrict__ pool, const T *__restrict__ stage, Geom g,
              const mamr_split_job *__restrict__ jobs)
 {
    const int job = blockIdx.x >> 3, o = blockIdx.x & 7, var = blockIdx.y;
-   const T *P = pool + bv_offset(g, jobs[job].parent, var);
+   const T *P = read_base(pool, stage, g, jobs[job].parent, var);
    T *C = pool + bv_offset(g, jobs[job].child[o], var);
    const int i1 = (o & 1) * (g.nx / 2), j1 = ((o >> 1) & 1) * (g.ny / 2),
              k1 = (o >> 2) * (g.nz / 2);
@@ -310,12 +357,12 @@ split_kernel(T *__restrict__ pool, Geom g,
 }
 
 template <typename T>
-int launch_split(T *pool, const Geom &g, const mamr_split_job *jobs, int n,
-                 cudaStream_t s)
+int launch_split(T *pool, const T *stage, const Geom &g,
+                 const mamr_split_job *jobs, int n, cudaStream_t s)
 {
    if (n == 0)
       return 0;
-   split_kernel<T><<<dim3(n * 8, g.V), 256, 0, s>>>(pool, g, jobs);
+   split_kernel<T><<<dim3(n * 8, g.V), 256, 0, s>>>(pool, stage, g, jobs);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -325,12 +372,12 @@ int launch_split(T *pool, const Geom &g, const mamr_split_job *jobs, int n,
 // once to FP32 for FP32 pools).
 template <typename T>
 __global__ void __launch_bounds__(256)
-consolidate_kernel(T *__restrict__ pool, Geom g,
+consolidate_kernel(T *__restrict__ pool, const T *__restrict__ stage, Geom g,
                    const mamr_consolidate_job *__restrict__ jobs)
 {
    const int job = blockIdx.x >> 3, o = blockIdx.x & 7, var = blockIdx.y;
    T *P = pool + bv_offset(g, jobs[job].target, var);
-   const T *C = pool + bv_offset(g, jobs[job].child[o], var);
+   const T *C = read_base(pool, stage, g, jobs[job].child[o], var);
    const int xh = g.nx / 2, yh = g.ny / 2, zh = g.nz / 2;
    const int i1 = (o & 1) * xh, j1 = ((o >> 1) & 1) * yh, k1 = (o >> 2) * zh;
    for (int e = threadIdx.x; e < xh * yh * zh; e += blockDim.x) {
@@ -350,13 +397,14 @@ consolidate_kernel(T *__restrict__ pool, Geom g,
 }
 
 template <typename T>
-int launch_consolidate(T *pool, const Geom &g,
+int launch_consolidate(T *pool, const T *stage, const Geom &g,
                        const mamr_consolidate_job *jobs, int n,
                        cudaStream_t s)
 {
    if (n == 0)
       return 0;
-   consolidate_kernel<T><<<dim3(n * 8, g.V), 256, 0, s>>>(pool, g, jobs);
+   consolidate_kernel<T><<<dim3(n * 8, g.V), 256, 0, s>>>(pool, stage, g,
+                                                          jobs);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -429,9 +477,11 @@ int launch_download(const T *pool, const Geom &g, const int32_t *slots,
                                    const DirTasks &, int, int, cudaStream_t); \
    template int launch_stencil<T>(T *, const Geom &, int, const int32_t *,    \
                                   int, int, cudaStream_t);                    \
-   template int launch_split<T>(T *, const Geom &, const mamr_split_job *,    \
-                                int, cudaStream_t);                           \
-   template int launch_consolidate<T>(T *, const Geom &,                      \
+   template int launch_stage_blocks<T>(T *, const T *, const Geom &,          \
+                                       const int32_t *, int, cudaStream_t);   \
+   template int launch_split<T>(T *, const T *, const Geom &,                 \
+                                const mamr_split_job *, int, cudaStream_t);   \
+   template int launch_consolidate<T>(T *, const T *, const Geom &,           \
                                       const mamr_consolidate_job *, int,      \
                                       cudaStream_t);                          \
    template int launch_upload<T>(T *, const Geom &, const int32_t *, int,     \

@@ -71,6 +71,39 @@ def test_batched_equals_plain_amr7(gpu_lib, name, dtype):
         assert np.array_equal(bits(a), bits(b))
 
 
+@pytest.mark.parametrize("stencil", [7, 27])
+@pytest.mark.parametrize("dtype", [FP64, FP32])
+def test_pencil_division_fixup(gpu_lib, dtype, stencil):
+    """Sums outside the window where the three-step quotient is exact
+    (-0, zero, subnormal, huge) on the 16^3 pencil path: the kernel's
+    fix-up pass stores the IEEE quotient and moves the FP32 checksum term,
+    so every cell and every checksum equals the plain path's."""
+    rng = np.random.default_rng(11)
+    ix, iy, iz, V = 2, 1, 3, 3
+    n0 = ix * iy * iz
+    cfg = Config.make(16, 16, 16, V, n0 + 8, stencil=stencil, dtype=dtype)
+    mant = rng.uniform(-2, 2, size=(n0, V, 16, 16, 16))
+    lo, hi = (-1070, 1015) if dtype == FP64 else (-149, 8)
+    expo = rng.integers(lo, hi, size=mant.shape)
+    vals = np.zeros((n0, V, 18, 18, 18))
+    inner = vals[:, :, 1:17, 1:17, 1:17]
+    inner[...] = np.ldexp(mant, expo) / (64.0 if dtype == FP64 else 1.0)
+    inner[0, 0] = -0.0                      # sums of -0: the quotient is -0
+    inner[1, 1] = np.ldexp(mant[1, 1], lo + 8)   # subnormal sums
+    inner[2, 2, :8] = 0.0
+    outs = []
+    for fl in (0, RUN_BATCHED | RUN_GRAPH):
+        m = meshmod.initial_mesh(ix, iy, iz, 0, n0 + 8)
+        with gpu_lib.context(cfg) as ctx:
+            ctx.upload(np.arange(n0), vals)
+            ctx.set_mesh(m.blocks())
+            s = ctx.run_timesteps(2, 2, 1, flags=fl)
+            outs.append((s, ctx.download(np.arange(n0))))
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(bits(a), bits(b))
+    assert np.signbit(outs[1][1][0, 0, 8, 8, 8])
+
+
 def test_batched_27_multilevel_is_refused(gpu_lib):
     recs = read_trace(trace_path("amr27"))
     res = replay(gpu_lib, recs)
