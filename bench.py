@@ -305,6 +305,7 @@ def main():
         ev1.record(stream)
         torch.cuda.synchronize()
     launches = ctx.launch_count() - l0
+    shape = ctx.tuning()
     ms = max_over_ranks(ev0.elapsed_time(ev1), pg, "cuda")
     value = updates(K) * world / (ms / 1e3)
     n_stage_launches = K * SPT
@@ -366,7 +367,7 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic: the reference's init() values "
                                 "(rand(), seed 1), uniform mesh",
-        "config": WORKLOAD,
+        "config": dict(WORKLOAD, launch_shape=shape),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,

@@ -99,6 +99,9 @@ class Library:
             "mamr_run_timesteps": [vp, i32, i32, i32, i32, i32, vp,
                                    C.POINTER(i32)],
             "mamr_launch_count": [vp, C.POINTER(C.c_int64)],
+            "mamr_set_tuning": [vp, C.c_int32],
+            "mamr_get_tuning": [vp, C.POINTER(C.c_int32),
+                                C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -231,3 +234,19 @@ class Context:
         n = C.c_int64()
         self._call("mamr_launch_count", C.byref(n))
         return n.value
+
+    def set_tuning(self, choice: int = -1) -> None:
+        """Force launch-shape candidate `choice` of the batched path
+        (< 0: automatic)."""
+        self._call("mamr_set_tuning", int(choice))
+
+    def tuning(self) -> dict:
+        """The last batched run's launch shape: candidate index, number of
+        candidates, threads per variable, variables per CTA, rows per
+        thread, CTAs."""
+        ch, n = C.c_int32(), C.c_int32()
+        sh = (C.c_int32 * 4)()
+        self._call("mamr_get_tuning", C.byref(ch), C.byref(n), sh)
+        return {"choice": ch.value, "candidates": n.value,
+                "threads": sh[0], "vars_per_cta": sh[1],
+                "rows_per_thread": sh[2], "ctas": sh[3]}

@@ -7,6 +7,9 @@
 // returns a status; nothing here exits the process.
 #include <algorithm>
 #include <array>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <new>
 #include <cstdarg>
 #include <cstdio>
@@ -139,6 +142,9 @@ struct mamr_ctx {
    long long launches;
    int hw_slots;                    // 1 + highest slot ever holding data
    mamr::BatchedState *batched;
+   int tune_force = -1;             // forced launch-shape candidate
+   int tune_last = -1, tune_n = 0;  // last batched run's choice / count
+   mamr::StageShape tune_shape;
 };
 
 static size_t elem_size(const mamr_ctx *c) { return c->fp32 ? 4 : 8; }
@@ -922,6 +928,97 @@ static int build_items(mamr_ctx *c)
 }
 
 // The stage loop of ref/driver.c:73-108 as one fused launch per stage.
+// ---- launch-shape autotuner ----------------------------------------------
+// The first batched run for each (block shape, stencil, precision, kernel,
+// work size) times every candidate shape of the stage kernel -- one
+// warm-up and three timed stages each, current pool into the spare pool,
+// no checksum, no ghost writes -- and keeps the fastest for the process.
+// MAMR_TUNE=off in the environment keeps the first (default) candidate.
+namespace {
+struct TuneKey {
+   int nx, ny, nz, stencil, fp32, pencil, work_log2, n_cands;
+   bool operator<(const TuneKey &o) const
+   {
+      return std::tie(nx, ny, nz, stencil, fp32, pencil, work_log2, n_cands) <
+             std::tie(o.nx, o.ny, o.nz, o.stencil, o.fp32, o.pencil,
+                      o.work_log2, o.n_cands);
+   }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune_best;
+
+bool tuning_disabled()
+{
+   const char *e = getenv("MAMR_TUNE");
+   return e && (!strcmp(e, "off") || !strcmp(e, "0"));
+}
+}  // namespace
+
+template <typename Stage>
+static int tune_choice(mamr_ctx *c, const std::vector<StageShape> &cands,
+                       bool pencil, int nb, Stage &stage, int &choice)
+{
+   choice = 0;
+   if (cands.size() < 2 || tuning_disabled())
+      return MAMR_OK;
+   long long work = (long long) nb * c->cfg.num_vars;
+   int lg = 0;
+   while (work > 1) {
+      work >>= 1;
+      lg++;
+   }
+   const TuneKey key{c->g.nx, c->g.ny, c->g.nz, c->cfg.stencil,
+                     c->fp32 ? 1 : 0, pencil ? 1 : 0, lg,
+                     (int) cands.size()};
+   {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tune_best.find(key);
+      if (it != g_tune_best.end()) {
+         choice = it->second;
+         return MAMR_OK;
+      }
+   }
+   cudaEvent_t e0 = nullptr, e1 = nullptr;
+   CUDA_TRY(cudaEventCreate(&e0));
+   if (cudaEventCreate(&e1) != cudaSuccess) {
+      cudaEventDestroy(e0);
+      return fail(MAMR_ECUDA, "event creation failed");
+   }
+   float best = 0.f;
+   int status = MAMR_OK;
+   for (size_t q = 0; q < cands.size() && status == MAMR_OK; q++) {
+      int k = stage(c->pool, c->pool_alt, cands[q], 0, false, 0);
+      bool ok = k >= 0;
+      c->launches += ok ? k : 0;
+      ok = ok && cudaEventRecord(e0, c->stream) == cudaSuccess;
+      for (int rep = 0; rep < 3 && ok; rep++) {
+         k = stage(c->pool, c->pool_alt, cands[q], 0, false, 0);
+         ok = k >= 0;
+         c->launches += ok ? k : 0;
+      }
+      ok = ok && cudaEventRecord(e1, c->stream) == cudaSuccess;
+      ok = ok && cudaEventSynchronize(e1) == cudaSuccess;
+      float ms = 0.f;
+      ok = ok && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+      if (!ok) {
+         status = fail(MAMR_ECUDA, "timing launch shape %zu: %s", q,
+                       cudaGetErrorString(cudaGetLastError()));
+         break;
+      }
+      if (q == 0 || ms < best) {
+         best = ms;
+         choice = (int) q;
+      }
+   }
+   cudaEventDestroy(e0);
+   cudaEventDestroy(e1);
+   if (status == MAMR_OK) {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune_best[key] = choice;
+   }
+   return status;
+}
+
 static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
                        int32_t freq, bool graph, double *sums,
                        int32_t *n_sums)
@@ -950,12 +1047,6 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       CUDA_TRY(cudaMalloc(&c->pool_alt, c->pool_bytes));
       CUDA_TRY(cudaMemsetAsync(c->pool_alt, 0, c->pool_bytes, c->stream));
    }
-   // both pools start identical, so cells no stage writes (stale ghosts,
-   // free slots) read the same whichever pool ends up current
-   const size_t used = (size_t) c->hw_slots * c->g.V * c->g.bv * es;
-   if (used)
-      CUDA_TRY(cudaMemcpyAsync(c->pool_alt, c->pool, used,
-                               cudaMemcpyDeviceToDevice, c->stream));
    if (c->fp32) {
       CUDA_TRY(B->acc.ensure(std::max<size_t>(1, n_cs * V) * 16));
       CUDA_TRY(cudaMemsetAsync(B->acc.p, 0, std::max<size_t>(1, n_cs * V) * 16,
@@ -966,12 +1057,72 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    }
    const bool pencil = B->n_pencils > 0;
    const int np = B->n_pencils;
-   const int grid =
-      pencil ? (c->fp32 ? pencil_grid<float>(c->cfg.stencil, np * V)
-                        : pencil_grid<double>(c->cfg.stencil, np * V))
-             : (c->fp32 ? batched_grid<float>(c->g, c->cfg.stencil, nb * V)
-                        : batched_grid<double>(c->g, c->cfg.stencil, nb * V));
+   // one stage: cur -> oth with launch shape sh
+   auto stage = [&](const void *cur, void *oth, const StageShape &sh,
+                    int last, bool do_cs, int cnt) -> int {
+      unsigned long long *acc =
+         c->fp32 ? (unsigned long long *) B->acc.p + (size_t) cnt * V * 2
+                 : nullptr;
+      double *sums_at =
+         c->fp32 ? nullptr : (double *) B->sums.p + (size_t) cnt * V;
+      double *part = c->fp32 ? nullptr : (double *) B->partials.p;
+      if (pencil && c->fp32)
+         return launch_pencil_stage((const float *) cur, (float *) oth, c->g,
+                                    c->cfg.stencil,
+                                    (const BItem *) B->items.p, nb,
+                                    (const TileDesc *) B->chain.p,
+                                    (const int2 *) B->pencils.p, np, sh, last,
+                                    do_cs, part, sums_at, acc, c->d_err,
+                                    c->stream);
+      if (pencil)
+         return launch_pencil_stage((const double *) cur, (double *) oth,
+                                    c->g, c->cfg.stencil,
+                                    (const BItem *) B->items.p, nb,
+                                    (const TileDesc *) B->chain.p,
+                                    (const int2 *) B->pencils.p, np, sh, last,
+                                    do_cs, part, sums_at, acc, c->d_err,
+                                    c->stream);
+      if (c->fp32)
+         return launch_batched_stage((const float *) cur, (float *) oth,
+                                     c->g, c->cfg.stencil,
+                                     (const BItem *) B->items.p, nb, sh, last,
+                                     do_cs, part, sums_at, acc, c->d_err,
+                                     c->stream);
+      return launch_batched_stage((const double *) cur, (double *) oth, c->g,
+                                  c->cfg.stencil, (const BItem *) B->items.p,
+                                  nb, sh, last, do_cs, part, sums_at, acc,
+                                  c->d_err, c->stream);
+   };
+   std::vector<StageShape> cands;
+   if (pencil && c->fp32)
+      pencil_candidates<float>(c->cfg.stencil, np * V, cands);
+   else if (pencil)
+      pencil_candidates<double>(c->cfg.stencil, np * V, cands);
+   else if (c->fp32)
+      batched_candidates<float>(c->g, c->cfg.stencil, nb, cands);
+   else
+      batched_candidates<double>(c->g, c->cfg.stencil, nb, cands);
    CUDA_TRY(cudaGetLastError());
+   if (cands.empty())
+      return fail(MAMR_ECUDA, "no launch shape of the stage kernel fits "
+                  "this block size");
+   int choice = 0;
+   if (c->tune_force >= 0) {
+      choice = std::min<int>(c->tune_force, (int) cands.size() - 1);
+   } else if ((r = tune_choice(c, cands, pencil, nb, stage, choice))) {
+      return r;
+   }
+   const StageShape sh = cands[choice];
+   c->tune_last = choice;
+   c->tune_n = (int) cands.size();
+   c->tune_shape = sh;
+   // both pools start identical, so cells no stage writes (stale ghosts,
+   // free slots) read the same whichever pool ends up current (the tuner
+   // above wrote only interiors of the spare pool)
+   const size_t used = (size_t) c->hw_slots * c->g.V * c->g.bv * es;
+   if (used)
+      CUDA_TRY(cudaMemcpyAsync(c->pool_alt, c->pool, used,
+                               cudaMemcpyDeviceToDevice, c->stream));
 
    cudaGraph_t g_graph = nullptr;
    if (graph)
@@ -985,41 +1136,7 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       for (int st = 0; st < spt; st++, q++) {
          const bool do_cs = freq && !(st % freq);
          const int last = (q == total - 1);
-         int k;
-         if (pencil && c->fp32)
-            k = launch_pencil_stage((const float *) cur, (float *) oth, c->g,
-                                    c->cfg.stencil,
-                                    (const BItem *) B->items.p, nb,
-                                    (const TileDesc *) B->chain.p,
-                                    (const int2 *) B->pencils.p, np, grid,
-                                    last, do_cs, nullptr, nullptr,
-                                    (unsigned long long *) B->acc.p +
-                                       (size_t) cnt * V * 2,
-                                    c->d_err, c->stream);
-         else if (pencil)
-            k = launch_pencil_stage((const double *) cur, (double *) oth,
-                                    c->g, c->cfg.stencil,
-                                    (const BItem *) B->items.p, nb,
-                                    (const TileDesc *) B->chain.p,
-                                    (const int2 *) B->pencils.p, np, grid,
-                                    last, do_cs, (double *) B->partials.p,
-                                    (double *) B->sums.p + (size_t) cnt * V,
-                                    nullptr, c->d_err, c->stream);
-         else if (c->fp32)
-            k = launch_batched_stage((const float *) cur, (float *) oth, c->g,
-                                     c->cfg.stencil,
-                                     (const BItem *) B->items.p, nb, grid,
-                                     last, do_cs, nullptr, nullptr,
-                                     (unsigned long long *) B->acc.p +
-                                        (size_t) cnt * V * 2,
-                                     c->d_err, c->stream);
-         else
-            k = launch_batched_stage((const double *) cur, (double *) oth,
-                                     c->g, c->cfg.stencil,
-                                     (const BItem *) B->items.p, nb, grid,
-                                     last, do_cs, (double *) B->partials.p,
-                                     (double *) B->sums.p + (size_t) cnt * V,
-                                     nullptr, c->d_err, c->stream);
+         const int k = stage(cur, oth, sh, last, do_cs, cnt);
          if (k < 0) {
             status = fail(MAMR_ECUDA, "batched stage launch: %s",
                           cudaGetErrorString(cudaGetLastError()));
@@ -1094,4 +1211,30 @@ extern "C" int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts,
       return fail(MAMR_EINVAL, "MAMR_RUN_PER_BLOCK applies to the plain path");
    return run_batched(c, num_ts, stages_per_ts, checksum_freq,
                       (flags & MAMR_RUN_GRAPH) != 0, sums, n_sums);
+}
+
+extern "C" int mamr_set_tuning(mamr_ctx *c, int32_t choice)
+{
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   c->tune_force = choice < 0 ? -1 : choice;
+   return MAMR_OK;
+}
+
+extern "C" int mamr_get_tuning(const mamr_ctx *c, int32_t *choice,
+                               int32_t *n_candidates, int32_t *shape)
+{
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   if (choice)
+      *choice = c->tune_last;
+   if (n_candidates)
+      *n_candidates = c->tune_n;
+   if (shape) {
+      shape[0] = c->tune_shape.threads;
+      shape[1] = c->tune_shape.vpc;
+      shape[2] = c->tune_shape.rows;
+      shape[3] = c->tune_shape.grid;
+   }
+   return MAMR_OK;
 }

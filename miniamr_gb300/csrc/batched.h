@@ -4,6 +4,8 @@
 // separates the exchange from the update.
 #pragma once
 
+#include <vector>
+
 #include "mamr_internal.h"
 
 namespace mamr {
@@ -47,31 +49,44 @@ struct BatchedState;
 void batched_destroy(BatchedState *b);
 void batched_mesh_changed(BatchedState *b);
 
+// Launch shape of a stage kernel, one of the autotuner's candidates.
+//   generic kernel: `threads` per variable (whole warps), `vpc` variables
+//                   of one block per CTA (blockDim = vpc * threads)
+//   pencil kernel:  `rows` j-rows per thread (threads = 256 / rows)
+//   both:           `grid` CTAs
+struct StageShape {
+   int threads = 0, vpc = 1, rows = 1, grid = 1;
+};
+
 // Launches one fused stage: src -> dst for every block and variable.
 // FP64 checksums: per-block serial sums into partials[var][block], then
 // finalize into sums[var]; FP32: exact fixed-point into acc[var][2].
 template <typename T>
 int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
-                         const BItem *items, int n_blocks, int grid,
-                         int write_ghosts, int do_cs, double *partials,
-                         double *sums, unsigned long long *acc,
-                         unsigned *err, cudaStream_t s);
-// Persistent grid size for the stage kernel (CTAs resident at once).
+                         const BItem *items, int n_blocks,
+                         const StageShape &sh, int write_ghosts, int do_cs,
+                         double *partials, double *sums,
+                         unsigned long long *acc, unsigned *err,
+                         cudaStream_t s);
+// The generic kernel's launch shapes for this geometry (first = default).
 template <typename T>
-int batched_grid(const Geom &g, int stencil, int n_items);
+void batched_candidates(const Geom &g, int stencil, int n_blocks,
+                        std::vector<StageShape> &out);
 
 // Pencil variant for single-level meshes of 16^3 blocks: CTAs walk chains
-// of blocks along z (chain[pencils[p].x .. +pencils[p].y), bottom to top).  FP32 checksums are fused (acc); FP64 checksums
-// run as a separate all-variable pass into partials and sums.
+// of blocks along z (chain[pencils[p].x .. +pencils[p].y), bottom to
+// top).  FP32 checksums are fused (acc); FP64 checksums run as a separate
+// all-variable pass into partials and sums.
 template <typename T>
 int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
                         const BItem *items, int n_blocks,
                         const TileDesc *chain, const int2 *pencils,
-                        int n_pencils, int grid, int write_ghosts, int do_cs,
-                        double *partials, double *sums,
+                        int n_pencils, const StageShape &sh, int write_ghosts,
+                        int do_cs, double *partials, double *sums,
                         unsigned long long *acc, unsigned *err,
                         cudaStream_t s);
+// The pencil kernel's launch shapes for n_work = pencils x variables.
 template <typename T>
-int pencil_grid(int stencil, int n_work);
+void pencil_candidates(int stencil, int n_work, std::vector<StageShape> &out);
 
 }  // namespace mamr

@@ -14,6 +14,9 @@
 // which is what comm()'s x, y, z sweeps compose to when all blocks share
 // one level; the host only selects this path for 27-point stencils on such
 // meshes.
+#include <algorithm>
+#include <vector>
+
 #include "batched.h"
 #include "arith.cuh"
 
@@ -45,10 +48,33 @@ __device__ __forceinline__ long long fcell(const Geom &g, int dir, int nc,
    return cell_offset(g, a, b, nc);
 }
 
+// Adds a warp's 128-bit fixed-point partial sums into acc[0..1] (every
+// lane of the warp calls it).
+__device__ __forceinline__ void warp_acc128_flush(unsigned long long lo,
+                                                  unsigned long long hi,
+                                                  unsigned long long *acc)
+{
+#pragma unroll
+   for (int off = 16; off; off >>= 1) {
+      unsigned long long l2 = __shfl_down_sync(0xffffffffu, lo, off);
+      unsigned long long h2 = __shfl_down_sync(0xffffffffu, hi, off);
+      acc128_merge(lo, hi, l2, h2);
+   }
+   if ((threadIdx.x & 31) == 0) {
+      unsigned long long old = atomicAdd(acc, lo);
+      unsigned long long hadd = hi + ((old + lo < old) ? 1ull : 0ull);
+      if (hadd)
+         atomicAdd(acc + 1, hadd);
+   }
+}
+
+// A CTA takes the variables [vg * vpc, vg * vpc + vpc) of one block per
+// work item: blockDim.x / vpc threads (whole warps) and one shared tile
+// per variable, the block's neighbour record loaded once.
 template <typename T, int ST>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
-                     const BItem *__restrict__ items, int nb,
+                     const BItem *__restrict__ items, int nb, int vpc,
                      int write_ghosts, int do_cs,
                      double *__restrict__ partials,
                      unsigned long long *__restrict__ acc,
@@ -56,17 +82,34 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
 {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ BItem sI;
-   T *tile = reinterpret_cast<T *>(smem_raw);
    constexpr int VW = 16 / (int) sizeof(T), KO = VW - 1;
    const int nx = g.nx, ny = g.ny, nz = g.nz, Y = g.Y;
    const int Zs = tile_zs(nz, VW);
+   const int gthreads = blockDim.x / vpc;
+   const int grp = threadIdx.x / gthreads, gtid = threadIdx.x - grp * gthreads;
+   T *tile = reinterpret_cast<T *>(smem_raw) + (size_t) grp * g.X * Y * Zs;
 #define TS(i, j, k) tile[((i) * Y + (j)) * Zs + KO + (k)]
-   const int n_items = nb * g.V;
+   const int n_groups = (g.V + vpc - 1) / vpc;
+   const int n_items = nb * n_groups;
    const int nvec = nz / VW;
    const bool vec = (nz % VW) == 0;
+   // FP32 checksum terms of this thread's variable, flushed per warp when
+   // the variable changes and at the end
+   unsigned long long lo = 0, hi = 0;
+   bool ok = true;
+   int cs_var = -1;
 
    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
-      const int var = it / nb, b = it - var * nb;
+      const int vg = it / nb, b = it - vg * nb;
+      const int var = vg * vpc + grp;
+      const bool active = var < g.V;
+      if (sizeof(T) == 4 && do_cs && var != cs_var) {
+         if (cs_var >= 0) {
+            warp_acc128_flush(lo, hi, acc + 2 * cs_var);
+            lo = hi = 0;
+         }
+         cs_var = active ? var : -1;
+      }
       {
          const int32_t *from = reinterpret_cast<const int32_t *>(items + b);
          int32_t *to = reinterpret_cast<int32_t *>(&sI);
@@ -75,196 +118,198 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
             to[q] = from[q];
       }
       __syncthreads();
-      const T *s = src + bv_offset(g, sI.slot, var);
-      T *d = dst + bv_offset(g, sI.slot, var);
+      const T *s = src + bv_offset(g, sI.slot, active ? var : 0);
+      T *d = dst + bv_offset(g, sI.slot, active ? var : 0);
 
-      // interior rows, 16-byte vectors (rows start on a sector boundary)
-      if (vec) {
-         using V = typename Vec16<T>::type;
-         for (int e = threadIdx.x; e < nx * ny * nvec; e += blockDim.x) {
-            int r = e / nvec, q = e - r * nvec;
-            int i = r / ny + 1, j = r - (i - 1) * ny + 1;
-            V v = __ldg(reinterpret_cast<const V *>(s + cell_offset(g, i, j, 1)) + q);
-            *reinterpret_cast<V *>(&TS(i, j, 1 + q * VW)) = v;
+      if (active) {
+         // interior rows, 16-byte vectors (rows start on a sector boundary)
+         if (vec) {
+            using V = typename Vec16<T>::type;
+            for (int e = gtid; e < nx * ny * nvec; e += gthreads) {
+               int r = e / nvec, q = e - r * nvec;
+               int i = r / ny + 1, j = r - (i - 1) * ny + 1;
+               V v = __ldg(reinterpret_cast<const V *>(
+                              s + cell_offset(g, i, j, 1)) + q);
+               *reinterpret_cast<V *>(&TS(i, j, 1 + q * VW)) = v;
+            }
+         } else {
+            for (int e = gtid; e < nx * ny * nz; e += gthreads) {
+               int r = e / nz, k = e - r * nz + 1;
+               int i = r / ny + 1, j = r - (i - 1) * ny + 1;
+               TS(i, j, k) = s[cell_offset(g, i, j, k)];
+            }
          }
-      } else {
-         for (int e = threadIdx.x; e < nx * ny * nz; e += blockDim.x) {
-            int r = e / nz, k = e - r * nz + 1;
-            int i = r / ny + 1, j = r - (i - 1) * ny + 1;
-            TS(i, j, k) = s[cell_offset(g, i, j, k)];
-         }
-      }
 
-      // face ghosts (tangential interior), one face per pass
-      for (int l = 0; l < 6; l++) {
-         const int dir = l >> 1;
-         const bool low = !(l & 1);
-         const int n = dir == 0 ? nx : (dir == 1 ? ny : nz);
-         const int na = dir == 0 ? ny : nx;
-         const int nbb = dir == 2 ? ny : nz;
-         const int type = sI.f[l].type;
-         const int gn = low ? 0 : n + 1;
-         for (int e = threadIdx.x; e < na * nbb; e += blockDim.x) {
-            const int a = e / nbb + 1, bq = e - (a - 1) * nbb + 1;
-            T v;
-            if (type == FACE_SAME) {
-               v = src[bv_offset(g, sI.f[l].nb[0], var) +
-                       fcell(g, dir, low ? n : 1, a, bq)];
-            } else if (type == FACE_BC) {
-               v = s[fcell(g, dir, low ? 1 : n, a, bq)];
-            } else if (type == FACE_COARSE) {
-               const int ha = na / 2, hb = nbb / 2;
-               v = quarter(src[bv_offset(g, sI.f[l].nb[0], var) +
-                               fcell(g, dir, low ? n : 1,
-                                     (a + 1) / 2 + sI.f[l].jq * ha,
-                                     (bq + 1) / 2 + sI.f[l].iq * hb)]);
-            } else {
-               const int ha = na / 2, hb = nbb / 2;
-               const int jq = a > ha, iq = bq > hb;
-               const int a2 = a - jq * ha, b2 = bq - iq * hb;
-               const int p = low ? n : 1;
-               const T *f = src + bv_offset(g, sI.f[l].nb[iq * 2 + jq], var);
-               T t = f[fcell(g, dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
-                     f[fcell(g, dir, p, 2 * a2 - 1, 2 * b2)];
-               t = t + f[fcell(g, dir, p, 2 * a2, 2 * b2 - 1)];
-               t = t + f[fcell(g, dir, p, 2 * a2, 2 * b2)];
-               v = t;
+         // face ghosts (tangential interior), one face per pass
+         for (int l = 0; l < 6; l++) {
+            const int dir = l >> 1;
+            const bool low = !(l & 1);
+            const int n = dir == 0 ? nx : (dir == 1 ? ny : nz);
+            const int na = dir == 0 ? ny : nx;
+            const int nbb = dir == 2 ? ny : nz;
+            const int type = sI.f[l].type;
+            const int gn = low ? 0 : n + 1;
+            for (int e = gtid; e < na * nbb; e += gthreads) {
+               const int a = e / nbb + 1, bq = e - (a - 1) * nbb + 1;
+               T v;
+               if (type == FACE_SAME) {
+                  v = src[bv_offset(g, sI.f[l].nb[0], var) +
+                          fcell(g, dir, low ? n : 1, a, bq)];
+               } else if (type == FACE_BC) {
+                  v = s[fcell(g, dir, low ? 1 : n, a, bq)];
+               } else if (type == FACE_COARSE) {
+                  const int ha = na / 2, hb = nbb / 2;
+                  v = quarter(src[bv_offset(g, sI.f[l].nb[0], var) +
+                                  fcell(g, dir, low ? n : 1,
+                                        (a + 1) / 2 + sI.f[l].jq * ha,
+                                        (bq + 1) / 2 + sI.f[l].iq * hb)]);
+               } else {
+                  const int ha = na / 2, hb = nbb / 2;
+                  const int jq = a > ha, iq = bq > hb;
+                  const int a2 = a - jq * ha, b2 = bq - iq * hb;
+                  const int p = low ? n : 1;
+                  const T *f = src + bv_offset(g, sI.f[l].nb[iq * 2 + jq], var);
+                  T t = f[fcell(g, dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
+                        f[fcell(g, dir, p, 2 * a2 - 1, 2 * b2)];
+                  t = t + f[fcell(g, dir, p, 2 * a2, 2 * b2 - 1)];
+                  t = t + f[fcell(g, dir, p, 2 * a2, 2 * b2)];
+                  v = t;
+               }
+               int gi, gj, gk;
+               if (dir == 0) { gi = gn; gj = a; gk = bq; }
+               else if (dir == 1) { gi = a; gj = gn; gk = bq; }
+               else { gi = a; gj = bq; gk = gn; }
+               TS(gi, gj, gk) = v;
+               if (write_ghosts)
+                  d[cell_offset(g, gi, gj, gk)] = v;
             }
-            int gi, gj, gk;
-            if (dir == 0) { gi = gn; gj = a; gk = bq; }
-            else if (dir == 1) { gi = a; gj = gn; gk = bq; }
-            else { gi = a; gj = bq; gk = gn; }
-            TS(gi, gj, gk) = v;
-            if (write_ghosts)
-               d[cell_offset(g, gi, gj, gk)] = v;
          }
-      }
 
-      if (ST == 27) {
-         // 12 edges and 8 corners, resolved axis by axis
-         const int ne = 4 * (nx + ny + nz) + 8;
-         for (int e = threadIdx.x; e < ne; e += blockDim.x) {
-            int gi, gj, gk;
-            if (e < 4 * nz) {
-               int q = e / nz;
-               gk = e - q * nz + 1;
-               gi = (q & 1) ? nx + 1 : 0;
-               gj = (q & 2) ? ny + 1 : 0;
-            } else if (e < 4 * (nz + ny)) {
-               int e2 = e - 4 * nz, q = e2 / ny;
-               gj = e2 - q * ny + 1;
-               gi = (q & 1) ? nx + 1 : 0;
-               gk = (q & 2) ? nz + 1 : 0;
-            } else if (e < 4 * (nz + ny + nx)) {
-               int e2 = e - 4 * (nz + ny), q = e2 / nx;
-               gi = e2 - q * nx + 1;
-               gj = (q & 1) ? ny + 1 : 0;
-               gk = (q & 2) ? nz + 1 : 0;
-            } else {
-               int q = e - 4 * (nx + ny + nz);
-               gi = (q & 1) ? nx + 1 : 0;
-               gj = (q & 2) ? ny + 1 : 0;
-               gk = (q & 4) ? nz + 1 : 0;
+         if (ST == 27) {
+            // 12 edges and 8 corners, resolved axis by axis
+            const int ne = 4 * (nx + ny + nz) + 8;
+            for (int e = gtid; e < ne; e += gthreads) {
+               int gi, gj, gk;
+               if (e < 4 * nz) {
+                  int q = e / nz;
+                  gk = e - q * nz + 1;
+                  gi = (q & 1) ? nx + 1 : 0;
+                  gj = (q & 2) ? ny + 1 : 0;
+               } else if (e < 4 * (nz + ny)) {
+                  int e2 = e - 4 * nz, q = e2 / ny;
+                  gj = e2 - q * ny + 1;
+                  gi = (q & 1) ? nx + 1 : 0;
+                  gk = (q & 2) ? nz + 1 : 0;
+               } else if (e < 4 * (nz + ny + nx)) {
+                  int e2 = e - 4 * (nz + ny), q = e2 / nx;
+                  gi = e2 - q * nx + 1;
+                  gj = (q & 1) ? ny + 1 : 0;
+                  gk = (q & 2) ? nz + 1 : 0;
+               } else {
+                  int q = e - 4 * (nx + ny + nz);
+                  gi = (q & 1) ? nx + 1 : 0;
+                  gj = (q & 2) ? ny + 1 : 0;
+                  gk = (q & 4) ? nz + 1 : 0;
+               }
+               int dx = gi == 0 ? -1 : (gi == nx + 1 ? 1 : 0);
+               int dy = gj == 0 ? -1 : (gj == ny + 1 ? 1 : 0);
+               int dz = gk == 0 ? -1 : (gk == nz + 1 ? 1 : 0);
+               int si = gi, sj = gj, sk = gk;
+               if (dx) {
+                  if (sI.bmask & (1 << (dx < 0 ? 0 : 1))) { si = dx < 0 ? 1 : nx; dx = 0; }
+                  else si = dx < 0 ? nx : 1;
+               }
+               if (dy) {
+                  if (sI.bmask & (1 << (dy < 0 ? 2 : 3))) { sj = dy < 0 ? 1 : ny; dy = 0; }
+                  else sj = dy < 0 ? ny : 1;
+               }
+               if (dz) {
+                  if (sI.bmask & (1 << (dz < 0 ? 4 : 5))) { sk = dz < 0 ? 1 : nz; dz = 0; }
+                  else sk = dz < 0 ? nz : 1;
+               }
+               const int nbs = sI.nb27[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)];
+               const T v = src[bv_offset(g, nbs, var) + cell_offset(g, si, sj, sk)];
+               TS(gi, gj, gk) = v;
+               if (write_ghosts)
+                  d[cell_offset(g, gi, gj, gk)] = v;
             }
-            int dx = gi == 0 ? -1 : (gi == nx + 1 ? 1 : 0);
-            int dy = gj == 0 ? -1 : (gj == ny + 1 ? 1 : 0);
-            int dz = gk == 0 ? -1 : (gk == nz + 1 ? 1 : 0);
-            int si = gi, sj = gj, sk = gk;
-            if (dx) {
-               if (sI.bmask & (1 << (dx < 0 ? 0 : 1))) { si = dx < 0 ? 1 : nx; dx = 0; }
-               else si = dx < 0 ? nx : 1;
-            }
-            if (dy) {
-               if (sI.bmask & (1 << (dy < 0 ? 2 : 3))) { sj = dy < 0 ? 1 : ny; dy = 0; }
-               else sj = dy < 0 ? ny : 1;
-            }
-            if (dz) {
-               if (sI.bmask & (1 << (dz < 0 ? 4 : 5))) { sk = dz < 0 ? 1 : nz; dz = 0; }
-               else sk = dz < 0 ? nz : 1;
-            }
-            const int nbs = sI.nb27[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)];
-            const T v = src[bv_offset(g, nbs, var) + cell_offset(g, si, sj, sk)];
-            TS(gi, gj, gk) = v;
-            if (write_ghosts)
-               d[cell_offset(g, gi, gj, gk)] = v;
          }
       }
       __syncthreads();
 
       // stencil, one (j, k) column per thread sweeping i
-      unsigned long long lo = 0, hi = 0;
-      bool ok = true;
-      for (int col = threadIdx.x; col < ny * nz; col += blockDim.x) {
-         const int j = col / nz + 1, k = col - (j - 1) * nz + 1;
-         if (ST == 7) {
-            T am = TS(0, j, k), ac = TS(1, j, k);
-            for (int i = 1; i <= nx; i++) {
-               const T ap = TS(i + 1, j, k);
-               T w = am + TS(i, j - 1, k);
-               w = w + TS(i, j, k - 1);
-               w = w + ac;
-               w = w + TS(i, j, k + 1);
-               w = w + TS(i, j + 1, k);
-               w = w + ap;
-               const T out = div7(w);
-               d[cell_offset(g, i, j, k)] = out;
-               if (sizeof(T) == 4 && do_cs) {
-                  long long q;
-                  ok &= fixed52((float) out, q);
-                  acc128_add(lo, hi, q);
+      if (active)
+         for (int col = gtid; col < ny * nz; col += gthreads) {
+            const int j = col / nz + 1, k = col - (j - 1) * nz + 1;
+            if (ST == 7) {
+               T am = TS(0, j, k), ac = TS(1, j, k);
+               for (int i = 1; i <= nx; i++) {
+                  const T ap = TS(i + 1, j, k);
+                  T w = am + TS(i, j - 1, k);
+                  w = w + TS(i, j, k - 1);
+                  w = w + ac;
+                  w = w + TS(i, j, k + 1);
+                  w = w + TS(i, j + 1, k);
+                  w = w + ap;
+                  const T out = div7(w);
+                  d[cell_offset(g, i, j, k)] = out;
+                  if (sizeof(T) == 4 && do_cs) {
+                     long long q;
+                     ok &= fixed52((float) out, q);
+                     acc128_add(lo, hi, q);
+                  }
+                  am = ac;
+                  ac = ap;
                }
-               am = ac;
-               ac = ap;
-            }
-         } else {
-            auto S = [&](int p) -> T {
-               T t = TS(p, j - 1, k - 1) + TS(p, j - 1, k);
-               t = t + TS(p, j - 1, k + 1);
-               t = t + TS(p, j, k - 1);
-               t = t + TS(p, j, k);
-               t = t + TS(p, j, k + 1);
-               t = t + TS(p, j + 1, k - 1);
-               t = t + TS(p, j + 1, k);
-               t = t + TS(p, j + 1, k + 1);
-               return t;
-            };
-            T s0 = S(0), s1 = S(1);
-            for (int i = 1; i <= nx; i++) {
-               const T s2 = S(i + 1);
-               const T out = div27((s0 + s1) + s2);
-               d[cell_offset(g, i, j, k)] = out;
-               if (sizeof(T) == 4 && do_cs) {
-                  long long q;
-                  ok &= fixed52((float) out, q);
-                  acc128_add(lo, hi, q);
+            } else {
+               auto S = [&](int p) -> T {
+                  T t = TS(p, j - 1, k - 1) + TS(p, j - 1, k);
+                  t = t + TS(p, j - 1, k + 1);
+                  t = t + TS(p, j, k - 1);
+                  t = t + TS(p, j, k);
+                  t = t + TS(p, j, k + 1);
+                  t = t + TS(p, j + 1, k - 1);
+                  t = t + TS(p, j + 1, k);
+                  t = t + TS(p, j + 1, k + 1);
+                  return t;
+               };
+               T s0 = S(0), s1 = S(1);
+               for (int i = 1; i <= nx; i++) {
+                  const T s2 = S(i + 1);
+                  const T out = div27((s0 + s1) + s2);
+                  d[cell_offset(g, i, j, k)] = out;
+                  if (sizeof(T) == 4 && do_cs) {
+                     long long q;
+                     ok &= fixed52((float) out, q);
+                     acc128_add(lo, hi, q);
+                  }
+                  s0 = s1;
+                  s1 = s2;
                }
-               s0 = s1;
-               s1 = s2;
             }
          }
-      }
-      if (do_cs) {
-         if (sizeof(T) == 4) {
-            if (!ok)
-               atomicOr(err, ERR_FIXED_RANGE);
-            block_acc128_flush(lo, hi, acc + 2 * var);
-         } else {
-            // the reference's order: serial over i, j, k of this block
-            __syncthreads();
-            if (threadIdx.x == 0) {
-               double bs = 0.0;
-               for (int i = 1; i <= nx; i++)
-                  for (int j = 1; j <= ny; j++) {
-                     const T *row = d + cell_offset(g, i, j, 1);
+      if (sizeof(T) == 8 && do_cs) {
+         // the reference's order: serial over i, j, k of this block
+         __syncthreads();
+         if (active && gtid == 0) {
+            double bs = 0.0;
+            for (int i = 1; i <= nx; i++)
+               for (int j = 1; j <= ny; j++) {
+                  const T *row = d + cell_offset(g, i, j, 1);
 #pragma unroll 8
-                     for (int k = 0; k < nz; k++)
-                        bs = bs + (double) row[k];
-                  }
-               partials[(size_t) var * nb + b] = bs;
-            }
+                  for (int k = 0; k < nz; k++)
+                     bs = bs + (double) row[k];
+               }
+            partials[(size_t) var * nb + b] = bs;
          }
       }
       __syncthreads();
+   }
+   if (sizeof(T) == 4 && do_cs) {
+      if (cs_var >= 0)
+         warp_acc128_flush(lo, hi, acc + 2 * cs_var);
+      if (!ok)
+         atomicOr(err, ERR_FIXED_RANGE);
    }
 #undef TS
 }
@@ -285,59 +330,81 @@ __global__ void finalize_fp64(const double *__restrict__ partials, int nb,
 }
 
 template <typename T, int ST>
-static void set_smem(size_t bytes)
+static int batched_per_sm(size_t smem, int threads)
 {
+   int per_sm = 0;
    cudaFuncSetAttribute(batched_stage_kernel<T, ST>,
                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                        (int) bytes);
+                        (int) smem);
+   cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, batched_stage_kernel<T, ST>, threads, smem);
+   return per_sm;
 }
 
-static int block_threads(const Geom &g)
-{
-   int t = g.ny * g.nz;
-   return t >= 256 ? 256 : ((t + 31) / 32) * 32;
-}
-
+// Candidates: threads per variable = the (j, k) columns rounded up to
+// whole warps (at most 256) or half that (at least one warp), times 1, 2
+// or 4 variables per CTA (at most 512 threads and 200 KB of tiles); a
+// persistent grid of the CTAs one wave holds.
 template <typename T>
-int batched_grid(const Geom &g, int stencil, int n_items)
+void batched_candidates(const Geom &g, int stencil, int n_blocks,
+                        std::vector<StageShape> &out)
 {
-   const size_t smem = tile_bytes<T>(g);
-   int per_sm = 0, dev = 0, sms = 0;
-   const int thr = block_threads(g);
+   int dev = 0, sms = 0;
    cudaGetDevice(&dev);
    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-   if (stencil == 7) {
-      set_smem<T, 7>(smem);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &per_sm, batched_stage_kernel<T, 7>, thr, smem);
-   } else {
-      set_smem<T, 27>(smem);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &per_sm, batched_stage_kernel<T, 27>, thr, smem);
+   out.clear();
+   const int cols = g.ny * g.nz;
+   const int full = std::min(256, (cols + 31) / 32 * 32);
+   for (int thr : {full, std::max(32, full / 2 / 32 * 32)}) {
+      for (int vpc : {1, 2, 4}) {
+         if (thr * vpc > 512 || vpc > g.V)
+            continue;
+         const size_t smem = tile_bytes<T>(g) * vpc;
+         if (smem > 200 * 1024)
+            continue;
+         const int per_sm = stencil == 7
+                               ? batched_per_sm<T, 7>(smem, thr * vpc)
+                               : batched_per_sm<T, 27>(smem, thr * vpc);
+         if (per_sm <= 0)
+            continue;
+         const long long items =
+            (long long) n_blocks * ((g.V + vpc - 1) / vpc);
+         StageShape sh;
+         sh.threads = thr;
+         sh.vpc = vpc;
+         sh.grid = (int) std::max(1LL, std::min<long long>(
+                                          (long long) per_sm * sms, items));
+         bool dup = false;
+         for (const StageShape &o : out)
+            dup |= o.threads == sh.threads && o.vpc == sh.vpc;
+         if (!dup)
+            out.push_back(sh);
+      }
+      if (full == 32)
+         break;
    }
-   long long grid = (long long) (per_sm > 0 ? per_sm : 1) * sms;
-   return (int) (grid < n_items ? grid : (n_items > 0 ? n_items : 1));
 }
 
 template <typename T>
 int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
-                         const BItem *items, int n_blocks, int grid,
-                         int write_ghosts, int do_cs, double *partials,
-                         double *sums, unsigned long long *acc,
-                         unsigned *err, cudaStream_t s)
+                         const BItem *items, int n_blocks,
+                         const StageShape &sh, int write_ghosts, int do_cs,
+                         double *partials, double *sums,
+                         unsigned long long *acc, unsigned *err,
+                         cudaStream_t s)
 {
    if (n_blocks == 0)
       return 0;
-   const size_t smem = tile_bytes<T>(g);
-   const int thr = block_threads(g);
+   const size_t smem = tile_bytes<T>(g) * sh.vpc;
+   const int thr = sh.threads * sh.vpc;
    if (stencil == 7)
-      batched_stage_kernel<T, 7><<<grid, thr, smem, s>>>(
-         src, dst, g, items, n_blocks, write_ghosts, do_cs, partials, acc,
-         err);
+      batched_stage_kernel<T, 7><<<sh.grid, thr, smem, s>>>(
+         src, dst, g, items, n_blocks, sh.vpc, write_ghosts, do_cs, partials,
+         acc, err);
    else
-      batched_stage_kernel<T, 27><<<grid, thr, smem, s>>>(
-         src, dst, g, items, n_blocks, write_ghosts, do_cs, partials, acc,
-         err);
+      batched_stage_kernel<T, 27><<<sh.grid, thr, smem, s>>>(
+         src, dst, g, items, n_blocks, sh.vpc, write_ghosts, do_cs, partials,
+         acc, err);
    int launches = 1;
    if (do_cs && sizeof(T) == 8) {
       finalize_fp64<<<(g.V + 127) / 128, 128, 0, s>>>(partials, n_blocks,
@@ -347,17 +414,21 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
    return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
 }
 
-template int batched_grid<float>(const Geom &, int, int);
-template int batched_grid<double>(const Geom &, int, int);
+template void batched_candidates<float>(const Geom &, int, int,
+                                        std::vector<StageShape> &);
+template void batched_candidates<double>(const Geom &, int, int,
+                                         std::vector<StageShape> &);
 template int launch_batched_stage<float>(const float *, float *, const Geom &,
-                                         int, const BItem *, int, int, int,
-                                         int, double *, double *,
+                                         int, const BItem *, int,
+                                         const StageShape &, int, int,
+                                         double *, double *,
                                          unsigned long long *, unsigned *,
                                          cudaStream_t);
 template int launch_batched_stage<double>(const double *, double *,
                                           const Geom &, int, const BItem *,
-                                          int, int, int, int, double *,
-                                          double *, unsigned long long *,
-                                          unsigned *, cudaStream_t);
+                                          int, const StageShape &, int, int,
+                                          double *, double *,
+                                          unsigned long long *, unsigned *,
+                                          cudaStream_t);
 
 }  // namespace mamr

@@ -23,6 +23,9 @@
 // as comm() leaves them on a single-level mesh (axis-by-axis neighbour or
 // reflection), the reference's summation order, correctly rounded
 // division, and the FP32 checksum as exact 128-bit fixed point.
+#include <algorithm>
+#include <vector>
+
 #include "batched.h"
 #include "arith.cuh"
 
@@ -46,15 +49,11 @@ __device__ __forceinline__ int trow(int i, int j)
    return i * TileGeom<T>::PW + j * RS;
 }
 
-// Work split: JP j-rows per thread.  FP32 (bound by shared-memory
-// bandwidth): 2 rows, 128 threads, three CTAs per SM.  FP64 (bound by the
-// FP64 pipe): 1 row, 256 threads, one CTA per SM.
-template <typename T> struct Shape;
-template <> struct Shape<float> {
-   static constexpr int JP = 2, THREADS = 128, CTAS = 3;
-};
-template <> struct Shape<double> {
-   static constexpr int JP = 1, THREADS = 256, CTAS = 1;
+// Work split: JP j-rows per thread (1 or 2; the autotuner picks), so
+// 256 / JP threads per tile; FP32 tiles allow three CTAs per SM, FP64 one.
+template <typename T, int JP> struct Shape {
+   static constexpr int THREADS = 256 / JP;
+   static constexpr int CTAS = sizeof(T) == 4 ? 3 : 1;
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -371,8 +370,8 @@ __device__ __noinline__ PassState tile_fix(const T *tq, const T *eg, T *d,
 
 }  // namespace
 
-template <typename T, int ST>
-__global__ void __launch_bounds__(Shape<T>::THREADS, Shape<T>::CTAS)
+template <typename T, int ST, int JP>
+__global__ void __launch_bounds__(Shape<T, JP>::THREADS, Shape<T, JP>::CTAS)
 pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                     const TileDesc *__restrict__ chain,
                     const int2 *__restrict__ pencils, int n_pencils,
@@ -380,7 +379,7 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                     unsigned long long *__restrict__ acc,
                     unsigned *__restrict__ err)
 {
-   constexpr int JP = Shape<T>::JP, THREADS = Shape<T>::THREADS;
+   constexpr int THREADS = Shape<T, JP>::THREADS;
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ TileDesc s_desc[PENCIL_MAX];
    T *tiles = reinterpret_cast<T *>(
@@ -543,41 +542,55 @@ __global__ void finalize_all_fp64(const double *__restrict__ partials,
    }
 }
 
-template <typename T, int ST>
-static cudaError_t pencil_attr()
+template <typename T, int ST, int JP>
+static int pencil_per_sm()
 {
-   return cudaFuncSetAttribute(pencil_stage_kernel<T, ST>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int) pencil_smem_bytes<T>());
+   int per_sm = 0;
+   cudaFuncSetAttribute(pencil_stage_kernel<T, ST, JP>,
+                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                        (int) pencil_smem_bytes<T>());
+   cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, pencil_stage_kernel<T, ST, JP>, Shape<T, JP>::THREADS,
+      pencil_smem_bytes<T>());
+   return per_sm > 0 ? per_sm : 1;
 }
 
+// Candidates: JP = 2 or 1 rows per thread, times a persistent grid (the
+// CTAs one wave holds, each looping over work items) or one CTA per work
+// item (the hardware balances the tail).
 template <typename T>
-int pencil_grid(int stencil, int n_work)
+void pencil_candidates(int stencil, int n_work, std::vector<StageShape> &out)
 {
-   int per_sm = 0, dev = 0, sms = 0;
+   int dev = 0, sms = 0;
    cudaGetDevice(&dev);
    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-   if (stencil == 7) {
-      pencil_attr<T, 7>();
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &per_sm, pencil_stage_kernel<T, 7>, Shape<T>::THREADS,
-         pencil_smem_bytes<T>());
-   } else {
-      pencil_attr<T, 27>();
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-         &per_sm, pencil_stage_kernel<T, 27>, Shape<T>::THREADS,
-         pencil_smem_bytes<T>());
+   out.clear();
+   for (int jp : {2, 1}) {
+      const int per_sm =
+         stencil == 7 ? (jp == 2 ? pencil_per_sm<T, 7, 2>()
+                                 : pencil_per_sm<T, 7, 1>())
+                      : (jp == 2 ? pencil_per_sm<T, 27, 2>()
+                                 : pencil_per_sm<T, 27, 1>());
+      const long long wave = (long long) per_sm * sms;
+      StageShape a;
+      a.rows = jp;
+      a.vpc = 1;
+      a.threads = 256 / jp;
+      a.grid = (int) std::max(1LL, std::min<long long>(wave, n_work));
+      out.push_back(a);
+      if (n_work > wave) {
+         a.grid = n_work;
+         out.push_back(a);
+      }
    }
-   long long grid = (long long) (per_sm > 0 ? per_sm : 1) * sms;
-   return (int) (grid < n_work ? grid : (n_work > 0 ? n_work : 1));
 }
 
 template <typename T>
 int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
                         const BItem *items, int n_blocks,
                         const TileDesc *chain, const int2 *pencils,
-                        int n_pencils, int grid, int write_ghosts, int do_cs,
-                        double *partials, double *sums,
+                        int n_pencils, const StageShape &sh, int write_ghosts,
+                        int do_cs, double *partials, double *sums,
                         unsigned long long *acc, unsigned *err,
                         cudaStream_t s)
 {
@@ -585,14 +598,17 @@ int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
       return 0;
    const size_t smem = pencil_smem_bytes<T>();
    const int fused_cs = (sizeof(T) == 4) ? do_cs : 0;
-   if (stencil == 7)
-      pencil_stage_kernel<T, 7><<<grid, Shape<T>::THREADS, smem, s>>>(
-         src, dst, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc,
-         err);
-   else
-      pencil_stage_kernel<T, 27><<<grid, Shape<T>::THREADS, smem, s>>>(
-         src, dst, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc,
-         err);
+   const int grid = sh.grid;
+#define MAMR_PENCIL(ST, JP)                                                   \
+   pencil_stage_kernel<T, ST, JP><<<grid, Shape<T, JP>::THREADS, smem, s>>>( \
+      src, dst, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc,   \
+      err)
+   if (stencil == 7) {
+      if (sh.rows == 2) MAMR_PENCIL(7, 2); else MAMR_PENCIL(7, 1);
+   } else {
+      if (sh.rows == 2) MAMR_PENCIL(27, 2); else MAMR_PENCIL(27, 1);
+   }
+#undef MAMR_PENCIL
    int launches = 1;
    if (do_cs && sizeof(T) == 8) {
       const long long n = (long long) n_blocks * g.V;
@@ -605,19 +621,20 @@ int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
    return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
 }
 
-template int pencil_grid<float>(int, int);
-template int pencil_grid<double>(int, int);
+template void pencil_candidates<float>(int, int, std::vector<StageShape> &);
+template void pencil_candidates<double>(int, int, std::vector<StageShape> &);
 template int launch_pencil_stage<float>(const float *, float *, const Geom &,
                                         int, const BItem *, int,
                                         const TileDesc *, const int2 *, int,
-                                        int, int, int, double *, double *,
-                                        unsigned long long *, unsigned *,
-                                        cudaStream_t);
+                                        const StageShape &, int, int, double *,
+                                        double *, unsigned long long *,
+                                        unsigned *, cudaStream_t);
 template int launch_pencil_stage<double>(const double *, double *,
                                          const Geom &, int, const BItem *,
                                          int, const TileDesc *, const int2 *,
-                                         int, int, int, int, double *,
-                                         double *, unsigned long long *,
-                                         unsigned *, cudaStream_t);
+                                         int, const StageShape &, int, int,
+                                         double *, double *,
+                                         unsigned long long *, unsigned *,
+                                         cudaStream_t);
 
 }  // namespace mamr

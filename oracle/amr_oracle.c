@@ -136,6 +136,29 @@ int mamr_launch_count(mamr_ctx *c, int64_t *count)
    return MAMR_OK;
 }
 
+/* The oracle has no launch shapes: the setting is accepted and ignored,
+ * and no choice is ever reported. */
+int mamr_set_tuning(mamr_ctx *c, int32_t choice)
+{
+   (void) choice;
+   return c ? MAMR_OK : fail(MAMR_EINVAL, "null context");
+}
+
+int mamr_get_tuning(const mamr_ctx *c, int32_t *choice,
+                    int32_t *n_candidates, int32_t *shape)
+{
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   if (choice)
+      *choice = -1;
+   if (n_candidates)
+      *n_candidates = 0;
+   if (shape)
+      for (int q = 0; q < 4; q++)
+         shape[q] = 0;
+   return MAMR_OK;
+}
+
 static int check_slot(const mamr_ctx *c, int32_t s)
 {
    return s >= 0 && s < c->cfg.max_blocks;

@@ -71,6 +71,49 @@ def test_batched_equals_plain_amr7(gpu_lib, name, dtype):
         assert np.array_equal(bits(a), bits(b))
 
 
+SHAPE_CASES = [
+    ((2, 1, 2), (16, 16, 16), 3, 27, 1),   # pencil kernel
+    ((1, 2, 2), (16, 16, 16), 2, 7, 1),
+    ((2, 2, 2), (8, 8, 8), 5, 7, 1),       # generic kernel, 5 vars: the
+    ((3, 1, 2), (4, 6, 8), 5, 27, 1),      # 4-per-CTA shape has a part group
+]
+
+
+@pytest.mark.parametrize("dtype", [FP64, FP32])
+@pytest.mark.parametrize("case", SHAPE_CASES)
+def test_every_launch_shape_equals_plain(gpu_lib, case, dtype):
+    """Each launch-shape candidate of the autotuner, forced in turn, gives
+    the plain path's cells and checksums bit for bit; the automatic choice
+    is one of them."""
+    (ix, iy, iz), (nx, ny, nz), V, st, passes = case
+    n0 = ix * iy * iz
+    cap = n0 * (1 + 8 ** passes) + 8
+    cfg = Config.make(nx, ny, nz, V, cap, stencil=st, dtype=dtype)
+    init = gpu_lib.initial_values(cfg, n0)
+
+    def run(flags, choice=None):
+        m = meshmod.initial_mesh(ix, iy, iz, passes, cap)
+        with gpu_lib.context(cfg) as ctx:
+            if choice is not None:
+                ctx.set_tuning(choice)
+            ctx.upload(np.arange(n0), init)
+            for _ in range(passes):
+                ctx.split(m.split_all())
+            ctx.set_mesh(m.blocks())
+            s = ctx.run_timesteps(2, 2, 1, flags=flags)
+            return s, ctx.download(np.arange(cap)), ctx.tuning()
+
+    ref = run(0)
+    auto = run(RUN_BATCHED)
+    n = auto[2]["candidates"]
+    assert n >= 2 and 0 <= auto[2]["choice"] < n
+    for k in range(n):
+        got = run(RUN_BATCHED | RUN_GRAPH, k)
+        assert got[2]["choice"] == k
+        for a, b in zip(ref[:2], got[:2]):
+            assert np.array_equal(bits(a), bits(b)), (k, got[2])
+
+
 @pytest.mark.parametrize("stencil", [7, 27])
 @pytest.mark.parametrize("dtype", [FP64, FP32])
 def test_pencil_division_fixup(gpu_lib, dtype, stencil):
