@@ -70,11 +70,12 @@ def updates(steps):
     return steps * SPT * UPD_PER_STAGE
 
 
-def build_mesh(lib, dtype, init=INIT, cap=CAP, ctx=None, host=None):
+def build_mesh(lib, dtype, init=INIT, cap=CAP, ctx=None, host=None,
+               stencil=STENCIL):
     from miniamr_gb300 import mesh as meshmod
     from miniamr_gb300.abi import Config
     n0 = init[0] * init[1] * init[2]
-    cfg = Config.make(N, N, N, V, cap, stencil=STENCIL, dtype=dtype)
+    cfg = Config.make(N, N, N, V, cap, stencil=stencil, dtype=dtype)
     if ctx is None:
         ctx = lib.context(cfg)
     if host is None:
@@ -181,6 +182,69 @@ def oracle_rate(steps, threads=None):
     return steps * SPT * n0 * 8 * N ** 3 * V / dt, threads, dt
 
 
+def uniform_fp64_7pt(lib, steps):
+    """The uniform 4096-block mesh with 40 FP64 variables and the 7-point
+    stencil, 4 stages per timestep: the batched path (fused ghost+stencil,
+    CUDA graph, autotuned launch shape) against one stencil launch per
+    (block, variable) after the per-call exchange (updates/s)."""
+    import torch
+    from miniamr_gb300.abi import FP64, RUN_BATCHED, RUN_GRAPH, RUN_PER_BLOCK
+    ctx, _ = build_mesh(lib, FP64, stencil=7)
+    ctx.run_timesteps(1, SPT, FREQ, flags=RUN_BATCHED | RUN_GRAPH)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.run_timesteps(steps, SPT, FREQ, first_stage=SPT,
+                      flags=RUN_BATCHED | RUN_GRAPH)
+    batched = updates(steps) / (time.perf_counter() - t0)
+    shape = ctx.tuning()
+    t0 = time.perf_counter()
+    ctx.run_timesteps(1, 1, 0, flags=RUN_PER_BLOCK)
+    per_block = UPD_PER_STAGE / (time.perf_counter() - t0)
+    ctx.close()
+    return {"workload": "4096 blocks of 16^3, 40 FP64 vars, 7-point, 4 "
+                        "stages/ts", "batched_graph": batched,
+            "batched_timesteps": steps, "launch_shape": shape,
+            "one_launch_per_block_var": per_block,
+            "speedup": batched / per_block}
+
+
+def stress_multilevel(lib, dtype):
+    """The multi-level stress run (4^3 blocks of 8^3, 5 levels, four moving
+    objects, refine every 2 steps, 7-point, 20 timesteps x 2 stages; about
+    22k blocks, 35,884 at most) replayed from the reference's recorded mesh
+    sequence with 40 variables: each stretch of stages between refinements
+    is one batched run under a freshly captured CUDA graph.  Rate = updates
+    over the run calls' wall time (graph capture included); refinement data
+    movement and mesh set-up are timed separately."""
+    import torch
+    from miniamr_gb300.abi import RUN_BATCHED, RUN_GRAPH
+    from miniamr_gb300.trace import read_trace, replay_batched
+    path = os.path.join(REPO, "tests", "golden", "config5.trace.xz")
+    if not os.path.exists(path):
+        return None
+    recs = read_trace(path)
+    # first pass: the autotuner times its candidates for each work size
+    _, ctx, _ = replay_batched(lib, recs, RUN_BATCHED | RUN_GRAPH,
+                               dtype=dtype, num_vars=V)
+    ctx.close()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, ctx, timings = replay_batched(lib, recs, RUN_BATCHED | RUN_GRAPH,
+                                     dtype=dtype, num_vars=V)
+    torch.cuda.synchronize()
+    total = time.perf_counter() - t0
+    stages = sum(n for n, _, _ in timings)
+    run_s = sum(t for _, t, _ in timings)
+    cells = 8 ** 3
+    upd = sum(n * nb * cells * V for n, _, nb in timings)
+    ctx.close()
+    return {"stages": stages, "runs": len(timings),
+            "mean_blocks": upd / (stages * cells * V),
+            "max_blocks": max(nb for _, _, nb in timings),
+            "updates_per_s": upd / run_s, "run_seconds": run_s,
+            "replay_seconds_incl_refinement_and_host": total}
+
+
 def profile_case(name):
     """Small batched run for ncu captures: 4096 blocks of 16^3, 4 vars
     (268 MB of FP32 interior cells per pool, twice the L2), two timesteps
@@ -263,6 +327,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the FP64 7-point and multi-level stress "
+                         "measurements")
     ap.add_argument("--fp64-steps", type=int, default=None,
                     help="timesteps of the FP64 comparison runs")
     ap.add_argument("--profile-case", default=None,
@@ -384,6 +451,12 @@ def main():
         "fp32_checksum_error": err,
         "clocks": clk.summary(),
     }
+    if not args.no_configs:
+        line["configs"] = {
+            "uniform_fp64_7pt": uniform_fp64_7pt(lib, 2),
+            "stress_multilevel_7pt_fp32": stress_multilevel(lib, FP32),
+            "stress_multilevel_7pt_fp64": stress_multilevel(lib, FP64),
+        }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, threads, dt = oracle_rate(3)
         line["cpu_baseline"] = {

@@ -190,7 +190,8 @@ def replay_batched(lib: Library, records: list[Record], flags: int,
     changes executed as one mamr_run_timesteps call (flags: RUN_BATCHED,
     RUN_GRAPH ...), one timestep of one stage per recorded stage.  Returns
     (checksums [(var, replayed, recorded)], ReplayResult-like context),
-    plus per-call timings [(stages, seconds)] for throughput figures.
+    plus per-call timings [(stages, seconds, active blocks)] for throughput
+    figures.
 
     Checksum cadence must be uniform inside a run: stages are grouped by
     whether they computed checksums.  num_vars overrides the recorded
@@ -216,7 +217,7 @@ def replay_batched(lib: Library, records: list[Record], flags: int,
             t0 = time.perf_counter()
             got = ctx.run_timesteps(n, 1, 1 if cs else 0, pending[i][0],
                                     flags=flags)
-            timings.append((n, time.perf_counter() - t0))
+            timings.append((n, time.perf_counter() - t0, n_active))
             if cs:
                 for q in range(n):
                     for var, rec in pending[i + q][2]:
@@ -226,6 +227,7 @@ def replay_batched(lib: Library, records: list[Record], flags: int,
         pending.clear()
 
     stage = None
+    n_active = 0
     for r in records:
         if r.op == OP_CREATE:
             cfg = Config.from_buffer_copy(bytes(r.args[0]))
@@ -245,6 +247,7 @@ def replay_batched(lib: Library, records: list[Record], flags: int,
             flush()
             if r.op == OP_SET_MESH:
                 ctx.set_mesh(r.args[0])
+                n_active = len(r.args[0])
             elif r.op == OP_SPLIT:
                 ctx.split(r.args[0])
             else:
