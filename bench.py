@@ -246,22 +246,49 @@ def stress_multilevel(lib, dtype):
 
 
 def profile_case(name):
-    """Small batched run for ncu captures: 4096 blocks of 16^3, 4 vars
-    (268 MB of FP32 interior cells per pool, twice the L2), two timesteps
-    of four stages launched one by one (checksums on each timestep's first
-    stage, as in the benchmark)."""
+    """Small batched runs for ncu captures, launched stage by stage (no
+    graph), with the stage kernel's launch shape forced to candidate
+    MAMR_PROFILE_SHAPE (default 0, the one the tuner keeps for the
+    benchmark workload) so that launch indices are stable.
+      fp32_27, fp32_7, fp64_27, fp64_7: 4096 blocks of 16^3, 4 vars (268 MB
+        of FP32 interior cells per pool, twice the L2), two timesteps of
+        four stages (checksums on each timestep's first stage, as in the
+        benchmark);
+      stress_fp32, stress_fp64: the recorded multi-level stress run (8^3
+        blocks, ~22k of them, 4 vars, 7-point), replayed batched: 40
+        stages, one run per stretch between refinements."""
     global V, UPD_PER_STAGE
     import torch
     from miniamr_gb300 import build, load
     from miniamr_gb300.abi import FP32, FP64, RUN_BATCHED
     global STENCIL
-    dtype = FP32 if name.startswith("fp32") else FP64
+    dtype = FP32 if "fp32" in name else FP64
+    shape = int(os.environ.get("MAMR_PROFILE_SHAPE", "0"))
+    build.build_library()
+    lib = load()
+    if name.startswith("stress"):
+        from miniamr_gb300.trace import read_trace, replay_batched
+        import miniamr_gb300.trace as tr
+        recs = read_trace(os.path.join(REPO, "tests", "golden",
+                                       "config5.trace.xz"))
+        orig = lib.context
+
+        def forced(cfg):
+            c = orig(cfg)
+            c.set_tuning(shape)
+            return c
+        lib.context = forced
+        _, ctx, timings = replay_batched(lib, recs, RUN_BATCHED, dtype=dtype)
+        torch.cuda.synchronize()
+        ctx.close()
+        print(f"profile case {name}: {sum(n for n, _, _ in timings)} "
+              f"batched stages in {len(timings)} runs")
+        return 0
     STENCIL = 27 if name.endswith("27") else 7
     V = 4
     UPD_PER_STAGE = N_BLOCKS * N ** 3 * V
-    build.build_library()
-    lib = load()
     ctx, _ = build_mesh(lib, dtype)
+    ctx.set_tuning(shape)
     # the benchmark's cadence: 4 stages per timestep, checksum on stage 0
     ctx.run_timesteps(1, SPT, FREQ, flags=RUN_BATCHED)
     ctx.run_timesteps(1, SPT, FREQ, first_stage=SPT, flags=RUN_BATCHED)
@@ -333,10 +360,9 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=None,
                     help="timesteps of the FP64 comparison runs")
     ap.add_argument("--profile-case", default=None,
-                    choices=["fp32_27", "fp32_7", "fp64_27", "fp64_7"],
-                    help="a small case for ncu: the 4096-block mesh with 4 "
-                         "variables, 2 warm-up + 2 profiled batched stages "
-                         "launched without a graph")
+                    choices=["fp32_27", "fp32_7", "fp64_27", "fp64_7",
+                             "stress_fp32", "stress_fp64"],
+                    help="a small case for ncu (see profile_case)")
     args = ap.parse_args()
     if args.profile_case:
         return profile_case(args.profile_case)

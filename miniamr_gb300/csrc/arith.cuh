@@ -29,8 +29,8 @@ __device__ __forceinline__ bool div_window(double x)
 }
 __device__ __forceinline__ bool div_window(float x)
 {
-   const unsigned e = (__float_as_uint(x) >> 23) & 0xffu;
-   return e - 61u < 189u;                     // 60 < e < 250
+   // 60 < e < 250 on the magnitude's bits (NaN and inf fall outside)
+   return (__float_as_uint(x) & 0x7fffffffu) - (61u << 23) < (189u << 23);
 }
 
 template <int C>

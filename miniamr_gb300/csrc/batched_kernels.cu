@@ -40,13 +40,32 @@ __host__ __device__ inline size_t tile_bytes(const Geom &g)
    return (size_t) g.X * g.Y * tile_zs(g.nz, vw) * sizeof(T);
 }
 
-__device__ __forceinline__ long long fcell(const Geom &g, int dir, int nc,
-                                           int a, int b)
-{
-   if (dir == 0) return cell_offset(g, nc, a, b);
-   if (dir == 1) return cell_offset(g, a, nc, b);
-   return cell_offset(g, a, b, nc);
-}
+// Block dimensions: compile-time constants for the common block sizes (so
+// that every index folds), taken from g when zero.
+template <int BX, int BY, int BZ> struct Dims {
+   const int nx, ny, nz, X, Y;
+   __device__ explicit Dims(const Geom &g)
+      : nx(BX ? BX : g.nx), ny(BY ? BY : g.ny), nz(BZ ? BZ : g.nz),
+        X((BX ? BX : g.nx) + 2), Y((BY ? BY : g.ny) + 2)
+   {
+   }
+   // cell (i, j, k) of a block-variable in the split layout (contexts
+   // always use it): interior rows of nz values, then the k = 0 and
+   // k = nz+1 planes
+   __device__ __forceinline__ int cell(int i, int j, int k) const
+   {
+      const int row = i * Y + j;
+      if (k >= 1 && k <= nz)
+         return row * nz + (k - 1);
+      return X * Y * nz + (k == 0 ? 0 : X * Y) + row;
+   }
+   __device__ __forceinline__ int fcell(int dir, int nc, int a, int b) const
+   {
+      if (dir == 0) return cell(nc, a, b);
+      if (dir == 1) return cell(a, nc, b);
+      return cell(a, b, nc);
+   }
+};
 
 // Adds a warp's 128-bit fixed-point partial sums into acc[0..1] (every
 // lane of the warp calls it).
@@ -71,7 +90,7 @@ __device__ __forceinline__ void warp_acc128_flush(unsigned long long lo,
 // A CTA takes the variables [vg * vpc, vg * vpc + vpc) of one block per
 // work item: blockDim.x / vpc threads (whole warps) and one shared tile
 // per variable, the block's neighbour record loaded once.
-template <typename T, int ST>
+template <typename T, int ST, int BX, int BY, int BZ>
 __global__ void __launch_bounds__(512)
 batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                      const BItem *__restrict__ items, int nb, int vpc,
@@ -83,11 +102,12 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ BItem sI;
    constexpr int VW = 16 / (int) sizeof(T), KO = VW - 1;
-   const int nx = g.nx, ny = g.ny, nz = g.nz, Y = g.Y;
+   const Dims<BX, BY, BZ> D(g);
+   const int nx = D.nx, ny = D.ny, nz = D.nz, Y = D.Y;
    const int Zs = tile_zs(nz, VW);
    const int gthreads = blockDim.x / vpc;
    const int grp = threadIdx.x / gthreads, gtid = threadIdx.x - grp * gthreads;
-   T *tile = reinterpret_cast<T *>(smem_raw) + (size_t) grp * g.X * Y * Zs;
+   T *tile = reinterpret_cast<T *>(smem_raw) + (size_t) grp * D.X * Y * Zs;
 #define TS(i, j, k) tile[((i) * Y + (j)) * Zs + KO + (k)]
    const int n_groups = (g.V + vpc - 1) / vpc;
    const int n_items = nb * n_groups;
@@ -129,14 +149,14 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                int r = e / nvec, q = e - r * nvec;
                int i = r / ny + 1, j = r - (i - 1) * ny + 1;
                V v = __ldg(reinterpret_cast<const V *>(
-                              s + cell_offset(g, i, j, 1)) + q);
+                              s + D.cell(i, j, 1)) + q);
                *reinterpret_cast<V *>(&TS(i, j, 1 + q * VW)) = v;
             }
          } else {
             for (int e = gtid; e < nx * ny * nz; e += gthreads) {
                int r = e / nz, k = e - r * nz + 1;
                int i = r / ny + 1, j = r - (i - 1) * ny + 1;
-               TS(i, j, k) = s[cell_offset(g, i, j, k)];
+               TS(i, j, k) = s[D.cell(i, j, k)];
             }
          }
 
@@ -154,13 +174,13 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                T v;
                if (type == FACE_SAME) {
                   v = src[bv_offset(g, sI.f[l].nb[0], var) +
-                          fcell(g, dir, low ? n : 1, a, bq)];
+                          D.fcell(dir, low ? n : 1, a, bq)];
                } else if (type == FACE_BC) {
-                  v = s[fcell(g, dir, low ? 1 : n, a, bq)];
+                  v = s[D.fcell(dir, low ? 1 : n, a, bq)];
                } else if (type == FACE_COARSE) {
                   const int ha = na / 2, hb = nbb / 2;
                   v = quarter(src[bv_offset(g, sI.f[l].nb[0], var) +
-                                  fcell(g, dir, low ? n : 1,
+                                  D.fcell(dir, low ? n : 1,
                                         (a + 1) / 2 + sI.f[l].jq * ha,
                                         (bq + 1) / 2 + sI.f[l].iq * hb)]);
                } else {
@@ -169,10 +189,10 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                   const int a2 = a - jq * ha, b2 = bq - iq * hb;
                   const int p = low ? n : 1;
                   const T *f = src + bv_offset(g, sI.f[l].nb[iq * 2 + jq], var);
-                  T t = f[fcell(g, dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
-                        f[fcell(g, dir, p, 2 * a2 - 1, 2 * b2)];
-                  t = t + f[fcell(g, dir, p, 2 * a2, 2 * b2 - 1)];
-                  t = t + f[fcell(g, dir, p, 2 * a2, 2 * b2)];
+                  T t = f[D.fcell(dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
+                        f[D.fcell(dir, p, 2 * a2 - 1, 2 * b2)];
+                  t = t + f[D.fcell(dir, p, 2 * a2, 2 * b2 - 1)];
+                  t = t + f[D.fcell(dir, p, 2 * a2, 2 * b2)];
                   v = t;
                }
                int gi, gj, gk;
@@ -181,7 +201,7 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                else { gi = a; gj = bq; gk = gn; }
                TS(gi, gj, gk) = v;
                if (write_ghosts)
-                  d[cell_offset(g, gi, gj, gk)] = v;
+                  d[D.cell(gi, gj, gk)] = v;
             }
          }
 
@@ -228,10 +248,10 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                   else sk = dz < 0 ? nz : 1;
                }
                const int nbs = sI.nb27[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)];
-               const T v = src[bv_offset(g, nbs, var) + cell_offset(g, si, sj, sk)];
+               const T v = src[bv_offset(g, nbs, var) + D.cell(si, sj, sk)];
                TS(gi, gj, gk) = v;
                if (write_ghosts)
-                  d[cell_offset(g, gi, gj, gk)] = v;
+                  d[D.cell(gi, gj, gk)] = v;
             }
          }
       }
@@ -252,7 +272,7 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                   w = w + TS(i, j + 1, k);
                   w = w + ap;
                   const T out = div7(w);
-                  d[cell_offset(g, i, j, k)] = out;
+                  d[D.cell(i, j, k)] = out;
                   if (sizeof(T) == 4 && do_cs) {
                      long long q;
                      ok &= fixed52((float) out, q);
@@ -277,7 +297,7 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                for (int i = 1; i <= nx; i++) {
                   const T s2 = S(i + 1);
                   const T out = div27((s0 + s1) + s2);
-                  d[cell_offset(g, i, j, k)] = out;
+                  d[D.cell(i, j, k)] = out;
                   if (sizeof(T) == 4 && do_cs) {
                      long long q;
                      ok &= fixed52((float) out, q);
@@ -295,7 +315,7 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
             double bs = 0.0;
             for (int i = 1; i <= nx; i++)
                for (int j = 1; j <= ny; j++) {
-                  const T *row = d + cell_offset(g, i, j, 1);
+                  const T *row = d + D.cell(i, j, 1);
 #pragma unroll 8
                   for (int k = 0; k < nz; k++)
                      bs = bs + (double) row[k];
@@ -329,16 +349,37 @@ __global__ void finalize_fp64(const double *__restrict__ partials, int nb,
    }
 }
 
-template <typename T, int ST>
-static int batched_per_sm(size_t smem, int threads)
+// Compile-time block size of a geometry: 8^3 and 16^3 get their own
+// instantiations, anything else the run-time one.
+static int dims_kind(const Geom &g)
+{
+   if (g.nx == 8 && g.ny == 8 && g.nz == 8)
+      return 1;
+   if (g.nx == 16 && g.ny == 16 && g.nz == 16)
+      return 2;
+   return 0;
+}
+
+template <typename T, int ST, int BX, int BY, int BZ>
+static int per_sm_of(size_t smem, int threads)
 {
    int per_sm = 0;
-   cudaFuncSetAttribute(batched_stage_kernel<T, ST>,
+   cudaFuncSetAttribute(batched_stage_kernel<T, ST, BX, BY, BZ>,
                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                         (int) smem);
    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, batched_stage_kernel<T, ST>, threads, smem);
+      &per_sm, batched_stage_kernel<T, ST, BX, BY, BZ>, threads, smem);
    return per_sm;
+}
+
+template <typename T, int ST>
+static int batched_per_sm(const Geom &g, size_t smem, int threads)
+{
+   switch (dims_kind(g)) {
+   case 1: return per_sm_of<T, ST, 8, 8, 8>(smem, threads);
+   case 2: return per_sm_of<T, ST, 16, 16, 16>(smem, threads);
+   default: return per_sm_of<T, ST, 0, 0, 0>(smem, threads);
+   }
 }
 
 // Candidates: threads per variable = the (j, k) columns rounded up to
@@ -363,8 +404,8 @@ void batched_candidates(const Geom &g, int stencil, int n_blocks,
          if (smem > 200 * 1024)
             continue;
          const int per_sm = stencil == 7
-                               ? batched_per_sm<T, 7>(smem, thr * vpc)
-                               : batched_per_sm<T, 27>(smem, thr * vpc);
+                               ? batched_per_sm<T, 7>(g, smem, thr * vpc)
+                               : batched_per_sm<T, 27>(g, smem, thr * vpc);
          if (per_sm <= 0)
             continue;
          const long long items =
@@ -397,14 +438,21 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
       return 0;
    const size_t smem = tile_bytes<T>(g) * sh.vpc;
    const int thr = sh.threads * sh.vpc;
-   if (stencil == 7)
-      batched_stage_kernel<T, 7><<<sh.grid, thr, smem, s>>>(
-         src, dst, g, items, n_blocks, sh.vpc, write_ghosts, do_cs, partials,
-         acc, err);
-   else
-      batched_stage_kernel<T, 27><<<sh.grid, thr, smem, s>>>(
-         src, dst, g, items, n_blocks, sh.vpc, write_ghosts, do_cs, partials,
-         acc, err);
+#define MAMR_GENERIC(ST, BX, BY, BZ)                                          \
+   batched_stage_kernel<T, ST, BX, BY, BZ><<<sh.grid, thr, smem, s>>>(         \
+      src, dst, g, items, n_blocks, sh.vpc, write_ghosts, do_cs, partials,    \
+      acc, err)
+   const int kind = dims_kind(g);
+   if (stencil == 7) {
+      if (kind == 1) MAMR_GENERIC(7, 8, 8, 8);
+      else if (kind == 2) MAMR_GENERIC(7, 16, 16, 16);
+      else MAMR_GENERIC(7, 0, 0, 0);
+   } else {
+      if (kind == 1) MAMR_GENERIC(27, 8, 8, 8);
+      else if (kind == 2) MAMR_GENERIC(27, 16, 16, 16);
+      else MAMR_GENERIC(27, 0, 0, 0);
+   }
+#undef MAMR_GENERIC
    int launches = 1;
    if (do_cs && sizeof(T) == 8) {
       finalize_fp64<<<(g.V + 127) / 128, 128, 0, s>>>(partials, n_blocks,
