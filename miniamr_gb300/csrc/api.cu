@@ -1116,11 +1116,14 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    c->tune_last = choice;
    c->tune_n = (int) cands.size();
    c->tune_shape = sh;
-   // both pools start identical, so cells no stage writes (stale ghosts,
-   // free slots) read the same whichever pool ends up current (the tuner
-   // above wrote only interiors of the spare pool)
+   // A run of an odd number of stages ends in the spare pool: it must then
+   // hold what no stage writes (stale ghosts, free slots) as the current
+   // pool does, so it starts as a copy.  With an even number the run ends
+   // in the current pool and no stage reads a spare-pool cell that an
+   // earlier stage of the run did not write, so no copy is needed (the
+   // tuner above wrote only interiors of the spare pool).
    const size_t used = (size_t) c->hw_slots * c->g.V * c->g.bv * es;
-   if (used)
+   if (used && (num_ts * spt) % 2 == 1)
       CUDA_TRY(cudaMemcpyAsync(c->pool_alt, c->pool, used,
                                cudaMemcpyDeviceToDevice, c->stream));
 

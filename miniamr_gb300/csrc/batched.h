@@ -85,6 +85,14 @@ int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
                         int do_cs, double *partials, double *sums,
                         unsigned long long *acc, unsigned *err,
                         cudaStream_t s);
+// FP64 checksums of every (block, variable) of a pool in the reference's
+// order: per-block serial sums into partials[var][block] (one thread per
+// block-variable), then sums[var] serially over blocks.  Returns the
+// number of kernels launched.
+int launch_fp64_checksums(const double *pool, const Geom &g,
+                          const BItem *items, int n_blocks, double *partials,
+                          double *sums, cudaStream_t s);
+
 // The pencil kernel's launch shapes for n_work = pencils x variables.
 template <typename T>
 void pencil_candidates(int stencil, int n_work, std::vector<StageShape> &out);

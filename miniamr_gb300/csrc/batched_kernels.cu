@@ -5,8 +5,10 @@
 // (same-level copy, coarse/4 prolongation, 4-cell restriction sum,
 // reflection; ref/comm.c:1465-1965) -- applies the stencil in the
 // reference's operation order (ref/stencil.c:82-144), writes the interior
-// to the destination pool and folds the checksum of the result
-// (ref/check_sum.c:44-53) into the same pass.
+// to the destination pool and, for FP32 pools, folds the exact fixed-point
+// checksum of the result into the same pass (FP64 checksums, serial in the
+// reference's order ref/check_sum.c:44-53, run as a separate pass over all
+// block-variables).
 //
 // Exactness: face ghosts are exact for every mesh.  27-point edge and
 // corner ghosts are resolved axis by axis (neighbour across each
@@ -95,7 +97,6 @@ __global__ void __launch_bounds__(512)
 batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                      const BItem *__restrict__ items, int nb, int vpc,
                      int write_ghosts, int do_cs,
-                     double *__restrict__ partials,
                      unsigned long long *__restrict__ acc,
                      unsigned *__restrict__ err)
 {
@@ -308,21 +309,6 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                }
             }
          }
-      if (sizeof(T) == 8 && do_cs) {
-         // the reference's order: serial over i, j, k of this block
-         __syncthreads();
-         if (active && gtid == 0) {
-            double bs = 0.0;
-            for (int i = 1; i <= nx; i++)
-               for (int j = 1; j <= ny; j++) {
-                  const T *row = d + D.cell(i, j, 1);
-#pragma unroll 8
-                  for (int k = 0; k < nz; k++)
-                     bs = bs + (double) row[k];
-               }
-            partials[(size_t) var * nb + b] = bs;
-         }
-      }
       __syncthreads();
    }
    if (sizeof(T) == 4 && do_cs) {
@@ -332,21 +318,6 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
          atomicOr(err, ERR_FIXED_RANGE);
    }
 #undef TS
-}
-
-// Sum over blocks in sorted_list order, one thread per variable.
-__global__ void finalize_fp64(const double *__restrict__ partials, int nb,
-                              int V, double *__restrict__ sums)
-{
-   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V;
-        v += gridDim.x * blockDim.x) {
-      const double *p = partials + (size_t) v * nb;
-      double s = 0.0;
-#pragma unroll 8
-      for (int b = 0; b < nb; b++)
-         s = s + p[b];
-      sums[v] = s;
-   }
 }
 
 // Compile-time block size of a geometry: 8^3 and 16^3 get their own
@@ -440,8 +411,8 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
    const int thr = sh.threads * sh.vpc;
 #define MAMR_GENERIC(ST, BX, BY, BZ)                                          \
    batched_stage_kernel<T, ST, BX, BY, BZ><<<sh.grid, thr, smem, s>>>(         \
-      src, dst, g, items, n_blocks, sh.vpc, write_ghosts, do_cs, partials,    \
-      acc, err)
+      src, dst, g, items, n_blocks, sh.vpc, write_ghosts,                     \
+      sizeof(T) == 4 ? do_cs : 0, acc, err)
    const int kind = dims_kind(g);
    if (stencil == 7) {
       if (kind == 1) MAMR_GENERIC(7, 8, 8, 8);
@@ -454,11 +425,9 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
    }
 #undef MAMR_GENERIC
    int launches = 1;
-   if (do_cs && sizeof(T) == 8) {
-      finalize_fp64<<<(g.V + 127) / 128, 128, 0, s>>>(partials, n_blocks,
-                                                       g.V, sums);
-      launches++;
-   }
+   if (do_cs && sizeof(T) == 8)
+      launches += launch_fp64_checksums((const double *) dst, g, items,
+                                        n_blocks, partials, sums, s);
    return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
 }
 

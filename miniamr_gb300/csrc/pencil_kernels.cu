@@ -542,6 +542,20 @@ __global__ void finalize_all_fp64(const double *__restrict__ partials,
    }
 }
 
+int launch_fp64_checksums(const double *pool, const Geom &g,
+                          const BItem *items, int n_blocks, double *partials,
+                          double *sums, cudaStream_t s)
+{
+   const long long n = (long long) n_blocks * g.V;
+   if (n == 0)
+      return 0;
+   block_sums_all_fp64<<<(unsigned) ((n + 127) / 128), 128, 0, s>>>(
+      pool, g, items, n_blocks, partials);
+   finalize_all_fp64<<<(g.V + 127) / 128, 128, 0, s>>>(partials, n_blocks,
+                                                        g.V, sums);
+   return 2;
+}
+
 template <typename T, int ST, int JP>
 static int pencil_per_sm()
 {
@@ -610,14 +624,9 @@ int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
    }
 #undef MAMR_PENCIL
    int launches = 1;
-   if (do_cs && sizeof(T) == 8) {
-      const long long n = (long long) n_blocks * g.V;
-      block_sums_all_fp64<<<(unsigned) ((n + 127) / 128), 128, 0, s>>>(
-         (const double *) dst, g, items, n_blocks, partials);
-      finalize_all_fp64<<<(g.V + 127) / 128, 128, 0, s>>>(partials, n_blocks,
-                                                           g.V, sums);
-      launches += 2;
-   }
+   if (do_cs && sizeof(T) == 8)
+      launches += launch_fp64_checksums((const double *) dst, g, items,
+                                        n_blocks, partials, sums, s);
    return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
 }
 
