@@ -164,9 +164,10 @@ def ncu_traffic():
         return None
 
 
-def oracle_rate(steps, threads=None):
+def oracle_rate(steps, threads=None, stages=SPT, warm=True):
     """The reference algorithm on the host cores: CPU oracle, FP64, OpenMP
-    over blocks, on the 512-block sample; returns (updates/s, threads)."""
+    over blocks, on the 512-block sample, `steps` timesteps of `stages`
+    stages; returns (updates/s, threads, seconds)."""
     from miniamr_gb300 import build
     from miniamr_gb300.abi import FP64, Library
     threads = threads or os.cpu_count() or 1
@@ -174,12 +175,60 @@ def oracle_rate(steps, threads=None):
     lib = Library(build.build_oracle())
     n0 = SAMPLE_INIT[0] * SAMPLE_INIT[1] * SAMPLE_INIT[2]
     ctx, _ = build_mesh(lib, FP64, init=SAMPLE_INIT, cap=n0 * 9 + 8)
-    ctx.run_timesteps(1, SPT, FREQ)           # warm-up
+    if warm:
+        ctx.run_timesteps(1, stages, FREQ)
     t0 = time.perf_counter()
-    ctx.run_timesteps(steps, SPT, FREQ)
+    ctx.run_timesteps(steps, stages, FREQ)
     dt = time.perf_counter() - t0
     ctx.close()
-    return steps * SPT * n0 * 8 * N ** 3 * V / dt, threads, dt
+    return steps * stages * n0 * 8 * N ** 3 * V / dt, threads, dt
+
+
+def amr_plain_fp64(lib):
+    """The AMR run with one moving sphere (4^3 blocks of 16^3, 40 FP64
+    vars, 27-point, 4 levels, refine every 5 steps, 100 timesteps; up to
+    7429 blocks) replayed from the reference's recorded mesh sequence
+    through the plain FP64 path -- the drop-in's call sequence of comm,
+    stencil and check_sum, queued without host syncs -- with every checksum
+    compared bit for bit with the reference's."""
+    import torch
+    from miniamr_gb300.abi import FP64, RUN_PLAIN
+    from miniamr_gb300.trace import read_trace, replay_batched
+    path = os.path.join(REPO, "tests", "golden", "config2.trace.xz")
+    if not os.path.exists(path):
+        return None
+    recs = read_trace(path)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sums, ctx, timings = replay_batched(lib, recs, RUN_PLAIN, dtype=FP64)
+    torch.cuda.synchronize()
+    total = time.perf_counter() - t0
+    ctx.close()
+    cells = N ** 3
+    stages = sum(n for n, _, _ in timings)
+    upd = sum(n * nb * cells * V for n, _, nb in timings)
+    run_s = sum(t for _, t, _ in timings)
+    exact = all(np.float64(a).tobytes() == np.float64(b).tobytes()
+                for _, a, b in sums)
+    return {"stages": stages, "runs": len(timings),
+            "mean_blocks": upd / (stages * cells * V),
+            "max_blocks": max(nb for _, _, nb in timings),
+            "updates_per_s": upd / run_s, "run_seconds": run_s,
+            "replay_seconds_incl_refinement_and_host": total,
+            "checksums": len(sums), "checksums_bit_exact": exact}
+
+
+def one_thread_oracle_rate():
+    """The CPU oracle on one host thread (a fresh process, so that OpenMP
+    starts with one thread): one stage of the 512-block sample."""
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    r = subprocess.run([sys.executable, os.path.abspath(__file__),
+                        "--oracle-rate-steps", "1"], env=env,
+                       capture_output=True, text=True)
+    try:
+        return json.loads(r.stdout.strip().splitlines()[-1])
+    except (ValueError, IndexError):
+        return None
 
 
 def uniform_fp64_7pt(lib, steps):
@@ -354,6 +403,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--oracle-rate-steps", type=int, default=0,
+                    help=argparse.SUPPRESS)
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the FP64 7-point and multi-level stress "
                          "measurements")
@@ -364,6 +415,14 @@ def main():
                              "stress_fp32", "stress_fp64"],
                     help="a small case for ncu (see profile_case)")
     args = ap.parse_args()
+    if args.oracle_rate_steps:
+        rate, threads, dt = oracle_rate(
+            args.oracle_rate_steps, int(os.environ.get("OMP_NUM_THREADS",
+                                                       "1")),
+            stages=1, warm=False)
+        print(json.dumps({"value": rate, "unit": UNIT, "cores": threads,
+                          "seconds": dt}))
+        return 0
     if args.profile_case:
         return profile_case(args.profile_case)
     world, rank, local, pg = dist_setup()
@@ -463,6 +522,7 @@ def main():
         "config": dict(WORKLOAD, launch_shape=shape),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,
+                     "frac_of_nominal_8000": achieved / 8000.0,
                      "traffic": traffic, "peak_source": peak_kind,
                      "kernel": "pencil_stage_kernel<float,27>",
                      "alg_bytes_per_launch": alg_bytes},
@@ -480,16 +540,20 @@ def main():
     if not args.no_configs:
         line["configs"] = {
             "uniform_fp64_7pt": uniform_fp64_7pt(lib, 2),
+            "amr_sphere_27pt_plain_fp64": amr_plain_fp64(lib),
             "stress_multilevel_7pt_fp32": stress_multilevel(lib, FP32),
             "stress_multilevel_7pt_fp64": stress_multilevel(lib, FP64),
         }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        one = one_thread_oracle_rate()
         rate, threads, dt = oracle_rate(3)
         line["cpu_baseline"] = {
             "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "512 blocks of 16^3, 40 vars, 27-point, FP64, 3 "
                       "timesteps; CPU oracle with OpenMP over blocks "
                       f"({dt:.1f} s)"}
+        if one:
+            line["cpu_baseline"]["single_thread"] = one
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg:
