@@ -242,11 +242,12 @@ class Context:
 
     def tuning(self) -> dict:
         """The last batched run's launch shape: candidate index, number of
-        candidates, threads per variable, variables per CTA, rows per
-        thread, CTAs."""
+        candidates, threads, variables per CTA, rows and planes per thread,
+        CTAs."""
         ch, n = C.c_int32(), C.c_int32()
-        sh = (C.c_int32 * 4)()
+        sh = (C.c_int32 * 5)()
         self._call("mamr_get_tuning", C.byref(ch), C.byref(n), sh)
         return {"choice": ch.value, "candidates": n.value,
                 "threads": sh[0], "vars_per_cta": sh[1],
-                "rows_per_thread": sh[2], "ctas": sh[3]}
+                "rows_per_thread": sh[2], "planes_per_thread": sh[3],
+                "ctas": sh[4]}

@@ -1237,7 +1237,8 @@ extern "C" int mamr_get_tuning(const mamr_ctx *c, int32_t *choice,
       shape[0] = c->tune_shape.threads;
       shape[1] = c->tune_shape.vpc;
       shape[2] = c->tune_shape.rows;
-      shape[3] = c->tune_shape.grid;
+      shape[3] = c->tune_shape.planes;
+      shape[4] = c->tune_shape.grid;
    }
    return MAMR_OK;
 }

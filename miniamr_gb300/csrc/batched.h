@@ -52,10 +52,11 @@ void batched_mesh_changed(BatchedState *b);
 // Launch shape of a stage kernel, one of the autotuner's candidates.
 //   generic kernel: `threads` per variable (whole warps), `vpc` variables
 //                   of one block per CTA (blockDim = vpc * threads)
-//   pencil kernel:  `rows` j-rows per thread (threads = 256 / rows)
+//   pencil kernel:  `rows` j-rows and `planes` i-planes per thread
+//                   (threads = 1024 / (rows * planes))
 //   both:           `grid` CTAs
 struct StageShape {
-   int threads = 0, vpc = 1, rows = 1, grid = 1;
+   int threads = 0, vpc = 1, rows = 1, planes = 4, grid = 1;
 };
 
 // Launches one fused stage: src -> dst for every block and variable.

@@ -49,10 +49,12 @@ __device__ __forceinline__ int trow(int i, int j)
    return i * TileGeom<T>::PW + j * RS;
 }
 
-// Work split: JP j-rows per thread (1 or 2; the autotuner picks), so
-// 256 / JP threads per tile; FP32 tiles allow three CTAs per SM, FP64 one.
-template <typename T, int JP> struct Shape {
-   static constexpr int THREADS = 256 / JP;
+// Work split: JP j-rows and IH i-planes per thread (JP x IH = 1x4, 2x4 or
+// 1x8; the autotuner picks), so 1024 / (JP * IH) threads per tile; FP32
+// tiles allow three CTAs per SM, FP64 one.  More planes per thread share
+// each 9-term plane sum among more outputs (IH + 2 sums per IH planes).
+template <typename T, int JP, int IH> struct Shape {
+   static constexpr int THREADS = 1024 / (JP * IH);
    static constexpr int CTAS = sizeof(T) == 4 ? 3 : 1;
 };
 
@@ -261,7 +263,7 @@ __device__ __forceinline__ void emit4(const T (&w)[4], T *p, int do_cs,
 // k values on planes 4*ih+1 .. 4*ih+4.  `tq` is the thread's quad of row
 // (4*ih, jrow) in the tile, `eg` its ghost column from the same row, `d`
 // the matching global position.  Every lane of the warp runs it together.
-template <typename T, int ST, int JP, bool FIX>
+template <typename T, int ST, int JP, int IH, bool FIX>
 __device__ __forceinline__ void tile_pass(const T *tq, const T *eg, T *d,
                                           int kq, int do_cs, PassState &st)
 {
@@ -274,7 +276,7 @@ __device__ __forceinline__ void tile_pass(const T *tq, const T *eg, T *d,
          row6(tq, eg, 1, jj, kq, r[jj]);
       }
 #pragma unroll
-      for (int ii = 1; ii <= 4; ii++) {
+      for (int ii = 1; ii <= IH; ii++) {
          T qm[4], qp[4], c[JP][6];
          Quad<T>::ld(tq + trow<T>(ii, -1), qm);
          Quad<T>::ld(tq + trow<T>(ii, JP), qp);
@@ -337,7 +339,7 @@ __device__ __forceinline__ void tile_pass(const T *tq, const T *eg, T *d,
       S(0, s0);
       S(1, s1);
 #pragma unroll
-      for (int ii = 1; ii <= 4; ii++) {
+      for (int ii = 1; ii <= IH; ii++) {
          S(ii + 1, s2);
 #pragma unroll
          for (int jj = 0; jj < JP; jj++) {
@@ -360,18 +362,19 @@ __device__ __forceinline__ void tile_pass(const T *tq, const T *eg, T *d,
 
 // The fix-up pass out of line, so that its registers do not weigh on the
 // fast pass; called only when a warp met a sum outside the window.
-template <typename T, int ST, int JP>
+template <typename T, int ST, int JP, int IH>
 __device__ __noinline__ PassState tile_fix(const T *tq, const T *eg, T *d,
                                            int kq, int do_cs, PassState st)
 {
-   tile_pass<T, ST, JP, true>(tq, eg, d, kq, do_cs, st);
+   tile_pass<T, ST, JP, IH, true>(tq, eg, d, kq, do_cs, st);
    return st;
 }
 
 }  // namespace
 
-template <typename T, int ST, int JP>
-__global__ void __launch_bounds__(Shape<T, JP>::THREADS, Shape<T, JP>::CTAS)
+template <typename T, int ST, int JP, int IH>
+__global__ void __launch_bounds__(Shape<T, JP, IH>::THREADS,
+                                  Shape<T, JP, IH>::CTAS)
 pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                     const TileDesc *__restrict__ chain,
                     const int2 *__restrict__ pencils, int n_pencils,
@@ -379,7 +382,7 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                     unsigned long long *__restrict__ acc,
                     unsigned *__restrict__ err)
 {
-   constexpr int THREADS = Shape<T, JP>::THREADS;
+   constexpr int THREADS = Shape<T, JP, IH>::THREADS;
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ TileDesc s_desc[PENCIL_MAX];
    T *tiles = reinterpret_cast<T *>(
@@ -396,6 +399,7 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       ? 2 * (((lane >> 3) & 3) + 4 * ((tid >> 5) & 1)) + 1
       : ((tid >> 2) & 15) + 1;
    const int ih = JP == 2 ? ((lane >> 2) & 1) + 2 * (tid >> 6) : tid >> 6;
+   static_assert(JP == 1 || IH == 4, "two rows per thread need 4 planes");
 
    // the ghost-column rows this thread copies each step, walked i fastest
    // (fewer bank conflicts): (tile offset << 9) | column index
@@ -451,14 +455,14 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
             issue_tile<T, ST, THREADS>(src, g, s_desc + s + 2, var,
                                        tiles + ((s + 2) % 3) * TILE);
          // the thread's quad of row (4*ih, jrow) and its ghost column
-         const T *tq = t + trow<T>(4 * ih, jrow) + 4 * kq;
-         const T *eg = (kq == 3 ? khi : kcur) + 4 * ih * G + jrow;
+         const T *tq = t + trow<T>(IH * ih, jrow) + 4 * kq;
+         const T *eg = (kq == 3 ? khi : kcur) + IH * ih * G + jrow;
          const int slot = s_desc[s].slot;
-         T *d = dst + bv_offset(g, slot, var) + grow(4 * ih, jrow) + 4 * kq;
+         T *d = dst + bv_offset(g, slot, var) + grow(IH * ih, jrow) + 4 * kq;
          st.slow = false;
-         tile_pass<T, ST, JP, false>(tq, eg, d, kq, do_cs, st);
+         tile_pass<T, ST, JP, IH, false>(tq, eg, d, kq, do_cs, st);
          if (__any_sync(0xffffffffu, st.slow))
-            st = tile_fix<T, ST, JP>(tq, eg, d, kq, do_cs, st);
+            st = tile_fix<T, ST, JP, IH>(tq, eg, d, kq, do_cs, st);
          if (write_ghosts) {
             T *base = dst + bv_offset(g, slot, var);
             // the ghost cells comm() writes: face interiors for 7 points,
@@ -556,22 +560,22 @@ int launch_fp64_checksums(const double *pool, const Geom &g,
    return 2;
 }
 
-template <typename T, int ST, int JP>
+template <typename T, int ST, int JP, int IH>
 static int pencil_per_sm()
 {
    int per_sm = 0;
-   cudaFuncSetAttribute(pencil_stage_kernel<T, ST, JP>,
+   cudaFuncSetAttribute(pencil_stage_kernel<T, ST, JP, IH>,
                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                         (int) pencil_smem_bytes<T>());
    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, pencil_stage_kernel<T, ST, JP>, Shape<T, JP>::THREADS,
-      pencil_smem_bytes<T>());
+      &per_sm, pencil_stage_kernel<T, ST, JP, IH>,
+      Shape<T, JP, IH>::THREADS, pencil_smem_bytes<T>());
    return per_sm > 0 ? per_sm : 1;
 }
 
-// Candidates: JP = 2 or 1 rows per thread, times a persistent grid (the
-// CTAs one wave holds, each looping over work items) or one CTA per work
-// item (the hardware balances the tail).
+// Candidates: (rows, planes) per thread = (2, 4), (1, 4), (1, 8), each
+// with a persistent grid (the CTAs one wave holds, looping over work
+// items) or one CTA per work item (the hardware balances the tail).
 template <typename T>
 void pencil_candidates(int stencil, int n_work, std::vector<StageShape> &out)
 {
@@ -579,17 +583,24 @@ void pencil_candidates(int stencil, int n_work, std::vector<StageShape> &out)
    cudaGetDevice(&dev);
    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
    out.clear();
-   for (int jp : {2, 1}) {
-      const int per_sm =
-         stencil == 7 ? (jp == 2 ? pencil_per_sm<T, 7, 2>()
-                                 : pencil_per_sm<T, 7, 1>())
-                      : (jp == 2 ? pencil_per_sm<T, 27, 2>()
-                                 : pencil_per_sm<T, 27, 1>());
+   const int shapes[3][2] = {{2, 4}, {1, 4}, {1, 8}};
+   for (const auto &sp : shapes) {
+      const int jp = sp[0], ih = sp[1];
+      int per_sm;
+      if (stencil == 7)
+         per_sm = jp == 2 ? pencil_per_sm<T, 7, 2, 4>()
+                : ih == 4 ? pencil_per_sm<T, 7, 1, 4>()
+                          : pencil_per_sm<T, 7, 1, 8>();
+      else
+         per_sm = jp == 2 ? pencil_per_sm<T, 27, 2, 4>()
+                : ih == 4 ? pencil_per_sm<T, 27, 1, 4>()
+                          : pencil_per_sm<T, 27, 1, 8>();
       const long long wave = (long long) per_sm * sms;
       StageShape a;
       a.rows = jp;
+      a.planes = ih;
       a.vpc = 1;
-      a.threads = 256 / jp;
+      a.threads = 1024 / (jp * ih);
       a.grid = (int) std::max(1LL, std::min<long long>(wave, n_work));
       out.push_back(a);
       if (n_work > wave) {
@@ -613,14 +624,19 @@ int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
    const size_t smem = pencil_smem_bytes<T>();
    const int fused_cs = (sizeof(T) == 4) ? do_cs : 0;
    const int grid = sh.grid;
-#define MAMR_PENCIL(ST, JP)                                                   \
-   pencil_stage_kernel<T, ST, JP><<<grid, Shape<T, JP>::THREADS, smem, s>>>( \
-      src, dst, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc,   \
-      err)
+#define MAMR_PENCIL(ST, JP, IH)                                               \
+   pencil_stage_kernel<T, ST, JP, IH>                                        \
+      <<<grid, Shape<T, JP, IH>::THREADS, smem, s>>>(                         \
+         src, dst, g, chain, pencils, n_pencils, write_ghosts, fused_cs, acc, \
+         err)
    if (stencil == 7) {
-      if (sh.rows == 2) MAMR_PENCIL(7, 2); else MAMR_PENCIL(7, 1);
+      if (sh.rows == 2) MAMR_PENCIL(7, 2, 4);
+      else if (sh.planes == 8) MAMR_PENCIL(7, 1, 8);
+      else MAMR_PENCIL(7, 1, 4);
    } else {
-      if (sh.rows == 2) MAMR_PENCIL(27, 2); else MAMR_PENCIL(27, 1);
+      if (sh.rows == 2) MAMR_PENCIL(27, 2, 4);
+      else if (sh.planes == 8) MAMR_PENCIL(27, 1, 8);
+      else MAMR_PENCIL(27, 1, 4);
    }
 #undef MAMR_PENCIL
    int launches = 1;

@@ -154,7 +154,7 @@ int mamr_get_tuning(const mamr_ctx *c, int32_t *choice,
    if (n_candidates)
       *n_candidates = 0;
    if (shape)
-      for (int q = 0; q < 4; q++)
+      for (int q = 0; q < 5; q++)
          shape[q] = 0;
    return MAMR_OK;
 }
