@@ -64,7 +64,7 @@ typedef struct {
    int32_t nx, ny, nz;   /* x/y/z_block_size: cells per block, even */
    int32_t num_vars;     /* num_vars */
    int32_t max_blocks;   /* max_num_blocks: pool capacity in block slots */
-   int32_t stencil;      /* 7 or 27 (stencil 0 is not run here) */
+   int32_t stencil;      /* 7, 27, or 0 (variable work; FP64, plain path) */
    int32_t code;         /* ghost-exchange variant; only 0 is run here */
    int32_t permute;      /* --permute: direction order cycles with stage */
    int32_t dtype;        /* MAMR_FP64 or MAMR_FP32 */
@@ -152,9 +152,19 @@ int mamr_set_mesh(mamr_ctx *ctx, const mamr_block *blocks, int32_t n);
  * permuted by stage when cfg.permute). */
 int mamr_comm(mamr_ctx *ctx, int32_t start, int32_t num_comm, int32_t stage);
 
-/* stencil_driver(var, calc_stage) -> stencil_calc(var, stencil):
- * ref/stencil.c:43-145. */
+/* stencil_driver(var, calc_stage): ref/stencil.c:43-74.  Stencil 7 or 27:
+ * stencil_calc(var, stencil) (ref/stencil.c:76-145).  Stencil 0: variable
+ * 0 and variables >= 4*mat take stencil_calc(var, 7); the others the
+ * variable-work kernel of calc_stage % 6 (stencil_0, _x, _y, _z, _7, _27;
+ * ref/stencil.c:147-957) followed by stencil_check (ref/stencil.c:959-983),
+ * with the coefficients mamr_set_work_params gave. */
 int mamr_stencil(mamr_ctx *ctx, int32_t var, int32_t calc_stage);
+
+/* The coefficients of the variable-work stencils: the reference's globals
+ * a1 and a0[0 .. num_vars/4) (ref/init.c:418-423).  Required before the
+ * first mamr_stencil of a stencil-0 context; n_a0 must be num_vars/4. */
+int mamr_set_work_params(mamr_ctx *ctx, double a1, const double *a0,
+                         int32_t n_a0);
 
 /* check_sum(var): ref/check_sum.c:36-65.  FP64 pools sum each block's
  * interior serially (k fastest) and the block sums in sorted_list order,
@@ -209,15 +219,22 @@ int mamr_set_tuning(mamr_ctx *ctx, int32_t choice);
 int mamr_get_tuning(const mamr_ctx *ctx, int32_t *choice,
                     int32_t *n_candidates, int32_t *shape);
 
-/* ---- host-side helper (no device work) --------------------------------- */
+/* ---- host-side helpers (no device work) -------------------------------- */
+
+/* The coefficients init() draws for stencil 0 before any cell value
+ * (ref/init.c:418-423): a1, then a0[0 .. num_vars/4), each rand()/RAND_MAX
+ * from the unseeded (seed 1) stream. */
+int mamr_work_coefficients(int32_t num_vars, double *a1, double *a0);
 
 /* The cell values the reference's init() gives its first n_blocks blocks
  * on one rank (ref/init.c:484-495): per block in lattice order, per
  * variable, every cell (ghosts included) zero, then the interior filled
  * with rand()/RAND_MAX in i, j, k order (k fastest), from the C library's
- * unseeded rand() stream (seed 1).  A private random_r state is used, so
- * the caller's rand() state is untouched.  out: [n_blocks][num_vars]
- * [nx+2][ny+2][nz+2] doubles.  Uses cfg's nx, ny, nz and num_vars. */
+ * unseeded rand() stream (seed 1) -- after the 1 + num_vars/4
+ * coefficient draws when cfg->stencil is 0.  A private random_r state is
+ * used, so the caller's rand() state is untouched.  out: [n_blocks]
+ * [num_vars][nx+2][ny+2][nz+2] doubles.  Uses cfg's nx, ny, nz, num_vars
+ * and stencil. */
 int mamr_initial_values(const mamr_config *cfg, int32_t n_blocks,
                         double *out);
 

@@ -100,6 +100,7 @@ class Library:
                                    C.POINTER(i32)],
             "mamr_launch_count": [vp, C.POINTER(C.c_int64)],
             "mamr_set_tuning": [vp, C.c_int32],
+            "mamr_set_work_params": [vp, C.c_double, vp, C.c_int32],
             "mamr_get_tuning": [vp, C.POINTER(C.c_int32),
                                 C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
         }
@@ -111,6 +112,8 @@ class Library:
         L.mamr_last_error.restype = C.c_char_p
         L.mamr_initial_values.argtypes = [C.POINTER(Config), i32, vp]
         L.mamr_initial_values.restype = C.c_int
+        L.mamr_work_coefficients.argtypes = [i32, C.POINTER(C.c_double), vp]
+        L.mamr_work_coefficients.restype = C.c_int
 
     def check(self, status: int, where: str) -> None:
         if status != 0:
@@ -119,6 +122,15 @@ class Library:
 
     def context(self, cfg: Config) -> "Context":
         return Context(self, cfg)
+
+    def work_coefficients(self, num_vars: int):
+        """(a1, a0[num_vars/4]) that init() draws for --stencil 0
+        (mamr_work_coefficients)."""
+        a1 = C.c_double()
+        a0 = np.zeros(max(1, num_vars // 4))
+        self.check(self.lib.mamr_work_coefficients(
+            int(num_vars), C.byref(a1), _ptr(a0)), "mamr_work_coefficients")
+        return a1.value, a0[:num_vars // 4]
 
     def initial_values(self, cfg: Config, n_blocks: int) -> np.ndarray:
         """The reference's init() values for its first n_blocks blocks,
@@ -208,6 +220,12 @@ class Context:
     def consolidate(self, jobs: np.ndarray) -> None:
         jobs = np.ascontiguousarray(jobs, dtype=CONSOLIDATE_DTYPE)
         self._call("mamr_consolidate", _ptr(jobs), len(jobs))
+
+    def set_work_params(self, a1: float, a0) -> None:
+        """--stencil 0 coefficients a1 and a0[num_vars/4]
+        (mamr_set_work_params)."""
+        a0 = np.ascontiguousarray(a0, dtype=np.float64)
+        self._call("mamr_set_work_params", float(a1), _ptr(a0), len(a0))
 
     def run_timesteps(self, num_ts: int, stages_per_ts: int,
                       checksum_freq: int, first_stage: int = 0,

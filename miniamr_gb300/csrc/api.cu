@@ -142,6 +142,9 @@ struct mamr_ctx {
    long long launches;
    int hw_slots;                    // 1 + highest slot ever holding data
    mamr::BatchedState *batched;
+   mamr_work_par work{};            // --stencil 0 coefficients
+   bool work_set = false;
+   DevBuf d_work;                   // --stencil 0 work values
    int tune_force = -1;             // forced launch-shape candidate
    int tune_last = -1, tune_n = 0;  // last batched run's choice / count
    mamr::StageShape tune_shape;
@@ -176,8 +179,14 @@ extern "C" int mamr_create(const mamr_config *cfg, mamr_ctx **out)
    if (cfg->num_vars < 1 || cfg->num_vars > 65535 || cfg->max_blocks < 1)
       return fail(MAMR_EINVAL, "num_vars must be in 1..65535 and "
                   "max_blocks >= 1");
-   if (cfg->stencil != 7 && cfg->stencil != 27)
+   if (cfg->stencil != 0 && cfg->stencil != 7 && cfg->stencil != 27)
       return fail(MAMR_EUNSUP, "stencil %d not supported", cfg->stencil);
+   if (cfg->stencil == 0 && cfg->dtype != MAMR_FP64)
+      return fail(MAMR_EUNSUP, "stencil 0 runs on FP64 pools only");
+   if (cfg->stencil == 0 &&
+       (cfg->num_vars < 8 || cfg->num_vars / 4 > MAMR_WORK_MAX_MAT))
+      return fail(MAMR_EINVAL, "stencil 0 needs 8 <= num_vars <= %d",
+                  4 * MAMR_WORK_MAX_MAT + 3);
    if (cfg->code != 0)
       return fail(MAMR_EUNSUP, "code %d not supported", cfg->code);
    if (cfg->dtype != MAMR_FP64 && cfg->dtype != MAMR_FP32)
@@ -252,7 +261,7 @@ extern "C" int mamr_destroy(mamr_ctx *c)
    for (auto &b : c->d_tasks) b.release();
    c->d_slots.release(); c->d_partials.release(); c->d_jobs.release();
    c->d_stage.release(); c->d_stage_slots.release(); c->d_sums.release();
-   c->d_xfer.release(); c->d_xfer_slots.release();
+   c->d_xfer.release(); c->d_xfer_slots.release(); c->d_work.release();
    if (c->d_acc) cudaFree(c->d_acc);
    if (c->d_sum) cudaFree(c->d_sum);
    if (c->d_err) cudaFree(c->d_err);
@@ -513,9 +522,31 @@ extern "C" int mamr_comm(mamr_ctx *c, int32_t start, int32_t num,
    return comm_impl(c, start, num, stage);
 }
 
-static int stencil_impl(mamr_ctx *c, int32_t var, bool per_block = false)
+static int stencil_impl(mamr_ctx *c, int32_t var, int32_t calc_stage,
+                        bool per_block = false)
 {
    const int n = (int) c->mesh.size();
+   if (c->cfg.stencil == 0) {
+      // stencil_driver (ref/stencil.c:43-74): var 0 and var >= 4*mat take
+      // the 7-point stencil, the others the variable-work kernels
+      const int mat = c->cfg.num_vars / 4;
+      if (var != 0 && var < 4 * mat) {
+         if (!c->work_set)
+            return fail(MAMR_EINVAL, "stencil 0 needs mamr_set_work_params "
+                        "before the first stencil");
+         CUDA_TRY(c->d_work.ensure(sizeof(double) * std::max(1, n) *
+                                   c->cfg.nx * c->cfg.ny * c->cfg.nz));
+         LAUNCH_TRY(c, launch_work_stencil(
+                          (double *) c->pool, c->g,
+                          (const int32_t *) c->d_slots.p, n, var, calc_stage,
+                          c->work, (double *) c->d_work.p, c->stream));
+         return MAMR_OK;
+      }
+      LAUNCH_TRY(c, launch_stencil((double *) c->pool, c->g, 7,
+                                   (const int32_t *) c->d_slots.p, n, var,
+                                   c->stream));
+      return MAMR_OK;
+   }
    if (per_block) {
       for (int b = 0; b < n; b++) {
          const int32_t *one = (const int32_t *) c->d_slots.p + b;
@@ -543,12 +574,31 @@ static int stencil_impl(mamr_ctx *c, int32_t var, bool per_block = false)
 
 extern "C" int mamr_stencil(mamr_ctx *c, int32_t var, int32_t calc_stage)
 {
-   (void) calc_stage;
    if (!c)
       return fail(MAMR_EINVAL, "null context");
    if (var < 0 || var >= c->cfg.num_vars)
       return fail(MAMR_EINVAL, "variable %d out of range", var);
-   return stencil_impl(c, var);
+   if (calc_stage < 0)
+      return fail(MAMR_EINVAL, "negative calc_stage");
+   return stencil_impl(c, var, calc_stage);
+}
+
+extern "C" int mamr_set_work_params(mamr_ctx *c, double a1, const double *a0,
+                                    int32_t n_a0)
+{
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   if (c->cfg.stencil != 0)
+      return fail(MAMR_EINVAL, "work parameters belong to stencil 0");
+   if (!a0 || n_a0 != c->cfg.num_vars / 4)
+      return fail(MAMR_EINVAL, "a0 must hold num_vars/4 = %d values",
+                  c->cfg.num_vars / 4);
+   c->work.mat = n_a0;
+   c->work.a1 = a1;
+   for (int q = 0; q < n_a0; q++)
+      c->work.a0[q] = a0[q];
+   c->work_set = true;
+   return MAMR_OK;
 }
 
 // Converts a 128-bit fixed-point accumulator (units of 2^-52) to double
@@ -760,7 +810,7 @@ static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
          if ((r = comm_impl(c, 0, V, gstage)))
             return r;
          for (int var = 0; var < V; var++) {
-            if ((r = stencil_impl(c, var, per_block)))
+            if ((r = stencil_impl(c, var, gstage, per_block)))
                return r;
             if (do_cs) {
                size_t idx = (size_t) cnt * V + var;
@@ -1032,6 +1082,9 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    BatchedState *B = c->batched;
    if (!B->valid && (r = build_items(c)))
       return r;
+   if (c->cfg.stencil == 0)
+      return fail(MAMR_EUNSUP, "the batched path runs stencils 7 and 27; "
+                  "stencil 0 runs on the plain path");
    if (c->cfg.stencil == 27 && !B->single_level)
       return fail(MAMR_EUNSUP, "batched 27-point stencil needs a "
                   "single-level mesh (edge/corner ghosts at level jumps "

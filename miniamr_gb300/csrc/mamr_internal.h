@@ -7,6 +7,7 @@
 #include <cstddef>
 
 #include "miniamr_gb300.h"
+#include "work_formulas.h"
 
 namespace mamr {
 
@@ -69,6 +70,14 @@ enum : unsigned {
    ERR_FIXED_RANGE = 1u,   // a cell outside the fixed-point checksum range
    ERR_TASK = 2u           // a task that does not fit the geometry
 };
+
+// --stencil 0: the variable-work kernel of calc_stage % 6 and
+// stencil_check for one variable (1 <= var < 4*mat), FP64 pools; scratch
+// holds nb * nx*ny*nz doubles.
+int launch_work_stencil(double *pool, const Geom &g, const int32_t *slots,
+                        int nb, int var, int calc_stage,
+                        const mamr_work_par &P, double *scratch,
+                        cudaStream_t s);
 
 // Records a failure for mamr_last_error() and returns code.
 int report_error(int code, const char *fmt, ...);

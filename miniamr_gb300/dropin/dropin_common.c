@@ -58,6 +58,10 @@ mamr_ctx *mamr_dropin_ctx(void)
          exit(-1);
       }
       mamr_dropin_check(mamr_create(&cfg, &ctx), "mamr_create");
+      /* --stencil 0: the coefficients init() drew (ref/init.c:418-423) */
+      if (stencil == 0)
+         mamr_dropin_check(mamr_set_work_params(ctx, a1, a0, mat),
+                           "mamr_set_work_params");
    }
    return ctx;
 }

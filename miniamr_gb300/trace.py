@@ -25,7 +25,7 @@ from .abi import (BLOCK_DTYPE, CONSOLIDATE_DTYPE, SPLIT_DTYPE, Config,
                   Context, Library)
 
 OP_CREATE, OP_UPLOAD, OP_SET_MESH, OP_COMM, OP_STENCIL, OP_CHECK_SUM, \
-    OP_SPLIT, OP_CONSOLIDATE = range(1, 9)
+    OP_SPLIT, OP_CONSOLIDATE, OP_WORK_PARAMS = range(1, 10)
 
 
 @dataclass
@@ -81,6 +81,11 @@ def read_trace(path: str) -> list[Record]:
             (m,) = struct.unpack_from("<i", p, 0)
             out.append(Record(op, (np.frombuffer(p, CONSOLIDATE_DTYPE, m,
                                                  4).copy(),)))
+        elif op == OP_WORK_PARAMS:
+            (m,) = struct.unpack_from("<i", p, 0)
+            (a1,) = struct.unpack_from("<d", p, 8)
+            a0 = np.frombuffer(p, "<f8", m, 16).copy()
+            out.append(Record(op, (a1, a0)))
         else:
             raise ValueError(f"{path}: unknown op {op}")
     return out
@@ -181,6 +186,8 @@ def replay(lib: Library, records: list[Record], dtype: int | None = None,
             ctx.split(r.args[0])
         elif r.op == OP_CONSOLIDATE:
             ctx.consolidate(r.args[0])
+        elif r.op == OP_WORK_PARAMS:
+            ctx.set_work_params(*r.args)
     return ReplayResult(sums, hashes, ctx, mesh, numbers)
 
 
@@ -252,6 +259,8 @@ def replay_batched(lib: Library, records: list[Record], flags: int,
                 ctx.split(r.args[0])
             else:
                 ctx.consolidate(r.args[0])
+        elif r.op == OP_WORK_PARAMS:
+            ctx.set_work_params(*r.args)
         elif r.op == OP_COMM:
             if r.args[0] != 0 or r.args[1] != rec_vars:
                 raise ValueError("batched replay needs comm over all vars")

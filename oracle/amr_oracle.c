@@ -25,6 +25,7 @@
 #include <string.h>
 
 #include "miniamr_gb300.h"
+#include "work_formulas.h"
 
 struct mamr_ctx {
    mamr_config cfg;
@@ -36,6 +37,8 @@ struct mamr_ctx {
    int32_t n_mesh;
    int32_t *slot_pos;      /* slot -> position in mesh, -1 if inactive */
    int64_t launches;       /* stays 0: the oracle launches nothing */
+   mamr_work_par work;     /* --stencil 0 coefficients */
+   int work_set;
 };
 
 static __thread char err_buf[256];
@@ -64,6 +67,20 @@ static inline double *blk(const mamr_ctx *c, int slot, int var)
 
 #define AT(p, i, j, k) (p)[((size_t) (i) * c->Y + (j)) * c->Z + (k)]
 
+/* Per-cell formulas of the variable-work stencils (--stencil 0), shared
+ * with the GB300 kernels; this file supplies the dense-layout accessor
+ * and the loops (ref/stencil.c:147-983). */
+typedef struct {
+   const struct mamr_ctx *c;
+   int slot;
+} oracle_wview;
+#define MAMR_WFN static inline
+#define MAMR_WVIEW oracle_wview
+#define MAMR_AT(w, v, i, j, k) \
+   (((w)->c->pool + ((size_t) (w)->slot * (w)->c->cfg.num_vars + (v)) * \
+     (w)->c->bv)[((size_t) (i) * (w)->c->Y + (j)) * (w)->c->Z + (k)])
+#include "work_formulas.h"
+
 int mamr_create(const mamr_config *cfg, mamr_ctx **out)
 {
    mamr_ctx *c;
@@ -75,8 +92,14 @@ int mamr_create(const mamr_config *cfg, mamr_ctx **out)
       return fail(MAMR_EINVAL, "block sizes must be even and >= 2");
    if (cfg->num_vars < 1 || cfg->max_blocks < 1)
       return fail(MAMR_EINVAL, "num_vars and max_blocks must be >= 1");
-   if (cfg->stencil != 7 && cfg->stencil != 27)
+   if (cfg->stencil != 0 && cfg->stencil != 7 && cfg->stencil != 27)
       return fail(MAMR_EUNSUP, "stencil %d not supported", cfg->stencil);
+   if (cfg->stencil == 0 && cfg->dtype != MAMR_FP64)
+      return fail(MAMR_EUNSUP, "stencil 0 runs on FP64 pools only");
+   if (cfg->stencil == 0 &&
+       (cfg->num_vars < 8 || cfg->num_vars / 4 > MAMR_WORK_MAX_MAT))
+      return fail(MAMR_EINVAL, "stencil 0 needs 8 <= num_vars <= %d",
+                  4 * MAMR_WORK_MAX_MAT + 3);
    if (cfg->code != 0)
       return fail(MAMR_EUNSUP, "code %d not supported", cfg->code);
    if (cfg->dtype != MAMR_FP64 && cfg->dtype != MAMR_FP32)
@@ -453,14 +476,14 @@ int mamr_comm(mamr_ctx *c, int32_t start, int32_t num, int32_t stage)
 
 /* ref/stencil.c:76-145 (stencil_calc), Jacobi update of every active
  * block's interior for one variable. */
-static void stencil_block(mamr_ctx *c, double *a, double *work)
+static void stencil_block(mamr_ctx *c, int st, double *a, double *work)
 {
    int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz, i, j, k;
    for (i = 1; i <= nx; i++)
       for (j = 1; j <= ny; j++)
          for (k = 1; k <= nz; k++) {
             double w;
-            if (c->cfg.stencil == 7) {
+            if (st == 7) {
                w = RF(c, AT(a, i - 1, j, k) + AT(a, i, j - 1, k));
                w = RF(c, w + AT(a, i, j, k - 1));
                w = RF(c, w + AT(a, i, j, k));
@@ -497,14 +520,88 @@ static void stencil_block(mamr_ctx *c, double *a, double *work)
 /* ref/stencil.c:76-145 (stencil_calc), Jacobi update of every active
  * block's interior for one variable; blocks are independent (threaded over
  * blocks as in openmp/stencil.c:84,107). */
+/* The variable-work branch of stencil_driver (ref/stencil.c:51-71) for
+ * one block: the kernel of calc_stage % 6 in the reference's loop order,
+ * then stencil_check. */
+static void work_block(mamr_ctx *c, int slot, int var, int calc_stage,
+                       double *work)
+{
+   int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz, i, j, k;
+   oracle_wview w;
+   double *a = blk(c, slot, var);
+   w.c = c;
+   w.slot = slot;
+   switch (calc_stage % 6) {
+   case 0:
+      for (i = 1; i <= nx; i++)
+         for (j = 1; j <= ny; j++)
+            for (k = 1; k <= nz; k++)
+               AT(a, i, j, k) = mamr_w_stencil0(&w, var, i, j, k, &c->work);
+      break;
+   case 1:
+   case 2:
+   case 3:
+      /* stencil_x/y/z update in place as the i, j, k loops advance */
+      for (i = 1; i <= nx; i++)
+         for (j = 1; j <= ny; j++)
+            for (k = 1; k <= nz; k++)
+               AT(a, i, j, k) = mamr_w_line(&w, var, calc_stage % 6 - 1, i,
+                                            j, k, &c->work);
+      break;
+   default:
+      for (i = 1; i <= nx; i++)
+         for (j = 1; j <= ny; j++)
+            for (k = 1; k <= nz; k++)
+               AT(work, i, j, k) =
+                  calc_stage % 6 == 4
+                     ? mamr_w_seven(&w, var, i, j, k, &c->work)
+                     : mamr_w_twentyseven(&w, var, i, j, k, &c->work);
+      for (i = 1; i <= nx; i++)
+         for (j = 1; j <= ny; j++)
+            for (k = 1; k <= nz; k++)
+               AT(a, i, j, k) = AT(work, i, j, k);
+      break;
+   }
+   for (i = 1; i <= nx; i++)
+      for (j = 1; j <= ny; j++)
+         for (k = 1; k <= nz; k++)
+            AT(a, i, j, k) = mamr_w_check(AT(a, i, j, k), &c->work);
+}
+
+int mamr_set_work_params(mamr_ctx *c, double a1, const double *a0,
+                         int32_t n_a0)
+{
+   int q;
+   if (!c)
+      return fail(MAMR_EINVAL, "null context");
+   if (c->cfg.stencil != 0)
+      return fail(MAMR_EINVAL, "work parameters belong to stencil 0");
+   if (!a0 || n_a0 != c->cfg.num_vars / 4)
+      return fail(MAMR_EINVAL, "a0 must hold num_vars/4 = %d values",
+                  c->cfg.num_vars / 4);
+   c->work.mat = n_a0;
+   c->work.a1 = a1;
+   for (q = 0; q < n_a0; q++)
+      c->work.a0[q] = a0[q];
+   c->work_set = 1;
+   return MAMR_OK;
+}
+
 int mamr_stencil(mamr_ctx *c, int32_t var, int32_t calc_stage)
 {
-   int bad = 0;
-   (void) calc_stage;
+   int bad = 0, st, varwork;
    if (!c)
       return fail(MAMR_EINVAL, "null context");
    if (var < 0 || var >= c->cfg.num_vars)
       return fail(MAMR_EINVAL, "variable out of range");
+   if (calc_stage < 0)
+      return fail(MAMR_EINVAL, "negative calc_stage");
+   /* stencil_driver (ref/stencil.c:43-74) */
+   st = c->cfg.stencil ? c->cfg.stencil : 7;
+   varwork = c->cfg.stencil == 0 && var != 0 && var < 4 * (c->cfg.num_vars / 4);
+   if (varwork && !c->work_set)
+      return fail(MAMR_EINVAL, "stencil 0 needs mamr_set_work_params before "
+                  "the first stencil");
 #pragma omp parallel reduction(|:bad)
    {
       double *work = (double *) malloc(sizeof(double) * c->bv);
@@ -513,8 +610,12 @@ int mamr_stencil(mamr_ctx *c, int32_t var, int32_t calc_stage)
          bad = 1;
 #pragma omp for schedule(dynamic, 4)
       for (in = 0; in < c->n_mesh; in++)
-         if (work)
-            stencil_block(c, blk(c, c->mesh[in].slot, var), work);
+         if (work) {
+            if (varwork)
+               work_block(c, c->mesh[in].slot, var, calc_stage, work);
+            else
+               stencil_block(c, st, blk(c, c->mesh[in].slot, var), work);
+         }
       free(work);
    }
    if (bad)
@@ -758,6 +859,12 @@ int mamr_initial_values(const mamr_config *cfg, int32_t n_blocks, double *out)
       return fail(MAMR_EINVAL, "initstate_r failed");
    X = cfg->nx + 2; Y = cfg->ny + 2; Z = cfg->nz + 2;
    bv = (size_t) X * Y * Z;
+   /* stencil 0: init() draws a1 and a0[] first (ref/init.c:418-423) */
+   if (cfg->stencil == 0)
+      for (i = 0; i < 1 + cfg->num_vars / 4; i++) {
+         int32_t r;
+         random_r(&rd, &r);
+      }
    for (b = 0; b < n_blocks; b++)
       for (v = 0; v < cfg->num_vars; v++) {
          double *a = out + ((size_t) b * cfg->num_vars + v) * bv;
@@ -771,5 +878,28 @@ int mamr_initial_values(const mamr_config *cfg, int32_t n_blocks, double *out)
                      ((double) r) / ((double) RAND_MAX);
                }
       }
+   return MAMR_OK;
+}
+
+/* ref/init.c:418-423: a1, then a0[0 .. num_vars/4), from the seed-1 rand()
+ * stream before any cell value. */
+int mamr_work_coefficients(int32_t num_vars, double *a1, double *a0)
+{
+   char state[128];
+   struct random_data rd;
+   int32_t r;
+   int i;
+   if (num_vars < 1 || !a1 || (num_vars >= 4 && !a0))
+      return fail(MAMR_EINVAL, "bad coefficient arguments");
+   memset(&rd, 0, sizeof(rd));
+   memset(state, 0, sizeof(state));
+   if (initstate_r(1u, state, sizeof(state), &rd))
+      return fail(MAMR_EINVAL, "initstate_r failed");
+   random_r(&rd, &r);
+   *a1 = ((double) r) / ((double) RAND_MAX);
+   for (i = 0; i < num_vars / 4; i++) {
+      random_r(&rd, &r);
+      a0[i] = ((double) r) / ((double) RAND_MAX);
+   }
    return MAMR_OK;
 }

@@ -20,6 +20,7 @@
  *   6 check_sum   int32 var, int32 pad, double result
  *   7 split       int32 n, mamr_split_job[n]
  *   8 consolidate int32 n, mamr_consolidate_job[n]
+ *   9 work params int32 n, int32 pad, double a1, double a0[n]
  * Little-endian, as written by the host.
  */
 #include <stdint.h>
@@ -41,6 +42,8 @@ int __real_mamr_check_sum(mamr_ctx *ctx, int32_t var, double *sum);
 int __real_mamr_split(mamr_ctx *ctx, const mamr_split_job *j, int32_t n);
 int __real_mamr_consolidate(mamr_ctx *ctx, const mamr_consolidate_job *j,
                             int32_t n);
+int __real_mamr_set_work_params(mamr_ctx *ctx, double a1, const double *a0,
+                                int32_t n);
 
 static FILE *fp;
 static int opened;
@@ -117,6 +120,14 @@ int __wrap_mamr_comm(mamr_ctx *ctx, int32_t start, int32_t num, int32_t stage)
    int32_t a[3] = { start, num, stage };
    rec(4, a, sizeof(a), NULL, 0, NULL, 0);
    return __real_mamr_comm(ctx, start, num, stage);
+}
+
+int __wrap_mamr_set_work_params(mamr_ctx *ctx, double a1, const double *a0,
+                                int32_t n)
+{
+   int32_t h[2] = { n, 0 };
+   rec(9, h, sizeof(h), &a1, sizeof(double), a0, sizeof(double) * n);
+   return __real_mamr_set_work_params(ctx, a1, a0, n);
 }
 
 int __wrap_mamr_stencil(mamr_ctx *ctx, int32_t var, int32_t stage)

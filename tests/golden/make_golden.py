@@ -96,6 +96,16 @@ CASES = {
                 "0.004", "0.12", "0.03", "0.03", "0", "0", "0",
                 "--object", "0", "1", "0.3", "0.7", "0.7", "0.007", "-0.005",
                 "-0.009", "0.06", "0.06", "0.06", "0", "0", "0"],
+    # the variable-work stencils (--stencil 0): 8 variables (mat = 2), six
+    # stages per timestep so that every kernel (calc_stage % 6) runs on
+    # every variable class, refinement and coarsening around a moving
+    # sphere, checksums every stage
+    "stencil0": ["--init_x", "2", "--init_y", "2", "--init_z", "2", "--nx",
+                 "8", "--ny", "8", "--nz", "8", "--num_vars", "8",
+                 "--stencil", "0", "--num_refine", "3", "--refine_freq",
+                 "2", "--num_tsteps", "8", "--stages_per_ts", "6",
+                 "--checksum_freq", "1", "--error_tol", "0",
+                 "--max_blocks", "4000"] + SPHERE,
     # two objects, volume + surface refinement, 7-point, 4 levels, default
     # checksum cadence (every 5th stage of 3)
     "amr7_objects": ["--init_x", "2", "--init_y", "2", "--init_z", "2",

@@ -10,6 +10,10 @@ from miniamr_gb300.trace import read_trace, replay
 
 pytestmark = pytest.mark.gpu
 CASES = sorted(cases())
+# the variable-work stencils (--stencil 0) run on FP64 pools only
+FP32_CASES = [c for c in CASES if "--stencil" not in cases()[c]["args"] or
+              cases()[c]["args"][cases()[c]["args"].index("--stencil") + 1]
+              != "0"]
 
 
 def bits(a):
@@ -34,7 +38,7 @@ def test_trace_fp64_bit_exact_vs_reference(gpu_lib, name):
     res.ctx.close()
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", FP32_CASES)
 def test_trace_fp32_vs_oracle_and_reference(gpu_lib, oracle_lib, name):
     """FP32 pools: bit-identical to the FP32 oracle (same operation order,
     correctly rounded FP32 division, exact fixed-point checksum) and within
@@ -149,3 +153,21 @@ def test_division_selftest(gpu_lib):
     out = (C.c_int64 * 4)()
     assert f(1 << 26, out) == 0
     assert list(out) == [0, 0, 0, 0]
+
+
+def test_stencil0_fp32_and_batched_are_refused(gpu_lib):
+    """--stencil 0 runs on FP64 pools through the plain path only."""
+    with pytest.raises(MamrError) as e:
+        gpu_lib.context(Config.make(8, 8, 8, 8, 16, stencil=0, dtype=FP32))
+    assert e.value.status == -5
+    from miniamr_gb300.abi import RUN_BATCHED
+    cfg = Config.make(8, 8, 8, 8, 16, stencil=0)
+    with gpu_lib.context(cfg) as ctx:
+        m = meshmod.initial_mesh(2, 1, 1, 0, 16)
+        ctx.upload(np.arange(2), gpu_lib.initial_values(cfg, 2))
+        ctx.set_mesh(m.blocks())
+        ctx.set_work_params(*gpu_lib.work_coefficients(8))
+        with pytest.raises(MamrError) as e:
+            ctx.run_timesteps(1, 1, 1, flags=RUN_BATCHED)
+        assert e.value.status == -5
+        ctx.run_timesteps(1, 6, 1)           # the plain path runs

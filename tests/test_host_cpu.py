@@ -44,8 +44,14 @@ def test_oracle_rejects_bad_arguments(oracle_lib):
     with pytest.raises(MamrError) as e:
         oracle_lib.context(Config.make(7, 8, 8, 2, 4))     # odd block size
     assert e.value.status == -1
-    with pytest.raises(MamrError) as e:
+    with pytest.raises(MamrError) as e:                    # needs 8 vars
         oracle_lib.context(Config.make(8, 8, 8, 2, 4, stencil=0))
+    assert e.value.status == -1
+    with pytest.raises(MamrError) as e:                    # FP64 only
+        oracle_lib.context(Config.make(8, 8, 8, 8, 4, stencil=0, dtype=1))
+    assert e.value.status == -5
+    with pytest.raises(MamrError) as e:
+        oracle_lib.context(Config.make(8, 8, 8, 8, 4, stencil=5))
     assert e.value.status == -5
     with oracle_lib.context(Config.make(8, 8, 8, 2, 4)) as ctx:
         with pytest.raises(MamrError):
@@ -114,3 +120,14 @@ def test_dropin_matches_reference_on_fresh_case(tmp_path):
         logs.append(log.read_text())
     assert len(logs[0]) > 0 and logs[0] == logs[1]
     assert "mesh" in logs[0]
+
+
+def test_work_coefficients_match_reference_init(oracle_lib):
+    """--stencil 0: a1 and a0[] as the reference's init() drew them
+    (recorded by the hybrid run that pins the stencil-0 golden case)."""
+    from golden_util import trace_path
+    from miniamr_gb300.trace import OP_WORK_PARAMS, read_trace
+    recs = read_trace(trace_path("stencil0"))
+    a1, a0 = next(r.args for r in recs if r.op == OP_WORK_PARAMS)
+    got1, got0 = oracle_lib.work_coefficients(8)
+    assert got1 == a1 and np.array_equal(got0, a0)
