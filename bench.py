@@ -231,6 +231,38 @@ def one_thread_oracle_rate():
         return None
 
 
+def uniform_stencil0(lib):
+    """The variable-work stencils (--stencil 0) on the uniform 4096-block
+    mesh, 40 FP64 vars: one cycle of six stages (stencil_0, _x, _y, _z,
+    _7, _27, each followed by stencil_check; variable 0 takes the 7-point
+    stencil), checksums every 5th stage, through the plain path; beside it
+    the CPU oracle (OpenMP) on the 512-block sample of the same setup."""
+    import torch
+    from miniamr_gb300 import build
+    from miniamr_gb300.abi import FP64, Library
+    out = {}
+    for name, L, init, cap in (
+            ("gpu", lib, INIT, CAP),
+            ("cpu_oracle", Library(build.build_oracle()), SAMPLE_INIT,
+             SAMPLE_INIT[0] * SAMPLE_INIT[1] * SAMPLE_INIT[2] * 9 + 8)):
+        ctx, _ = build_mesh(L, FP64, init=init, cap=cap, stencil=0)
+        ctx.set_work_params(*L.work_coefficients(V))
+        ctx.run_timesteps(1, 6, 5)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.run_timesteps(1, 6, 5, first_stage=6)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        ctx.close()
+        n = init[0] * init[1] * init[2] * 8
+        out[name] = 6 * n * N ** 3 * V / dt
+    out["cpu_threads"] = os.cpu_count()
+    out["speedup"] = out["gpu"] / out["cpu_oracle"]
+    out["workload"] = ("4096 blocks of 16^3 (CPU: 512), 40 FP64 vars, "
+                       "--stencil 0, six stages")
+    return out
+
+
 def uniform_fp64_7pt(lib, steps):
     """The uniform 4096-block mesh with 40 FP64 variables and the 7-point
     stencil, 4 stages per timestep: the batched path (fused ghost+stencil,
@@ -541,6 +573,7 @@ def main():
         line["configs"] = {
             "uniform_fp64_7pt": uniform_fp64_7pt(lib, 2),
             "amr_sphere_27pt_plain_fp64": amr_plain_fp64(lib),
+            "uniform_stencil0_fp64": uniform_stencil0(lib),
             "stress_multilevel_7pt_fp32": stress_multilevel(lib, FP32),
             "stress_multilevel_7pt_fp64": stress_multilevel(lib, FP64),
         }
