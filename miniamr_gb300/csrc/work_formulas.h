@@ -4,8 +4,11 @@
  *
  * Plain C shared by the GB300 kernels (miniamr_gb300/csrc/work_kernels.cu)
  * and the CPU oracle (oracle/amr_oracle.c).  Each includer first defines
- *   MAMR_WFN               the function qualifiers (static inline, or
- *                          static __device__ __forceinline__)
+ *   MAMR_WFN               the qualifiers of the functions that take a view
+ *                          (static inline, or a template over the view
+ *                          type with __device__)
+ *   MAMR_WFN0              optional, those of the one that does not
+ *                          (defaults to MAMR_WFN)
  *   MAMR_WVIEW             the type of a block view
  *   MAMR_AT(w, v, i, j, k) the value of variable v at cell (i, j, k)
  * and owns the loops and the stores: these functions only evaluate one
@@ -31,6 +34,9 @@ typedef struct {
 #define MAMR_WORK_FNS_DONE
 
 #define MAMR_A(v, i, j, k) MAMR_AT(w, (v), (i), (j), (k))
+#ifndef MAMR_WFN0
+#define MAMR_WFN0 MAMR_WFN
+#endif
 
 /* stencil_0 (ref/stencil.c:147-226): the new value of cell (i, j, k) of
  * var; reads only that cell's variables. */
@@ -187,7 +193,7 @@ MAMR_WFN double mamr_w_twentyseven(const MAMR_WVIEW *w, int var, int i,
 }
 
 /* stencil_check (ref/stencil.c:959-983) on one value. */
-MAMR_WFN double mamr_w_check(double x, const mamr_work_par *P)
+MAMR_WFN0 double mamr_w_check(double x, const mamr_work_par *P)
 {
    x = fabs(x);
    if (x >= 1.0)
