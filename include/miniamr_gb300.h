@@ -65,7 +65,9 @@ typedef struct {
    int32_t num_vars;     /* num_vars */
    int32_t max_blocks;   /* max_num_blocks: pool capacity in block slots */
    int32_t stencil;      /* 7, 27, or 0 (variable work; FP64, plain path) */
-   int32_t code;         /* ghost-exchange variant; only 0 is run here */
+   int32_t code;         /* ghost-exchange variant 0, 1 or 2 (1 and 2, which
+                            differ only in how ranks pack messages, are one
+                            exchange on one rank; plain path) */
    int32_t permute;      /* --permute: direction order cycles with stage */
    int32_t dtype;        /* MAMR_FP64 or MAMR_FP32 */
    int32_t reserved[7];  /* must be zero */
@@ -147,7 +149,8 @@ int mamr_set_mesh(mamr_ctx *ctx, const mamr_block *blocks, int32_t n);
 
 /* comm(start, num_comm, stage): ref/comm.c:42-242 on one rank --
  * on_proc_comm (ref/comm.c:1465-1580), on_proc_comm_diff
- * (ref/comm.c:1585-1908) and apply_bc (ref/comm.c:1911-1965) for
+ * (ref/comm.c:1585-1908; code 1/2: whole ghost planes, level-jump edges
+ * included) and apply_bc (ref/comm.c:1911-1965) for
  * variables [start, start+num_comm), directions x, y, z in order (or
  * permuted by stage when cfg.permute). */
 int mamr_comm(mamr_ctx *ctx, int32_t start, int32_t num_comm, int32_t stage);

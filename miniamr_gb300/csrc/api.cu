@@ -187,7 +187,7 @@ extern "C" int mamr_create(const mamr_config *cfg, mamr_ctx **out)
        (cfg->num_vars < 8 || cfg->num_vars / 4 > MAMR_WORK_MAX_MAT))
       return fail(MAMR_EINVAL, "stencil 0 needs 8 <= num_vars <= %d",
                   4 * MAMR_WORK_MAX_MAT + 3);
-   if (cfg->code != 0)
+   if (cfg->code < 0 || cfg->code > 2)
       return fail(MAMR_EUNSUP, "code %d not supported", cfg->code);
    if (cfg->dtype != MAMR_FP64 && cfg->dtype != MAMR_FP32)
       return fail(MAMR_EINVAL, "bad dtype");
@@ -501,12 +501,12 @@ static int comm_impl(mamr_ctx *c, int32_t start, int32_t num, int32_t stage)
       int dir = c->cfg.permute ? kPerm[((stage % 6) + 6) % 6][o] : o;
       if (c->fp32)
          LAUNCH_TRY(c, launch_comm_dir((float *) c->pool, c->g, dir,
-                                       c->cfg.stencil, c->tasks[dir], start,
-                                       num, c->stream));
+                                       c->cfg.stencil, c->cfg.code,
+                                       c->tasks[dir], start, num, c->stream));
       else
          LAUNCH_TRY(c, launch_comm_dir((double *) c->pool, c->g, dir,
-                                       c->cfg.stencil, c->tasks[dir], start,
-                                       num, c->stream));
+                                       c->cfg.stencil, c->cfg.code,
+                                       c->tasks[dir], start, num, c->stream));
    }
    return MAMR_OK;
 }
@@ -1085,6 +1085,9 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    if (c->cfg.stencil == 0)
       return fail(MAMR_EUNSUP, "the batched path runs stencils 7 and 27; "
                   "stencil 0 runs on the plain path");
+   if (c->cfg.code != 0)
+      return fail(MAMR_EUNSUP, "the batched path gathers code-0 ghosts; "
+                  "code %d runs on the plain path", c->cfg.code);
    if (c->cfg.stencil == 27 && !B->single_level)
       return fail(MAMR_EUNSUP, "batched 27-point stencil needs a "
                   "single-level mesh (edge/corner ghosts at level jumps "

@@ -85,7 +85,7 @@ int report_error(int code, const char *fmt, ...);
 // Kernel launchers (plain path).  All return the launch count they issued
 // (>= 0) or -1 after a launch error (cudaGetLastError is left set).
 template <typename T>
-int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil,
+int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil, int code,
                     const DirTasks &t, int var0, int nvar, cudaStream_t s);
 template <typename T>
 int launch_stencil(T *pool, const Geom &g, int stencil, const int32_t *slots,

@@ -25,7 +25,7 @@ __device__ __forceinline__ long long face_cell(const Geom &g, int dir, int nc,
 template <typename T>
 __global__ void __launch_bounds__(128)
 comm_dir_kernel(T *__restrict__ pool, Geom g, int dir, int stencil,
-                DirTasks t, int var0)
+                int code, DirTasks t, int var0)
 {
    int task = blockIdx.x, var = var0 + blockIdx.y;
    const int n = dir == 0 ? g.nx : (dir == 1 ? g.ny : g.nz);
@@ -38,7 +38,10 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int dir, int stencil,
       T *lo = pool + bv_offset(g, st.lo, var);
       T *hi = pool + bv_offset(g, st.hi, var);
       int a0 = 1, a1 = na, b0 = 1, b1 = nb;
-      if (stencil != 7) {
+      if (code) {
+         // code 1/2 (ref/comm.c:1535-1579): whole planes
+         a0 = 0; a1 = na + 1; b0 = 0; b1 = nb + 1;
+      } else if (stencil != 7) {
          if (dir >= 1) { a0 = 0; a1 = na + 1; }
          if (dir == 2) { b0 = 0; b1 = nb + 1; }
       }
@@ -61,6 +64,46 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int dir, int stencil,
       const int f2 = low ? n + 1 : 0, f3 = low ? n : 1;
       const int ha = na / 2, hb = nb / 2;
       const int oa = dt.jq * ha, ob = dt.iq * hb;
+      if (code) {
+         // code 1/2 (ref/comm.c:1689-1907), the reference's three
+         // direction branches in one form: the fine ghost plane whole,
+         // tangential index A reading coarse offset + (A=0: 0, A=na+1:
+         // na/2+1, else (A+1)/2); the coarse ghost plane the quarter's 2x2
+         // sums plus the fine ghost row / column pair sums on the jq / iq
+         // sides and one corner.  Thread (p, q) of (ha+1) x (hb+1) writes
+         // coarse cell (p ? p+oa : edge row, q ? q+ob : edge column).
+         const int cnt = (na + 2) * (nb + 2);
+         for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+            const int A = e / (nb + 2), B = e % (nb + 2);
+            const int ca = A == 0 ? oa
+                         : (A == na + 1 ? ha + 1 + oa : (A + 1) / 2 + oa);
+            const int cb = B == 0 ? ob
+                         : (B == nb + 1 ? hb + 1 + ob : (B + 1) / 2 + ob);
+            F[face_cell(g, dir, f2, A, B)] =
+               quarter(C[face_cell(g, dir, c1, ca, cb)]);
+         }
+         const int ae = dt.jq ? na + 1 : 0, be = dt.iq ? nb + 1 : 0;
+         for (int e = threadIdx.x; e < (ha + 1) * (hb + 1); e += blockDim.x) {
+            const int p = e / (hb + 1), q = e % (hb + 1);
+            T v;
+            if (p && q) {
+               v = F[face_cell(g, dir, f3, 2*p - 1, 2*q - 1)] +
+                   F[face_cell(g, dir, f3, 2*p - 1, 2*q)];
+               v = v + F[face_cell(g, dir, f3, 2*p, 2*q - 1)];
+               v = v + F[face_cell(g, dir, f3, 2*p, 2*q)];
+            } else if (q) {
+               v = F[face_cell(g, dir, f3, ae, 2*q - 1)] +
+                   F[face_cell(g, dir, f3, ae, 2*q)];
+            } else if (p) {
+               v = F[face_cell(g, dir, f3, 2*p - 1, be)] +
+                   F[face_cell(g, dir, f3, 2*p, be)];
+            } else {
+               v = F[face_cell(g, dir, f3, ae, be)];
+            }
+            C[face_cell(g, dir, c0, p ? p + oa : ae, q ? q + ob : be)] = v;
+         }
+         return;
+      }
       for (int e = threadIdx.x; e < ha * hb; e += blockDim.x) {
          int a = 1 + e / hb, b = 1 + e % hb;
          T q = quarter(C[face_cell(g, dir, c1, a + oa, b + ob)]);
@@ -83,7 +126,7 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int dir, int stencil,
       T *B = pool + bv_offset(g, bt.slot, var);
       const bool hiside = (bt.l % 2) == 1;
       const int tp = hiside ? n + 1 : 0, fp = hiside ? n : 1;
-      const bool full = stencil != 7;
+      const bool full = code != 0 || stencil != 7;
       const int a0 = full ? 0 : 1, a1 = full ? na + 1 : na;
       const int b0 = full ? 0 : 1, b1 = full ? nb + 1 : nb;
       const int cb = b1 - b0 + 1, cnt = (a1 - a0 + 1) * cb;
@@ -95,14 +138,14 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int dir, int stencil,
 }
 
 template <typename T>
-int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil,
+int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil, int code,
                     const DirTasks &t, int var0, int nvar, cudaStream_t s)
 {
    int n = t.n_same + t.n_diff + t.n_bc;
    if (n == 0 || nvar == 0)
       return 0;
-   comm_dir_kernel<T><<<dim3(n, nvar), 128, 0, s>>>(pool, g, dir, stencil, t,
-                                                    var0);
+   comm_dir_kernel<T><<<dim3(n, nvar), 128, 0, s>>>(pool, g, dir, stencil,
+                                                    code, t, var0);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -473,7 +516,7 @@ int launch_download(const T *pool, const Geom &g, const int32_t *slots,
 }
 
 #define INSTANTIATE(T)                                                        \
-   template int launch_comm_dir<T>(T *, const Geom &, int, int,               \
+   template int launch_comm_dir<T>(T *, const Geom &, int, int, int,          \
                                    const DirTasks &, int, int, cudaStream_t); \
    template int launch_stencil<T>(T *, const Geom &, int, const int32_t *,    \
                                   int, int, cudaStream_t);                    \

@@ -100,7 +100,7 @@ int mamr_create(const mamr_config *cfg, mamr_ctx **out)
        (cfg->num_vars < 8 || cfg->num_vars / 4 > MAMR_WORK_MAX_MAT))
       return fail(MAMR_EINVAL, "stencil 0 needs 8 <= num_vars <= %d",
                   4 * MAMR_WORK_MAX_MAT + 3);
-   if (cfg->code != 0)
+   if (cfg->code < 0 || cfg->code > 2)
       return fail(MAMR_EUNSUP, "code %d not supported", cfg->code);
    if (cfg->dtype != MAMR_FP64 && cfg->dtype != MAMR_FP32)
       return fail(MAMR_EINVAL, "bad dtype");
@@ -286,28 +286,91 @@ static void on_proc_comm(mamr_ctx *c, int n, int n1, int l, int start,
    hi = (l % 2 == 0) ? n1 : n;   /* bp1 */
    for (m = start; m < start + num; m++) {
       double *bp = blk(c, lo, m), *bp1 = blk(c, hi, m);
+      /* code 1/2 (ref/comm.c:1535-1579): every plane whole */
+      const int all = c->cfg.code != 0;
       if (l / 2 == 0) {
-         for (j = 1; j <= ny; j++)
-            for (k = 1; k <= nz; k++) {
+         js = all ? 0 : 1; je = all ? ny + 1 : ny;
+         for (j = js; j <= je; j++)
+            for (k = js ? 1 : 0; k <= (all ? nz + 1 : nz); k++) {
                AT(bp1, nx + 1, j, k) = AT(bp, 1, j, k);
                AT(bp, 0, j, k) = AT(bp1, nx, j, k);
             }
       } else if (l / 2 == 1) {
-         if (c->cfg.stencil == 7) { is = 1; ie = nx; }
+         if (c->cfg.stencil == 7 && !all) { is = 1; ie = nx; }
          else { is = 0; ie = nx + 1; }
          for (i = is; i <= ie; i++)
-            for (k = 1; k <= nz; k++) {
+            for (k = all ? 0 : 1; k <= (all ? nz + 1 : nz); k++) {
                AT(bp1, i, ny + 1, k) = AT(bp, i, 1, k);
                AT(bp, i, 0, k) = AT(bp1, i, ny, k);
             }
       } else {
-         if (c->cfg.stencil == 7) { is = 1; ie = nx; js = 1; je = ny; }
+         if (c->cfg.stencil == 7 && !all) { is = 1; ie = nx; js = 1; je = ny; }
          else { is = 0; ie = nx + 1; js = 0; je = ny + 1; }
          for (i = is; i <= ie; i++)
             for (j = js; j <= je; j++) {
                AT(bp1, i, j, nz + 1) = AT(bp, i, j, 1);
                AT(bp, i, j, 0) = AT(bp1, i, j, nz);
             }
+      }
+   }
+}
+
+/* Cell (nc, a, b) of a face normal to dir: tangential (a, b) are (j, k)
+ * for x faces, (i, k) for y faces, (i, j) for z faces. */
+static double *face_at(const mamr_ctx *c, double *p, int dir, int nc, int a,
+                       int b)
+{
+   if (dir == 0)
+      return &AT(p, nc, a, b);
+   if (dir == 1)
+      return &AT(p, a, nc, b);
+   return &AT(p, a, b, nc);
+}
+
+/* ref/comm.c:1689-1907 (code 1/2: ghosts transferred whole), one
+ * direction-generic form of the reference's three branches.  Block n is
+ * coarse, n1 fine, (iq, jq) the quarter of n's face l: the fine ghost
+ * plane gets coarse/4 over its whole (na+2) x (nb+2) extent (tangential
+ * index A maps to coarse offset + A=0 -> 0, A=na+1 -> na/2+1, else
+ * (A+1)/2); the coarse ghost plane gets the quarter's 2x2 sums, the pair
+ * sums of the fine ghost row and column on the jq and iq sides, and one
+ * corner copied. */
+static void comm_diff_all(mamr_ctx *c, int n, int n1, int l, int iq, int jq,
+                          int start, int num)
+{
+   const int dir = l / 2;
+   const int nn = dir == 0 ? c->cfg.nx : (dir == 1 ? c->cfg.ny : c->cfg.nz);
+   const int na = dir == 0 ? c->cfg.ny : c->cfg.nx;
+   const int nb = dir == 2 ? c->cfg.ny : c->cfg.nz;
+   const int ha = na / 2, hb = nb / 2, oa = jq * ha, ob = iq * hb;
+   const int c0 = (l % 2 == 0) ? 0 : nn + 1, c1 = (l % 2 == 0) ? 1 : nn;
+   const int f2 = (l % 2 == 0) ? nn + 1 : 0, f3 = (l % 2 == 0) ? nn : 1;
+   const int ae = jq ? na + 1 : 0, be = iq ? nb + 1 : 0;  /* edge sides */
+   int m, A, B, a, b;
+   for (m = start; m < start + num; m++) {
+      double *C = blk(c, n, m), *F = blk(c, n1, m);
+      for (A = 0; A <= na + 1; A++)
+         for (B = 0; B <= nb + 1; B++) {
+            int ca = A == 0 ? oa : (A == na + 1 ? ha + 1 + oa : (A + 1) / 2 + oa);
+            int cb = B == 0 ? ob : (B == nb + 1 ? hb + 1 + ob : (B + 1) / 2 + ob);
+            *face_at(c, F, dir, f2, A, B) =
+               RF(c, *face_at(c, C, dir, c1, ca, cb) / 4.0);
+         }
+      *face_at(c, C, dir, c0, ae, be) = *face_at(c, F, dir, f3, ae, be);
+      for (b = 1; b <= hb; b++)
+         *face_at(c, C, dir, c0, ae, b + ob) =
+            RF(c, *face_at(c, F, dir, f3, ae, 2*b - 1) +
+                  *face_at(c, F, dir, f3, ae, 2*b));
+      for (a = 1; a <= ha; a++) {
+         *face_at(c, C, dir, c0, a + oa, be) =
+            RF(c, *face_at(c, F, dir, f3, 2*a - 1, be) +
+                  *face_at(c, F, dir, f3, 2*a, be));
+         for (b = 1; b <= hb; b++)
+            *face_at(c, C, dir, c0, a + oa, b + ob) =
+               RF(c, RF(c, RF(c, *face_at(c, F, dir, f3, 2*a - 1, 2*b - 1) +
+                                 *face_at(c, F, dir, f3, 2*a - 1, 2*b)) +
+                          *face_at(c, F, dir, f3, 2*a, 2*b - 1)) +
+                     *face_at(c, F, dir, f3, 2*a, 2*b));
       }
    }
 }
@@ -321,6 +384,10 @@ static void on_proc_comm_diff(mamr_ctx *c, int n, int n1, int l, int iq,
    int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz;
    int xh = nx / 2, yh = ny / 2, zh = nz / 2, m, i, j, k;
    int a0, a1, a2, a3, o1, o2;
+   if (c->cfg.code != 0) {
+      comm_diff_all(c, n, n1, l, iq, jq, start, num);
+      return;
+   }
    for (m = start; m < start + num; m++) {
       double *bp = blk(c, n, m), *bp1 = blk(c, n1, m);
       if (l / 2 == 0) {
@@ -387,7 +454,7 @@ static void on_proc_comm_diff(mamr_ctx *c, int n, int n1, int l, int iq,
 static void apply_bc(mamr_ctx *c, int l, int n, int start, int num)
 {
    int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz, var, i, j, k, t, f;
-   int full = !(c->cfg.stencil == 7);
+   int full = !(c->cfg.code == 0 && c->cfg.stencil == 7);
    int lo0 = full ? 0 : 1;
    for (var = start; var < start + num; var++) {
       double *bp = blk(c, n, var);

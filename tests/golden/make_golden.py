@@ -96,6 +96,11 @@ CASES = {
                 "0.004", "0.12", "0.03", "0.03", "0", "0", "0",
                 "--object", "0", "1", "0.3", "0.7", "0.7", "0.007", "-0.005",
                 "-0.009", "0.06", "0.06", "0.06", "0", "0", "0"],
+    # whole-ghost exchanges (--code 1 and 2; identical on one rank: the two
+    # differ only in how ranks pack messages): level jumps fill the edge
+    # ghosts too, so the 27-point stencil reads no stale values
+    "code1_amr27": small(27, ["--code", "1"]),
+    "code2_amr7": small(7, ["--code", "2"]),
     # the variable-work stencils (--stencil 0): 8 variables (mat = 2), six
     # stages per timestep so that every kernel (calc_stage % 6) runs on
     # every variable class, refinement and coarsening around a moving

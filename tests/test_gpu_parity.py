@@ -171,3 +171,18 @@ def test_stencil0_fp32_and_batched_are_refused(gpu_lib):
             ctx.run_timesteps(1, 1, 1, flags=RUN_BATCHED)
         assert e.value.status == -5
         ctx.run_timesteps(1, 6, 1)           # the plain path runs
+
+
+def test_code12_batched_is_refused(gpu_lib):
+    """--code 1/2 exchanges whole ghost planes; the batched path gathers
+    code-0 ghosts and refuses them (the plain path runs them)."""
+    from miniamr_gb300.abi import RUN_BATCHED
+    cfg = Config.make(8, 8, 8, 2, 16, stencil=27, code=1)
+    with gpu_lib.context(cfg) as ctx:
+        m = meshmod.initial_mesh(2, 1, 1, 0, 16)
+        ctx.upload(np.arange(2), gpu_lib.initial_values(cfg, 2))
+        ctx.set_mesh(m.blocks())
+        with pytest.raises(MamrError) as e:
+            ctx.run_timesteps(1, 1, 1, flags=RUN_BATCHED)
+        assert e.value.status == -5
+        ctx.run_timesteps(1, 2, 1)
