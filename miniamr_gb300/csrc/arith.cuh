@@ -139,39 +139,75 @@ __device__ __forceinline__ float sum8(const float *t)
 }
 
 // ---- exact fixed-point checksum of FP32 cells ------------------------------
-// A cell v becomes trunc(v * 2^52) (toward zero), using integer operations
-// only.  Returns false (and q = 0) for |v| >= 2^10, inf or nan.
-__device__ __forceinline__ bool fixed52(float v, long long &q)
+// A cell v contributes trunc(v * 2^52) (toward zero), summed exactly in
+// 128-bit two's complement; |v| must be below 2^10 (finite).
+//
+// The term is formed with FP32 additions only (an FP64 or 64-bit integer
+// conversion would run on this part's slow FP64 pipe): with x = |v| and
+// magic constants M = 2^11, 2^-11, 2^-29, a round-toward-zero addition
+// t = RZ(r + M) keeps r's bits down to ulp(M) = 2^-12, 2^-34, 2^-52 in the
+// mantissa of t (r < 2^22 ulp(M), so t stays in M's binade), and
+// r - (t - M) is the exact remainder.  So
+//   floor(x * 2^52) = I1 * 2^40 + I2 * 2^18 + I3,
+//   Ik = mantissa of tk = bits(tk) - bits(Mk)  (I1, I2 < 2^22, I3 < 2^18),
+// and trunc(v * 2^52) = sign(v) * floor(x * 2^52).  The three pieces are
+// summed in 32-bit words (mod 2^32, the sign as a factor of +-1, bits(Mk)
+// removed once per term through the sum of the signs) and folded into the
+// 128-bit accumulator by fixed52_flush at least every 512 terms, before
+// |sum of I1| can reach 2^31.
+struct Fixed52 {
+   unsigned a1 = 0, a2 = 0, a3 = 0;   // sums of sign * bits(tk), mod 2^32
+   int cnt = 0;                       // sum of the signs
+};
+
+// Adds the term of v (negate: its opposite); returns whether |v| < 2^10.
+__device__ __forceinline__ bool fixed52_add(float v, Fixed52 &p,
+                                            bool negate = false)
 {
-   const unsigned u = __float_as_uint(v);
-   const unsigned e = (u >> 23) & 0xffu;
-   if (e >= 137u) {            // |v| >= 1024, inf, nan
-      q = 0;
-      return false;
-   }
-   unsigned long long m = u & 0x7fffffu;
-   int sh;
-   if (e == 0)
-      sh = -149 + 52;          // subnormal: v = m * 2^-149
-   else {
-      m |= 0x800000u;
-      sh = (int) e - 150 + 52; // v = m * 2^(e-150)
-   }
-   unsigned long long mag = sh >= 0 ? (m << sh)
-                                    : (sh > -64 ? (m >> (-sh)) : 0ull);
-   q = (u >> 31) ? -(long long) mag : (long long) mag;
-   return true;
+   const float x = fabsf(v);
+   const float t1 = __fadd_rz(x, 0x1p11f);
+   const float r1 = __fsub_rn(x, __fsub_rn(t1, 0x1p11f));
+   const float t2 = __fadd_rz(r1, 0x1p-11f);
+   const float r2 = __fsub_rn(r1, __fsub_rn(t2, 0x1p-11f));
+   const float t3 = __fadd_rz(r2, 0x1p-29f);
+   int s = ((int) __float_as_uint(v) >> 31) | 1;
+   if (negate)
+      s = -s;
+   p.a1 += (unsigned) s * __float_as_uint(t1);
+   p.a2 += (unsigned) s * __float_as_uint(t2);
+   p.a3 += (unsigned) s * __float_as_uint(t3);
+   p.cnt += s;
+   return x < 1024.0f;
 }
 
-// 128-bit two's complement accumulator held as (lo, hi).
+// 128-bit two's complement accumulator held as (lo, hi): adds the
+// sign-extended q with one carry chain.
 __device__ __forceinline__ void acc128_add(unsigned long long &lo,
                                            unsigned long long &hi,
                                            long long q)
 {
-   unsigned long long x = (unsigned long long) q;
-   unsigned long long n = lo + x;
-   hi += (n < lo ? 1ull : 0ull) + (q < 0 ? ~0ull : 0ull);
-   lo = n;
+   const unsigned long long s = (unsigned long long) (q >> 63);
+   asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;"
+       : "+l"(lo), "+l"(hi)
+       : "l"((unsigned long long) q), "l"(s));
+}
+
+// Folds the piece sums into (lo, hi) and clears them.
+__device__ __forceinline__ void fixed52_flush(Fixed52 &p,
+                                              unsigned long long &lo,
+                                              unsigned long long &hi)
+{
+   const unsigned c = (unsigned) p.cnt;
+   const long long i1 = (int) (p.a1 - c * __float_as_uint(0x1p11f));
+   const long long i2 = (int) (p.a2 - c * __float_as_uint(0x1p-11f));
+   const long long i3 = (int) (p.a3 - c * __float_as_uint(0x1p-29f));
+   // i1 * 2^40 needs 128 bits; i2 * 2^18 + i3 fits in 64
+   asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;"
+       : "+l"(lo), "+l"(hi)
+       : "l"((unsigned long long) i1 << 40),
+         "l"((unsigned long long) (i1 >> 24)));
+   acc128_add(lo, hi, i2 * (1ll << 18) + i3);
+   p = Fixed52();
 }
 
 __device__ __forceinline__ void acc128_merge(unsigned long long &lo,
@@ -182,6 +218,26 @@ __device__ __forceinline__ void acc128_merge(unsigned long long &lo,
    unsigned long long n = lo + lo2;
    hi = hi + hi2 + (n < lo ? 1ull : 0ull);
    lo = n;
+}
+
+// Adds a warp's 128-bit fixed-point partial sums into acc[0..1] (every
+// lane of the warp calls it).
+__device__ __forceinline__ void warp_acc128_flush(unsigned long long lo,
+                                                  unsigned long long hi,
+                                                  unsigned long long *acc)
+{
+#pragma unroll
+   for (int off = 16; off; off >>= 1) {
+      unsigned long long l2 = __shfl_down_sync(0xffffffffu, lo, off);
+      unsigned long long h2 = __shfl_down_sync(0xffffffffu, hi, off);
+      acc128_merge(lo, hi, l2, h2);
+   }
+   if ((threadIdx.x & 31) == 0) {
+      unsigned long long old = atomicAdd(acc, lo);
+      unsigned long long hadd = hi + ((old + lo < old) ? 1ull : 0ull);
+      if (hadd)
+         atomicAdd(acc + 1, hadd);
+   }
 }
 
 // Adds the CTA's accumulators into the global 128-bit acc[0..1].  Two

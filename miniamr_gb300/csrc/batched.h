@@ -55,8 +55,11 @@ void batched_mesh_changed(BatchedState *b);
 //   pencil kernel:  `rows` j-rows and `planes` i-planes per thread
 //                   (threads = 1024 / (rows * planes))
 //   both:           `grid` CTAs
+//   warp-per-item kernel (8^3 blocks, 7-point; kernel = 1): threads = 32,
+//                   vpc = warps per CTA, rows = 2, planes = 0
 struct StageShape {
    int threads = 0, vpc = 1, rows = 1, planes = 4, grid = 1;
+   int kernel = 0;
 };
 
 // Launches one fused stage: src -> dst for every block and variable.
@@ -73,6 +76,17 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
 template <typename T>
 void batched_candidates(const Geom &g, int stencil, int n_blocks,
                         std::vector<StageShape> &out);
+
+// Warp-per-item variant for 8^3 blocks and the 7-point stencil (any mesh):
+// its launch shapes, and one stage (FP32 checksums fused into acc).
+template <typename T>
+void brick_candidates(const Geom &g, int stencil, int n_blocks,
+                      std::vector<StageShape> &out);
+template <typename T>
+int launch_brick_stage(const T *src, T *dst, const Geom &g,
+                       const BItem *items, int n_blocks, const StageShape &sh,
+                       int write_ghosts, int do_cs, unsigned long long *acc,
+                       unsigned *err, cudaStream_t s);
 
 // Pencil variant for single-level meshes of 16^3 blocks: CTAs walk chains
 // of blocks along z (chain[pencils[p].x .. +pencils[p].y), bottom to

@@ -44,26 +44,6 @@ __host__ __device__ inline size_t tile_bytes(const Geom &g)
 }
 
 
-// Adds a warp's 128-bit fixed-point partial sums into acc[0..1] (every
-// lane of the warp calls it).
-__device__ __forceinline__ void warp_acc128_flush(unsigned long long lo,
-                                                  unsigned long long hi,
-                                                  unsigned long long *acc)
-{
-#pragma unroll
-   for (int off = 16; off; off >>= 1) {
-      unsigned long long l2 = __shfl_down_sync(0xffffffffu, lo, off);
-      unsigned long long h2 = __shfl_down_sync(0xffffffffu, hi, off);
-      acc128_merge(lo, hi, l2, h2);
-   }
-   if ((threadIdx.x & 31) == 0) {
-      unsigned long long old = atomicAdd(acc, lo);
-      unsigned long long hadd = hi + ((old + lo < old) ? 1ull : 0ull);
-      if (hadd)
-         atomicAdd(acc + 1, hadd);
-   }
-}
-
 // A CTA takes the variables [vg * vpc, vg * vpc + vpc) of one block per
 // work item: blockDim.x / vpc threads (whole warps) and one shared tile
 // per variable, the block's neighbour record loaded once.
@@ -92,6 +72,7 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
    // FP32 checksum terms of this thread's variable, flushed per warp when
    // the variable changes and at the end
    unsigned long long lo = 0, hi = 0;
+   Fixed52 part;
    bool ok = true;
    int cs_var = -1;
 
@@ -250,9 +231,9 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                   const T out = div7(w);
                   d[D.cell(i, j, k)] = out;
                   if (sizeof(T) == 4 && do_cs) {
-                     long long q;
-                     ok &= fixed52((float) out, q);
-                     acc128_add(lo, hi, q);
+                     ok &= fixed52_add((float) out, part);
+                     if (nx > 256 && (i & 255) == 0)
+                        fixed52_flush(part, lo, hi);
                   }
                   am = ac;
                   ac = ap;
@@ -275,14 +256,16 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                   const T out = div27((s0 + s1) + s2);
                   d[D.cell(i, j, k)] = out;
                   if (sizeof(T) == 4 && do_cs) {
-                     long long q;
-                     ok &= fixed52((float) out, q);
-                     acc128_add(lo, hi, q);
+                     ok &= fixed52_add((float) out, part);
+                     if (nx > 256 && (i & 255) == 0)
+                        fixed52_flush(part, lo, hi);
                   }
                   s0 = s1;
                   s1 = s2;
                }
             }
+            if (sizeof(T) == 4 && do_cs)
+               fixed52_flush(part, lo, hi);
          }
       __syncthreads();
    }
@@ -296,13 +279,19 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
 }
 
 
+// CTAs per SM for one shape; the kernel's dynamic shared memory limit only
+// grows, so that every candidate queried stays launchable.
 template <typename T, int ST, int BX, int BY, int BZ>
 static int per_sm_of(size_t smem, int threads)
 {
    int per_sm = 0;
-   cudaFuncSetAttribute(batched_stage_kernel<T, ST, BX, BY, BZ>,
-                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                        (int) smem);
+   cudaFuncAttributes fa;
+   if (cudaFuncGetAttributes(&fa, batched_stage_kernel<T, ST, BX, BY, BZ>) !=
+          cudaSuccess ||
+       (size_t) fa.maxDynamicSharedSizeBytes < smem)
+      cudaFuncSetAttribute(batched_stage_kernel<T, ST, BX, BY, BZ>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int) smem);
    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
       &per_sm, batched_stage_kernel<T, ST, BX, BY, BZ>, threads, smem);
    return per_sm;
@@ -330,6 +319,8 @@ void batched_candidates(const Geom &g, int stencil, int n_blocks,
    cudaGetDevice(&dev);
    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
    out.clear();
+   // 8^3 blocks, 7-point: the warp-per-item kernel first
+   brick_candidates<T>(g, stencil, n_blocks, out);
    const int cols = g.ny * g.nz;
    const int full = std::min(256, (cols + 31) / 32 * 32);
    for (int thr : {full, std::max(32, full / 2 / 32 * 32)}) {
@@ -353,7 +344,8 @@ void batched_candidates(const Geom &g, int stencil, int n_blocks,
                                           (long long) per_sm * sms, items));
          bool dup = false;
          for (const StageShape &o : out)
-            dup |= o.threads == sh.threads && o.vpc == sh.vpc;
+            dup |= o.kernel == 0 && o.threads == sh.threads &&
+                   o.vpc == sh.vpc;
          if (!dup)
             out.push_back(sh);
       }
@@ -372,6 +364,14 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
 {
    if (n_blocks == 0)
       return 0;
+   if (sh.kernel == 1) {
+      int launches = launch_brick_stage(src, dst, g, items, n_blocks, sh,
+                                        write_ghosts, do_cs, acc, err, s);
+      if (launches >= 0 && do_cs && sizeof(T) == 8)
+         launches += launch_fp64_checksums((const double *) dst, g, items,
+                                           n_blocks, partials, sums, s);
+      return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
+   }
    const size_t smem = tile_bytes<T>(g) * sh.vpc;
    const int thr = sh.threads * sh.vpc;
 #define MAMR_GENERIC(ST, BX, BY, BZ)                                          \

@@ -1,0 +1,438 @@
+// Stage kernel for meshes of 8^3 blocks with the 7-point stencil: one warp
+// per work item (block, variable) and no CTA-wide barrier, so that every
+// warp of an SM streams independently.  Each warp owns two tiles in shared
+// memory and fills the next item's tile -- interior rows, and the face
+// ghosts that are copies (same-level neighbour, reflection) or single
+// values (coarser neighbour, scaled by 1/4 afterwards) -- with cp.async
+// while it computes the current item; ghosts from finer neighbours (sums of
+// four cells) are gathered after the wait.  The values and the operation
+// order are those of the generic stage kernel (batched_kernels.cu): the
+// reference's face exchange (ref/comm.c:1465-1965) and 7-point update
+// (ref/stencil.c:82-101), with the FP32 fixed-point checksum of every
+// result folded in.
+#include <algorithm>
+#include <vector>
+
+#include "batched.h"
+#include "arith.cuh"
+#include "cp_async.cuh"
+#include "dims.cuh"
+
+namespace mamr {
+
+namespace {
+
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; };
+template <> struct Vec16<double> { using type = double2; };
+
+// Tile of one item: cell (i, j, k), 0 <= i, j, k <= 9, at
+// (i*10 + j)*S + k - 1.  A row (i, j) holds k = 1..8 in columns 0..7 (two
+// or four 16-byte vectors) and k = 9 in column 8; its k = 0 ghost sits in
+// the last column of the row before (only interior rows have one).  With
+// S = 12 (FP32) or 10 (FP64) the eight rows j = 1..8 of one plane start in
+// eight different 16-byte bank groups, so the vector loads of eight
+// consecutive lanes do not conflict.
+template <typename T> struct Brick {
+   static constexpr int VW = 16 / (int) sizeof(T);   // elements per vector
+   static constexpr int R = 8 / VW;                  // vectors per row
+   static constexpr int S = sizeof(T) == 4 ? 12 : 10;
+   static constexpr int TILE = 100 * S;
+   static constexpr int DESC = 44;   // ints of a BItem read: slot .. f[5]
+   __device__ static int at(int i, int j, int k)
+   {
+      return (i * 10 + j) * S + k - 1;
+   }
+   // pool offset of interior cell (i, j, k) (split layout, 1 <= k <= 8)
+   __device__ static int gat(int i, int j, int k)
+   {
+      return (i * 10 + j) * 8 + k - 1;
+   }
+   // face plane p of direction dir, tangential (a, b)
+   __device__ static int face_gat(int dir, int p, int a, int b)
+   {
+      return dir == 0 ? gat(p, a, b) : (dir == 1 ? gat(a, p, b)
+                                                 : gat(a, b, p));
+   }
+   __device__ static int ghost_at(int dir, int gn, int a, int b)
+   {
+      return dir == 0 ? at(gn, a, b) : (dir == 1 ? at(a, gn, b)
+                                                 : at(a, b, gn));
+   }
+   static size_t smem_per_warp()
+   {
+      return 2 * (TILE * sizeof(T) + DESC * sizeof(int));
+   }
+};
+
+template <typename T>
+__device__ __forceinline__ void ld4(const T *p, T (&v)[4])
+{
+   using V = typename Vec16<T>::type;
+   if (sizeof(T) == 4) {
+      const float4 x = *reinterpret_cast<const float4 *>(p);
+      v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+   } else {
+      const V x = *reinterpret_cast<const V *>(p);
+      const V y = *reinterpret_cast<const V *>(p + 2);
+      v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+   }
+}
+
+template <typename T>
+__device__ __forceinline__ void st4(T *p, const T (&v)[4])
+{
+   if (sizeof(T) == 4) {
+      *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+   } else {
+      *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+      *reinterpret_cast<double2 *>(p + 2) = make_double2(v[2], v[3]);
+   }
+}
+
+// Queues the copies that fill the tile of item (block sd[0], var): the
+// interior rows, and the face ghosts of same-level, boundary and coarser
+// faces (the coarse values unscaled).  sd = the block's BItem, ints
+// 0..DESC-1.  Returns whether the tile needs brick_fix (a face at a level
+// jump).
+template <typename T>
+__device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
+                                            const Geom &g, int var,
+                                            const int *sd, T *tile, int lane)
+{
+   bool fix = false;
+   using B = Brick<T>;
+   constexpr int VW = B::VW, R = B::R;
+   const T *own = src + bv_offset(g, sd[0], var);
+#pragma unroll
+   for (int t = 0; t < 2 * R; t++) {
+      const int c = lane + 32 * t, r = c / R, k = 1 + (c % R) * VW;
+      const int i = (r >> 3) + 1, j = (r & 7) + 1;
+      cp_async16(tile + B::at(i, j, k), own + B::gat(i, j, k));
+   }
+#pragma unroll
+   for (int l = 0; l < 6; l++) {
+      const int *f = sd + 2 + 7 * l;
+      const int type = f[0];
+      const int dir = l >> 1;
+      const bool low = !(l & 1);
+      const int gn = low ? 0 : 9;
+      if (type == FACE_SAME || type == FACE_BC) {
+         const T *sb = type == FACE_SAME ? src + bv_offset(g, f[1], var)
+                                         : own;
+         // same level: the neighbour's near plane; boundary: reflection
+         const int p = (type == FACE_SAME) == low ? 8 : 1;
+         if (dir < 2) {
+            if (lane < 8 * R) {
+               const int a = lane / R + 1, k = 1 + (lane % R) * VW;
+               if (dir == 0)
+                  cp_async16(tile + B::at(gn, a, k), sb + B::gat(p, a, k));
+               else
+                  cp_async16(tile + B::at(a, gn, k), sb + B::gat(a, p, k));
+            }
+         } else {
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+               const int e = lane + 32 * u, i = (e >> 3) + 1, j = (e & 7) + 1;
+               cp_async_elem(tile + B::at(i, j, gn), sb + B::gat(i, j, p));
+            }
+         }
+      } else if (type == FACE_COARSE) {
+         fix = true;
+         const T *sb = src + bv_offset(g, f[1], var);
+         const int p = low ? 8 : 1, iq = f[5], jq = f[6];
+#pragma unroll
+         for (int u = 0; u < 2; u++) {
+            const int e = lane + 32 * u, a = (e >> 3) + 1, b = (e & 7) + 1;
+            cp_async_elem(tile + B::ghost_at(dir, gn, a, b),
+                          sb + B::face_gat(dir, p, (a + 1) / 2 + 4 * jq,
+                                           (b + 1) / 2 + 4 * iq));
+         }
+      } else {
+         fix = true;                   // finer neighbours: summed later
+      }
+   }
+   return fix;
+}
+
+// After the copies landed: coarse ghosts scaled by 1/4 (each lane the
+// elements it copied) and fine ghosts summed from the four finer
+// neighbours' cells, in the reference's order.
+template <typename T>
+__device__ __forceinline__ void brick_fix(const T *__restrict__ src,
+                                          const Geom &g, int var,
+                                          const int *sd, T *tile, int lane)
+{
+   using B = Brick<T>;
+#pragma unroll
+   for (int l = 0; l < 6; l++) {
+      const int *f = sd + 2 + 7 * l;
+      const int type = f[0];
+      if (type != FACE_COARSE && type != FACE_FINE)
+         continue;
+      const int dir = l >> 1;
+      const bool low = !(l & 1);
+      const int gn = low ? 0 : 9, p = low ? 8 : 1;
+#pragma unroll
+      for (int u = 0; u < 2; u++) {
+         const int e = lane + 32 * u, a = (e >> 3) + 1, b = (e & 7) + 1;
+         T &x = tile[B::ghost_at(dir, gn, a, b)];
+         if (type == FACE_COARSE) {
+            x = quarter(x);
+         } else {
+            const int jq = a > 4, iq = b > 4;
+            const int a2 = a - 4 * jq, b2 = b - 4 * iq;
+            const T *fb = src + bv_offset(g, f[1 + iq * 2 + jq], var);
+            T t = fb[B::face_gat(dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
+                  fb[B::face_gat(dir, p, 2 * a2 - 1, 2 * b2)];
+            t = t + fb[B::face_gat(dir, p, 2 * a2, 2 * b2 - 1)];
+            t = t + fb[B::face_gat(dir, p, 2 * a2, 2 * b2)];
+            x = t;
+         }
+      }
+   }
+}
+
+// At most 4 warps per CTA; registers for the CTAs whose tiles fill the
+// shared memory (5 with FP32 tiles, 3 with FP64).
+template <typename T>
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 3)
+brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
+                   const BItem *__restrict__ items, int nb, int write_ghosts,
+                   int do_cs, unsigned long long *__restrict__ acc,
+                   unsigned *__restrict__ err)
+{
+   using B = Brick<T>;
+   constexpr int DESC = B::DESC;
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+   const int wpc = blockDim.x >> 5;
+   T *tiles = reinterpret_cast<T *>(smem_raw) + (size_t) warp * 2 * B::TILE;
+   int *sdesc = reinterpret_cast<int *>(reinterpret_cast<T *>(smem_raw) +
+                                        (size_t) wpc * 2 * B::TILE) +
+                warp * 2 * DESC;
+   // work items (block b, variable var), variable-major; warp w takes
+   // items w, w + nw, w + 2 nw, ... tracked as (var, b) without divisions
+   const int nw = gridDim.x * wpc;
+   const int it0 = blockIdx.x * wpc + warp;
+   struct Pos {
+      int var, b;
+   };
+   Pos cur{it0 / nb, it0 % nb};
+   if (cur.var >= g.V)
+      return;
+   const int step_v = nw / nb, step_b = nw - step_v * nb;
+   auto advance = [&](Pos q) {
+      q.var += step_v;
+      q.b += step_b;
+      if (q.b >= nb) {
+         q.b -= nb;
+         q.var++;
+      }
+      return q;
+   };
+   const Dims<8, 8, 8> D(g);
+   // this lane's two output rows (i0, j), (i0 + 1, j)
+   const int j = (lane & 7) + 1, i0 = 2 * (lane >> 3) + 1;
+
+   auto load_desc = [&](const Pos &q, int &d0, int &d1) {
+      const int *p = reinterpret_cast<const int *>(items + q.b);
+      d0 = __ldg(p + lane);
+      d1 = lane < DESC - 32 ? __ldg(p + 32 + lane) : 0;
+   };
+   auto put_desc = [&](int *sd, int d0, int d1) {
+      sd[lane] = d0;
+      if (lane < DESC - 32)
+         sd[32 + lane] = d1;
+      __syncwarp();
+   };
+
+   int d0, d1;
+   load_desc(cur, d0, d1);
+   put_desc(sdesc, d0, d1);
+   bool fix_cur = brick_issue(src, g, cur.var, sdesc, tiles, lane);
+   cp_async_commit();
+   Pos nxt = advance(cur);
+   if (nxt.var < g.V)
+      load_desc(nxt, d0, d1);
+
+   unsigned long long lo = 0, hi = 0;
+   Fixed52 part;
+   bool ok = true;
+   int cs_var = -1;
+   for (int n = 0;; n++) {
+      const int cb = n & 1;
+      T *tile = tiles + cb * B::TILE;
+      const int *sd = sdesc + cb * DESC;
+      // the next item: descriptor into shared memory, copies in flight
+      bool fix_next = false;
+      if (nxt.var < g.V) {
+         int *sdn = sdesc + (cb ^ 1) * DESC;
+         put_desc(sdn, d0, d1);
+         fix_next = brick_issue(src, g, nxt.var, sdn,
+                                tiles + (cb ^ 1) * B::TILE, lane);
+         const Pos nn = advance(nxt);
+         if (nn.var < g.V)
+            load_desc(nn, d0, d1);
+      }
+      cp_async_commit();
+      cp_async_wait_group<1>();
+      const int var = cur.var;
+      if (fix_cur)
+         brick_fix(src, g, var, sd, tile, lane);
+      __syncwarp();
+      T *d = dst + bv_offset(g, sd[0], var);
+      if (write_ghosts) {
+#pragma unroll
+         for (int l = 0; l < 6; l++) {
+            const int dir = l >> 1, gn = (l & 1) ? 9 : 0;
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+               const int e = lane + 32 * u, a = (e >> 3) + 1, b = (e & 7) + 1;
+               int gi, gj, gk;
+               if (dir == 0) { gi = gn; gj = a; gk = b; }
+               else if (dir == 1) { gi = a; gj = gn; gk = b; }
+               else { gi = a; gj = b; gk = gn; }
+               d[D.cell(gi, gj, gk)] = tile[B::at(gi, gj, gk)];
+            }
+         }
+      }
+      if (sizeof(T) == 4 && do_cs && var != cs_var) {
+         if (cs_var >= 0) {
+            warp_acc128_flush(lo, hi, acc + 2 * cs_var);
+            lo = hi = 0;
+         }
+         cs_var = var;
+      }
+      // 7-point update of rows (i0, j) and (i0 + 1, j), four k at a time
+#pragma unroll
+      for (int m = 0; m < 2; m++) {
+         const int i = i0 + m;
+#pragma unroll
+         for (int h = 0; h < 2; h++) {
+            const int k0 = 1 + 4 * h;
+            T a[4], jm[4], c[4], jp[4], bq[4];
+            ld4(tile + B::at(i - 1, j, k0), a);
+            ld4(tile + B::at(i, j - 1, k0), jm);
+            ld4(tile + B::at(i, j, k0), c);
+            ld4(tile + B::at(i, j + 1, k0), jp);
+            ld4(tile + B::at(i + 1, j, k0), bq);
+            const T cm = tile[B::at(i, j, k0 - 1)];
+            const T cp = tile[B::at(i, j, k0 + 4)];
+            T w[4], q[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+               const T km = t == 0 ? cm : c[t - 1];
+               const T kp = t == 3 ? cp : c[t + 1];
+               T s = a[t] + jm[t];
+               s = s + km;
+               s = s + c[t];
+               s = s + kp;
+               s = s + jp[t];
+               s = s + bq[t];
+               w[t] = s;
+            }
+            div_const4<7>(w, q);
+            st4(d + B::gat(i, j, k0), q);
+            if (sizeof(T) == 4 && do_cs) {
+#pragma unroll
+               for (int t = 0; t < 4; t++)
+                  ok &= fixed52_add((float) q[t], part);
+            }
+         }
+      }
+      if (sizeof(T) == 4 && do_cs)
+         fixed52_flush(part, lo, hi);
+      __syncwarp();
+      cur = nxt;
+      fix_cur = fix_next;
+      if (cur.var >= g.V)
+         break;
+      nxt = advance(nxt);
+   }
+   if (sizeof(T) == 4 && do_cs) {
+      if (cs_var >= 0)
+         warp_acc128_flush(lo, hi, acc + 2 * cs_var);
+      if (!ok)
+         atomicOr(err, ERR_FIXED_RANGE);
+   }
+}
+
+}  // namespace
+
+// CTAs per SM with wpc warps each; the kernel's dynamic shared memory limit
+// is raised once to what the largest shape (4 warps) needs.
+template <typename T>
+static int brick_per_sm(int wpc)
+{
+   int per_sm = 0;
+   cudaFuncSetAttribute(brick_stage_kernel<T>,
+                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                        (int) (Brick<T>::smem_per_warp() * 4));
+   cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, brick_stage_kernel<T>, 32 * wpc,
+      Brick<T>::smem_per_warp() * wpc);
+   return per_sm;
+}
+
+// Candidates: 4 or 2 warps per CTA, a persistent grid of the CTAs one
+// wave holds.  Shape fields: threads = 32 (one warp per item), vpc = warps
+// per CTA, rows = 2 (rows of 8 cells per lane), planes = 0 (marks this
+// kernel).
+template <typename T>
+void brick_candidates(const Geom &g, int stencil, int n_blocks,
+                      std::vector<StageShape> &out)
+{
+   if (stencil != 7 || dims_kind(g) != 1)
+      return;
+   int dev = 0, sms = 0;
+   cudaGetDevice(&dev);
+   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+   const long long items = (long long) n_blocks * g.V;
+   for (int wpc : {4, 2}) {
+      const int per_sm = brick_per_sm<T>(wpc);
+      if (per_sm <= 0)
+         continue;
+      StageShape sh;
+      sh.kernel = 1;
+      sh.threads = 32;
+      sh.vpc = wpc;
+      sh.rows = 2;
+      sh.planes = 0;
+      sh.grid = (int) std::max(1LL, std::min<long long>(
+                                       (long long) per_sm * sms,
+                                       (items + wpc - 1) / wpc));
+      out.push_back(sh);
+   }
+}
+
+template <typename T>
+int launch_brick_stage(const T *src, T *dst, const Geom &g,
+                       const BItem *items, int n_blocks, const StageShape &sh,
+                       int write_ghosts, int do_cs, unsigned long long *acc,
+                       unsigned *err, cudaStream_t s)
+{
+   if (n_blocks == 0)
+      return 0;
+   const size_t smem = Brick<T>::smem_per_warp() * sh.vpc;
+   brick_stage_kernel<T><<<sh.grid, 32 * sh.vpc, smem, s>>>(
+      src, dst, g, items, n_blocks, write_ghosts, sizeof(T) == 4 ? do_cs : 0,
+      acc, err);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+template void brick_candidates<float>(const Geom &, int, int,
+                                      std::vector<StageShape> &);
+template void brick_candidates<double>(const Geom &, int, int,
+                                       std::vector<StageShape> &);
+template int launch_brick_stage<float>(const float *, float *, const Geom &,
+                                       const BItem *, int, const StageShape &,
+                                       int, int, unsigned long long *,
+                                       unsigned *, cudaStream_t);
+template int launch_brick_stage<double>(const double *, double *,
+                                        const Geom &, const BItem *, int,
+                                        const StageShape &, int, int,
+                                        unsigned long long *, unsigned *,
+                                        cudaStream_t);
+
+}  // namespace mamr

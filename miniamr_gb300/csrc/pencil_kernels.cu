@@ -28,6 +28,7 @@
 
 #include "batched.h"
 #include "arith.cuh"
+#include "cp_async.cuh"
 
 namespace mamr {
 
@@ -57,21 +58,6 @@ template <typename T, int JP, int IH> struct Shape {
    static constexpr int THREADS = 1024 / (JP * IH);
    static constexpr int CTAS = sizeof(T) == 4 ? 3 : 1;
 };
-
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-   unsigned s = (unsigned) __cvta_generic_to_shared(smem);
-   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s),
-                "l"(gmem));
-}
-__device__ __forceinline__ void cp_async_commit()
-{
-   asm volatile("cp.async.commit_group;\n" ::);
-}
-__device__ __forceinline__ void cp_async_wait_all()
-{
-   asm volatile("cp.async.wait_all;\n" ::: "memory");
-}
 
 // Four consecutive k values (16-byte aligned).
 template <typename T> struct Quad;
@@ -196,15 +182,11 @@ __device__ __forceinline__ void row6(const T *tq, const T *eg, int i, int j,
 
 template <typename T>
 __device__ __forceinline__ void checksum4(const T (&out)[4], bool &ok,
-                                          unsigned long long &lo,
-                                          unsigned long long &hi)
+                                          Fixed52 &part)
 {
 #pragma unroll
-   for (int m = 0; m < 4; m++) {
-      long long q;
-      ok &= fixed52((float) out[m], q);
-      acc128_add(lo, hi, q);
-   }
+   for (int m = 0; m < 4; m++)
+      ok &= fixed52_add((float) out[m], part);
 }
 
 __device__ __forceinline__ float div_rn_inline(float x, float c)
@@ -220,6 +202,7 @@ __device__ __forceinline__ double div_rn_inline(double x, double c)
 struct PassState {
    bool slow;                       // some sum fell outside div_window
    bool ok;                         // every FP32 checksum term in range
+   Fixed52 part;                    // this tile's FP32 checksum terms
    unsigned long long lo, hi;       // FP32 fixed-point checksum
 };
 
@@ -240,7 +223,7 @@ __device__ __forceinline__ void emit4(const T (&w)[4], T *p, int do_cs,
       }
       Quad<T>::st(p, q);
       if (sizeof(T) == 4 && do_cs)
-         checksum4(q, st.ok, st.lo, st.hi);
+         checksum4(q, st.ok, st.part);
    } else {
 #pragma unroll
       for (int m = 0; m < 4; m++)
@@ -249,11 +232,8 @@ __device__ __forceinline__ void emit4(const T (&w)[4], T *p, int do_cs,
             const T qc = div_rn_inline(w[m], (T) C);
             p[m] = qc;
             if (sizeof(T) == 4 && do_cs) {
-               long long a, b;
-               st.ok &= fixed52((float) qc, a);
-               fixed52((float) qf, b);
-               acc128_add(st.lo, st.hi, a);
-               acc128_add(st.lo, st.hi, -b);
+               st.ok &= fixed52_add((float) qc, st.part);
+               fixed52_add((float) qf, st.part, true);
             }
          }
    }
@@ -463,6 +443,8 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
          tile_pass<T, ST, JP, IH, false>(tq, eg, d, kq, do_cs, st);
          if (__any_sync(0xffffffffu, st.slow))
             st = tile_fix<T, ST, JP, IH>(tq, eg, d, kq, do_cs, st);
+         if (sizeof(T) == 4 && do_cs)
+            fixed52_flush(st.part, st.lo, st.hi);
          if (write_ghosts) {
             T *base = dst + bv_offset(g, slot, var);
             // the ghost cells comm() writes: face interiors for 7 points,

@@ -305,15 +305,17 @@ checksum_fp32_kernel(const float *__restrict__ pool, Geom g,
 {
    const float *base = pool + bv_offset(g, slots[blockIdx.x], var);
    unsigned long long lo = 0, hi = 0;
+   Fixed52 part;
    bool ok = true;
    const int cells = g.nx * g.ny * g.nz;
-   for (int e = threadIdx.x; e < cells; e += blockDim.x) {
+   for (int e = threadIdx.x, t = 1; e < cells; e += blockDim.x, t++) {
       int i = e / (g.ny * g.nz) + 1, r = e % (g.ny * g.nz);
       int j = r / g.nz + 1, k = r % g.nz + 1;
-      long long q;
-      ok &= fixed52(base[cell_offset(g, i, j, k)], q);
-      acc128_add(lo, hi, q);
+      ok &= fixed52_add(base[cell_offset(g, i, j, k)], part);
+      if ((t & 255) == 0)
+         fixed52_flush(part, lo, hi);
    }
+   fixed52_flush(part, lo, hi);
    if (!ok)
       atomicOr(err, ERR_FIXED_RANGE);
    block_acc128_flush(lo, hi, acc);

@@ -57,18 +57,35 @@ def test_batched_equals_plain_uniform(gpu_lib, case, dtype, flags):
 def test_batched_equals_plain_amr7(gpu_lib, name, dtype):
     """7-point stencil on the reference's own multi-level meshes (states
     reached by replaying its recorded runs): face ghosts across level jumps
-    (coarse/4 and 4-cell sums) gathered inside the fused kernel."""
+    (coarse/4 and 4-cell sums) gathered inside the fused kernel, by every
+    launch-shape candidate (amr7's 8^3 blocks include the warp-per-block
+    kernel's)."""
     recs = read_trace(trace_path(name))
-    outs = []
-    for fl in (0, RUN_BATCHED | RUN_GRAPH):
-        res = replay(gpu_lib, recs, dtype=dtype)
-        assert len(np.unique(res.mesh["level"])) > 1
-        s = res.ctx.run_timesteps(2, 2, 1, flags=fl)
-        cap = res.ctx.cfg.max_blocks
-        outs.append((s, res.ctx.download(np.arange(cap))))
-        res.ctx.close()
-    for a, b in zip(outs[0], outs[1]):
-        assert np.array_equal(bits(a), bits(b))
+    res = replay(gpu_lib, recs, dtype=dtype)
+    assert len(np.unique(res.mesh["level"])) > 1
+    ctx = res.ctx
+    cap = ctx.cfg.max_blocks
+    every = np.arange(cap)
+    state = ctx.download(every)
+
+    def run(flags, choice=None):
+        ctx.upload(every, state)
+        ctx.set_tuning(-1 if choice is None else choice)
+        s = ctx.run_timesteps(2, 2, 1, flags=flags)
+        return s, ctx.download(every), ctx.tuning()
+
+    ref = run(0)
+    n = run(RUN_BATCHED)[2]["candidates"]
+    kernels = set()
+    for k in range(n):
+        got = run(RUN_BATCHED | RUN_GRAPH, k)
+        assert got[2]["choice"] == k
+        kernels.add(got[2]["planes_per_thread"] == 0)
+        for a, b in zip(ref[:2], got[:2]):
+            assert np.array_equal(bits(a), bits(b)), (k, got[2])
+    if name == "amr7":
+        assert kernels == {True, False}
+    ctx.close()
 
 
 SHAPE_CASES = [
