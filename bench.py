@@ -326,6 +326,45 @@ def stress_multilevel(lib, dtype):
             "replay_seconds_incl_refinement_and_host": total}
 
 
+def refine_marking(lib):
+    """Refinement marking (mamr_mark_refine: reset_all, check_objects and
+    refine_level of one rank) on the recorded steps of the multi-level
+    stress run (config5.mark.xz: about 20k blocks of five levels, four
+    moving objects).  Time per call -- block and parent lists to the device,
+    the object tests and the rule passes, flags back -- after two warm-up
+    calls, best of three, against the CPU oracle on one thread; both checked
+    against the reference's own flags."""
+    from miniamr_gb300 import build
+    from miniamr_gb300.abi import Config, Library
+    from miniamr_gb300.trace import read_marks
+    path = os.path.join(REPO, "tests", "golden", "config5.mark.xz")
+    if not os.path.exists(path):
+        return None
+    steps = read_marks(path)
+    cap = max(int(st.blocks["slot"].max()) for st in steps) + 1
+    out = {"steps": len(steps), "blocks": [len(st.blocks) for st in steps],
+           "objects": len(steps[0].objects)}
+    for name, L in (("gpu", lib), ("cpu_oracle_1_thread",
+                                   Library(build.build_oracle()))):
+        ms, same = [], True
+        with L.context(Config.make(*steps[0].block_size, 1, cap)) as ctx:
+            for st in steps:
+                ts = []
+                for _ in range(5):
+                    t0 = time.perf_counter()
+                    br, pr = ctx.mark_refine(st.params, st.objects,
+                                             st.blocks, st.parents)
+                    ts.append(time.perf_counter() - t0)
+                act = st.parents["active"] == 1
+                same &= bool(np.array_equal(br, st.block_refine) and
+                             np.array_equal(pr[act], st.parent_refine[act]))
+                ms.append(min(ts[2:]) * 1e3)
+        out[name + "_ms"] = ms
+        out[name + "_flags_equal_reference"] = same
+    out["speedup"] = sum(out["cpu_oracle_1_thread_ms"]) / sum(out["gpu_ms"])
+    return out
+
+
 def profile_case(name):
     """Small batched runs for ncu captures, launched stage by stage (no
     graph), with the stage kernel's launch shape forced to candidate
@@ -576,6 +615,7 @@ def main():
             "uniform_stencil0_fp64": uniform_stencil0(lib),
             "stress_multilevel_7pt_fp32": stress_multilevel(lib, FP32),
             "stress_multilevel_7pt_fp64": stress_multilevel(lib, FP64),
+            "refine_marking_stress": refine_marking(lib),
         }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         one = one_thread_oracle_rate()

@@ -99,6 +99,49 @@ typedef struct {
    int32_t target;
 } mamr_consolidate_job;
 
+/* ---- refinement marking types (ref/move.c, ref/refine.c) -------------- */
+
+/* One refinement object after move() (ref/block.h object; ref/move.c:37-63
+ * moves it on the host).  type: 0 surface / 1 solid box; 2..15 spheroid,
+ * even = surface, odd = solid, 4..15 the half on one side of the centre
+ * plane (4/5 x < centre dropped ... 14/15 z > centre dropped, as
+ * ref/move.c:369-382 and 489-502); 20/22/24 cylinder surface along x/y/z,
+ * 21/23/25 solid.  Any negative size disables the object. */
+typedef struct {
+   int32_t type;
+   int32_t reserved;     /* must be zero */
+   double cen[3];
+   double size[3];
+} mamr_object;
+
+/* The globals the marking reads (ref/block.h:83-137). */
+typedef struct {
+   int32_t num_refine;      /* maximum level */
+   int32_t refine_ghost;    /* --refine_ghost: test the extent with ghosts */
+   int32_t uniform_refine;  /* --uniform_refine: every block below the
+                               maximum level refines; no objects */
+   int32_t mesh_size[3];    /* mesh_size[] (ref/init.c:430-437) */
+   int32_t reserved[10];    /* must be zero */
+} mamr_mark_params;
+
+/* One active block as the marking sees it (ref/block.h:36-53). */
+typedef struct {
+   int32_t slot;            /* index into blocks[] */
+   int32_t level;
+   int32_t parent;          /* index into parents[], -1 for an initial block */
+   int32_t cen[3];          /* integer centre */
+   int32_t nei_level[6];    /* W,E,S,N,D,U; -2 = boundary */
+   int32_t nei[6];          /* nei[l][0][0]: blocks[] index of a same-level
+                               or coarser neighbour (ignored otherwise) */
+} mamr_mark_block;
+
+/* One entry of parents[] (ref/block.h:55-70). */
+typedef struct {
+   int32_t active;          /* parents[p].number >= 0 */
+   int32_t child[8];        /* blocks[] index, or -1 - (parents[] index)
+                               for a child that is itself a parent */
+} mamr_mark_parent;
+
 /* Flags for mamr_run_timesteps(). */
 enum {
    MAMR_RUN_PLAIN   = 0,  /* per-call path: comm, then stencil/check_sum per
@@ -200,6 +243,28 @@ int mamr_run_timesteps(mamr_ctx *ctx, int32_t num_ts, int32_t stages_per_ts,
 /* Number of kernels this context has launched since creation (for the
  * launch counts the benchmark reports). */
 int mamr_launch_count(mamr_ctx *ctx, int64_t *count);
+
+/* ---- refinement marking ------------------------------------------------ */
+
+/* The refine decisions of one refinement step on one rank: what
+ * reset_all() (ref/refine.c:500-527), check_objects() (ref/move.c:65-141,
+ * with check_block :143-623) -- or the uniform_refine assignment
+ * (ref/refine.c:68-74) -- and refine_level() (ref/refine.c:325-496) leave
+ * in blocks[].refine and parents[].refine (1 refine, 0 stay, -1 coarsen),
+ * computed on the device.  On one rank comm_refine(), comm_parent() and
+ * comm_parent_reverse() exchange nothing, and every rule of those routines
+ * only raises a flag (-1 < 0 < 1), so the result is the least fixed point
+ * of the rules above the initial state whatever order they are applied
+ * in; the device applies them to all blocks at once until nothing
+ * changes.  blocks[] lists the active blocks (any order); block_refine[i]
+ * receives blocks[i]'s flag and parent_refine[p] parents[p]'s for the
+ * active entries.  The cell block size is the context's.  Returns
+ * MAMR_EINVAL for indices out of range. */
+int mamr_mark_refine(mamr_ctx *ctx, const mamr_mark_params *params,
+                     const mamr_object *objects, int32_t n_objects,
+                     const mamr_mark_block *blocks, int32_t n_blocks,
+                     const mamr_mark_parent *parents, int32_t n_parents,
+                     int32_t *block_refine, int32_t *parent_refine);
 
 /* ---- launch-shape autotuner of the batched path ------------------------ */
 

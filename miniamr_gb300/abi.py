@@ -41,6 +41,32 @@ BLOCK_DTYPE = np.dtype([
 SPLIT_DTYPE = np.dtype([("parent", "<i4"), ("child", "<i4", (8,))])
 # struct mamr_consolidate_job
 CONSOLIDATE_DTYPE = np.dtype([("child", "<i4", (8,)), ("target", "<i4")])
+# struct mamr_object
+OBJECT_DTYPE = np.dtype([("type", "<i4"), ("reserved", "<i4"),
+                         ("cen", "<f8", (3,)), ("size", "<f8", (3,))])
+# struct mamr_mark_block
+MARK_BLOCK_DTYPE = np.dtype([
+    ("slot", "<i4"), ("level", "<i4"), ("parent", "<i4"),
+    ("cen", "<i4", (3,)), ("nei_level", "<i4", (6,)), ("nei", "<i4", (6,)),
+])
+# struct mamr_mark_parent
+MARK_PARENT_DTYPE = np.dtype([("active", "<i4"), ("child", "<i4", (8,))])
+
+
+class MarkParams(C.Structure):
+    """struct mamr_mark_params."""
+
+    _fields_ = [
+        ("num_refine", C.c_int32), ("refine_ghost", C.c_int32),
+        ("uniform_refine", C.c_int32), ("mesh_size", C.c_int32 * 3),
+        ("reserved", C.c_int32 * 10),
+    ]
+
+    @classmethod
+    def make(cls, num_refine, mesh_size, refine_ghost=0,
+             uniform_refine=0) -> "MarkParams":
+        return cls(num_refine, refine_ghost, uniform_refine,
+                   (C.c_int32 * 3)(*mesh_size))
 
 
 class MamrError(RuntimeError):
@@ -103,6 +129,8 @@ class Library:
             "mamr_set_work_params": [vp, C.c_double, vp, C.c_int32],
             "mamr_get_tuning": [vp, C.POINTER(C.c_int32),
                                 C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
+            "mamr_mark_refine": [vp, C.POINTER(MarkParams), vp, i32, vp,
+                                 i32, vp, i32, vp, vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -226,6 +254,20 @@ class Context:
         (mamr_set_work_params)."""
         a0 = np.ascontiguousarray(a0, dtype=np.float64)
         self._call("mamr_set_work_params", float(a1), _ptr(a0), len(a0))
+
+    def mark_refine(self, params: "MarkParams", objects, blocks, parents):
+        """Refine flags of one refinement step (mamr_mark_refine): returns
+        (flags of `blocks` in their order, flags of `parents`, -2 for the
+        inactive entries)."""
+        objects = np.ascontiguousarray(objects, dtype=OBJECT_DTYPE)
+        blocks = np.ascontiguousarray(blocks, dtype=MARK_BLOCK_DTYPE)
+        parents = np.ascontiguousarray(parents, dtype=MARK_PARENT_DTYPE)
+        bref = np.zeros(max(len(blocks), 1), dtype=np.int32)
+        pref = np.full(max(len(parents), 1), -2, dtype=np.int32)
+        self._call("mamr_mark_refine", C.byref(params), _ptr(objects),
+                   len(objects), _ptr(blocks), len(blocks), _ptr(parents),
+                   len(parents), _ptr(bref), _ptr(pref))
+        return bref[:len(blocks)], pref[:len(parents)]
 
     def run_timesteps(self, num_ts: int, stages_per_ts: int,
                       checksum_freq: int, first_stage: int = 0,

@@ -19,6 +19,7 @@
 
 #include "mamr_internal.h"
 #include "batched.h"
+#include "mark_geometry.h"
 #include "segments.h"
 
 using namespace mamr;
@@ -98,6 +99,8 @@ const int kPerm[6][3] = { {0, 1, 2}, {1, 2, 0}, {2, 0, 1},
 namespace mamr {
 struct BatchedState {
    DevBuf items, partials, sums, acc, chain, pencils;
+   BItem *h_items = nullptr;   // pinned staging of the item upload
+   size_t h_cap = 0;           // its capacity in items
    int n = 0;
    bool valid = false;
    bool single_level = false;
@@ -110,6 +113,8 @@ void batched_destroy(BatchedState *b)
       return;
    b->items.release(); b->partials.release(); b->sums.release();
    b->acc.release(); b->chain.release(); b->pencils.release();
+   if (b->h_items)
+      cudaFreeHost(b->h_items);
    delete b;
 }
 void batched_mesh_changed(BatchedState *b)
@@ -145,6 +150,7 @@ struct mamr_ctx {
    mamr_work_par work{};            // --stencil 0 coefficients
    bool work_set = false;
    DevBuf d_work;                   // --stencil 0 work values
+   DevBuf d_mark;                   // refinement marking lists and flags
    int tune_force = -1;             // forced launch-shape candidate
    int tune_last = -1, tune_n = 0;  // last batched run's choice / count
    mamr::StageShape tune_shape;
@@ -163,6 +169,8 @@ static int check_error_word(mamr_ctx *c)
       if (h & ERR_FIXED_RANGE)
          return fail(MAMR_EDEVICE, "a cell is outside the FP32 checksum's "
                      "fixed-point range (|v| < 1024, finite)");
+      if (h & ERR_MARK)
+         return fail(MAMR_EDEVICE, "refinement marking did not settle");
       return fail(MAMR_EDEVICE, "device error word 0x%x", h);
    }
    return MAMR_OK;
@@ -262,6 +270,7 @@ extern "C" int mamr_destroy(mamr_ctx *c)
    c->d_slots.release(); c->d_partials.release(); c->d_jobs.release();
    c->d_stage.release(); c->d_stage_slots.release(); c->d_sums.release();
    c->d_xfer.release(); c->d_xfer_slots.release(); c->d_work.release();
+   c->d_mark.release();
    if (c->d_acc) cudaFree(c->d_acc);
    if (c->d_sum) cudaFree(c->d_sum);
    if (c->d_err) cudaFree(c->d_err);
@@ -853,16 +862,27 @@ static int build_items(mamr_ctx *c)
 {
    BatchedState *B = c->batched;
    const int n = (int) c->mesh.size();
-   std::vector<BItem> items(std::max(1, n));
+   // built straight into pinned memory (reused across meshes), so that the
+   // upload runs at full copy speed
+   if (B->h_cap < (size_t) std::max(1, n)) {
+      if (B->h_items)
+         cudaFreeHost(B->h_items);
+      B->h_items = nullptr;
+      B->h_cap = 0;
+      const size_t want = (size_t) std::max(1, n) * 5 / 4 + 64;
+      CUDA_TRY(cudaMallocHost((void **) &B->h_items, sizeof(BItem) * want));
+      B->h_cap = want;
+   }
+   BItem *items = B->h_items;
    bool single = true;
    const int lev0 = n ? c->mesh[0].level : 0;
+   for (int q = 0; q < n; q++)
+      single = single && c->mesh[q].level == lev0;
    for (int q = 0; q < n; q++) {
       const mamr_block &bp = c->mesh[q];
       BItem &it = items[q];
       memset(&it, 0, sizeof(it));
       it.slot = bp.slot;
-      if (bp.level != lev0)
-         single = false;
       for (int l = 0; l < 6; l++) {
          BFace &f = it.f[l];
          const int nl = bp.nei_level[l];
@@ -897,7 +917,12 @@ static int build_items(mamr_ctx *c)
                            "coarser neighbour %d", bp.slot, m);
          }
       }
-      // neighbours across edges and corners: hop x, then y, then z
+      // neighbours across edges and corners, for single-level meshes only
+      // (27-point edge/corner ghosts and the pencil kernel's in-plane
+      // neighbours; neither applies to a multi-level mesh): hop x, then y,
+      // then z
+      if (!single)
+         continue;
       for (int dz = -1; dz <= 1; dz++)
          for (int dy = -1; dy <= 1; dy++)
             for (int dx = -1; dx <= 1; dx++) {
@@ -966,9 +991,9 @@ static int build_items(mamr_ctx *c)
          B->n_pencils = (int) pencils.size();
       }
    }
-   CUDA_TRY(B->items.ensure(sizeof(BItem) * items.size()));
-   CUDA_TRY(cudaMemcpyAsync(B->items.p, items.data(),
-                            sizeof(BItem) * items.size(),
+   const size_t n_items = (size_t) std::max(1, n);
+   CUDA_TRY(B->items.ensure(sizeof(BItem) * n_items));
+   CUDA_TRY(cudaMemcpyAsync(B->items.p, items, sizeof(BItem) * n_items,
                             cudaMemcpyHostToDevice, c->stream));
    CUDA_TRY(cudaStreamSynchronize(c->stream));
    B->n = n;
@@ -1270,6 +1295,70 @@ extern "C" int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts,
       return fail(MAMR_EINVAL, "MAMR_RUN_PER_BLOCK applies to the plain path");
    return run_batched(c, num_ts, stages_per_ts, checksum_freq,
                       (flags & MAMR_RUN_GRAPH) != 0, sums, n_sums);
+}
+
+extern "C" int mamr_mark_refine(mamr_ctx *c, const mamr_mark_params *p,
+                                const mamr_object *objs, int32_t n_objs,
+                                const mamr_mark_block *mb, int32_t nb,
+                                const mamr_mark_parent *pa, int32_t np,
+                                int32_t *block_refine, int32_t *parent_refine)
+{
+   if (!c || (nb && !block_refine) || (np && !parent_refine))
+      return fail(MAMR_EINVAL, "mark_refine: bad arguments");
+   const int32_t cap = c->cfg.max_blocks;
+   std::vector<unsigned char> listed((size_t) cap + 1, 0);
+   if (const char *msg = mamr_mark_validate(p, objs, n_objs, mb, nb, pa, np,
+                                            cap, listed.data()))
+      return fail(MAMR_EINVAL, "%s", msg);
+   // one device allocation: objects, blocks, parents, flags by slot,
+   // parent flags, output, each 256-byte aligned
+   auto up = [](size_t b) { return (b + 255) & ~(size_t) 255; };
+   const size_t b_obj = up(sizeof(mamr_object) * n_objs),
+                b_mb = up(sizeof(mamr_mark_block) * nb),
+                b_pa = up(sizeof(mamr_mark_parent) * np),
+                b_ref = up(sizeof(int32_t) * cap),
+                b_pref = up(sizeof(int32_t) * np),
+                b_out = up(sizeof(int32_t) * nb), b_flags = up(3 * sizeof(int));
+   CUDA_TRY(c->d_mark.ensure(b_obj + b_mb + b_pa + b_ref + b_pref + b_out +
+                             b_flags));
+   char *base = (char *) c->d_mark.p;
+   mamr_object *d_obj = (mamr_object *) base;
+   mamr_mark_block *d_mb = (mamr_mark_block *) (base + b_obj);
+   mamr_mark_parent *d_pa = (mamr_mark_parent *) (base + b_obj + b_mb);
+   int32_t *d_ref = (int32_t *) (base + b_obj + b_mb + b_pa);
+   int32_t *d_pref = (int32_t *) ((char *) d_ref + b_ref);
+   int32_t *d_out = (int32_t *) ((char *) d_pref + b_pref);
+   int *d_flags = (int *) ((char *) d_out + b_out);
+   if (n_objs)
+      CUDA_TRY(cudaMemcpyAsync(d_obj, objs, sizeof(mamr_object) * n_objs,
+                               cudaMemcpyHostToDevice, c->stream));
+   if (nb)
+      CUDA_TRY(cudaMemcpyAsync(d_mb, mb, sizeof(mamr_mark_block) * nb,
+                               cudaMemcpyHostToDevice, c->stream));
+   if (np)
+      CUDA_TRY(cudaMemcpyAsync(d_pa, pa, sizeof(mamr_mark_parent) * np,
+                               cudaMemcpyHostToDevice, c->stream));
+   const int k = launch_mark_refine(
+      *p, make_int3(c->cfg.nx, c->cfg.ny, c->cfg.nz), d_obj, n_objs, d_mb,
+      nb, d_pa, np, cap, d_ref, d_pref, d_out, d_flags, c->d_err, c->stream);
+   if (k < 0)
+      return fail(MAMR_ECUDA, "mark_refine launch: %s",
+                  cudaGetErrorString(cudaGetLastError()));
+   c->launches += k;
+   std::vector<int32_t> hp((size_t) np);
+   if (nb)
+      CUDA_TRY(cudaMemcpyAsync(block_refine, d_out, sizeof(int32_t) * nb,
+                               cudaMemcpyDeviceToHost, c->stream));
+   if (np)
+      CUDA_TRY(cudaMemcpyAsync(hp.data(), d_pref, sizeof(int32_t) * np,
+                               cudaMemcpyDeviceToHost, c->stream));
+   int r = check_error_word(c);        // synchronises the stream
+   if (r)
+      return r;
+   for (int32_t q = 0; q < np; q++)
+      if (pa[q].active)
+         parent_refine[q] = hp[q];
+   return MAMR_OK;
 }
 
 extern "C" int mamr_set_tuning(mamr_ctx *c, int32_t choice)

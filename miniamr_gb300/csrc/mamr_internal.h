@@ -68,7 +68,8 @@ struct DirTasks {
 // Error word bits written by kernels (context error word).
 enum : unsigned {
    ERR_FIXED_RANGE = 1u,   // a cell outside the fixed-point checksum range
-   ERR_TASK = 2u           // a task that does not fit the geometry
+   ERR_TASK = 2u,          // a task that does not fit the geometry
+   ERR_MARK = 4u           // refinement marking did not settle
 };
 
 // --stencil 0: the variable-work kernel of calc_stage % 6 and
@@ -118,5 +119,16 @@ int launch_upload(T *pool, const Geom &g, const int32_t *slots, int n,
 template <typename T>
 int launch_download(const T *pool, const Geom &g, const int32_t *slots,
                     int n, double *dense, cudaStream_t s);
+
+// Refinement marking (mark_kernels.cu): flags of the listed blocks into
+// d_out (list order) and of the parents into d_pref; d_ref holds
+// max_blocks flags by slot, d_flags 3 pass flags.  Returns kernels
+// launched or -1.
+int launch_mark_refine(const mamr_mark_params &p, int3 bsize,
+                       const mamr_object *d_objs, int n_objs,
+                       const mamr_mark_block *d_mb, int nb,
+                       const mamr_mark_parent *d_pa, int np, int max_blocks,
+                       int32_t *d_ref, int32_t *d_pref, int32_t *d_out,
+                       int *d_flags, unsigned *err, cudaStream_t s);
 
 }  // namespace mamr

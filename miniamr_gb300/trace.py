@@ -277,3 +277,60 @@ def replay_batched(lib: Library, records: list[Record], flags: int,
                 stage[2].append(r.args)
     flush()
     return sums, ctx, timings
+
+
+@dataclass
+class MarkStep:
+    """One refinement step's marking as the reference computed it: the
+    inputs of mamr_mark_refine and the reference's flags (oracle/ref_hooks.c
+    writes them at each split_blocks() call)."""
+    call: int
+    block_size: tuple
+    params: object
+    objects: np.ndarray
+    blocks: np.ndarray
+    parents: np.ndarray
+    block_refine: np.ndarray
+    parent_refine: np.ndarray
+
+
+def read_marks(path: str) -> list[MarkStep]:
+    """Parses a marking dump (format in oracle/ref_hooks.c)."""
+    from .abi import (MARK_BLOCK_DTYPE, MARK_PARENT_DTYPE, OBJECT_DTYPE,
+                      MarkParams)
+    lines = _open(path).decode().splitlines()
+    steps, i = [], 0
+    while i < len(lines):
+        h = lines[i].split()
+        if h[0] != "step":
+            raise ValueError(f"{path}: line {i + 1}: expected a step")
+        call, nb, npar, nref, ghost, uni, m0, m1, m2, bx, by, bz, nobj = \
+            map(int, h[1:])
+        i += 1
+        objs = np.zeros(nobj, dtype=OBJECT_DTYPE)
+        for o in range(nobj):
+            f = lines[i + o].split()
+            objs[o]["type"] = int(f[1])
+            v = np.array([int(x, 16) for x in f[2:8]], dtype=np.uint64)
+            d = v.view(np.float64)
+            objs[o]["cen"] = d[:3]
+            objs[o]["size"] = d[3:]
+        i += nobj
+        b = np.array([list(map(int, lines[i + k].split()[1:]))
+                      for k in range(nb)], dtype=np.int32).reshape(nb, 19)
+        i += nb
+        p = np.array([list(map(int, lines[i + k].split()[1:]))
+                      for k in range(npar)], dtype=np.int32).reshape(npar, 11)
+        i += npar
+        blocks = np.zeros(nb, dtype=MARK_BLOCK_DTYPE)
+        blocks["slot"], blocks["level"], blocks["parent"] = b[:, 0], b[:, 1], \
+            b[:, 2]
+        blocks["cen"], blocks["nei_level"], blocks["nei"] = b[:, 3:6], \
+            b[:, 6:12], b[:, 12:18]
+        parents = np.zeros(npar, dtype=MARK_PARENT_DTYPE)
+        parents["active"], parents["child"] = p[:, 1], p[:, 2:10]
+        steps.append(MarkStep(
+            call, (bx, by, bz),
+            MarkParams.make(nref, (m0, m1, m2), ghost, uni), objs, blocks,
+            parents, b[:, 18].copy(), p[:, 10].copy()))
+    return steps

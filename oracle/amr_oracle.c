@@ -26,6 +26,8 @@
 
 #include "miniamr_gb300.h"
 #include "work_formulas.h"
+#define MAMR_MFN static inline
+#include "mark_geometry.h"
 
 struct mamr_ctx {
    mamr_config cfg;
@@ -968,5 +970,116 @@ int mamr_work_coefficients(int32_t num_vars, double *a1, double *a0)
       random_r(&rd, &r);
       a0[i] = ((double) r) / ((double) RAND_MAX);
    }
+   return MAMR_OK;
+}
+
+/* ---- refinement marking ------------------------------------------------- */
+
+/* Raises *x to v (flags only rise: -1 < 0 < 1); counts the change. */
+static void mark_raise(int32_t *x, int32_t v, int *changed)
+{
+   if (*x < v) {
+      *x = v;
+      *changed = 1;
+   }
+}
+
+/* reset_all + check_objects (or the uniform assignment) + refine_level on
+ * one rank (ref/refine.c:500-527, ref/move.c:65-623, ref/refine.c:68-74,
+ * 325-496), as the least fixed point of their rules, applied in passes
+ * over all blocks until none changes:
+ *   initial   a block: 1 if an object meets it (0 at the maximum level),
+ *             else 0 if, with refine_ghost, one meets its parent's extent,
+ *             else 0 at level 0, else -1 (uniform: 1 below the maximum
+ *             level, 0 at it); a parent: 0 if a child is itself a parent,
+ *             else -1;
+ *   family    a block at 1 -- or at 0, except the initial zeros of the
+ *             uniform assignment, whose families the reference never
+ *             touches -- raises its parent to 0; a parent at 0 raises its
+ *             children to 0 (ref/move.c:124-135, refine.c:348-359);
+ *   refine    a block at 1 raises same-level neighbours to 0 and coarser
+ *             ones to 1 (refine.c:360-396);
+ *   keep      a block with a finer neighbour rises to 0 (refine.c:397-415);
+ *             a block at 0 raises coarser neighbours to 0
+ *             (refine.c:437-462). */
+int mamr_mark_refine(mamr_ctx *c, const mamr_mark_params *p,
+                     const mamr_object *objs, int32_t n_objs,
+                     const mamr_mark_block *mb, int32_t nb,
+                     const mamr_mark_parent *pa, int32_t np,
+                     int32_t *block_refine, int32_t *parent_refine)
+{
+   const int32_t cap = c ? c->cfg.max_blocks : 0;
+   unsigned char *listed;
+   int32_t *ref, *pref, i, k;
+   const char *msg;
+   int changed, uni, bsize[3];
+   if (!c || (nb && !block_refine) || (np && !parent_refine))
+      return fail(MAMR_EINVAL, "mark_refine: bad arguments");
+   listed = (unsigned char *) calloc((size_t) cap + 1, 1);
+   ref = (int32_t *) malloc(sizeof(int32_t) * ((size_t) cap + 1));
+   pref = (int32_t *) malloc(sizeof(int32_t) * ((size_t) np + 1));
+   if (!listed || !ref || !pref) {
+      free(listed); free(ref); free(pref);
+      return fail(MAMR_ENOMEM, "mark_refine: out of host memory");
+   }
+   if ((msg = mamr_mark_validate(p, objs, n_objs, mb, nb, pa, np, cap,
+                                 listed))) {
+      free(listed); free(ref); free(pref);
+      return fail(MAMR_EINVAL, "%s", msg);
+   }
+   uni = p->uniform_refine != 0;
+   bsize[0] = c->cfg.nx; bsize[1] = c->cfg.ny; bsize[2] = c->cfg.nz;
+   for (i = 0; i < np; i++) {
+      pref[i] = -1;
+      for (k = 0; k < 8; k++)
+         if (pa[i].child[k] < 0)
+            pref[i] = 0;
+   }
+   for (i = 0; i < nb; i++) {
+      const mamr_mark_block *b = &mb[i];
+      int r;
+      if (uni) {
+         r = b->level < p->num_refine ? 1 : 0;
+      } else {
+         r = mamr_mg_block_state(b->cen, b->level, p, bsize, objs, n_objs);
+         if (r == 1 && b->level == p->num_refine)
+            r = 0;
+         if (r == -1 && b->level == 0)
+            r = 0;
+      }
+      ref[b->slot] = r;
+   }
+   do {
+      changed = 0;
+      for (i = 0; i < nb; i++) {
+         const mamr_mark_block *b = &mb[i];
+         const int32_t v = ref[b->slot];
+         int l;
+         if ((v == 1 || (v == 0 && !uni)) && b->parent >= 0)
+            mark_raise(&pref[b->parent], 0, &changed);
+         for (l = 0; l < 6; l++) {
+            const int nl = b->nei_level[l];
+            if (nl == b->level + 1)
+               mark_raise(&ref[b->slot], 0, &changed);
+            else if (v == 1 && nl == b->level)
+               mark_raise(&ref[b->nei[l]], 0, &changed);
+            else if (v >= 0 && nl == b->level - 1)
+               mark_raise(&ref[b->nei[l]], v, &changed);
+         }
+      }
+      for (i = 0; i < np; i++)
+         if (pa[i].active && pref[i] >= 0)
+            for (k = 0; k < 8; k++) {
+               const int32_t ch = pa[i].child[k];
+               if (ch >= 0 && listed[ch])
+                  mark_raise(&ref[ch], 0, &changed);
+            }
+   } while (changed);
+   for (i = 0; i < nb; i++)
+      block_refine[i] = ref[mb[i].slot];
+   for (i = 0; i < np; i++)
+      if (pa[i].active)
+         parent_refine[i] = pref[i];
+   free(listed); free(ref); free(pref);
    return MAMR_OK;
 }

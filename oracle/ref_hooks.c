@@ -18,6 +18,20 @@
  *     mesh <ts> <n_active> <hash of (slot,number,level,nei_level,nei,cen)>
  *
  * plus, when MAMR_REF_MESH_DUMP is set, the per-block records themselves.
+ *
+ * With -Wl,--wrap=split_blocks, when MAMR_MARK_DUMP names a file, every
+ * split_blocks() call (ref/refine.c:112, right after the marking of
+ * ref/refine.c:66-110) first appends the marking's inputs and results:
+ *
+ *     step <call#> <n_blocks> <n_parent_slots> <num_refine> <refine_ghost>
+ *          <uniform_refine> <mesh_size x3> <block size x3> <num_objects>
+ *     o <type> <cen x3> <size x3>          (doubles as 16 hex digits)
+ *     b <slot> <level> <parent> <cen x3> <nei_level x6> <nei[l][0][0] x6>
+ *       <refine>                           (active blocks, sorted order)
+ *     p <index> <active> <child x8> <refine>     (parents[0..max_active))
+ *
+ * MAMR_MARK_DUMP_EVERY=n keeps every n-th call, MAMR_MARK_DUMP_MAX=m at
+ * most m of them.
  * The hybrid build holds its cell data behind the mamr_* C ABI; there the
  * drop-in's mamr_dropin_fetch() (a weak reference here) supplies the cells.
  */
@@ -33,6 +47,7 @@
 
 double __real_check_sum(int var);
 void __real_refine(int ts);
+void __real_split_blocks(void);
 
 /* Provided by the drop-in check_sum.c replacement in the hybrid build. */
 extern int mamr_dropin_fetch(int slot, int var, double *out)
@@ -177,4 +192,70 @@ void __wrap_refine(int ts)
               (unsigned long long) h);
       fflush(fp);
    }
+}
+
+static long env_long(const char *name, long dflt)
+{
+   const char *p = getenv(name);
+   return (p && *p) ? atol(p) : dflt;
+}
+
+static void put_f64(FILE *fp, double x)
+{
+   uint64_t b;
+   memcpy(&b, &x, sizeof(b));
+   fprintf(fp, " %016llx", (unsigned long long) b);
+}
+
+void __wrap_split_blocks(void)
+{
+   static FILE *mfp;
+   static int opened;
+   static long calls, dumped;
+   if (!opened) {
+      const char *p = getenv("MAMR_MARK_DUMP");
+      opened = 1;
+      if (p && *p && !(mfp = fopen(p, "w"))) {
+         fprintf(stderr, "ref_hooks: cannot open %s\n", p);
+         exit(-1);
+      }
+   }
+   if (mfp && calls % env_long("MAMR_MARK_DUMP_EVERY", 1) == 0 &&
+       dumped < env_long("MAMR_MARK_DUMP_MAX", 1L << 30)) {
+      int in, o, l, d, k, nb = sorted_index[num_refine+1];
+      fprintf(mfp, "step %ld %d %d %d %d %d %d %d %d %d %d %d %d\n", calls,
+              nb, max_active_parent, num_refine, refine_ghost,
+              uniform_refine, mesh_size[0], mesh_size[1], mesh_size[2],
+              x_block_size, y_block_size, z_block_size, num_objects);
+      for (o = 0; o < num_objects; o++) {
+         fprintf(mfp, "o %d", objects[o].type);
+         for (d = 0; d < 3; d++)
+            put_f64(mfp, objects[o].cen[d]);
+         for (d = 0; d < 3; d++)
+            put_f64(mfp, objects[o].size[d]);
+         fprintf(mfp, "\n");
+      }
+      for (in = 0; in < nb; in++) {
+         int n = sorted_list[in].n;
+         block *bp = &blocks[n];
+         fprintf(mfp, "b %d %d %d %d %d %d", n, bp->level, (int) bp->parent,
+                 bp->cen[0], bp->cen[1], bp->cen[2]);
+         for (l = 0; l < 6; l++)
+            fprintf(mfp, " %d", bp->nei_level[l]);
+         for (l = 0; l < 6; l++)
+            fprintf(mfp, " %d", bp->nei[l][0][0]);
+         fprintf(mfp, " %d\n", bp->refine);
+      }
+      for (k = 0; k < max_active_parent; k++) {
+         parent *pp = &parents[k];
+         fprintf(mfp, "p %d %d", k, pp->number >= 0);
+         for (o = 0; o < 8; o++)
+            fprintf(mfp, " %d", (int) pp->child[o]);
+         fprintf(mfp, " %d\n", pp->refine);
+      }
+      fflush(mfp);
+      dumped++;
+   }
+   calls++;
+   __real_split_blocks();
 }

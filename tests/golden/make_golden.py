@@ -8,7 +8,9 @@ For every case in CASES it
   1. runs the unmodified reference (oracle/_ref/miniamr_ref) with its
      check_sum/refine hooks, producing <name>.reflog.xz: every checksum the
      reference computed (exact bits) with a hash of every cell of that
-     variable, and a hash of the mesh after each refine();
+     variable, and a hash of the mesh after each refine(); for the cases in
+     MARK also <name>.mark.xz: the inputs and the reference's flags of each
+     refinement step's marking (oracle/ref_hooks.c, split_blocks hook);
   2. runs the reference's driver over the drop-in translation units and the
      CPU oracle (oracle/_ref/miniamr_hybrid_trace), which must produce the
      identical log, and records every mamr_* call it made as
@@ -111,6 +113,65 @@ CASES = {
                  "2", "--num_tsteps", "8", "--stages_per_ts", "6",
                  "--checksum_freq", "1", "--error_tol", "0",
                  "--max_blocks", "4000"] + SPHERE,
+    # refinement marking across object types: surface and solid boxes,
+    # the x half-spheroids (surface and solid, both halves), surface and
+    # solid cylinders along x, a sphere whose negative x size (it grows)
+    # keeps it disabled for the first steps, and two solid spheres that
+    # leave the domain with bounce 2 and bounce 0 (neither reflects: the
+    # reference's bounce-2 branch cannot run); 4^3 blocks, 1 variable
+    "mark_shapes": ["--init_x", "2", "--init_y", "2", "--init_z", "2",
+                    "--nx", "4", "--ny", "4", "--nz", "4", "--num_vars", "1",
+                    "--stencil", "7", "--num_refine", "3", "--refine_freq",
+                    "1", "--num_tsteps", "10", "--stages_per_ts", "1",
+                    "--checksum_freq", "1", "--error_tol", "0",
+                    "--max_blocks", "20000", "--num_objects", "11",
+                    "--object", "0", "1", "0.3", "0.3", "0.3", "0.01",
+                    "0.02", "0.015", "0.12", "0.08", "0.1", "0", "0", "0",
+                    "--object", "1", "1", "0.7", "0.25", "0.6", "-0.02",
+                    "0.01", "0.0", "0.05", "0.07", "0.04", "0", "0", "0",
+                    "--object", "4", "1", "0.5", "0.7", "0.3", "0.0",
+                    "-0.01", "0.01", "0.15", "0.15", "0.15", "0", "0", "0",
+                    "--object", "5", "1", "0.25", "0.75", "0.75", "0.01",
+                    "0.0", "-0.01", "0.1", "0.08", "0.06", "0", "0", "0",
+                    "--object", "6", "1", "0.75", "0.5", "0.8", "-0.01",
+                    "0.01", "0.0", "0.1", "0.1", "0.1", "0", "0", "0",
+                    "--object", "7", "1", "0.6", "0.6", "0.5", "0.0", "0.0",
+                    "0.02", "0.07", "0.09", "0.08", "0", "0", "0",
+                    "--object", "20", "1", "0.5", "0.3", "0.7", "0.0",
+                    "0.01", "-0.01", "0.3", "0.05", "0.06", "0", "0", "0",
+                    "--object", "21", "1", "0.4", "0.85", "0.2", "0.01",
+                    "0.0", "0.0", "0.2", "0.04", "0.04", "0", "0", "0",
+                    "--object", "2", "1", "0.2", "0.5", "0.5", "0.0", "0.0",
+                    "0.0", "-0.05", "0.1", "0.1", "0.02", "0.0", "0.0",
+                    "--object", "3", "2", "0.93", "0.4", "0.6", "0.02",
+                    "0.0", "0.0", "0.05", "0.05", "0.05", "0", "0", "0",
+                    "--object", "3", "0", "0.06", "0.6", "0.4", "-0.02",
+                    "0.0", "0.0", "0.05", "0.05", "0.05", "0", "0", "0"],
+    # the y and z half-spheroids and the y/z cylinders, with --refine_ghost
+    # (the extent with ghosts, and the parent's extent before coarsening)
+    "mark_shapes_ghost": ["--init_x", "2", "--init_y", "2", "--init_z",
+                          "2", "--nx", "4", "--ny", "4", "--nz", "4",
+                          "--num_vars", "1", "--stencil", "7",
+                          "--num_refine", "3", "--refine_freq", "1",
+                          "--num_tsteps", "10", "--stages_per_ts", "1",
+                          "--checksum_freq", "1", "--error_tol", "0",
+                          "--max_blocks", "20000", "--refine_ghost",
+                          "--num_objects", "12"] + sum(
+        (["--object", str(t), "1"] + [str(x) for x in v] + ["0", "0", "0"]
+         for t, v in [
+             (8, (0.3, 0.3, 0.3, 0.01, 0.0, 0.01, 0.12, 0.12, 0.12)),
+             (9, (0.7, 0.3, 0.3, 0.0, 0.01, 0.01, 0.08, 0.1, 0.08)),
+             (10, (0.3, 0.7, 0.3, 0.01, -0.01, 0.0, 0.1, 0.1, 0.1)),
+             (11, (0.7, 0.7, 0.3, -0.01, 0.0, 0.01, 0.09, 0.09, 0.09)),
+             (12, (0.3, 0.3, 0.7, 0.0, 0.01, -0.01, 0.11, 0.11, 0.11)),
+             (13, (0.7, 0.3, 0.7, 0.01, 0.01, 0.0, 0.08, 0.08, 0.08)),
+             (14, (0.3, 0.7, 0.7, -0.01, 0.0, 0.0, 0.1, 0.12, 0.1)),
+             (15, (0.7, 0.7, 0.7, 0.0, -0.01, -0.01, 0.09, 0.09, 0.09)),
+             (22, (0.5, 0.5, 0.2, 0.01, 0.0, 0.0, 0.05, 0.3, 0.05)),
+             (23, (0.2, 0.5, 0.8, 0.0, 0.0, 0.01, 0.04, 0.25, 0.04)),
+             (24, (0.8, 0.2, 0.5, 0.0, 0.01, 0.0, 0.05, 0.05, 0.3)),
+             (25, (0.15, 0.85, 0.5, 0.01, -0.01, 0.0, 0.04, 0.04, 0.2)),
+         ]), []),
     # two objects, volume + surface refinement, 7-point, 4 levels, default
     # checksum cadence (every 5th stage of 3)
     "amr7_objects": ["--init_x", "2", "--init_y", "2", "--init_z", "2",
@@ -127,6 +188,10 @@ CASES = {
 
 
 HASH_STRIDE = {"config2": 10, "config5": 8}
+# cases whose marking is dumped: (every n-th refinement step, at most m)
+MARK = {"amr7": (1, 1000), "amr7_objects": (1, 1000), "uniform27": (1, 1000),
+        "mark_shapes": (1, 1000), "mark_shapes_ghost": (1, 1000),
+        "config2": (8, 2), "config5": (6, 2)}
 
 
 def run_case(name, args):
@@ -136,11 +201,20 @@ def run_case(name, args):
         trc = os.path.join(td, "t.trc")
         base_env = dict(os.environ,
                         MAMR_REF_HASH_STRIDE=str(HASH_STRIDE.get(name, 1)))
+        mlog = os.path.join(td, "m.mark")
         env = dict(base_env, MAMR_REF_LOG=rlog)
+        if name in MARK:
+            env.update(MAMR_MARK_DUMP=mlog,
+                       MAMR_MARK_DUMP_EVERY=str(MARK[name][0]),
+                       MAMR_MARK_DUMP_MAX=str(MARK[name][1]))
         r = subprocess.run([REF_BIN] + args, cwd=td, env=env,
                            capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"{name}: reference failed\n{r.stdout[-2000:]}")
+        if name in MARK:
+            with lzma.open(os.path.join(HERE, name + ".mark.xz"), "wb",
+                           preset=9) as f:
+                f.write(open(mlog, "rb").read())
         env = dict(base_env, MAMR_REF_LOG=hlog, MAMR_TRACE=trc)
         h = subprocess.run([HYB_BIN] + args, cwd=td, env=env,
                            capture_output=True, text=True)

@@ -49,3 +49,13 @@ def hashed_stages(hashes, V):
     returns first, middle and last of them."""
     st = [s for s in range(len(hashes) // V) if hashes[s * V] != 0]
     return {st[0], st[len(st) // 2], st[-1]} if st else set()
+
+
+def mark_cases():
+    """Cases with a marking fixture (<name>.mark.xz)."""
+    return sorted(f[:-len(".mark.xz")] for f in os.listdir(GOLDEN)
+                  if f.endswith(".mark.xz"))
+
+
+def mark_path(name):
+    return os.path.join(GOLDEN, name + ".mark.xz")

@@ -1,0 +1,96 @@
+"""Refinement marking (mamr_mark_refine: reset_all, check_objects /
+uniform assignment and refine_level of one rank) against the reference's
+own flags, recorded at every split_blocks() of its golden runs
+(tests/golden/*.mark.xz, oracle/ref_hooks.c): the CPU oracle here, the GPU
+library under -m gpu.  The cases cover every object type (boxes,
+spheroids and their halves, cylinders along each axis, surface and solid),
+--refine_ghost, the uniform assignment, a disabled (negative size) object,
+and the reference's multi-object stress mesh."""
+import numpy as np
+import pytest
+
+from golden_util import mark_cases, mark_path
+from miniamr_gb300.abi import (MARK_BLOCK_DTYPE, MARK_PARENT_DTYPE,
+                               OBJECT_DTYPE, Config, MamrError, MarkParams)
+from miniamr_gb300.trace import read_marks
+
+
+def check_case(lib, name):
+    steps = read_marks(mark_path(name))
+    assert steps
+    cap = max(int(st.blocks["slot"].max()) for st in steps) + 1
+    for st in steps:
+        cfg = Config.make(*st.block_size, 1, cap)
+        with lib.context(cfg) as ctx:
+            br, pr = ctx.mark_refine(st.params, st.objects, st.blocks,
+                                     st.parents)
+        act = st.parents["active"] == 1
+        assert np.array_equal(br, st.block_refine), (name, st.call)
+        assert np.array_equal(pr[act], st.parent_refine[act]), (name, st.call)
+    return len(steps)
+
+
+@pytest.mark.parametrize("name", mark_cases())
+def test_oracle_marking_equals_reference(oracle_lib, name):
+    assert check_case(oracle_lib, name) > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", mark_cases())
+def test_gpu_marking_equals_reference(gpu_lib, name):
+    assert check_case(gpu_lib, name) > 0
+
+
+def bad_inputs():
+    """(what, params, objects, blocks, parents) each of which the library
+    must refuse with MAMR_EINVAL."""
+    prm = MarkParams.make(2, (16, 16, 16))
+    obj = np.zeros(1, dtype=OBJECT_DTYPE)
+    obj["type"], obj["size"] = 2, 0.1
+    blk = np.zeros(2, dtype=MARK_BLOCK_DTYPE)
+    blk["slot"], blk["parent"], blk["nei_level"] = [0, 1], -1, -2
+    blk["cen"] = [[4, 4, 4], [12, 4, 4]]
+    par = np.zeros(1, dtype=MARK_PARENT_DTYPE)
+    out = []
+    b = blk.copy(); b["slot"] = [0, 0]
+    out.append(("slot listed twice", prm, obj, b, par))
+    b = blk.copy(); b["slot"][1] = 99
+    out.append(("slot out of range", prm, obj, b, par))
+    b = blk.copy(); b["parent"][0] = 5
+    out.append(("parent out of range", prm, obj, b, par))
+    b = blk.copy(); b["level"][0] = 3
+    out.append(("level above num_refine", prm, obj, b, par))
+    b = blk.copy(); b["nei_level"][0, 1] = 0; b["nei"][0, 1] = 7
+    out.append(("neighbour not listed", prm, obj, b, par))
+    p = par.copy(); p["active"] = 1; p["child"][0, 0] = -9
+    out.append(("child parent out of range", prm, obj, blk, p))
+    q = MarkParams.make(2, (16, 0, 16))
+    out.append(("mesh size", q, obj, blk, par))
+    q = MarkParams.make(2, (16, 16, 16)); q.reserved[3] = 1
+    out.append(("reserved parameter", q, obj, blk, par))
+    return out
+
+
+def check_refusals(lib):
+    cfg = Config.make(8, 8, 8, 1, 16)
+    with lib.context(cfg) as ctx:
+        for what, prm, obj, blk, par in bad_inputs():
+            with pytest.raises(MamrError) as e:
+                ctx.mark_refine(prm, obj, blk, par)
+            assert e.value.status == -1, what
+        # the context stays usable: two level-0 blocks, the object at the
+        # first one's corner region refines it, the other stays
+        prm, obj, blk, par = bad_inputs()[0][1:]
+        blk = blk.copy(); blk["slot"] = [0, 1]
+        obj = obj.copy(); obj["cen"] = [0.25, 0.25, 0.25]
+        br, _ = ctx.mark_refine(prm, obj, blk, par)
+        assert list(br) == [1, 0]
+
+
+def test_oracle_refuses_bad_marking_input(oracle_lib):
+    check_refusals(oracle_lib)
+
+
+@pytest.mark.gpu
+def test_gpu_refuses_bad_marking_input(gpu_lib):
+    check_refusals(gpu_lib)
