@@ -82,56 +82,68 @@ class UniformMesh:
         lev = int(levels[0])
         nx, ny, nz = self.dims(lev)
         start = self.block_start(lev)
-        slot_of = {int(self.number[s]): int(s) for s in order}
+        nl = self.number[order] - start
+        x, y, z = nl % nx, (nl // nx) % ny, nl // (nx * ny)
+        # the slot holding each lattice position of the level
+        slot_at = np.full(nx * ny * nz, -1, dtype=np.int64)
+        slot_at[nl] = order
         out = np.zeros(len(order), dtype=BLOCK_DTYPE)
-        for q, s in enumerate(order):
-            x, y, z, _ = self.lattice(int(s))
-            out["slot"][q] = s
-            out["level"][q] = lev
-            for l, (dx, dy, dz) in enumerate(((-1, 0, 0), (1, 0, 0),
-                                              (0, -1, 0), (0, 1, 0),
-                                              (0, 0, -1), (0, 0, 1))):
-                xx, yy, zz = x + dx, y + dy, z + dz
-                if 0 <= xx < nx and 0 <= yy < ny and 0 <= zz < nz:
-                    out["nei_level"][q, l] = lev
-                    out["nei"][q, l, 0, 0] = slot_of[start + (zz * ny + yy)
-                                                     * nx + xx]
-                else:
-                    out["nei_level"][q, l] = -2
-                    out["nei"][q, l, 0, 0] = 0
+        out["slot"] = order
+        out["level"] = lev
+        for l, (dx, dy, dz) in enumerate(((-1, 0, 0), (1, 0, 0), (0, -1, 0),
+                                          (0, 1, 0), (0, 0, -1), (0, 0, 1))):
+            xx, yy, zz = x + dx, y + dy, z + dz
+            inside = ((xx >= 0) & (xx < nx) & (yy >= 0) & (yy < ny) &
+                      (zz >= 0) & (zz < nz))
+            pos = np.where(inside, (zz * ny + yy) * nx + xx, 0)
+            out["nei_level"][:, l] = np.where(inside, lev, -2)
+            out["nei"][:, l, 0, 0] = np.where(inside, slot_at[pos], 0)
         return out
 
     def split_all(self) -> np.ndarray:
         """Refines every active block once (one uniform-refine pass) and
-        returns the split jobs in the reference's order."""
+        returns the split jobs in the reference's order.  Free slots are
+        kept in a sorted list, so "the first free slot at or after the
+        running index" is one bisection."""
+        import bisect
+        number = self.number.tolist()
+        level = self.level.tolist()
+        free = [q for q in range(self.max_blocks) if number[q] < 0]
         jobs = []
         m = 0
-        cur_max = int(self.level[self.number >= 0].max())
-        max_active = int(np.nonzero(self.number >= 0)[0].max()) + 1
+        active = [q for q in range(self.max_blocks) if number[q] >= 0]
+        cur_max = max(level[q] for q in active)
+        max_active = active[-1] + 1
         for lev in range(cur_max + 1):
+            cnx, cny, _ = self.dims(lev + 1)
+            cstart = self.block_start(lev + 1)
+            nx, ny, _ = self.dims(lev)
+            start = self.block_start(lev)
             n = 0
             while n < max_active:
-                if self.number[n] >= 0 and self.level[n] == lev:
-                    x, y, z, _ = self.lattice(n)
-                    cnx, cny, _ = self.dims(lev + 1)
-                    cstart = self.block_start(lev + 1)
+                if number[n] >= 0 and level[n] == lev:
+                    nl = number[n] - start
+                    x, y, z = nl % nx, (nl // nx) % ny, nl // (nx * ny)
                     child = [0] * 8
                     for o in range(8):
-                        while m < self.max_blocks and self.number[m] >= 0:
-                            m += 1
-                        if m == self.max_blocks:
+                        i = bisect.bisect_left(free, m)
+                        if i == len(free):
                             raise RuntimeError("No inactive blocks available")
+                        m = free.pop(i)
                         max_active = max(max_active, m + 1)
                         i1, j1, k1 = o % 2, (o // 2) % 2, o // 4
-                        self.number[m] = ((2 * z + k1) * cny + (2 * y + j1)) \
+                        number[m] = ((2 * z + k1) * cny + (2 * y + j1)) \
                             * cnx + 2 * x + i1 + cstart
-                        self.level[m] = lev + 1
+                        level[m] = lev + 1
                         child[o] = m
                     jobs.append((n, child))
-                    self.number[n] = -1
+                    number[n] = -1
+                    bisect.insort(free, n)
                     if n < m:
                         m = n
                 n += 1
+        self.number[:] = number
+        self.level[:] = level
         out = np.zeros(len(jobs), dtype=SPLIT_DTYPE)
         for q, (p, ch) in enumerate(jobs):
             out["parent"][q] = p
