@@ -333,16 +333,6 @@ int launch_checksum_fp32(const float *pool, const Geom &g,
 }
 
 // ---------------------------------------------------------------------------
-// Source of a data-movement read: a pool slot, or (slot < 0) entry -slot-1
-// of the staging copy taken before a batch whose later jobs overwrite it.
-template <typename T>
-__device__ __forceinline__ const T *read_base(const T *pool, const T *stage,
-                                              const Geom &g, int slot, int var)
-{
-   return slot >= 0 ? pool + bv_offset(g, slot, var)
-                    : stage + bv_offset(g, -slot - 1, var);
-}
-
 // Copies whole blocks (all variables, ghosts included) from pool slots to
 // consecutive staging entries; one CTA row per block, 16-byte vectors when
 // the block size allows.
@@ -375,81 +365,6 @@ int launch_stage_blocks(T *stage, const T *pool, const Geom &g,
    long long vec = ((long long) g.V * g.bv * sizeof(T) + 15) / 16;
    int gx = (int) std::min<long long>((vec + 255) / 256, 64);
    stage_blocks_kernel<T><<<dim3(gx, n), 256, 0, s>>>(stage, pool, g, slots);
-   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
-}
-
-// split_blocks() data (ref/block.c:158-173): one CTA per (job, octant,
-// variable).  A child cell (ci, cj, ck) takes parent cell
-// ((ci+1)/2 + i1, ...) / 8 -- exact in binary floating point.
-template <typename T>
-__global__ void __launch_bounds__(256)
-split_kernel(T *__restrict__ pool, const T *__restrict__ stage, Geom g,
-             const mamr_split_job *__restrict__ jobs)
-{
-   const int job = blockIdx.x >> 3, o = blockIdx.x & 7, var = blockIdx.y;
-   const T *P = read_base(pool, stage, g, jobs[job].parent, var);
-   T *C = pool + bv_offset(g, jobs[job].child[o], var);
-   const int i1 = (o & 1) * (g.nx / 2), j1 = ((o >> 1) & 1) * (g.ny / 2),
-             k1 = (o >> 2) * (g.nz / 2);
-   const int cells = g.nx * g.ny * g.nz;
-   for (int e = threadIdx.x; e < cells; e += blockDim.x) {
-      int ci = e / (g.ny * g.nz) + 1, r = e % (g.ny * g.nz);
-      int cj = r / g.nz + 1, ck = r % g.nz + 1;
-      C[cell_offset(g, ci, cj, ck)] =
-         eighth(P[cell_offset(g, (ci + 1) / 2 + i1, (cj + 1) / 2 + j1,
-                              (ck + 1) / 2 + k1)]);
-   }
-}
-
-template <typename T>
-int launch_split(T *pool, const T *stage, const Geom &g,
-                 const mamr_split_job *jobs, int n, cudaStream_t s)
-{
-   if (n == 0)
-      return 0;
-   split_kernel<T><<<dim3(n * 8, g.V), 256, 0, s>>>(pool, stage, g, jobs);
-   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
-}
-
-// consolidate_blocks() data (ref/block.c:411-431): one CTA per (job,
-// octant, variable); each coarse cell is the sum of its 8 children in the
-// reference's term order (left to right in FP64; compensated FP64 rounded
-// once to FP32 for FP32 pools).
-template <typename T>
-__global__ void __launch_bounds__(256)
-consolidate_kernel(T *__restrict__ pool, const T *__restrict__ stage, Geom g,
-                   const mamr_consolidate_job *__restrict__ jobs)
-{
-   const int job = blockIdx.x >> 3, o = blockIdx.x & 7, var = blockIdx.y;
-   T *P = pool + bv_offset(g, jobs[job].target, var);
-   const T *C = read_base(pool, stage, g, jobs[job].child[o], var);
-   const int xh = g.nx / 2, yh = g.ny / 2, zh = g.nz / 2;
-   const int i1 = (o & 1) * xh, j1 = ((o >> 1) & 1) * yh, k1 = (o >> 2) * zh;
-   for (int e = threadIdx.x; e < xh * yh * zh; e += blockDim.x) {
-      int i = e / (yh * zh) + 1, r = e % (yh * zh);
-      int j = r / zh + 1, k = r % zh + 1;
-      int i2 = 2 * i - 1, j2 = 2 * j - 1, k2 = 2 * k - 1;
-      T t[8] = { C[cell_offset(g, i2, j2, k2)],
-                 C[cell_offset(g, i2 + 1, j2, k2)],
-                 C[cell_offset(g, i2, j2 + 1, k2)],
-                 C[cell_offset(g, i2 + 1, j2 + 1, k2)],
-                 C[cell_offset(g, i2, j2, k2 + 1)],
-                 C[cell_offset(g, i2 + 1, j2, k2 + 1)],
-                 C[cell_offset(g, i2, j2 + 1, k2 + 1)],
-                 C[cell_offset(g, i2 + 1, j2 + 1, k2 + 1)] };
-      P[cell_offset(g, i + i1, j + j1, k + k1)] = sum8(t);
-   }
-}
-
-template <typename T>
-int launch_consolidate(T *pool, const T *stage, const Geom &g,
-                       const mamr_consolidate_job *jobs, int n,
-                       cudaStream_t s)
-{
-   if (n == 0)
-      return 0;
-   consolidate_kernel<T><<<dim3(n * 8, g.V), 256, 0, s>>>(pool, stage, g,
-                                                          jobs);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -524,11 +439,6 @@ int launch_download(const T *pool, const Geom &g, const int32_t *slots,
                                   int, int, cudaStream_t);                    \
    template int launch_stage_blocks<T>(T *, const T *, const Geom &,          \
                                        const int32_t *, int, cudaStream_t);   \
-   template int launch_split<T>(T *, const T *, const Geom &,                 \
-                                const mamr_split_job *, int, cudaStream_t);   \
-   template int launch_consolidate<T>(T *, const T *, const Geom &,           \
-                                      const mamr_consolidate_job *, int,      \
-                                      cudaStream_t);                          \
    template int launch_upload<T>(T *, const Geom &, const int32_t *, int,     \
                                  const double *, cudaStream_t);               \
    template int launch_download<T>(const T *, const Geom &, const int32_t *,  \

@@ -186,3 +186,53 @@ def test_code12_batched_is_refused(gpu_lib):
             ctx.run_timesteps(1, 1, 1, flags=RUN_BATCHED)
         assert e.value.status == -5
         ctx.run_timesteps(1, 2, 1)
+
+
+@pytest.mark.parametrize("nxyz", [(8, 8, 8), (16, 16, 16), (4, 6, 8)])
+def test_fp32_split_consolidate_edge_values(gpu_lib, oracle_lib, nxyz):
+    """FP32 split and consolidation on values of every kind: children whose
+    exponents span a few binades (the exact-sum path of the consolidation)
+    or many (the compensated FP64 sum), +-0, float subnormals, huge
+    magnitudes, mixed signs; split of the result back into children.  Every
+    cell equals the oracle's bit for bit."""
+    from miniamr_gb300.abi import CONSOLIDATE_DTYPE, SPLIT_DTYPE
+    nx, ny, nz = nxyz
+    V = 3
+    rng = np.random.default_rng(11)
+    shape = (8, V, nx + 2, ny + 2, nz + 2)
+    # variable 0: exponents within a few binades (the exact-sum path);
+    # variable 1: the same with zeros; variable 2: every kind mixed
+    kind = rng.integers(0, 6, size=shape)
+    kind[:, 0] = 0
+    kind[:, 1] = np.where(kind[:, 1] % 2 == 0, 0, 3)
+    mant = rng.uniform(1.0, 2.0, size=shape) * rng.choice([-1.0, 1.0],
+                                                           size=shape)
+    expo = np.where(kind == 0, rng.integers(-3, 3, size=shape),
+           np.where(kind == 1, rng.integers(-40, 40, size=shape),
+           np.where(kind == 2, rng.integers(-120, -100, size=shape),
+                    rng.integers(-8, 8, size=shape))))
+    vals = np.ldexp(mant, expo)
+    vals[kind == 3] = 0.0
+    vals[kind == 4] *= np.float32(2.0 ** 90)          # huge
+    sub = rng.random(size=shape) < 0.03
+    sub[:, :2] = False
+    vals[sub] = rng.integers(1, 1 << 20, size=int(sub.sum())) * 2.0 ** -149
+    negz = rng.random(size=shape) < 0.02
+    negz[:, 0] = False
+    vals[negz] = -0.0
+    vals = vals.astype(np.float32).astype(np.float64)   # exact floats
+    cfg = Config.make(nx, ny, nz, V, 24, stencil=7, dtype=FP32)
+    cons = np.zeros(1, dtype=CONSOLIDATE_DTYPE)
+    cons["child"][0] = np.arange(8)
+    cons["target"][0] = 8
+    split = np.zeros(1, dtype=SPLIT_DTYPE)
+    split["parent"][0] = 8
+    split["child"][0] = np.arange(12, 20)
+    outs = []
+    for lib in (gpu_lib, oracle_lib):
+        with lib.context(cfg) as ctx:
+            ctx.upload(np.arange(8), vals)
+            ctx.consolidate(cons)
+            ctx.split(split)
+            outs.append(ctx.download(np.arange(24)))
+    assert np.array_equal(bits(outs[0]), bits(outs[1]))
