@@ -314,6 +314,32 @@ def stress_multilevel(lib, dtype):
                                      dtype=dtype, num_vars=V)
     torch.cuda.synchronize()
     total = time.perf_counter() - t0
+    ctx.close()
+    # a third pass with every split and consolidation call synchronised on
+    # both sides: the refinement data movement on its own
+    refine = {"split": [0.0, 0], "consolidate": [0.0, 0]}
+    orig = lib.context
+
+    def timed(cfg):
+        c = orig(cfg)
+        for name in refine:
+            f = getattr(c, name)
+
+            def wrapped(jobs, f=f, name=name):
+                c.sync()
+                t = time.perf_counter()
+                f(jobs)
+                c.sync()
+                refine[name][0] += time.perf_counter() - t
+                refine[name][1] += len(jobs)
+            setattr(c, name, wrapped)
+        return c
+    lib.context = timed
+    try:
+        _, ctx, _ = replay_batched(lib, recs, RUN_BATCHED | RUN_GRAPH,
+                                   dtype=dtype, num_vars=V)
+    finally:
+        lib.context = orig
     stages = sum(n for n, _, _ in timings)
     run_s = sum(t for _, t, _ in timings)
     cells = 8 ** 3
@@ -323,7 +349,11 @@ def stress_multilevel(lib, dtype):
             "mean_blocks": upd / (stages * cells * V),
             "max_blocks": max(nb for _, _, nb in timings),
             "updates_per_s": upd / run_s, "run_seconds": run_s,
-            "replay_seconds_incl_refinement_and_host": total}
+            "replay_seconds_incl_refinement_and_host": total,
+            "refinement_data_movement": {
+                name: {"jobs": n, "ms": t * 1e3,
+                       "ms_per_job": t * 1e3 / max(n, 1)}
+                for name, (t, n) in refine.items()}}
 
 
 def refine_marking(lib):
