@@ -405,8 +405,9 @@ def profile_case(name):
         four stages (checksums on each timestep's first stage, as in the
         benchmark);
       stress_fp32, stress_fp64: the recorded multi-level stress run (8^3
-        blocks, ~22k of them, 4 vars, 7-point), replayed batched: 40
-        stages, one run per stretch between refinements."""
+        blocks, ~22k of them, 4 vars -- MAMR_PROFILE_VARS sets another
+        count -- 7-point), replayed batched: 40 stages, one run per stretch
+        between refinements, with its splits and consolidations."""
     global V, UPD_PER_STAGE
     import torch
     from miniamr_gb300 import build, load
@@ -428,7 +429,9 @@ def profile_case(name):
             c.set_tuning(shape)
             return c
         lib.context = forced
-        _, ctx, timings = replay_batched(lib, recs, RUN_BATCHED, dtype=dtype)
+        nv = os.environ.get("MAMR_PROFILE_VARS")
+        _, ctx, timings = replay_batched(lib, recs, RUN_BATCHED, dtype=dtype,
+                                         num_vars=int(nv) if nv else None)
         torch.cuda.synchronize()
         ctx.close()
         print(f"profile case {name}: {sum(n for n, _, _ in timings)} "
