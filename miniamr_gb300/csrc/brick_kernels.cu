@@ -1,7 +1,7 @@
-// Stage kernel for meshes of 8^3 blocks with the 7-point stencil: one warp
-// per work item (block, variable) and no CTA-wide barrier, so that every
-// warp of an SM streams independently.  Each warp owns two tiles in shared
-// memory and fills the next item's tile -- interior rows, and the face
+// Stage kernel for meshes of 8^3 blocks with the 7-point stencil: one or
+// two warps per work item (block, variable) and no CTA-wide barrier, so
+// that every item of an SM streams independently.  Each item's warps own
+// two tiles in shared memory and fill the next item's tile -- interior rows, and the face
 // ghosts that are copies (same-level neighbour, reflection) or single
 // values (coarser neighbour, scaled by 1/4 afterwards) -- with cp.async
 // while it computes the current item; ghosts from finer neighbours (sums of
@@ -59,7 +59,7 @@ template <typename T> struct Brick {
       return dir == 0 ? at(gn, a, b) : (dir == 1 ? at(a, gn, b)
                                                  : at(a, b, gn));
    }
-   static size_t smem_per_warp()
+   static size_t smem_per_item()
    {
       return 2 * (TILE * sizeof(T) + DESC * sizeof(int));
    }
@@ -95,7 +95,7 @@ __device__ __forceinline__ void st4(T *p, const T (&v)[4])
 // faces (the coarse values unscaled).  sd = the block's BItem, ints
 // 0..DESC-1.  Returns whether the tile needs brick_fix (a face at a level
 // jump).
-template <typename T>
+template <typename T, int TPI>
 __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
                                             const Geom &g, int var,
                                             const int *sd, T *tile, int lane)
@@ -105,8 +105,8 @@ __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
    constexpr int VW = B::VW, R = B::R;
    const T *own = src + bv_offset(g, sd[0], var);
 #pragma unroll
-   for (int t = 0; t < 2 * R; t++) {
-      const int c = lane + 32 * t, r = c / R, k = 1 + (c % R) * VW;
+   for (int t = 0; t < 64 * R / TPI; t++) {
+      const int c = lane + TPI * t, r = c / R, k = 1 + (c % R) * VW;
       const int i = (r >> 3) + 1, j = (r & 7) + 1;
       cp_async16(tile + B::at(i, j, k), own + B::gat(i, j, k));
    }
@@ -123,8 +123,8 @@ __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
          // same level: the neighbour's near plane; boundary: reflection
          const int p = (type == FACE_SAME) == low ? 8 : 1;
          if (dir < 2) {
-            if (lane < 8 * R) {
-               const int a = lane / R + 1, k = 1 + (lane % R) * VW;
+            for (int c = lane; c < 8 * R; c += TPI) {
+               const int a = c / R + 1, k = 1 + (c % R) * VW;
                if (dir == 0)
                   cp_async16(tile + B::at(gn, a, k), sb + B::gat(p, a, k));
                else
@@ -132,8 +132,8 @@ __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
             }
          } else {
 #pragma unroll
-            for (int u = 0; u < 2; u++) {
-               const int e = lane + 32 * u, i = (e >> 3) + 1, j = (e & 7) + 1;
+            for (int u = 0; u < 64 / TPI; u++) {
+               const int e = lane + TPI * u, i = (e >> 3) + 1, j = (e & 7) + 1;
                cp_async_elem(tile + B::at(i, j, gn), sb + B::gat(i, j, p));
             }
          }
@@ -142,8 +142,8 @@ __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
          const T *sb = src + bv_offset(g, f[1], var);
          const int p = low ? 8 : 1, iq = f[5], jq = f[6];
 #pragma unroll
-         for (int u = 0; u < 2; u++) {
-            const int e = lane + 32 * u, a = (e >> 3) + 1, b = (e & 7) + 1;
+         for (int u = 0; u < 64 / TPI; u++) {
+            const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
             cp_async_elem(tile + B::ghost_at(dir, gn, a, b),
                           sb + B::face_gat(dir, p, (a + 1) / 2 + 4 * jq,
                                            (b + 1) / 2 + 4 * iq));
@@ -158,7 +158,7 @@ __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
 // After the copies landed: coarse ghosts scaled by 1/4 (each lane the
 // elements it copied) and fine ghosts summed from the four finer
 // neighbours' cells, in the reference's order.
-template <typename T>
+template <typename T, int TPI>
 __device__ __forceinline__ void brick_fix(const T *__restrict__ src,
                                           const Geom &g, int var,
                                           const int *sd, T *tile, int lane)
@@ -174,8 +174,8 @@ __device__ __forceinline__ void brick_fix(const T *__restrict__ src,
       const bool low = !(l & 1);
       const int gn = low ? 0 : 9, p = low ? 8 : 1;
 #pragma unroll
-      for (int u = 0; u < 2; u++) {
-         const int e = lane + 32 * u, a = (e >> 3) + 1, b = (e & 7) + 1;
+      for (int u = 0; u < 64 / TPI; u++) {
+         const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
          T &x = tile[B::ghost_at(dir, gn, a, b)];
          if (type == FACE_COARSE) {
             x = quarter(x);
@@ -193,10 +193,28 @@ __device__ __forceinline__ void brick_fix(const T *__restrict__ src,
    }
 }
 
-// At most 4 warps per CTA; registers for the CTAs whose tiles fill the
-// shared memory (5 with FP32 tiles, 3 with FP64).
-template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 3)
+// TPI threads (one or two warps) per work item, at most 4 items per CTA.
+// Registers for the CTAs whose tiles fill the shared memory: 5 CTAs of
+// 4 one-warp items (FP32) or 3 (FP64); 4 CTAs of 4 two-warp items.
+template <int TPI, int FP32> struct BrickBounds {
+   static constexpr int THREADS = 4 * TPI;
+   static constexpr int CTAS = TPI == 64 ? 4 : (FP32 ? 5 : 3);
+};
+
+// Barrier of the TPI threads that share an item: the warp itself, or a
+// named barrier (id 1 + group) over the group's two warps.
+template <int TPI> __device__ __forceinline__ void group_sync(int group)
+{
+   if (TPI == 32)
+      __syncwarp();
+   else
+      asm volatile("bar.sync %0, %1;\n" ::"r"(group + 1), "n"(TPI)
+                   : "memory");
+}
+
+template <typename T, int TPI>
+__global__ void __launch_bounds__(BrickBounds<TPI, sizeof(T) == 4>::THREADS,
+                                  BrickBounds<TPI, sizeof(T) == 4>::CTAS)
 brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                    const BItem *__restrict__ items, int nb, int write_ghosts,
                    int do_cs, unsigned long long *__restrict__ acc,
@@ -204,17 +222,19 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
 {
    using B = Brick<T>;
    constexpr int DESC = B::DESC;
+   constexpr int ND = (DESC + TPI - 1) / TPI;     // descriptor ints a thread
+   constexpr int RPT = 64 / TPI;                   // rows of 8 cells a thread
    extern __shared__ __align__(16) unsigned char smem_raw[];
-   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-   const int wpc = blockDim.x >> 5;
-   T *tiles = reinterpret_cast<T *>(smem_raw) + (size_t) warp * 2 * B::TILE;
+   const int lane = threadIdx.x % TPI, group = threadIdx.x / TPI;
+   const int gpc = blockDim.x / TPI;
+   T *tiles = reinterpret_cast<T *>(smem_raw) + (size_t) group * 2 * B::TILE;
    int *sdesc = reinterpret_cast<int *>(reinterpret_cast<T *>(smem_raw) +
-                                        (size_t) wpc * 2 * B::TILE) +
-                warp * 2 * DESC;
-   // work items (block b, variable var), variable-major; warp w takes
+                                        (size_t) gpc * 2 * B::TILE) +
+                group * 2 * DESC;
+   // work items (block b, variable var), variable-major; group w takes
    // items w, w + nw, w + 2 nw, ... tracked as (var, b) without divisions
-   const int nw = gridDim.x * wpc;
-   const int it0 = blockIdx.x * wpc + warp;
+   const int nw = gridDim.x * gpc;
+   const int it0 = blockIdx.x * gpc + group;
    struct Pos {
       int var, b;
    };
@@ -232,29 +252,31 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       return q;
    };
    const Dims<8, 8, 8> D(g);
-   // this lane's two output rows (i0, j), (i0 + 1, j)
-   const int j = (lane & 7) + 1, i0 = 2 * (lane >> 3) + 1;
+   // this thread's output rows (i0 + m, j), m < RPT
+   const int j = (lane & 7) + 1, i0 = RPT * (lane >> 3) + 1;
 
-   auto load_desc = [&](const Pos &q, int &d0, int &d1) {
+   int dr[ND];
+   auto load_desc = [&](const Pos &q) {
       const int *p = reinterpret_cast<const int *>(items + q.b);
-      d0 = __ldg(p + lane);
-      d1 = lane < DESC - 32 ? __ldg(p + 32 + lane) : 0;
+#pragma unroll
+      for (int u = 0; u < ND; u++)
+         dr[u] = lane + TPI * u < DESC ? __ldg(p + lane + TPI * u) : 0;
    };
-   auto put_desc = [&](int *sd, int d0, int d1) {
-      sd[lane] = d0;
-      if (lane < DESC - 32)
-         sd[32 + lane] = d1;
-      __syncwarp();
+   auto put_desc = [&](int *sd) {
+#pragma unroll
+      for (int u = 0; u < ND; u++)
+         if (lane + TPI * u < DESC)
+            sd[lane + TPI * u] = dr[u];
+      group_sync<TPI>(group);
    };
 
-   int d0, d1;
-   load_desc(cur, d0, d1);
-   put_desc(sdesc, d0, d1);
-   bool fix_cur = brick_issue(src, g, cur.var, sdesc, tiles, lane);
+   load_desc(cur);
+   put_desc(sdesc);
+   bool fix_cur = brick_issue<T, TPI>(src, g, cur.var, sdesc, tiles, lane);
    cp_async_commit();
    Pos nxt = advance(cur);
    if (nxt.var < g.V)
-      load_desc(nxt, d0, d1);
+      load_desc(nxt);
 
    unsigned long long lo = 0, hi = 0;
    Fixed52 part;
@@ -268,27 +290,27 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       bool fix_next = false;
       if (nxt.var < g.V) {
          int *sdn = sdesc + (cb ^ 1) * DESC;
-         put_desc(sdn, d0, d1);
-         fix_next = brick_issue(src, g, nxt.var, sdn,
-                                tiles + (cb ^ 1) * B::TILE, lane);
+         put_desc(sdn);
+         fix_next = brick_issue<T, TPI>(src, g, nxt.var, sdn,
+                                        tiles + (cb ^ 1) * B::TILE, lane);
          const Pos nn = advance(nxt);
          if (nn.var < g.V)
-            load_desc(nn, d0, d1);
+            load_desc(nn);
       }
       cp_async_commit();
       cp_async_wait_group<1>();
       const int var = cur.var;
       if (fix_cur)
-         brick_fix(src, g, var, sd, tile, lane);
-      __syncwarp();
+         brick_fix<T, TPI>(src, g, var, sd, tile, lane);
+      group_sync<TPI>(group);
       T *d = dst + bv_offset(g, sd[0], var);
       if (write_ghosts) {
 #pragma unroll
          for (int l = 0; l < 6; l++) {
             const int dir = l >> 1, gn = (l & 1) ? 9 : 0;
 #pragma unroll
-            for (int u = 0; u < 2; u++) {
-               const int e = lane + 32 * u, a = (e >> 3) + 1, b = (e & 7) + 1;
+            for (int u = 0; u < 64 / TPI; u++) {
+               const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
                int gi, gj, gk;
                if (dir == 0) { gi = gn; gj = a; gk = b; }
                else if (dir == 1) { gi = a; gj = gn; gk = b; }
@@ -304,9 +326,9 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
          }
          cs_var = var;
       }
-      // 7-point update of rows (i0, j) and (i0 + 1, j), four k at a time
+      // 7-point update of the thread's rows, four k at a time
 #pragma unroll
-      for (int m = 0; m < 2; m++) {
+      for (int m = 0; m < RPT; m++) {
          const int i = i0 + m;
 #pragma unroll
          for (int h = 0; h < 2; h++) {
@@ -343,7 +365,7 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       }
       if (sizeof(T) == 4 && do_cs)
          fixed52_flush(part, lo, hi);
-      __syncwarp();
+      group_sync<TPI>(group);
       cur = nxt;
       fix_cur = fix_next;
       if (cur.var >= g.V)
@@ -360,24 +382,25 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
 
 }  // namespace
 
-// CTAs per SM with wpc warps each; the kernel's dynamic shared memory limit
-// is raised once to what the largest shape (4 warps) needs.
-template <typename T>
-static int brick_per_sm(int wpc)
+// CTAs per SM with gpc items of TPI threads each; the kernel's dynamic
+// shared memory limit is raised once to what 4 items need.
+template <typename T, int TPI>
+static int brick_per_sm(int gpc)
 {
    int per_sm = 0;
-   cudaFuncSetAttribute(brick_stage_kernel<T>,
+   cudaFuncSetAttribute(brick_stage_kernel<T, TPI>,
                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                        (int) (Brick<T>::smem_per_warp() * 4));
+                        (int) (Brick<T>::smem_per_item() * 4));
    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, brick_stage_kernel<T>, 32 * wpc,
-      Brick<T>::smem_per_warp() * wpc);
+      &per_sm, brick_stage_kernel<T, TPI>, TPI * gpc,
+      Brick<T>::smem_per_item() * gpc);
    return per_sm;
 }
 
-// Candidates: 4 or 2 warps per CTA, a persistent grid of the CTAs one
-// wave holds.  Shape fields: threads = 32 (one warp per item), vpc = warps
-// per CTA, rows = 2 (rows of 8 cells per lane), planes = 0 (marks this
+// Candidates: one warp per item (two rows of 8 cells a lane) or two warps
+// per item (one row a thread), 4 or 2 items per CTA, a persistent grid of
+// the CTAs one wave holds.  Shape fields: threads = threads per item,
+// vpc = items per CTA, rows = rows per thread, planes = 0 (marks this
 // kernel).
 template <typename T>
 void brick_candidates(const Geom &g, int stencil, int n_blocks,
@@ -389,21 +412,23 @@ void brick_candidates(const Geom &g, int stencil, int n_blocks,
    cudaGetDevice(&dev);
    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
    const long long items = (long long) n_blocks * g.V;
-   for (int wpc : {4, 2}) {
-      const int per_sm = brick_per_sm<T>(wpc);
-      if (per_sm <= 0)
-         continue;
-      StageShape sh;
-      sh.kernel = 1;
-      sh.threads = 32;
-      sh.vpc = wpc;
-      sh.rows = 2;
-      sh.planes = 0;
-      sh.grid = (int) std::max(1LL, std::min<long long>(
-                                       (long long) per_sm * sms,
-                                       (items + wpc - 1) / wpc));
-      out.push_back(sh);
-   }
+   for (int tpi : {32, 64})
+      for (int gpc : {4, 2}) {
+         const int per_sm = tpi == 32 ? brick_per_sm<T, 32>(gpc)
+                                      : brick_per_sm<T, 64>(gpc);
+         if (per_sm <= 0)
+            continue;
+         StageShape sh;
+         sh.kernel = 1;
+         sh.threads = tpi;
+         sh.vpc = gpc;
+         sh.rows = 64 / tpi;
+         sh.planes = 0;
+         sh.grid = (int) std::max(1LL, std::min<long long>(
+                                          (long long) per_sm * sms,
+                                          (items + gpc - 1) / gpc));
+         out.push_back(sh);
+      }
 }
 
 template <typename T>
@@ -414,10 +439,14 @@ int launch_brick_stage(const T *src, T *dst, const Geom &g,
 {
    if (n_blocks == 0)
       return 0;
-   const size_t smem = Brick<T>::smem_per_warp() * sh.vpc;
-   brick_stage_kernel<T><<<sh.grid, 32 * sh.vpc, smem, s>>>(
-      src, dst, g, items, n_blocks, write_ghosts, sizeof(T) == 4 ? do_cs : 0,
-      acc, err);
+   const size_t smem = Brick<T>::smem_per_item() * sh.vpc;
+   const int cs = sizeof(T) == 4 ? do_cs : 0;
+   if (sh.threads == 64)
+      brick_stage_kernel<T, 64><<<sh.grid, 64 * sh.vpc, smem, s>>>(
+         src, dst, g, items, n_blocks, write_ghosts, cs, acc, err);
+   else
+      brick_stage_kernel<T, 32><<<sh.grid, 32 * sh.vpc, smem, s>>>(
+         src, dst, g, items, n_blocks, write_ghosts, cs, acc, err);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
