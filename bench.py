@@ -164,10 +164,11 @@ def ncu_traffic():
         return None
 
 
-def oracle_rate(steps, threads=None, stages=SPT, warm=True):
+def oracle_rate(steps, threads=None, stages=SPT, warm=1):
     """The reference algorithm on the host cores: CPU oracle, FP64, OpenMP
-    over blocks, on the 512-block sample, `steps` timesteps of `stages`
-    stages; returns (updates/s, threads, seconds)."""
+    over blocks, on the 512-block sample: `warm` untimed timesteps, then
+    `steps` timed timesteps of `stages` stages; returns (updates/s,
+    threads, seconds)."""
     from miniamr_gb300 import build
     from miniamr_gb300.abi import FP64, Library
     threads = threads or os.cpu_count() or 1
@@ -176,7 +177,7 @@ def oracle_rate(steps, threads=None, stages=SPT, warm=True):
     n0 = SAMPLE_INIT[0] * SAMPLE_INIT[1] * SAMPLE_INIT[2]
     ctx, _ = build_mesh(lib, FP64, init=SAMPLE_INIT, cap=n0 * 9 + 8)
     if warm:
-        ctx.run_timesteps(1, stages, FREQ)
+        ctx.run_timesteps(warm, stages, FREQ)
     t0 = time.perf_counter()
     ctx.run_timesteps(steps, stages, FREQ)
     dt = time.perf_counter() - t0
@@ -477,9 +478,7 @@ def reference_arm(args, world, rank, pg):
     if rank != 0:
         return 0
     steps = max(1, args.steps)
-    for _ in range(max(0, args.warmup)):
-        pass
-    rate, threads, dt = oracle_rate(steps)
+    rate, threads, dt = oracle_rate(steps, warm=max(0, args.warmup))
     line = {
         "metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference",
         "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
@@ -523,7 +522,7 @@ def main():
         rate, threads, dt = oracle_rate(
             args.oracle_rate_steps, int(os.environ.get("OMP_NUM_THREADS",
                                                        "1")),
-            stages=1, warm=False)
+            stages=1, warm=0)
         print(json.dumps({"value": rate, "unit": UNIT, "cores": threads,
                           "seconds": dt}))
         return 0

@@ -131,3 +131,27 @@ def test_work_coefficients_match_reference_init(oracle_lib):
     a1, a0 = next(r.args for r in recs if r.op == OP_WORK_PARAMS)
     got1, got0 = oracle_lib.work_coefficients(8)
     assert got1 == a1 and np.array_equal(got0, a0)
+
+
+def test_bench_reference_arm_json_line():
+    """bench.py --impl reference: the CPU algorithm on the host cores prints
+    one JSON line with the benchmark contract's keys, its own cpu_baseline
+    and an e2e block without host-device bytes."""
+    import json
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"),
+                        "--impl", "reference", "--steps", "1", "--warmup",
+                        "1"], capture_output=True, text=True, timeout=600,
+                       env=dict(os.environ, OMP_NUM_THREADS="4"))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup",
+                "ms_per_step", "higher_is_better", "scaling", "vs_baseline",
+                "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["value"] > 0
+    assert d["steps"] == 1 and d["warmup"] == 1
+    assert d["cpu_baseline"]["kind"] == "port"
+    assert d["e2e"]["h2d_bytes_per_step"] == 0
+    assert d["e2e"]["value"] == d["value"]
