@@ -272,8 +272,8 @@ int mamr_mark_refine(mamr_ctx *ctx, const mamr_mark_params *params,
  * The stage kernel of a batched run has several launch shapes: for meshes
  * of 16^3 blocks on one level, (j-rows, i-planes) per thread = (2, 4),
  * (1, 4) or (1, 8) and a persistent or a one-CTA-per-work-item grid;
- * for 8^3 blocks and the 7-point stencil, first one warp per (block,
- * variable) with 4 or 2 warps per CTA; otherwise threads per variable and
+ * for 8^3 blocks and the 7-point stencil, first one or two warps per
+ * (block, variable) with 4 or 2 items per CTA; otherwise threads per variable and
  * variables per CTA (1, 2, 4).  choice < 0 (the default): the first batched
  * run for each (block shape, stencil, precision, kernel, work size) times
  * every candidate for a few stages into the spare pool and keeps the
@@ -286,7 +286,8 @@ int mamr_set_tuning(mamr_ctx *ctx, int32_t choice);
  * were, and its shape: shape[0..4] = threads per variable (generic
  * kernel) or per tile (pencil kernel), variables per CTA, j-rows and
  * i-planes per thread (pencil kernel), CTAs.  The warp-per-block kernel
- * reports (32, warps per CTA, 2, 0, CTAs): i-planes 0 marks it. */
+ * reports (threads per (block, variable): 32 or 64, items per CTA, rows
+ * of 8 cells per thread: 2 or 1, 0, CTAs): i-planes 0 marks it. */
 int mamr_get_tuning(const mamr_ctx *ctx, int32_t *choice,
                     int32_t *n_candidates, int32_t *shape);
 
