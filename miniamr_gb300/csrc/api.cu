@@ -151,6 +151,12 @@ struct mamr_ctx {
    bool work_set = false;
    DevBuf d_work;                   // --stencil 0 work values
    DevBuf d_mark;                   // refinement marking lists and flags
+   // FP64 checksums of every variable, computed together on the first
+   // mamr_check_sum after the pool or the mesh last changed (gen counts
+   // those changes)
+   unsigned long long gen = 0, cs_gen = ~0ull;
+   std::vector<double> cs_host;
+   DevBuf d_cs;
    int tune_force = -1;             // forced launch-shape candidate
    int tune_last = -1, tune_n = 0;  // last batched run's choice / count
    mamr::StageShape tune_shape;
@@ -270,7 +276,7 @@ extern "C" int mamr_destroy(mamr_ctx *c)
    c->d_slots.release(); c->d_partials.release(); c->d_jobs.release();
    c->d_stage.release(); c->d_stage_slots.release(); c->d_sums.release();
    c->d_xfer.release(); c->d_xfer_slots.release(); c->d_work.release();
-   c->d_mark.release();
+   c->d_mark.release(); c->d_cs.release();
    if (c->d_acc) cudaFree(c->d_acc);
    if (c->d_sum) cudaFree(c->d_sum);
    if (c->d_err) cudaFree(c->d_err);
@@ -375,6 +381,7 @@ extern "C" int mamr_upload_blocks(mamr_ctx *c, const int32_t *slots,
 {
    if (!c)
       return fail(MAMR_EINVAL, "null context");
+   c->gen++;
    return transfer(c, slots, n, const_cast<double *>(host), true);
 }
 
@@ -395,6 +402,7 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
       return fail(MAMR_EINVAL, "bad mesh arguments");
    if (n > c->cfg.max_blocks)
       return fail(MAMR_EINVAL, "%d blocks exceed max_blocks", n);
+   c->gen++;
    std::vector<int32_t> pos(c->cfg.max_blocks, -1);
    for (int32_t b = 0; b < n; b++) {
       const mamr_block &bp = blocks[b];
@@ -494,7 +502,8 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
       c->tasks[d].bc = (const BcTask *) (base + o_bc);
       c->tasks[d].n_bc = (int) bc[d].size();
    }
-   CUDA_TRY(c->d_partials.ensure(sizeof(double) * std::max(1, n)));
+   CUDA_TRY(c->d_partials.ensure(sizeof(double) * std::max(1, n) *
+                                 c->cfg.num_vars));
    CUDA_TRY(cudaStreamSynchronize(c->stream));
    c->mesh.assign(blocks, blocks + n);
    c->slot_pos.swap(pos);
@@ -528,6 +537,7 @@ extern "C" int mamr_comm(mamr_ctx *c, int32_t start, int32_t num,
    if (start < 0 || num < 0 || start + num > c->cfg.num_vars)
       return fail(MAMR_EINVAL, "variable range [%d, %d) out of bounds",
                   start, start + num);
+   c->gen++;
    return comm_impl(c, start, num, stage);
 }
 
@@ -589,6 +599,7 @@ extern "C" int mamr_stencil(mamr_ctx *c, int32_t var, int32_t calc_stage)
       return fail(MAMR_EINVAL, "variable %d out of range", var);
    if (calc_stage < 0)
       return fail(MAMR_EINVAL, "negative calc_stage");
+   c->gen++;
    return stencil_impl(c, var, calc_stage);
 }
 
@@ -645,7 +656,31 @@ extern "C" int mamr_check_sum(mamr_ctx *c, int32_t var, double *sum)
       return fail(MAMR_EINVAL, "null argument");
    if (var < 0 || var >= c->cfg.num_vars)
       return fail(MAMR_EINVAL, "variable %d out of range", var);
-   int r = checksum_queue(c, var, c->d_sum, c->d_acc);
+   int r;
+   if (!c->fp32) {
+      // the driver asks for every variable in turn after a stage
+      // (ref/driver.c:90-103): the first call sums them all at once, the
+      // others read the result while the pool is unchanged
+      if (c->cs_gen != c->gen) {
+         const int V = c->cfg.num_vars;
+         CUDA_TRY(c->d_cs.ensure(sizeof(double) * V));
+         LAUNCH_TRY(c, launch_checksum_fp64_all(
+                          (const double *) c->pool, c->g,
+                          (const int32_t *) c->d_slots.p,
+                          (int) c->mesh.size(), (double *) c->d_partials.p,
+                          (double *) c->d_cs.p, c->stream));
+         c->cs_host.resize(V);
+         CUDA_TRY(cudaMemcpyAsync(c->cs_host.data(), c->d_cs.p,
+                                  sizeof(double) * V, cudaMemcpyDeviceToHost,
+                                  c->stream));
+         if ((r = check_error_word(c)))
+            return r;
+         c->cs_gen = c->gen;
+      }
+      *sum = c->cs_host[var];
+      return MAMR_OK;
+   }
+   r = checksum_queue(c, var, c->d_sum, c->d_acc);
    if (r)
       return r;
    if (c->fp32) {
@@ -725,6 +760,7 @@ extern "C" int mamr_split(mamr_ctx *c, const mamr_split_job *jobs, int32_t n)
 {
    if (!c || n < 0 || (n && !jobs))
       return fail(MAMR_EINVAL, "bad split arguments");
+   c->gen++;
    for (int32_t t = 0; t < n; t++) {
       if (!slot_ok(c, jobs[t].parent))
          return fail(MAMR_EINVAL, "split parent slot %d out of range",
@@ -763,6 +799,7 @@ extern "C" int mamr_consolidate(mamr_ctx *c, const mamr_consolidate_job *jobs,
 {
    if (!c || n < 0 || (n && !jobs))
       return fail(MAMR_EINVAL, "bad consolidate arguments");
+   c->gen++;
    for (int32_t t = 0; t < n; t++) {
       if (!slot_ok(c, jobs[t].target))
          return fail(MAMR_EINVAL, "consolidate target slot %d out of range",
@@ -821,19 +858,24 @@ static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
          for (int var = 0; var < V; var++) {
             if ((r = stencil_impl(c, var, gstage, per_block)))
                return r;
-            if (do_cs) {
-               size_t idx = (size_t) cnt * V + var;
-               if (c->fp32)
-                  r = checksum_queue(c, var, nullptr,
-                                     (unsigned long long *) c->d_sums.p +
-                                        2 * idx);
-               else
-                  r = checksum_queue(c, var, (double *) c->d_sums.p + idx,
-                                     nullptr);
-               if (r)
+            if (do_cs && c->fp32) {
+               const size_t idx = (size_t) cnt * V + var;
+               if ((r = checksum_queue(c, var, nullptr,
+                                       (unsigned long long *) c->d_sums.p +
+                                          2 * idx)))
                   return r;
             }
          }
+         // FP64: every variable's checksum in one launch (a variable's
+         // stencil writes only that variable, so the sums are those the
+         // driver's per-variable calls return)
+         if (do_cs && !c->fp32)
+            LAUNCH_TRY(c, launch_checksum_fp64_all(
+                             (const double *) c->pool, c->g,
+                             (const int32_t *) c->d_slots.p,
+                             (int) c->mesh.size(), (double *) c->d_partials.p,
+                             (double *) c->d_sums.p + (size_t) cnt * V,
+                             c->stream));
          if (do_cs)
             cnt++;
       }
@@ -1283,6 +1325,7 @@ extern "C" int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts,
 {
    if (!c || num_ts < 0 || stages_per_ts < 1 || checksum_freq < 0)
       return fail(MAMR_EINVAL, "bad run arguments");
+   c->gen++;
    if (flags & ~(MAMR_RUN_BATCHED | MAMR_RUN_GRAPH | MAMR_RUN_PER_BLOCK))
       return fail(MAMR_EINVAL, "unknown run flags 0x%x", flags);
    if (!(flags & MAMR_RUN_BATCHED)) {

@@ -96,6 +96,11 @@ int launch_stencil(T *pool, const Geom &g, int stencil, const int32_t *slots,
 int launch_checksum_fp64(const double *pool, const Geom &g,
                          const int32_t *slots, int n, int var,
                          double *d_partials, double *d_out, cudaStream_t s);
+// FP64 checksums of every variable at once into d_sums[V] (d_partials:
+// n * V doubles); the same bits as launch_checksum_fp64 per variable.
+int launch_checksum_fp64_all(const double *pool, const Geom &g,
+                             const int32_t *slots, int n, double *d_partials,
+                             double *d_sums, cudaStream_t s);
 // FP32: exact 128-bit fixed-point accumulation into acc[2] (lo, hi),
 // which must be zeroed first.
 int launch_checksum_fp32(const float *pool, const Geom &g,

@@ -293,6 +293,62 @@ int launch_checksum_fp64(const double *pool, const Geom &g,
    return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
 }
 
+// The same for every variable at once: one thread per (variable, block)
+// chain, so the latency of the serial FP64 additions overlaps across all
+// of them; then each variable's block sums serially in sorted_list order.
+// Same additions in the same order as launch_checksum_fp64 per variable.
+__global__ void __launch_bounds__(128)
+block_sums_vars_fp64(const double *__restrict__ pool, Geom g,
+                     const int32_t *__restrict__ slots, int n,
+                     double *__restrict__ partials)
+{
+   const long long e = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+   if (e >= (long long) n * g.V)
+      return;
+   const int var = (int) (e / n), b = (int) (e - (long long) var * n);
+   const double *base = pool + bv_offset(g, slots[b], var);
+   double s = 0.0;
+   for (int i = 1; i <= g.nx; i++)
+      for (int j = 1; j <= g.ny; j++) {
+         const double *row = base + cell_offset(g, i, j, 1);
+#pragma unroll 8
+         for (int k = 0; k < g.nz; k++)
+            s = s + row[k];
+      }
+   partials[e] = s;
+}
+
+__global__ void total_sums_vars_fp64(const double *__restrict__ partials,
+                                     int n, int V, double *__restrict__ sums)
+{
+   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V;
+        v += gridDim.x * blockDim.x) {
+      const double *p = partials + (size_t) v * n;
+      double s = 0.0;
+#pragma unroll 8
+      for (int b = 0; b < n; b++)
+         s = s + p[b];
+      sums[v] = s;
+   }
+}
+
+int launch_checksum_fp64_all(const double *pool, const Geom &g,
+                             const int32_t *slots, int n, double *d_partials,
+                             double *d_sums, cudaStream_t s)
+{
+   const long long m = (long long) n * g.V;
+   int launches = 0;
+   if (m > 0) {
+      block_sums_vars_fp64<<<(unsigned) ((m + 127) / 128), 128, 0, s>>>(
+         pool, g, slots, n, d_partials);
+      launches++;
+   }
+   total_sums_vars_fp64<<<(g.V + 127) / 128, 128, 0, s>>>(d_partials, n, g.V,
+                                                          d_sums);
+   launches++;
+   return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
+}
+
 // Checksum, FP32: every interior cell as a multiple of 2^-52 (truncated
 // toward zero), summed exactly in 128-bit two's complement.  Integer
 // addition is associative, so the result does not depend on the order in
