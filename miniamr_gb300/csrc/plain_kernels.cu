@@ -5,6 +5,7 @@
 
 #include "mamr_internal.h"
 #include "arith.cuh"
+#include "dims.cuh"
 
 namespace mamr {
 
@@ -21,16 +22,23 @@ __device__ __forceinline__ long long face_cell(const Geom &g, int dir, int nc,
 
 // One CTA per (task, variable).  Tasks of one direction are independent:
 // each ghost cell is written by exactly one task and every read is of a
-// plane that this direction does not write (ref/comm.c:162-203).
-template <typename T>
+// plane that this direction does not write (ref/comm.c:162-203).  The
+// direction and, for 8^3 and 16^3 blocks, the block size are compile-time
+// constants, so face addressing folds to a few multiply-adds.
+template <typename T, int DIR, int BX, int BY, int BZ>
 __global__ void __launch_bounds__(128)
-comm_dir_kernel(T *__restrict__ pool, Geom g, int dir, int stencil,
-                int code, DirTasks t, int var0)
+comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
+                DirTasks t, int var0)
 {
+   const Dims<BX, BY, BZ> D(g);
+   constexpr int dir = DIR;
    int task = blockIdx.x, var = var0 + blockIdx.y;
-   const int n = dir == 0 ? g.nx : (dir == 1 ? g.ny : g.nz);
-   const int na = dir == 0 ? g.ny : g.nx;
-   const int nb = dir == 2 ? g.ny : g.nz;
+   const int n = dir == 0 ? D.nx : (dir == 1 ? D.ny : D.nz);
+   const int na = dir == 0 ? D.ny : D.nx;
+   const int nb = dir == 2 ? D.ny : D.nz;
+   auto face_cell = [&](const Geom &, int, int nc, int a, int b) {
+      return D.fcell(DIR, nc, a, b);
+   };
 
    if (task < t.n_same) {
       // ref/comm.c:1473-1534 (code 0)
@@ -137,6 +145,26 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int dir, int stencil,
    }
 }
 
+template <typename T, int DIR>
+static void comm_dir_launch(T *pool, const Geom &g, int stencil, int code,
+                            const DirTasks &t, int var0, dim3 grid,
+                            cudaStream_t s)
+{
+   switch (dims_kind(g)) {
+   case 1:
+      comm_dir_kernel<T, DIR, 8, 8, 8><<<grid, 128, 0, s>>>(pool, g, stencil,
+                                                            code, t, var0);
+      break;
+   case 2:
+      comm_dir_kernel<T, DIR, 16, 16, 16><<<grid, 128, 0, s>>>(
+         pool, g, stencil, code, t, var0);
+      break;
+   default:
+      comm_dir_kernel<T, DIR, 0, 0, 0><<<grid, 128, 0, s>>>(pool, g, stencil,
+                                                            code, t, var0);
+   }
+}
+
 template <typename T>
 int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil, int code,
                     const DirTasks &t, int var0, int nvar, cudaStream_t s)
@@ -144,8 +172,13 @@ int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil, int code,
    int n = t.n_same + t.n_diff + t.n_bc;
    if (n == 0 || nvar == 0)
       return 0;
-   comm_dir_kernel<T><<<dim3(n, nvar), 128, 0, s>>>(pool, g, dir, stencil,
-                                                    code, t, var0);
+   const dim3 grid(n, nvar);
+   if (dir == 0)
+      comm_dir_launch<T, 0>(pool, g, stencil, code, t, var0, grid, s);
+   else if (dir == 1)
+      comm_dir_launch<T, 1>(pool, g, stencil, code, t, var0, grid, s);
+   else
+      comm_dir_launch<T, 2>(pool, g, stencil, code, t, var0, grid, s);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
