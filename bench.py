@@ -608,6 +608,14 @@ def main():
     ctx64.run_timesteps(1, 1, 0, flags=RUN_PLAIN | RUN_PER_BLOCK)
     fp64_per_block = UPD_PER_STAGE / (time.perf_counter() - t0)
     ctx64.close()
+    # the plain path on an FP32 pool (the drop-in with MAMR_DTYPE=fp32)
+    ctx32p, _ = build_mesh(lib, FP32)
+    ctx32p.run_timesteps(1, SPT, FREQ, flags=RUN_PLAIN)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx32p.run_timesteps(1, SPT, FREQ, flags=RUN_PLAIN)
+    fp32_plain = updates(1) / (time.perf_counter() - t0)
+    ctx32p.close()
     ref = s64[W:W + min(K, K64)]
     got = sums32[:len(ref)]
     rel = np.abs(got - ref) / np.abs(ref)
@@ -635,6 +643,7 @@ def main():
         "gpu_launches": launches,
         "paths": {"fp32_batched": value / world,
                   "fp64_batched": fp64_batched, "fp64_plain": fp64_plain,
+                  "fp32_plain": fp32_plain,
                   "fp64_one_launch_per_block_var": fp64_per_block,
                   "fp32_batched_over_fp64_plain": value / world / fp64_plain},
         "fp32_checksum_error": err,

@@ -187,34 +187,67 @@ int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil, int code,
 // included) staged in shared memory, each thread sweeping one (j, k) column
 // along i.  Results are written straight back to the pool: every read comes
 // from the staged copy, so the in-place update is the reference's
-// work-array Jacobi update (ref/stencil.c:82-99, 103-141).
-template <typename T, int ST>
+// work-array Jacobi update (ref/stencil.c:82-99, 103-141).  Staged rows
+// are Zs long with k = 1 at a 16-byte boundary, so the interior rows of the
+// split layout copy as vectors; 8^3 and 16^3 blocks get compile-time
+// dimensions.
+template <typename T> struct PlainVec;
+template <> struct PlainVec<float> { using V = float4; };
+template <> struct PlainVec<double> { using V = double2; };
+
+template <typename T>
+__host__ __device__ inline int plain_zs(int nz)
+{
+   const int vw = 16 / (int) sizeof(T);
+   return ((vw - 1 + nz + 2 + vw - 1) / vw) * vw;
+}
+
+template <typename T, int ST, int BX, int BY, int BZ>
 __global__ void __launch_bounds__(256)
 stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
                int var)
 {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    T *tile = reinterpret_cast<T *>(smem_raw);
-   const int X = g.X, Y = g.Y, Z = g.Z;
+   constexpr int VW = 16 / (int) sizeof(T), KO = VW - 1;
+   const Dims<BX, BY, BZ> D(g);
+   const int nx = D.nx, ny = D.ny, nz = D.nz, X = D.X, Y = D.Y;
+   const int Zs = plain_zs<T>(nz);
    T *base = pool + bv_offset(g, slots[blockIdx.x], var);
-   for (int e = threadIdx.x; e < X * Y * Z; e += blockDim.x) {
-      int row = e / Z, k = e - row * Z;
-      int i = row / Y, j = row - i * Y;
-      tile[e] = base[cell_offset(g, i, j, k)];
+#define TL(i, j, k) tile[((i) * Y + (j)) * Zs + KO + (k)]
+   // interior rows (k = 1..nz) of all X*Y rows, then the k ghost planes
+   if (nz % VW == 0) {
+      using V = typename PlainVec<T>::V;
+      const int nv = nz / VW;
+      for (int e = threadIdx.x; e < X * Y * nv; e += blockDim.x) {
+         const int row = e / nv, q = e - row * nv;
+         const V v = __ldg(reinterpret_cast<const V *>(base +
+                                                       (size_t) row * nz) + q);
+         *reinterpret_cast<V *>(&tile[row * Zs + KO + 1 + q * VW]) = v;
+      }
+   } else {
+      for (int e = threadIdx.x; e < X * Y * nz; e += blockDim.x) {
+         const int row = e / nz, k = e - row * nz;
+         tile[row * Zs + KO + 1 + k] = base[(size_t) row * nz + k];
+      }
+   }
+   for (int e = threadIdx.x; e < 2 * X * Y; e += blockDim.x) {
+      const int row = e % (X * Y), hi = e / (X * Y);
+      tile[row * Zs + KO + (hi ? nz + 1 : 0)] =
+         base[(size_t) X * Y * nz + (hi ? X * Y : 0) + row];
    }
    __syncthreads();
-#define TL(i, j, k) tile[((i) * Y + (j)) * Z + (k)]
-   for (int col = threadIdx.x; col < g.ny * g.nz; col += blockDim.x) {
-      const int j = col / g.nz + 1, k = col % g.nz + 1;
+   for (int col = threadIdx.x; col < ny * nz; col += blockDim.x) {
+      const int j = col / nz + 1, k = col - (j - 1) * nz + 1;
       if (ST == 7) {
-         for (int i = 1; i <= g.nx; i++) {
+         for (int i = 1; i <= nx; i++) {
             T w = TL(i - 1, j, k) + TL(i, j - 1, k);
             w = w + TL(i, j, k - 1);
             w = w + TL(i, j, k);
             w = w + TL(i, j, k + 1);
             w = w + TL(i, j + 1, k);
             w = w + TL(i + 1, j, k);
-            base[cell_offset(g, i, j, k)] = div7(w);
+            base[D.cell(i, j, k)] = div7(w);
          }
       } else {
          // S(p) = the 9-point left-to-right sum on plane p around (j, k):
@@ -233,9 +266,9 @@ stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
             return s;
          };
          T s0 = S(0), s1 = S(1);
-         for (int i = 1; i <= g.nx; i++) {
+         for (int i = 1; i <= nx; i++) {
             T s2 = S(i + 1);
-            base[cell_offset(g, i, j, k)] = div27((s0 + s1) + s2);
+            base[D.cell(i, j, k)] = div27((s0 + s1) + s2);
             s0 = s1;
             s1 = s2;
          }
@@ -244,26 +277,47 @@ stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
 #undef TL
 }
 
+template <typename T, int ST, int BX, int BY, int BZ>
+static void stencil_launch(T *pool, const Geom &g, const int32_t *slots,
+                           int n, int var, int threads, size_t smem,
+                           cudaStream_t s)
+{
+   cudaFuncAttributes fa;
+   if (cudaFuncGetAttributes(&fa, stencil_kernel<T, ST, BX, BY, BZ>) !=
+          cudaSuccess ||
+       (size_t) fa.maxDynamicSharedSizeBytes < smem)
+      cudaFuncSetAttribute(stencil_kernel<T, ST, BX, BY, BZ>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int) smem);
+   stencil_kernel<T, ST, BX, BY, BZ><<<n, threads, smem, s>>>(pool, g, slots,
+                                                              var);
+}
+
 template <typename T>
 int launch_stencil(T *pool, const Geom &g, int stencil, const int32_t *slots,
                    int n, int var, cudaStream_t s)
 {
    if (n == 0)
       return 0;
-   size_t smem = (size_t) g.X * g.Y * g.Z * sizeof(T);
+   const size_t smem = (size_t) g.X * g.Y * plain_zs<T>(g.nz) * sizeof(T);
    int threads = g.ny * g.nz;
    threads = threads > 256 ? 256 : ((threads + 31) / 32) * 32;
+   const int kind = dims_kind(g);
+#define MAMR_PLAIN_ST(ST)                                                     \
+   if (kind == 1)                                                             \
+      stencil_launch<T, ST, 8, 8, 8>(pool, g, slots, n, var, threads, smem,   \
+                                     s);                                      \
+   else if (kind == 2)                                                        \
+      stencil_launch<T, ST, 16, 16, 16>(pool, g, slots, n, var, threads,      \
+                                        smem, s);                             \
+   else                                                                       \
+      stencil_launch<T, ST, 0, 0, 0>(pool, g, slots, n, var, threads, smem, s)
    if (stencil == 7) {
-      cudaFuncSetAttribute(stencil_kernel<T, 7>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int) smem);
-      stencil_kernel<T, 7><<<n, threads, smem, s>>>(pool, g, slots, var);
+      MAMR_PLAIN_ST(7);
    } else {
-      cudaFuncSetAttribute(stencil_kernel<T, 27>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int) smem);
-      stencil_kernel<T, 27><<<n, threads, smem, s>>>(pool, g, slots, var);
+      MAMR_PLAIN_ST(27);
    }
+#undef MAMR_PLAIN_ST
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
