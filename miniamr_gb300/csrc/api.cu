@@ -855,20 +855,23 @@ static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
          const bool do_cs = freq && !(st % freq);
          if ((r = comm_impl(c, 0, V, gstage)))
             return r;
-         for (int var = 0; var < V; var++) {
+         for (int var = 0; var < V; var++)
             if ((r = stencil_impl(c, var, gstage, per_block)))
                return r;
-            if (do_cs && c->fp32) {
-               const size_t idx = (size_t) cnt * V + var;
-               if ((r = checksum_queue(c, var, nullptr,
-                                       (unsigned long long *) c->d_sums.p +
-                                          2 * idx)))
-                  return r;
-            }
+         // every variable's checksum in one launch (a variable's stencil
+         // writes only that variable, so the sums are those the driver's
+         // per-variable calls return)
+         if (do_cs && c->fp32) {
+            unsigned long long *acc =
+               (unsigned long long *) c->d_sums.p + 2 * (size_t) cnt * V;
+            CUDA_TRY(cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long) *
+                                                V,
+                                     c->stream));
+            LAUNCH_TRY(c, launch_checksum_fp32_all(
+                             (const float *) c->pool, c->g,
+                             (const int32_t *) c->d_slots.p,
+                             (int) c->mesh.size(), acc, c->d_err, c->stream));
          }
-         // FP64: every variable's checksum in one launch (a variable's
-         // stencil writes only that variable, so the sums are those the
-         // driver's per-variable calls return)
          if (do_cs && !c->fp32)
             LAUNCH_TRY(c, launch_checksum_fp64_all(
                              (const double *) c->pool, c->g,

@@ -101,6 +101,11 @@ int launch_checksum_fp64(const double *pool, const Geom &g,
 int launch_checksum_fp64_all(const double *pool, const Geom &g,
                              const int32_t *slots, int n, double *d_partials,
                              double *d_sums, cudaStream_t s);
+// FP32, every variable at once into acc[2 * V] (zeroed first).
+int launch_checksum_fp32_all(const float *pool, const Geom &g,
+                             const int32_t *slots, int n,
+                             unsigned long long *acc, unsigned *err,
+                             cudaStream_t s);
 // FP32: exact 128-bit fixed-point accumulation into acc[2] (lo, hi),
 // which must be zeroed first.
 int launch_checksum_fp32(const float *pool, const Geom &g,

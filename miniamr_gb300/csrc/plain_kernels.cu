@@ -464,6 +464,45 @@ checksum_fp32_kernel(const float *__restrict__ pool, Geom g,
    block_acc128_flush(lo, hi, acc);
 }
 
+// Every variable at once: CTA (block, variable) adds into acc[2 * var];
+// exact integer sums, so the grouping changes no bit.
+__global__ void __launch_bounds__(256)
+checksum_fp32_vars_kernel(const float *__restrict__ pool, Geom g,
+                          const int32_t *__restrict__ slots,
+                          unsigned long long *__restrict__ acc,
+                          unsigned *__restrict__ err)
+{
+   const int var = blockIdx.y;
+   const float *base = pool + bv_offset(g, slots[blockIdx.x], var);
+   unsigned long long lo = 0, hi = 0;
+   Fixed52 part;
+   bool ok = true;
+   const int cells = g.nx * g.ny * g.nz;
+   for (int e = threadIdx.x, t = 1; e < cells; e += blockDim.x, t++) {
+      int i = e / (g.ny * g.nz) + 1, r = e % (g.ny * g.nz);
+      int j = r / g.nz + 1, k = r % g.nz + 1;
+      ok &= fixed52_add(base[cell_offset(g, i, j, k)], part);
+      if ((t & 255) == 0)
+         fixed52_flush(part, lo, hi);
+   }
+   fixed52_flush(part, lo, hi);
+   if (!ok)
+      atomicOr(err, ERR_FIXED_RANGE);
+   block_acc128_flush(lo, hi, acc + 2 * var);
+}
+
+int launch_checksum_fp32_all(const float *pool, const Geom &g,
+                             const int32_t *slots, int n,
+                             unsigned long long *acc, unsigned *err,
+                             cudaStream_t s)
+{
+   if (n == 0)
+      return 0;
+   checksum_fp32_vars_kernel<<<dim3(n, g.V), 256, 0, s>>>(pool, g, slots, acc,
+                                                         err);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
 int launch_checksum_fp32(const float *pool, const Geom &g,
                          const int32_t *slots, int n, int var,
                          unsigned long long *acc, unsigned *err,
