@@ -296,8 +296,10 @@ def stress_multilevel(lib, dtype):
     22k blocks, 35,884 at most) replayed from the reference's recorded mesh
     sequence with 40 variables: each stretch of stages between refinements
     is one batched run under a freshly captured CUDA graph.  Rate = updates
-    over the run calls' wall time (graph capture included); refinement data
-    movement and mesh set-up are timed separately."""
+    over the run calls' wall time (descriptor build and graph capture
+    included; the device finishes the preceding refinement before each
+    run's clock starts); refinement data movement and mesh set-up are
+    timed separately."""
     import torch
     from miniamr_gb300.abi import RUN_BATCHED, RUN_GRAPH
     from miniamr_gb300.trace import read_trace, replay_batched

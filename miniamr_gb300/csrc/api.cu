@@ -98,7 +98,7 @@ const int kPerm[6][3] = { {0, 1, 2}, {1, 2, 0}, {2, 0, 1},
 
 namespace mamr {
 struct BatchedState {
-   DevBuf items, partials, sums, acc, chain, pencils;
+   DevBuf items, partials, sums, acc, chain, pencils, bad;
    BItem *h_items = nullptr;   // pinned staging of the item upload
    size_t h_cap = 0;           // its capacity in items
    int n = 0;
@@ -113,6 +113,7 @@ void batched_destroy(BatchedState *b)
       return;
    b->items.release(); b->partials.release(); b->sums.release();
    b->acc.release(); b->chain.release(); b->pencils.release();
+   b->bad.release();
    if (b->h_items)
       cudaFreeHost(b->h_items);
    delete b;
@@ -136,6 +137,7 @@ struct mamr_ctx {
    std::vector<mamr_block> mesh;
    std::vector<int32_t> slot_pos;   // slot -> index in mesh or -1
    DevBuf d_slots;                  // sorted slots
+   DevBuf d_mesh, d_slot_pos;       // device copies of mesh and slot_pos
    DevBuf d_tasks[3];
    DirTasks tasks[3];
    DevBuf d_partials, d_jobs, d_stage, d_stage_slots, d_sums;
@@ -277,6 +279,7 @@ extern "C" int mamr_destroy(mamr_ctx *c)
    c->d_stage.release(); c->d_stage_slots.release(); c->d_sums.release();
    c->d_xfer.release(); c->d_xfer_slots.release(); c->d_work.release();
    c->d_mark.release(); c->d_cs.release();
+   c->d_mesh.release(); c->d_slot_pos.release();
    if (c->d_acc) cudaFree(c->d_acc);
    if (c->d_sum) cudaFree(c->d_sum);
    if (c->d_err) cudaFree(c->d_err);
@@ -504,6 +507,15 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
    }
    CUDA_TRY(c->d_partials.ensure(sizeof(double) * std::max(1, n) *
                                  c->cfg.num_vars));
+   // the mesh on the device, for the batched path's descriptor build
+   CUDA_TRY(c->d_mesh.ensure(sizeof(mamr_block) * std::max(1, n)));
+   if (n)
+      CUDA_TRY(cudaMemcpyAsync(c->d_mesh.p, blocks, sizeof(mamr_block) * n,
+                               cudaMemcpyHostToDevice, c->stream));
+   CUDA_TRY(c->d_slot_pos.ensure(sizeof(int32_t) * pos.size()));
+   CUDA_TRY(cudaMemcpyAsync(c->d_slot_pos.p, pos.data(),
+                            sizeof(int32_t) * pos.size(),
+                            cudaMemcpyHostToDevice, c->stream));
    CUDA_TRY(cudaStreamSynchronize(c->stream));
    c->mesh.assign(blocks, blocks + n);
    c->slot_pos.swap(pos);
@@ -903,7 +915,7 @@ static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
 
 
 // Per-block descriptors for the batched stage kernel, from the mesh.
-static int build_items(mamr_ctx *c)
+static int build_items_host(mamr_ctx *c)
 {
    BatchedState *B = c->batched;
    const int n = (int) c->mesh.size();
@@ -1043,6 +1055,44 @@ static int build_items(mamr_ctx *c)
    CUDA_TRY(cudaStreamSynchronize(c->stream));
    B->n = n;
    B->single_level = single;
+   B->valid = true;
+   return MAMR_OK;
+}
+
+// The batched path's descriptors for the current mesh.  Meshes the pencil
+// kernel takes (one level, 16^3 blocks) need the host-side z chains and
+// are built on the host; every other mesh on the device, one thread per
+// block, from the copy mamr_set_mesh uploaded (after a refinement of the
+// 8^3 stress mesh, 24k blocks: about 1.6 ms on the host against tens of
+// microseconds).  A mesh the device build rejects is built again on the
+// host, which names what is wrong with it.
+static int build_items(mamr_ctx *c)
+{
+   BatchedState *B = c->batched;
+   const int n = (int) c->mesh.size();
+   bool single = true;
+   for (int q = 0; q < n; q++)
+      single = single && c->mesh[q].level == c->mesh[0].level;
+   if (single && n > 0 && c->g.nx == 16 && c->g.ny == 16 && c->g.nz == 16)
+      return build_items_host(c);
+   CUDA_TRY(B->items.ensure(sizeof(BItem) * (size_t) std::max(1, n)));
+   CUDA_TRY(B->bad.ensure(sizeof(int)));
+   CUDA_TRY(cudaMemsetAsync(B->bad.p, 0x7f, sizeof(int), c->stream));
+   if (launch_build_items((const mamr_block *) c->d_mesh.p, n,
+                          (const int32_t *) c->d_slot_pos.p, single ? 1 : 0,
+                          (BItem *) B->items.p, (int *) B->bad.p,
+                          c->stream) < 0)
+      return fail(MAMR_ECUDA, "descriptor build: %s",
+                  cudaGetErrorString(cudaGetLastError()));
+   int bad = 0;
+   CUDA_TRY(cudaMemcpyAsync(&bad, B->bad.p, sizeof(int),
+                            cudaMemcpyDeviceToHost, c->stream));
+   CUDA_TRY(cudaStreamSynchronize(c->stream));
+   if (bad != 0x7f7f7f7f)
+      return build_items_host(c);
+   B->n = n;
+   B->single_level = single;
+   B->n_pencils = 0;
    B->valid = true;
    return MAMR_OK;
 }

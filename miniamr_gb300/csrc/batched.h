@@ -108,6 +108,13 @@ int launch_fp64_checksums(const double *pool, const Geom &g,
                           const BItem *items, int n_blocks, double *partials,
                           double *sums, cudaStream_t s);
 
+// Per-block descriptors (items[0..n)) built on the device from the mesh
+// and its slot -> index map; single: also the edge and corner neighbours
+// (nb27).  *bad (set above n first) is lowered to the index of a block
+// whose coarser neighbour does not list it.
+int launch_build_items(const mamr_block *mesh, int n, const int32_t *slot_pos,
+                       int single, BItem *items, int *bad, cudaStream_t s);
+
 // The pencil kernel's launch shapes for n_work = pencils x variables.
 template <typename T>
 void pencil_candidates(int stencil, int n_work, std::vector<StageShape> &out);

@@ -396,6 +396,95 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
    return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
 }
 
+// Per-block descriptors of the batched stage kernels from the mesh, one
+// thread per block: each face's kind (same level, boundary, coarser with
+// the quarter of the coarse face this block covers, finer with its four
+// neighbours) and, on single-level meshes, the neighbours across edges and
+// corners, reached by hopping along x, then y, then z (a boundary hop
+// stays on the block).  A block whose coarser neighbour is inactive or
+// does not list it lowers *bad to its index; the descriptor is then left
+// with that face as a boundary so that no access leaves the pool.
+__global__ void build_items_kernel(const mamr_block *__restrict__ mesh, int n,
+                                   const int32_t *__restrict__ slot_pos,
+                                   int single, BItem *__restrict__ items,
+                                   int *__restrict__ bad)
+{
+   const int q = blockIdx.x * blockDim.x + threadIdx.x;
+   if (q >= n)
+      return;
+   const mamr_block &bp = mesh[q];
+   BItem it;
+   it.slot = bp.slot;
+   it.bmask = 0;
+#pragma unroll
+   for (int l = 0; l < 6; l++) {
+      BFace &f = it.f[l];
+      f.nb[0] = f.nb[1] = f.nb[2] = f.nb[3] = 0;
+      f.iq = f.jq = 0;
+      const int nl = bp.nei_level[l];
+      if (nl == bp.level) {
+         f.type = FACE_SAME;
+         f.nb[0] = bp.nei[l][0][0];
+      } else if (nl == bp.level + 1) {
+         f.type = FACE_FINE;
+         for (int iq = 0; iq < 2; iq++)
+            for (int jq = 0; jq < 2; jq++)
+               f.nb[iq * 2 + jq] = bp.nei[l][iq][jq];
+      } else if (nl == -2) {
+         f.type = FACE_BC;
+         it.bmask |= 1 << l;
+      } else {
+         const int m = bp.nei[l][0][0];
+         const int pm = slot_pos[m];
+         bool found = false;
+         if (pm >= 0)
+            for (int iq = 0; iq < 2 && !found; iq++)
+               for (int jq = 0; jq < 2 && !found; jq++)
+                  if (mesh[pm].nei[l ^ 1][iq][jq] == bp.slot) {
+                     f.iq = iq;
+                     f.jq = jq;
+                     found = true;
+                  }
+         if (found) {
+            f.type = FACE_COARSE;
+            f.nb[0] = m;
+         } else {
+            f.type = FACE_BC;
+            atomicMin(bad, q);
+         }
+      }
+   }
+   for (int d = 0; d < 27; d++) {
+      int cur = bp.slot;
+      if (single) {
+         const int dd[3] = {d % 3 - 1, (d / 3) % 3 - 1, d / 9 - 1};
+         for (int ax = 0; ax < 3 && cur >= 0; ax++) {
+            if (!dd[ax])
+               continue;
+            const mamr_block &cb = mesh[slot_pos[cur]];
+            const int l = 2 * ax + (dd[ax] > 0);
+            cur = (cb.nei_level[l] == cb.level) ? cb.nei[l][0][0] : -1;
+            if (cur >= 0 && slot_pos[cur] < 0)
+               cur = -1;
+         }
+         it.nb27[d] = cur >= 0 ? cur : bp.slot;
+      } else {
+         it.nb27[d] = 0;
+      }
+   }
+   items[q] = it;
+}
+
+int launch_build_items(const mamr_block *mesh, int n, const int32_t *slot_pos,
+                       int single, BItem *items, int *bad, cudaStream_t s)
+{
+   if (n == 0)
+      return 0;
+   build_items_kernel<<<(n + 127) / 128, 128, 0, s>>>(mesh, n, slot_pos,
+                                                      single, items, bad);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
 template void batched_candidates<float>(const Geom &, int, int,
                                         std::vector<StageShape> &);
 template void batched_candidates<double>(const Geom &, int, int,

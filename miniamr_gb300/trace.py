@@ -221,6 +221,9 @@ def replay_batched(lib: Library, records: list[Record], flags: int,
                 j += 1
             n = j - i + 1
             cs = pending[i][1]
+            # the refinement before this run (split, consolidate, mesh
+            # upload) is asynchronous: finish it outside the run's time
+            ctx.sync()
             t0 = time.perf_counter()
             got = ctx.run_timesteps(n, 1, 1 if cs else 0, pending[i][0],
                                     flags=flags)
