@@ -142,6 +142,45 @@ def test_errors_are_reported_and_context_survives(gpu_lib):
             ctx.comm(1, 5, 0)
 
 
+def test_batched_refuses_a_coarse_face_that_omits_the_block(gpu_lib):
+    """The batched descriptors of a multi-level mesh are built on the
+    device; a fine block whose coarser neighbour does not list it on the
+    shared face (which mamr_set_mesh does not check) is refused with the
+    host builder's message, and the context keeps working."""
+    from miniamr_gb300.abi import RUN_BATCHED
+    from miniamr_gb300.trace import OP_CREATE, OP_SET_MESH
+    recs = read_trace(trace_path("amr7"))
+    cfg = Config.from_buffer_copy(bytes(
+        next(r for r in recs if r.op == OP_CREATE).args[0]))
+    good = next(r.args[0] for r in recs if r.op == OP_SET_MESH
+                and len(set(r.args[0]["level"].tolist())) > 1)
+    bad = good.copy()
+    pos = {int(s): q for q, s in enumerate(bad["slot"])}
+    done = False
+    for q in range(len(bad)):
+        for l in range(6):
+            if bad["nei_level"][q, l] != bad["level"][q] - 1:
+                continue
+            pm = pos[int(bad["nei"][q, l, 0, 0])]
+            face = bad["nei"][pm, l ^ 1]
+            hit = np.argwhere(face == bad["slot"][q])
+            if len(hit):
+                iq, jq = hit[0]
+                face[iq, jq] = face[1 - iq, jq]   # another fine neighbour
+                done = True
+                break
+        if done:
+            break
+    assert done
+    with gpu_lib.context(cfg) as ctx:
+        ctx.set_mesh(bad)
+        with pytest.raises(MamrError) as e:
+            ctx.run_timesteps(1, 1, 0, flags=RUN_BATCHED)
+        assert e.value.status == -4 and "child face" in str(e.value)
+        ctx.set_mesh(good)
+        ctx.run_timesteps(1, 1, 0, flags=RUN_BATCHED)
+
+
 def test_division_selftest(gpu_lib):
     """The kernels' x/7 and x/27 equal IEEE division: FP32 on every float
     in [1, 2) (which decides its whole fast-path window) and on hashed
