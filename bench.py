@@ -185,13 +185,15 @@ def oracle_rate(steps, threads=None, stages=SPT, warm=1):
     return steps * stages * n0 * 8 * N ** 3 * V / dt, threads, dt
 
 
-def amr_plain_fp64(lib):
-    """The AMR run with one moving sphere (4^3 blocks of 16^3, 40 FP64
-    vars, 27-point, 4 levels, refine every 5 steps, 100 timesteps; up to
-    7429 blocks) replayed from the reference's recorded mesh sequence
-    through the plain FP64 path -- the drop-in's call sequence of comm,
-    stencil and check_sum, queued without host syncs -- with every checksum
-    compared bit for bit with the reference's."""
+def amr_plain(lib, dtype):
+    """The AMR run with one moving sphere (4^3 blocks of 16^3, 40 vars,
+    27-point, 4 levels, refine every 5 steps, 100 timesteps; up to 7429
+    blocks) replayed from the reference's recorded mesh sequence through
+    the plain path -- the drop-in's call sequence of comm, stencil and
+    check_sum, queued without host syncs.  FP64: every checksum compared
+    bit for bit with the reference's; FP32 pool (the drop-in with
+    MAMR_DTYPE=fp32): max and RMS relative error of every checksum against
+    the reference's FP64 checksums."""
     import torch
     from miniamr_gb300.abi import FP64, RUN_PLAIN
     from miniamr_gb300.trace import read_trace, replay_batched
@@ -201,7 +203,7 @@ def amr_plain_fp64(lib):
     recs = read_trace(path)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    sums, ctx, timings = replay_batched(lib, recs, RUN_PLAIN, dtype=FP64)
+    sums, ctx, timings = replay_batched(lib, recs, RUN_PLAIN, dtype=dtype)
     torch.cuda.synchronize()
     total = time.perf_counter() - t0
     ctx.close()
@@ -209,14 +211,21 @@ def amr_plain_fp64(lib):
     stages = sum(n for n, _, _ in timings)
     upd = sum(n * nb * cells * V for n, _, nb in timings)
     run_s = sum(t for _, t, _ in timings)
-    exact = all(np.float64(a).tobytes() == np.float64(b).tobytes()
-                for _, a, b in sums)
-    return {"stages": stages, "runs": len(timings),
-            "mean_blocks": upd / (stages * cells * V),
-            "max_blocks": max(nb for _, _, nb in timings),
-            "updates_per_s": upd / run_s, "run_seconds": run_s,
-            "replay_seconds_incl_refinement_and_host": total,
-            "checksums": len(sums), "checksums_bit_exact": exact}
+    out = {"stages": stages, "runs": len(timings),
+           "mean_blocks": upd / (stages * cells * V),
+           "max_blocks": max(nb for _, _, nb in timings),
+           "updates_per_s": upd / run_s, "run_seconds": run_s,
+           "replay_seconds_incl_refinement_and_host": total,
+           "checksums": len(sums)}
+    if dtype == FP64:
+        out["checksums_bit_exact"] = all(
+            np.float64(a).tobytes() == np.float64(b).tobytes()
+            for _, a, b in sums)
+    else:
+        rel = np.array([abs(a - b) / abs(b) for _, a, b in sums if b != 0.0])
+        out["checksum_rel_error_vs_reference_fp64"] = {
+            "max": float(rel.max()), "rms": float(np.sqrt(np.mean(rel ** 2)))}
+    return out
 
 
 def one_thread_oracle_rate():
@@ -654,7 +663,8 @@ def main():
     if not args.no_configs:
         line["configs"] = {
             "uniform_fp64_7pt": uniform_fp64_7pt(lib, 2),
-            "amr_sphere_27pt_plain_fp64": amr_plain_fp64(lib),
+            "amr_sphere_27pt_plain_fp64": amr_plain(lib, FP64),
+            "amr_sphere_27pt_plain_fp32": amr_plain(lib, FP32),
             "uniform_stencil0_fp64": uniform_stencil0(lib),
             "stress_multilevel_7pt_fp32": stress_multilevel(lib, FP32),
             "stress_multilevel_7pt_fp64": stress_multilevel(lib, FP64),
