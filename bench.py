@@ -419,7 +419,10 @@ def profile_case(name):
       stress_fp32, stress_fp64: the recorded multi-level stress run (8^3
         blocks, ~22k of them, 4 vars -- MAMR_PROFILE_VARS sets another
         count -- 7-point), replayed batched: 40 stages, one run per stretch
-        between refinements, with its splits and consolidations."""
+        between refinements, with its splits and consolidations;
+      plain_fp32_27, plain_fp64_27: the benchmark mesh (4096 blocks of
+        16^3, 40 vars) through the plain path, the driver's call sequence:
+        two timesteps of four stages."""
     global V, UPD_PER_STAGE
     import torch
     from miniamr_gb300 import build, load
@@ -448,6 +451,16 @@ def profile_case(name):
         ctx.close()
         print(f"profile case {name}: {sum(n for n, _, _ in timings)} "
               f"batched stages in {len(timings)} runs")
+        return 0
+    if name.startswith("plain"):
+        from miniamr_gb300.abi import RUN_PLAIN
+        STENCIL = 27 if name.endswith("27") else 7
+        ctx, _ = build_mesh(lib, dtype)
+        ctx.run_timesteps(1, SPT, FREQ, flags=RUN_PLAIN)
+        ctx.run_timesteps(1, SPT, FREQ, first_stage=SPT, flags=RUN_PLAIN)
+        torch.cuda.synchronize()
+        ctx.close()
+        print(f"profile case {name}: {2 * SPT} plain stages, {V} vars")
         return 0
     STENCIL = 27 if name.endswith("27") else 7
     V = 4
@@ -526,7 +539,8 @@ def main():
                     help="timesteps of the FP64 comparison runs")
     ap.add_argument("--profile-case", default=None,
                     choices=["fp32_27", "fp32_7", "fp64_27", "fp64_7",
-                             "stress_fp32", "stress_fp64"],
+                             "stress_fp32", "stress_fp64", "plain_fp32_27",
+                             "plain_fp64_27"],
                     help="a small case for ncu (see profile_case)")
     args = ap.parse_args()
     if args.oracle_rate_steps:
