@@ -185,7 +185,8 @@ int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil, int code,
 // ---------------------------------------------------------------------------
 // Stencil: one CTA per active block, the whole block-variable (ghosts
 // included) staged in shared memory, each thread sweeping one (j, k) column
-// along i.  Results are written straight back to the pool: every read comes
+// along i (FP32 8^3 and 16^3 blocks: four k values of one j-row on four
+// i-planes per thread).  Results are written straight back to the pool: every read comes
 // from the staged copy, so the in-place update is the reference's
 // work-array Jacobi update (ref/stencil.c:82-99, 103-141).  Staged rows
 // are Zs long with k = 1 at a 16-byte boundary, so the interior rows of the
