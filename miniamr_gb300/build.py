@@ -85,10 +85,21 @@ def build_oracle() -> str:
     return ORACLE_LIB
 
 
+def reference_sources() -> str | None:
+    """The reference's ref/ directory: MAMR_REFERENCE_SRC, else the ref/
+    directory of a miniAMR checkout named "reference" beside this
+    repository; None when neither exists."""
+    ref = os.environ.get("MAMR_REFERENCE_SRC")
+    if not ref:
+        ref = os.path.join(os.path.dirname(REPO), "reference", "ref")
+    ok = os.path.isfile(os.path.join(ref, "stencil.c"))
+    return ref if ok else None
+
+
 def build_reference_binaries() -> bool:
     """oracle/_ref/ binaries, from the reference sources when present."""
-    ref = os.environ.get("MAMR_REFERENCE_SRC", "/root/reference/ref")
-    if not os.path.isdir(ref):
+    ref = reference_sources()
+    if ref is None:
         return False
     _run(["make", "-s", "-j8", "-C", ORACLE_DIR, "ref", "hybrid",
           "REF=" + ref])

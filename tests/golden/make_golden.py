@@ -1,8 +1,9 @@
 """Generates the golden fixtures in tests/golden/ from the miniAMR reference.
 
-Needs the reference sources (default /root/reference/ref, or
-MAMR_REFERENCE_SRC) and runs only where they exist; the fixtures it writes
-are committed so that the tests need no reference at run time.
+Needs the reference sources -- the directory MAMR_REFERENCE_SRC names, or
+the ref/ directory of a miniAMR checkout named "reference" beside this
+repository -- and runs only where they exist; the fixtures it writes are
+committed so that the tests need no reference at run time.
 
 For every case in CASES it
   1. runs the unmodified reference (oracle/_ref/miniamr_ref) with its
@@ -174,6 +175,22 @@ CASES = {
          ]), []),
     # two objects, volume + surface refinement, 7-point, 4 levels, default
     # checksum cadence (every 5th stage of 3)
+    # the benchmark mesh at an eighth of its size: 4^3 blocks of 16^3
+    # uniformly refined once (512 blocks on one level), 40 variables, 4
+    # stages per timestep, 2 timesteps, a checksum and the cell hashes at
+    # every stage; 27-point (the benchmark's stencil) and its 7-point twin
+    "uniform16_27": ["--init_x", "4", "--init_y", "4", "--init_z", "4",
+                     "--nx", "16", "--ny", "16", "--nz", "16", "--num_vars",
+                     "40", "--stencil", "27", "--num_refine", "1",
+                     "--uniform_refine", "1", "--num_tsteps", "2",
+                     "--stages_per_ts", "4", "--checksum_freq", "1",
+                     "--error_tol", "0", "--max_blocks", "600"],
+    "uniform16_7": ["--init_x", "4", "--init_y", "4", "--init_z", "4",
+                    "--nx", "16", "--ny", "16", "--nz", "16", "--num_vars",
+                    "40", "--stencil", "7", "--num_refine", "1",
+                    "--uniform_refine", "1", "--num_tsteps", "2",
+                    "--stages_per_ts", "4", "--checksum_freq", "1",
+                    "--error_tol", "0", "--max_blocks", "600"],
     "amr7_objects": ["--init_x", "2", "--init_y", "2", "--init_z", "2",
                      "--nx", "6", "--ny", "6", "--nz", "6", "--num_vars", "3",
                      "--stencil", "7", "--num_refine", "4", "--refine_freq",
@@ -236,8 +253,11 @@ def run_case(name, args):
 
 def main(argv):
     if not os.path.exists(REF_BIN) or not os.path.exists(HYB_BIN):
-        subprocess.run(["make", "-s", "-j8", "-C",
-                        os.path.join(REPO, "oracle"), "all"], check=True)
+        sys.path.insert(0, REPO)
+        from miniamr_gb300 import build
+        if not build.build_reference_binaries():
+            sys.exit("make_golden.py: no reference sources (set "
+                     "MAMR_REFERENCE_SRC to miniAMR's ref/ directory)")
     names = argv or list(CASES)
     meta_path = os.path.join(HERE, "cases.json")
     meta = json.load(open(meta_path)) if os.path.exists(meta_path) else {}

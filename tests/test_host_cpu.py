@@ -93,10 +93,13 @@ def test_replica_time_is_max_over_ranks_gloo():
     assert got == [(0, 11.0), (1, 11.0)]
 
 
-REF = os.environ.get("MAMR_REFERENCE_SRC", "/root/reference/ref")
+def _reference_sources():
+    from miniamr_gb300 import build
+    return build.reference_sources()
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources absent")
+@pytest.mark.skipif(_reference_sources() is None,
+                    reason="reference sources absent")
 def test_dropin_matches_reference_on_fresh_case(tmp_path):
     """The reference's driver over the drop-in units and the oracle equals
     the unmodified reference on a case the fixtures do not contain
