@@ -319,6 +319,13 @@ int mamr_initial_values(const mamr_config *cfg, int32_t n_blocks,
  * kernels over n_fp64 hashed doubles.  Runs on the current device. */
 int mamr_selftest_division(int64_t n_fp64, int64_t *mismatches);
 
+/* FP64 pipe throughput of the current device (no counterpart in the
+ * reference): FP64 add and FMA instructions per second over the whole GPU,
+ * each from one timed launch of 8 independent dependent chains per thread
+ * (a few milliseconds).  The bit-exact FP64 paths are bound by this rate,
+ * not by HBM. */
+int mamr_probe_fp64_rate(double *add_per_s, double *fma_per_s);
+
 /* ---- allocation-free checksum ------------------------------------------ */
 
 /* No counterpart in the reference.  For callers that cannot allocate device
@@ -335,14 +342,18 @@ int mamr_selftest_division(int64_t n_fp64, int64_t *mismatches);
  *   blocks   device pointer: FP64 cells in the dense layout of the host
  *            buffers above, [slot][num_vars][nx+2][ny+2][nz+2]
  *   cfg      nx, ny, nz and num_vars of that layout (other fields unused)
- *   slots    device pointer: n_blocks slots in sorted_list order
+ *   slots    device pointer: n_blocks slots in sorted_list order; every
+ *            slot must index a block inside the caller's blocks buffer
+ *            (0 <= slot < the blocks it holds).  The slots live on the
+ *            device, so they are not checked: a slot beyond the buffer is
+ *            an out-of-bounds read.
  *   sum      device pointer that receives the checksum of variable var
  *   stream   cudaStream_t the two kernels are queued on (NULL: default)
  *
- * n_blocks above MAMR_STATIC_MAX_BLOCKS is rejected with MAMR_EINVAL.  The
- * first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  All calls on a device share the one array:
+ * n_blocks above MAMR_STATIC_MAX_BLOCKS is rejected with MAMR_EINVAL, and
+ * device ordinals from 64 up with MAMR_EUNSUP.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  All calls on a device share the one array:
  * calls that overlap on the GPU (other streams, other host threads) race
  * and give wrong sums, so keep them ordered.  Every partial is written
  * before it is read, so no clearing is needed between calls. */

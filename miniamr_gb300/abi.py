@@ -160,6 +160,14 @@ class Library:
             int(num_vars), C.byref(a1), _ptr(a0)), "mamr_work_coefficients")
         return a1.value, a0[:num_vars // 4]
 
+    def probe_fp64_rate(self) -> float:
+        """FP64 add instructions per second the device sustains
+        (mamr_probe_fp64_rate; GPU library only)."""
+        add, fma = C.c_double(), C.c_double()
+        self.check(self.lib.mamr_probe_fp64_rate(C.byref(add), C.byref(fma)),
+                   "mamr_probe_fp64_rate")
+        return add.value
+
     def initial_values(self, cfg: Config, n_blocks: int) -> np.ndarray:
         """The reference's init() values for its first n_blocks blocks,
         [n][num_vars][nx+2][ny+2][nz+2] (mamr_initial_values)."""

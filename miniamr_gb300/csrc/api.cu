@@ -438,11 +438,13 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
       const int s = bp.slot;
       for (int l = 0; l < 6; l++) {
          const int dir = l / 2;
+         // every listed neighbour must be active, whichever of the pair
+         // visits the face (the batched path reads each block's own list)
          if (bp.nei_level[l] == bp.level) {
             int m = bp.nei[l][0][0];
+            if (pos[m] < 0)
+               return fail(MAMR_EMESH, "neighbour slot %d not active", m);
             if (m > s) {
-               if (pos[m] < 0)
-                  return fail(MAMR_EMESH, "neighbour slot %d not active", m);
                // l even: the neighbour is on the low side
                same[dir].push_back(l % 2 == 0 ? SameTask{m, s}
                                               : SameTask{s, m});
@@ -451,18 +453,17 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
             for (int i = 0; i < 2; i++)
                for (int j = 0; j < 2; j++) {
                   int m = bp.nei[l][i][j];
-                  if (m > s) {
-                     if (pos[m] < 0)
-                        return fail(MAMR_EMESH,
-                                    "neighbour slot %d not active", m);
+                  if (pos[m] < 0)
+                     return fail(MAMR_EMESH, "neighbour slot %d not active",
+                                 m);
+                  if (m > s)
                      diff[dir].push_back(DiffTask{s, m, l, i, j});
-                  }
                }
          } else if (bp.nei_level[l] == bp.level - 1) {
             int m = bp.nei[l][0][0];
+            if (pos[m] < 0)
+               return fail(MAMR_EMESH, "neighbour slot %d not active", m);
             if (m > s) {
-               if (pos[m] < 0)
-                  return fail(MAMR_EMESH, "neighbour slot %d not active", m);
                const mamr_block &mb = blocks[pos[m]];
                int k = dir * 2 + 1 - l % 2;
                for (int i = 0; i < 2; i++)

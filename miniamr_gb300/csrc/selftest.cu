@@ -92,3 +92,91 @@ extern "C" int mamr_selftest_division(int64_t n_fp64, int64_t *mismatches)
       mismatches[q] = (int64_t) h[q];
    return MAMR_OK;
 }
+
+// ---- FP64 pipe throughput --------------------------------------------------
+// The bit-exact FP64 paths are bound by the FP64 pipe, not by HBM.  This
+// probe measures what that pipe sustains: every thread runs 8 independent
+// chains of dependent FP64 adds (or FMAs), enough warps in flight to cover
+// the pipe's latency, a fixed number of iterations (no data-dependent
+// loop), and the result is stored only under a condition the values never
+// meet, so that nothing is optimised away.
+namespace {
+
+constexpr int kProbeIters = 2048;
+
+template <bool FMA>
+__global__ void __launch_bounds__(256) fp64_probe(double seed, double *sink)
+{
+   double a[8];
+#pragma unroll
+   for (int q = 0; q < 8; q++)
+      a[q] = seed + (threadIdx.x + q) * 1e-9;
+   const double c = 1e-300, m = 1.0 - 1e-16;
+#pragma unroll 4
+   for (int it = 0; it < kProbeIters; it++)
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+         a[q] = FMA ? __fma_rn(a[q], m, c) : __dadd_rn(a[q], c);
+   double t = a[0];
+#pragma unroll
+   for (int q = 1; q < 8; q++)
+      t = __dadd_rn(t, a[q]);
+   if (t == 12345.678)
+      *sink = t;
+}
+
+template <bool FMA>
+float time_probe(int grid, double *sink, cudaStream_t s, cudaEvent_t e0,
+                 cudaEvent_t e1)
+{
+   fp64_probe<FMA><<<grid, 256, 0, s>>>(1.0, sink);           // warm-up
+   cudaEventRecord(e0, s);
+   fp64_probe<FMA><<<grid, 256, 0, s>>>(1.0, sink);
+   cudaEventRecord(e1, s);
+   float ms = 0.f;
+   if (cudaEventSynchronize(e1) != cudaSuccess ||
+       cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+      return -1.f;
+   return ms;
+}
+
+}  // namespace
+
+extern "C" int mamr_probe_fp64_rate(double *add_per_s, double *fma_per_s)
+{
+   if (!add_per_s || !fma_per_s)
+      return mamr::report_error(MAMR_EINVAL, "fp64 probe: null argument");
+   int dev = 0, sms = 0;
+   cudaError_t e = cudaGetDevice(&dev);
+   if (e == cudaSuccess)
+      e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+   double *sink = nullptr;
+   cudaStream_t s = nullptr;
+   cudaEvent_t e0 = nullptr, e1 = nullptr;
+   if (e == cudaSuccess)
+      e = cudaMalloc(&sink, sizeof(double));
+   if (e == cudaSuccess)
+      e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+   if (e == cudaSuccess)
+      e = cudaEventCreate(&e0);
+   if (e == cudaSuccess)
+      e = cudaEventCreate(&e1);
+   float ms_add = -1.f, ms_fma = -1.f;
+   const int grid = sms * 8;
+   if (e == cudaSuccess) {
+      ms_add = time_probe<false>(grid, sink, s, e0, e1);
+      ms_fma = time_probe<true>(grid, sink, s, e0, e1);
+      e = cudaGetLastError();
+   }
+   if (e0) cudaEventDestroy(e0);
+   if (e1) cudaEventDestroy(e1);
+   if (s) cudaStreamDestroy(s);
+   if (sink) cudaFree(sink);
+   if (e != cudaSuccess || ms_add <= 0.f || ms_fma <= 0.f)
+      return mamr::report_error(MAMR_ECUDA, "fp64 probe: %s",
+                                cudaGetErrorString(e));
+   const double ops = (double) grid * 256 * kProbeIters * 8;
+   *add_per_s = ops / (ms_add * 1e-3);
+   *fma_per_s = ops / (ms_fma * 1e-3);
+   return MAMR_OK;
+}

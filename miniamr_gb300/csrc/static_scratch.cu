@@ -25,18 +25,27 @@ double *g_partials_ptr[kMaxDevices];
 
 // Once per device, with that device current: the device address of
 // g_block_partials.  In host code the array's name is only a host-side
-// stand-in, so kernels must be given this address.
+// stand-in, so kernels must be given this address.  Failures are reported
+// here, with their own message.
 int partials_address(double **out)
 {
    int dev = 0;
-   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-      return MAMR_ECUDA;
+   cudaError_t e = cudaGetDevice(&dev);
+   if (e != cudaSuccess)
+      return mamr::report_error(MAMR_ECUDA, "noalloc checksum: no current "
+                                "device: %s", cudaGetErrorString(e));
+   if (dev < 0 || dev >= kMaxDevices)
+      return mamr::report_error(MAMR_EUNSUP, "noalloc checksum: device "
+                                "ordinal %d is beyond the %d devices it "
+                                "serves", dev, kMaxDevices);
    std::lock_guard<std::mutex> lock(g_setup_mutex);
    if (!g_partials_ptr[dev]) {
       void *p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, g_block_partials);
+      e = cudaGetSymbolAddress(&p, g_block_partials);
       if (e != cudaSuccess)
-         return MAMR_ECUDA;
+         return mamr::report_error(MAMR_ECUDA, "noalloc checksum: device "
+                                   "address of the static scratch: %s",
+                                   cudaGetErrorString(e));
       g_partials_ptr[dev] = static_cast<double *>(p);
    }
    *out = g_partials_ptr[dev];
@@ -65,9 +74,7 @@ extern "C" int mamr_check_sum_fp64_noalloc(const double *blocks,
    double *partials = nullptr;
    int r = partials_address(&partials);
    if (r != MAMR_OK)
-      return mamr::report_error(r, "noalloc checksum: device address of "
-                                "the static scratch: %s",
-                                cudaGetErrorString(cudaGetLastError()));
+      return r;
    // the dense layout of the ABI's host buffers: no row padding
    mamr::Geom g;
    g.nx = cfg->nx; g.ny = cfg->ny; g.nz = cfg->nz; g.V = cfg->num_vars;

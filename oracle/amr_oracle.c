@@ -7,8 +7,9 @@
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
  * it.  Parity of this restatement with the reference itself is pinned by
  * running the reference's own driver over these functions
- * (oracle/_ref/miniamr_hybrid_oracle vs oracle/_ref/miniamr_ref, see
- * tests/test_oracle_vs_reference.py) and by the committed golden logs.
+ * (oracle/_ref/miniamr_hybrid_oracle vs oracle/_ref/miniamr_ref:
+ * tests/golden/make_golden.py, tests/test_host_cpu.py) and by the committed
+ * golden logs (tests/test_oracle_golden.py).
  *
  * Every routine is a sequential restatement of the reference code it cites
  * (paths are inside the miniAMR repository).  Cells are held as doubles in
@@ -254,6 +255,31 @@ int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks, int32_t n)
                               "misconnected block (slot %d face %d nei %d)",
                               bp->slot, l, bp->nei[l][i][j]);
       }
+   }
+   /* every listed neighbour must be active (the library checks the same) */
+   {
+      unsigned char *act = (unsigned char *) calloc((size_t) c->cfg.max_blocks,
+                                                    1);
+      int bad = -1;
+      if (!act)
+         return fail(MAMR_ENOMEM, "host allocation");
+      for (b = 0; b < n; b++)
+         act[blocks[b].slot] = 1;
+      for (b = 0; b < n && bad < 0; b++)
+         for (l = 0; l < 6; l++) {
+            const mamr_block *bp = &blocks[b];
+            const int nl = bp->nei_level[l];
+            if (nl == -2)
+               continue;
+            for (i = 0; i < 2; i++)
+               for (j = 0; j < 2; j++)
+                  if ((nl == bp->level + 1 || (i == 0 && j == 0)) &&
+                      !act[bp->nei[l][i][j]])
+                     bad = bp->nei[l][i][j];
+         }
+      free(act);
+      if (bad >= 0)
+         return fail(MAMR_EMESH, "neighbour slot %d not active", bad);
    }
    m = (mamr_block *) malloc(sizeof(mamr_block) * (n ? n : 1));
    if (!m)
@@ -543,47 +569,114 @@ int mamr_comm(mamr_ctx *c, int32_t start, int32_t num, int32_t stage)
    return MAMR_OK;
 }
 
-/* ref/stencil.c:76-145 (stencil_calc), Jacobi update of every active
- * block's interior for one variable. */
-static void stencil_block(mamr_ctx *c, int st, double *a, double *work)
+/* Rounds to the pool's precision where f32 is a compile-time constant (the
+ * stencil and checksum loops below are instantiated once per precision, so
+ * the FP64 loops carry no test and vectorise along k). */
+#define RND(f32, x) ((f32) ? (double) (float) (x) : (x))
+#define ORACLE_INLINE static inline __attribute__((always_inline))
+
+/* ref/stencil.c:82-101: the 7-point average of interior plane i into out
+ * (rows of nz values, row j at (j-1)*nz), in the reference's term order. */
+ORACLE_INLINE void stencil7_plane(const mamr_ctx *c, const double *a, int i,
+                                  double *out, const int f32)
 {
-   int nx = c->cfg.nx, ny = c->cfg.ny, nz = c->cfg.nz, i, j, k;
-   for (i = 1; i <= nx; i++)
-      for (j = 1; j <= ny; j++)
-         for (k = 1; k <= nz; k++) {
-            double w;
-            if (st == 7) {
-               w = RF(c, AT(a, i - 1, j, k) + AT(a, i, j - 1, k));
-               w = RF(c, w + AT(a, i, j, k - 1));
-               w = RF(c, w + AT(a, i, j, k));
-               w = RF(c, w + AT(a, i, j, k + 1));
-               w = RF(c, w + AT(a, i, j + 1, k));
-               w = RF(c, w + AT(a, i + 1, j, k));
-               w = RF(c, w / 7.0);
-            } else {
-               double s[3];
-               int p, jj, kk;
-               for (p = 0; p < 3; p++) {
-                  double t = 0.0;
-                  int first = 1;
-                  for (jj = j - 1; jj <= j + 1; jj++)
-                     for (kk = k - 1; kk <= k + 1; kk++) {
-                        if (first) {
-                           t = AT(a, i - 1 + p, jj, kk);
-                           first = 0;
-                        } else
-                           t = RF(c, t + AT(a, i - 1 + p, jj, kk));
-                     }
-                  s[p] = t;
-               }
-               w = RF(c, RF(c, RF(c, s[0] + s[1]) + s[2]) / 27.0);
-            }
-            AT(work, i, j, k) = w;
-         }
-   for (i = 1; i <= nx; i++)
-      for (j = 1; j <= ny; j++)
-         for (k = 1; k <= nz; k++)
-            AT(a, i, j, k) = AT(work, i, j, k);
+   const int ny = c->cfg.ny, nz = c->cfg.nz;
+   const ptrdiff_t sy = c->Z, sx = (ptrdiff_t) c->Y * c->Z;
+   int j, k;
+   for (j = 1; j <= ny; j++) {
+      const double *p = a + i * sx + j * sy;
+      double *o = out + (size_t) (j - 1) * nz - 1;
+      for (k = 1; k <= nz; k++) {
+         double s = RND(f32, p[k - sx] + p[k - sy]);
+         s = RND(f32, s + p[k - 1]);
+         s = RND(f32, s + p[k]);
+         s = RND(f32, s + p[k + 1]);
+         s = RND(f32, s + p[k + sy]);
+         s = RND(f32, s + p[k + sx]);
+         o[k] = RND(f32, s / 7.0);
+      }
+   }
+}
+
+/* The 9-term sum of ref/stencil.c:108-134 for every interior (j, k) of
+ * plane p (sb, sm or sf of the cells whose i-1, i or i+1 plane it is),
+ * left to right over (j-1, k-1) .. (j+1, k+1). */
+ORACLE_INLINE void plane_sums9(const mamr_ctx *c, const double *a, int p,
+                               double *out, const int f32)
+{
+   const int ny = c->cfg.ny, nz = c->cfg.nz;
+   const ptrdiff_t sy = c->Z, sx = (ptrdiff_t) c->Y * c->Z;
+   int j, k;
+   for (j = 1; j <= ny; j++) {
+      const double *r0 = a + p * sx + (j - 1) * sy, *r1 = r0 + sy,
+                   *r2 = r1 + sy;
+      double *o = out + (size_t) (j - 1) * nz - 1;
+      for (k = 1; k <= nz; k++) {
+         double t = RND(f32, r0[k - 1] + r0[k]);
+         t = RND(f32, t + r0[k + 1]);
+         t = RND(f32, t + r1[k - 1]);
+         t = RND(f32, t + r1[k]);
+         t = RND(f32, t + r1[k + 1]);
+         t = RND(f32, t + r2[k - 1]);
+         t = RND(f32, t + r2[k]);
+         o[k] = RND(f32, t + r2[k + 1]);
+      }
+   }
+}
+
+/* Copies rows of nz values (row j at (j-1)*nz) into interior plane i. */
+static void store_plane(const mamr_ctx *c, double *a, int i, const double *in)
+{
+   const int ny = c->cfg.ny, nz = c->cfg.nz;
+   int j;
+   for (j = 1; j <= ny; j++)
+      memcpy(&AT(a, i, j, 1), in + (size_t) (j - 1) * nz,
+             sizeof(double) * nz);
+}
+
+/* ref/stencil.c:76-145 (stencil_calc), Jacobi update of one block-variable.
+ * Each output plane is written back as soon as no later plane reads its
+ * old values (the reference's work array holds the whole block): 7-point,
+ * plane i-1 after plane i is computed; 27-point, plane i as soon as the
+ * sums of plane i+1 exist -- each 9-term plane sum is formed once and used
+ * by the three cells that need it, the same additions in the same order.
+ * scratch holds 3 * ny * nz doubles. */
+ORACLE_INLINE void stencil_block_t(const mamr_ctx *c, int st, double *a,
+                                   double *scratch, const int f32)
+{
+   const int nx = c->cfg.nx;
+   const size_t pl = (size_t) c->cfg.ny * c->cfg.nz;
+   int i;
+   size_t q;
+   if (st == 7) {
+      double *buf[2] = {scratch, scratch + pl};
+      for (i = 1; i <= nx; i++) {
+         stencil7_plane(c, a, i, buf[i & 1], f32);
+         if (i > 1)
+            store_plane(c, a, i - 1, buf[(i - 1) & 1]);
+      }
+      store_plane(c, a, nx, buf[nx & 1]);
+      return;
+   }
+   double *s0 = scratch, *s1 = scratch + pl, *s2 = scratch + 2 * pl, *t;
+   plane_sums9(c, a, 0, s0, f32);
+   plane_sums9(c, a, 1, s1, f32);
+   for (i = 1; i <= nx; i++) {
+      plane_sums9(c, a, i + 1, s2, f32);
+      /* plane i's old values are no longer read: overwrite them */
+      for (q = 0; q < pl; q++)
+         s0[q] = RND(f32, RND(f32, RND(f32, s0[q] + s1[q]) + s2[q]) / 27.0);
+      store_plane(c, a, i, s0);
+      t = s0; s0 = s1; s1 = s2; s2 = t;
+   }
+}
+
+static void stencil_block(mamr_ctx *c, int st, double *a, double *scratch)
+{
+   if (c->fp32)
+      stencil_block_t(c, st, a, scratch, 1);
+   else
+      stencil_block_t(c, st, a, scratch, 0);
 }
 
 /* ref/stencil.c:76-145 (stencil_calc), Jacobi update of every active
@@ -673,7 +766,14 @@ int mamr_stencil(mamr_ctx *c, int32_t var, int32_t calc_stage)
                   "the first stencil");
 #pragma omp parallel reduction(|:bad)
    {
-      double *work = (double *) malloc(sizeof(double) * c->bv);
+      /* the variable-work kernels' block-sized work array, or the plain
+         stencil's three planes */
+      double *work = (double *) malloc(sizeof(double) *
+                                       (c->bv > 3 * (size_t) c->cfg.ny *
+                                                    c->cfg.nz
+                                           ? c->bv
+                                           : 3 * (size_t) c->cfg.ny *
+                                                c->cfg.nz));
       int in;
       if (!work)
          bad = 1;
@@ -724,16 +824,27 @@ int mamr_check_sum(mamr_ctx *c, int32_t var, double *sum)
                                               (c->n_mesh ? c->n_mesh : 1));
       if (!bs)
          return fail(MAMR_ENOMEM, "host allocation");
-#pragma omp parallel for schedule(dynamic, 8)
-      for (in = 0; in < c->n_mesh; in++) {
-         const double *a = blk(c, c->mesh[in].slot, var);
-         double block_sum = 0.0;
-         int i, j, k;
+      /* four blocks' serial sums side by side (independent chains in
+         flight; each block's additions in the reference's order) */
+#pragma omp parallel for schedule(dynamic, 2)
+      for (in = 0; in < c->n_mesh; in += 4) {
+         const double *a[4];
+         double t[4] = {0.0, 0.0, 0.0, 0.0};
+         int i, j, k, q, m = c->n_mesh - in < 4 ? c->n_mesh - in : 4;
+         for (q = 0; q < 4; q++)
+            a[q] = blk(c, c->mesh[in + (q < m ? q : 0)].slot, var);
          for (i = 1; i <= c->cfg.nx; i++)
-            for (j = 1; j <= c->cfg.ny; j++)
-               for (k = 1; k <= c->cfg.nz; k++)
-                  block_sum += AT(a, i, j, k);
-         bs[in] = block_sum;
+            for (j = 1; j <= c->cfg.ny; j++) {
+               const size_t r = ((size_t) i * c->Y + j) * c->Z;
+               for (k = 1; k <= c->cfg.nz; k++) {
+                  t[0] += a[0][r + k];
+                  t[1] += a[1][r + k];
+                  t[2] += a[2][r + k];
+                  t[3] += a[3][r + k];
+               }
+            }
+         for (q = 0; q < m; q++)
+            bs[in + q] = t[q];
       }
       for (in = 0; in < c->n_mesh; in++)
          s += bs[in];

@@ -34,7 +34,8 @@ def test_gpu_library_exports_every_abi_function():
 
 def test_oracle_exports_the_hot_path_abi(oracle_lib):
     for f in header_functions():
-        if f in ("mamr_check_sum_fp64_noalloc", "mamr_selftest_division"):
+        if f in ("mamr_check_sum_fp64_noalloc", "mamr_selftest_division",
+                 "mamr_probe_fp64_rate"):
             continue                     # device-only entry points
         assert hasattr(oracle_lib.lib, f), f
 
@@ -158,3 +159,45 @@ def test_bench_reference_arm_json_line():
     assert d["cpu_baseline"]["kind"] == "port"
     assert d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["e2e"]["value"] == d["value"]
+
+
+REF_BIN = os.path.join(REPO, "oracle", "_ref", "miniamr_ref")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BIN),
+                    reason="reference binary not built here")
+def test_cpu_port_keeps_up_with_the_reference_binary(tmp_path):
+    """The CPU baseline (bench.py's reference arm and cpu_baseline) times the
+    oracle, a restatement of the reference's code; it must run at least at
+    1/1.25 of the reference binary's own rate on this host, one thread,
+    same case: 64 blocks of 16^3 (2x2x2 initial, uniform refine 1), 40
+    variables, 27-point, 2 timesteps of 4 stages, checksum every 5th stage.
+    Reference rate from its Summary line (calc + comm + red,
+    ref/profile.c:1298); best of three runs each."""
+    n_upd = 2 * 4 * 64 * 16 ** 3 * 40
+    args = ["--init_x", "2", "--init_y", "2", "--init_z", "2", "--nx", "16",
+            "--ny", "16", "--nz", "16", "--num_vars", "40", "--stencil", "27",
+            "--num_refine", "1", "--uniform_refine", "1", "--num_tsteps", "2",
+            "--stages_per_ts", "4", "--checksum_freq", "5", "--max_blocks",
+            "100"]
+    ref = []
+    for _ in range(3):
+        r = subprocess.run([REF_BIN] + args, cwd=tmp_path, capture_output=True,
+                           text=True, check=True)
+        f = [l.split() for l in r.stdout.splitlines()
+             if l.startswith("Summary")][-1]
+        t = float(f[f.index("calc") + 1]) + float(f[f.index("comm") + 1]) + \
+            float(f[f.index("red") + 1])
+        ref.append(n_upd / t)
+    port = []
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    for _ in range(3):
+        r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"),
+                            "--oracle-rate-steps", "2"], env=env,
+                           capture_output=True, text=True, check=True)
+        port.append(__import__("json").loads(
+            r.stdout.strip().splitlines()[-1])["value"])
+    factor = max(ref) / max(port)
+    print(f"reference {max(ref):.3e}, port {max(port):.3e} updates/s: the "
+          f"port is {factor:.2f}x slower")
+    assert factor <= 1.25, (ref, port)

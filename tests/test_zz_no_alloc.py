@@ -46,12 +46,21 @@ def test_noalloc_checksum_equals_check_sum(gpu_lib):
         out = torch.zeros(1, dtype=torch.float64, device="cuda")
         f = _bind(gpu_lib)
         stream = torch.cuda.current_stream().cuda_stream
-        for var in (0, 2):     # two calls in a row share the scratch
+        want = {var: ctx.check_sum(var) for var in (0, 2)}
+
+        def call(var):
             rc = f(dev_blocks.data_ptr(), C.byref(cfg), dev_slots.data_ptr(),
                    len(slots), var, out.data_ptr(), stream)
             assert rc == 0, gpu_lib.lib.mamr_last_error()
             torch.cuda.synchronize()
-            assert out.item() == ctx.check_sum(var)     # bit-exact
+            return out.item()
+        # the first call on the device looks up the scratch's address
+        call(0)
+        free_before = torch.cuda.mem_get_info()[0]
+        got = {var: call(var) for var in (0, 2)}   # two calls in a row
+        assert torch.cuda.mem_get_info()[0] == free_before, \
+            "the allocation-free checksum changed the free device memory"
+        assert got == want                          # bit-exact
         rc = f(dev_blocks.data_ptr(), C.byref(cfg), dev_slots.data_ptr(),
                MAX_BLOCKS + 1, 0, out.data_ptr(), stream)
         assert rc == -1
