@@ -449,9 +449,9 @@ def profile_case(name):
     MAMR_PROFILE_SHAPE (default 0, the one the tuner keeps for the
     benchmark workload) so that launch indices are stable.
       fp32_27, fp32_7, fp64_27, fp64_7: 4096 blocks of 16^3, 4 vars (268 MB
-        of FP32 interior cells per pool, twice the L2), two timesteps of
-        four stages (checksums on each timestep's first stage, as in the
-        benchmark);
+        of FP32 interior cells per pool, twice the L2; MAMR_PROFILE_VARS
+        sets another count), two timesteps of four stages (checksums on
+        each timestep's first stage, as in the benchmark);
       stress_fp32, stress_fp64: the recorded multi-level stress run (8^3
         blocks, ~22k of them, 4 vars -- MAMR_PROFILE_VARS sets another
         count -- 7-point), replayed batched: 40 stages, one run per stretch
@@ -499,7 +499,7 @@ def profile_case(name):
         print(f"profile case {name}: {2 * SPT} plain stages, {V} vars")
         return 0
     STENCIL = 27 if name.endswith("27") else 7
-    V = 4
+    V = int(os.environ.get("MAMR_PROFILE_VARS", "4"))
     UPD_PER_STAGE = N_BLOCKS * N ** 3 * V
     ctx, _ = build_mesh(lib, dtype)
     ctx.set_tuning(shape)
