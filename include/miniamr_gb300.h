@@ -214,8 +214,15 @@ int mamr_set_work_params(mamr_ctx *ctx, double a1, const double *a0,
 
 /* check_sum(var): ref/check_sum.c:36-65.  FP64 pools sum each block's
  * interior serially (k fastest) and the block sums in sorted_list order,
- * the reference's exact order.  FP32 pools accumulate every cell exactly
- * in 128-bit fixed point (2^-52 units) and convert once. */
+ * the reference's exact order.  FP32 pools: when every cell v of the
+ * variable lies in the window v == 0 or 2^-52 <= |v| < 2^10, each cell
+ * contributes trunc(v * 2^52) exactly to a 128-bit fixed-point sum that is
+ * converted to double once (order-independent; error at most 2^-52 per
+ * cell); otherwise (a cell of 2^10 or more, infinite or NaN, or non-zero
+ * below 2^-52) the variable takes the reference's order in FP64 with
+ * Neumaier compensation -- each block serially into s + c, then the block
+ * values serially in sorted_list order.  Every path is deterministic and
+ * the same in mamr_run_timesteps' checksums. */
 int mamr_check_sum(mamr_ctx *ctx, int32_t var, double *sum);
 
 /* split_blocks() cell data: ref/block.c:158-173.  Jobs run in the given

@@ -99,6 +99,7 @@ const int kPerm[6][3] = { {0, 1, 2}, {1, 2, 0}, {2, 0, 1},
 namespace mamr {
 struct BatchedState {
    DevBuf items, partials, sums, acc, chain, pencils, bad;
+   DevBuf csflags;             // FP32: per checksum stage, 1 + V miss words
    BItem *h_items = nullptr;   // pinned staging of the item upload
    size_t h_cap = 0;           // its capacity in items
    int n = 0;
@@ -113,7 +114,7 @@ void batched_destroy(BatchedState *b)
       return;
    b->items.release(); b->partials.release(); b->sums.release();
    b->acc.release(); b->chain.release(); b->pencils.release();
-   b->bad.release();
+   b->bad.release(); b->csflags.release();
    if (b->h_items)
       cudaFreeHost(b->h_items);
    delete b;
@@ -142,6 +143,7 @@ struct mamr_ctx {
    DirTasks tasks[3];
    DevBuf d_partials, d_jobs, d_stage, d_stage_slots, d_sums;
    DevBuf d_xfer, d_xfer_slots;      // staging copies for split/consolidate
+   DevBuf d_csflags;                // FP32 checksum miss words (plain path)
    unsigned long long *d_acc;       // 2 words: fixed-point accumulator
    double *d_sum;                   // FP64 checksum result
    unsigned *d_err;                 // device error word
@@ -279,7 +281,7 @@ extern "C" int mamr_destroy(mamr_ctx *c)
    c->d_stage.release(); c->d_stage_slots.release(); c->d_sums.release();
    c->d_xfer.release(); c->d_xfer_slots.release(); c->d_work.release();
    c->d_mark.release(); c->d_cs.release();
-   c->d_mesh.release(); c->d_slot_pos.release();
+   c->d_mesh.release(); c->d_slot_pos.release(); c->d_csflags.release();
    if (c->d_acc) cudaFree(c->d_acc);
    if (c->d_sum) cudaFree(c->d_sum);
    if (c->d_err) cudaFree(c->d_err);
@@ -634,10 +636,16 @@ extern "C" int mamr_set_work_params(mamr_ctx *c, double a1, const double *a0,
    return MAMR_OK;
 }
 
-// Converts a 128-bit fixed-point accumulator (units of 2^-52) to double
-// with one correct rounding.
+// An FP32 checksum slot as a double: a 128-bit fixed-point accumulator
+// (units of 2^-52) converted with one correct rounding, or -- under the
+// fallback mark -- the compensated FP64 sum the fallback stored.
 static double fixed_to_double(unsigned long long lo, unsigned long long hi)
 {
+   if (hi == kChecksumFallbackMark) {
+      double d;
+      memcpy(&d, &lo, sizeof(d));
+      return d;
+   }
    __int128 v = (__int128) (((unsigned __int128) hi << 64) |
                             (unsigned __int128) lo);
    return (double) v * 0x1p-52;
@@ -649,11 +657,18 @@ static int checksum_queue(mamr_ctx *c, int32_t var, double *d_out,
 {
    const int n = (int) c->mesh.size();
    if (c->fp32) {
+      CUDA_TRY(c->d_csflags.ensure(2 * sizeof(unsigned)));
+      unsigned *flags = (unsigned *) c->d_csflags.p;
       CUDA_TRY(cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long),
                                c->stream));
+      CUDA_TRY(cudaMemsetAsync(flags, 0, 2 * sizeof(unsigned), c->stream));
       LAUNCH_TRY(c, launch_checksum_fp32((const float *) c->pool, c->g,
                                          (const int32_t *) c->d_slots.p, n,
-                                         var, acc, c->d_err, c->stream));
+                                         var, acc, flags, c->stream));
+      LAUNCH_TRY(c, launch_fp32_checksum_fallback(
+                       (const float *) c->pool, c->g,
+                       (const int32_t *) c->d_slots.p, n, var, 1, flags,
+                       (double *) c->d_partials.p, acc, c->stream));
    } else {
       LAUNCH_TRY(c, launch_checksum_fp64((const double *) c->pool, c->g,
                                          (const int32_t *) c->d_slots.p, n,
@@ -862,6 +877,11 @@ static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
    const size_t slot_bytes = c->fp32 ? 2 * sizeof(unsigned long long)
                                      : sizeof(double);
    CUDA_TRY(c->d_sums.ensure(std::max<size_t>(1, n_cs * V) * slot_bytes));
+   if (c->fp32) {
+      const size_t fb = std::max<size_t>(1, n_cs) * (1 + V) * sizeof(unsigned);
+      CUDA_TRY(c->d_csflags.ensure(fb));
+      CUDA_TRY(cudaMemsetAsync(c->d_csflags.p, 0, fb, c->stream));
+   }
    int cnt = 0, gstage = first_stage, r;
    for (int ts = 0; ts < num_ts; ts++)
       for (int st = 0; st < spt; st++, gstage++) {
@@ -880,10 +900,17 @@ static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
             CUDA_TRY(cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long) *
                                                 V,
                                      c->stream));
+            unsigned *flags = (unsigned *) c->d_csflags.p +
+                              (size_t) cnt * (1 + V);
             LAUNCH_TRY(c, launch_checksum_fp32_all(
                              (const float *) c->pool, c->g,
                              (const int32_t *) c->d_slots.p,
-                             (int) c->mesh.size(), acc, c->d_err, c->stream));
+                             (int) c->mesh.size(), acc, flags, c->stream));
+            LAUNCH_TRY(c, launch_fp32_checksum_fallback(
+                             (const float *) c->pool, c->g,
+                             (const int32_t *) c->d_slots.p,
+                             (int) c->mesh.size(), 0, V, flags,
+                             (double *) c->d_partials.p, acc, c->stream));
          }
          if (do_cs && !c->fp32)
             LAUNCH_TRY(c, launch_checksum_fp64_all(
@@ -1224,12 +1251,15 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       CUDA_TRY(cudaMalloc(&c->pool_alt, c->pool_bytes));
       CUDA_TRY(cudaMemsetAsync(c->pool_alt, 0, c->pool_bytes, c->stream));
    }
+   CUDA_TRY(B->partials.ensure(sizeof(double) * std::max(1, nb) * V));
    if (c->fp32) {
       CUDA_TRY(B->acc.ensure(std::max<size_t>(1, n_cs * V) * 16));
       CUDA_TRY(cudaMemsetAsync(B->acc.p, 0, std::max<size_t>(1, n_cs * V) * 16,
                                c->stream));
+      const size_t fb = std::max<size_t>(1, n_cs) * (1 + V) * sizeof(unsigned);
+      CUDA_TRY(B->csflags.ensure(fb));
+      CUDA_TRY(cudaMemsetAsync(B->csflags.p, 0, fb, c->stream));
    } else {
-      CUDA_TRY(B->partials.ensure(sizeof(double) * std::max(1, nb) * V));
       CUDA_TRY(B->sums.ensure(sizeof(double) * std::max<size_t>(1, n_cs * V)));
    }
    const bool pencil = B->n_pencils > 0;
@@ -1243,14 +1273,26 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       double *sums_at =
          c->fp32 ? nullptr : (double *) B->sums.p + (size_t) cnt * V;
       double *part = c->fp32 ? nullptr : (double *) B->partials.p;
+      // FP32 checksum stages: the stage kernel reports cells outside the
+      // fixed-point window in the stage's miss word, and the fallback
+      // (empty unless it was set) replaces those variables' sums
+      unsigned *flags = c->fp32 && do_cs
+                           ? (unsigned *) B->csflags.p + (size_t) cnt * (1 + V)
+                           : c->d_err;
+      auto fallback = [&](int k) -> int {
+         if (k < 0 || !c->fp32 || !do_cs)
+            return k;
+         const int f = launch_fp32_checksum_fallback(
+            (const float *) oth, c->g, (const int32_t *) c->d_slots.p, nb, 0,
+            V, flags, (double *) B->partials.p, acc, c->stream);
+         return f < 0 ? -1 : k + f;
+      };
       if (pencil && c->fp32)
-         return launch_pencil_stage((const float *) cur, (float *) oth, c->g,
-                                    c->cfg.stencil,
-                                    (const BItem *) B->items.p, nb,
-                                    (const TileDesc *) B->chain.p,
-                                    (const int2 *) B->pencils.p, np, sh, last,
-                                    do_cs, part, sums_at, acc, c->d_err,
-                                    c->stream);
+         return fallback(launch_pencil_stage(
+            (const float *) cur, (float *) oth, c->g, c->cfg.stencil,
+            (const BItem *) B->items.p, nb, (const TileDesc *) B->chain.p,
+            (const int2 *) B->pencils.p, np, sh, last, do_cs, part, sums_at,
+            acc, flags, c->stream));
       if (pencil)
          return launch_pencil_stage((const double *) cur, (double *) oth,
                                     c->g, c->cfg.stencil,
@@ -1260,11 +1302,10 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
                                     do_cs, part, sums_at, acc, c->d_err,
                                     c->stream);
       if (c->fp32)
-         return launch_batched_stage((const float *) cur, (float *) oth,
-                                     c->g, c->cfg.stencil,
-                                     (const BItem *) B->items.p, nb, sh, last,
-                                     do_cs, part, sums_at, acc, c->d_err,
-                                     c->stream);
+         return fallback(launch_batched_stage(
+            (const float *) cur, (float *) oth, c->g, c->cfg.stencil,
+            (const BItem *) B->items.p, nb, sh, last, do_cs, part, sums_at,
+            acc, flags, c->stream));
       return launch_batched_stage((const double *) cur, (double *) oth, c->g,
                                   c->cfg.stencil, (const BItem *) B->items.p,
                                   nb, sh, last, do_cs, part, sums_at, acc,

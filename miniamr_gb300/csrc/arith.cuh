@@ -140,7 +140,11 @@ __device__ __forceinline__ float sum8(const float *t)
 
 // ---- exact fixed-point checksum of FP32 cells ------------------------------
 // A cell v contributes trunc(v * 2^52) (toward zero), summed exactly in
-// 128-bit two's complement; |v| must be below 2^10 (finite).
+// 128-bit two's complement.  The exact window is v == 0 or
+// 2^-52 <= |v| < 2^10: larger or non-finite cells do not fit the
+// accumulator, smaller non-zero ones would vanish.  A variable with a cell
+// outside it takes the compensated FP64 sum instead (fp32_fallback_* in
+// plain_kernels.cu); fixed52_add reports the miss.
 //
 // The term is formed with FP32 additions only (an FP64 or 64-bit integer
 // conversion would run on this part's slow FP64 pipe): with x = |v| and
@@ -160,7 +164,8 @@ struct Fixed52 {
    int cnt = 0;                       // sum of the signs
 };
 
-// Adds the term of v (negate: its opposite); returns whether |v| < 2^10.
+// Adds the term of v (negate: its opposite); returns whether v lies in the
+// exact window (v == 0 or 2^-52 <= |v| < 2^10).
 __device__ __forceinline__ bool fixed52_add(float v, Fixed52 &p,
                                             bool negate = false)
 {
@@ -177,7 +182,24 @@ __device__ __forceinline__ bool fixed52_add(float v, Fixed52 &p,
    p.a2 += (unsigned) s * __float_as_uint(t2);
    p.a3 += (unsigned) s * __float_as_uint(t3);
    p.cnt += s;
-   return x < 1024.0f;
+   return x < 1024.0f && (x >= 0x1p-52f || x == 0.0f);
+}
+
+// The compensated (Neumaier) FP64 step the checksum fallback uses: adds x
+// to the running sum s with its correction c.  Once the sum is not finite
+// the correction is left alone (it would turn an infinite sum into NaN),
+// so an infinite cell gives an infinite sum, as plain summation does.
+__host__ __device__ __forceinline__ void neumaier_add(double &s, double &c,
+                                                      double x)
+{
+   const double t = s + x;
+   if (isfinite(t)) {
+      if (fabs(s) >= fabs(x))
+         c = c + ((s - t) + x);
+      else
+         c = c + ((x - t) + s);
+   }
+   s = t;
 }
 
 // 128-bit two's complement accumulator held as (lo, hi): adds the

@@ -65,6 +65,11 @@ struct DirTasks {
    const BcTask *bc; int n_bc;
 };
 
+// Marks an FP32 checksum slot (lo, hi) whose lo word holds the bits of a
+// double (the compensated FP64 fallback's result) instead of a fixed-point
+// sum: a genuine sum has |hi| < 2^40, so hi never takes this value.
+constexpr unsigned long long kChecksumFallbackMark = 0x8000000000000000ull;
+
 // Error word bits written by kernels (context error word).
 enum : unsigned {
    ERR_FIXED_RANGE = 1u,   // a cell outside the fixed-point checksum range
@@ -106,6 +111,18 @@ int launch_checksum_fp32_all(const float *pool, const Geom &g,
                              const int32_t *slots, int n,
                              unsigned long long *acc, unsigned *err,
                              cudaStream_t s);
+// FP32 checksum fallback for the variables var0 .. var0+nvar-1 whose cells
+// leave the fixed-point window: flags[0] is the miss word the checksum set
+// (nothing runs while it is clear), flags[1 .. nvar] per-variable miss
+// words (zeroed first), partials n * nvar doubles, acc the checksum slots
+// of var0 .. (two words each), overwritten for the variables that missed
+// with the compensated FP64 sum under kChecksumFallbackMark.  Returns 2
+// (kernels launched) or -1.
+int launch_fp32_checksum_fallback(const float *pool, const Geom &g,
+                                  const int32_t *slots, int n, int var0,
+                                  int nvar, unsigned *flags,
+                                  double *partials, unsigned long long *acc,
+                                  cudaStream_t s);
 // FP32: exact 128-bit fixed-point accumulation into acc[2] (lo, hi),
 // which must be zeroed first.
 int launch_checksum_fp32(const float *pool, const Geom &g,

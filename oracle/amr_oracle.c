@@ -794,15 +794,62 @@ int mamr_stencil(mamr_ctx *c, int32_t var, int32_t calc_stage)
 
 /* FP32 checksum unit: each cell truncated toward zero to a multiple of
  * 2^-52, accumulated exactly in 128 bits.  Returns 0 on success, -1 when a
- * cell is not finite or |v| >= 2^10 (outside the fixed-point range). */
+ * cell is outside the exact window v == 0 or 2^-52 <= |v| < 2^10 (too
+ * large or not finite for the accumulator, or too small to register). */
 static int fixed_cell(double v, int64_t *out)
 {
-   if (!(fabs(v) < 1024.0)) {
+   const double a = fabs(v);
+   if (!(a < 1024.0 && (a >= 0x1p-52 || a == 0.0))) {
       *out = 0;
       return -1;
    }
    *out = (int64_t) (v * 0x1p52);
    return 0;
+}
+
+/* Neumaier-compensated FP64 step: adds x to the running sum s with its
+ * correction c; once the sum is not finite the correction is left alone,
+ * so an infinite cell gives an infinite sum as plain summation does. */
+static void neumaier(double *s, double *c, double x)
+{
+   const double t = *s + x;
+   if (isfinite(t)) {
+      if (fabs(*s) >= fabs(x))
+         *c += (*s - t) + x;
+      else
+         *c += (x - t) + *s;
+   }
+   *s = t;
+}
+
+/* The FP32 checksum of a variable with a cell outside the fixed-point
+ * window: the reference's order (ref/check_sum.c:44-53) in FP64 with
+ * Neumaier compensation -- each block serially (k fastest) into s + c,
+ * then the block values serially in sorted order, S + C. */
+static int fp32_fallback_sum(const mamr_ctx *c, int var, double *sum)
+{
+   double S = 0.0, C = 0.0, *bs = (double *) malloc(sizeof(double) *
+                                                    (c->n_mesh ? c->n_mesh
+                                                               : 1));
+   int in;
+   if (!bs)
+      return fail(MAMR_ENOMEM, "host allocation");
+#pragma omp parallel for schedule(dynamic, 8)
+   for (in = 0; in < c->n_mesh; in++) {
+      const double *a = blk(c, c->mesh[in].slot, var);
+      double s = 0.0, cc = 0.0;
+      int i, j, k;
+      for (i = 1; i <= c->cfg.nx; i++)
+         for (j = 1; j <= c->cfg.ny; j++)
+            for (k = 1; k <= c->cfg.nz; k++)
+               neumaier(&s, &cc, AT(a, i, j, k));
+      bs[in] = s + cc;
+   }
+   for (in = 0; in < c->n_mesh; in++)
+      neumaier(&S, &C, bs[in]);
+   free(bs);
+   *sum = S + C;
+   return MAMR_OK;
 }
 
 static double fixed128_to_double(__int128 acc)
@@ -874,7 +921,7 @@ int mamr_check_sum(mamr_ctx *c, int32_t var, double *sum)
          acc += bs[in];
       free(bs);
       if (bad)
-         return fail(MAMR_EDEVICE, "cell outside the fixed-point range");
+         return fp32_fallback_sum(c, var, sum);
       *sum = fixed128_to_double(acc);
    }
    return MAMR_OK;

@@ -132,14 +132,13 @@ def test_errors_are_reported_and_context_survives(gpu_lib):
         assert e.value.status == -4
         ctx.set_mesh(m.blocks())
         v = np.zeros((8, 2, 10, 10, 10))
-        v[3, 1, 4, 4, 4] = 5000.0      # outside the FP32 checksum range
-        ctx.upload(np.arange(8), v)
-        with pytest.raises(MamrError) as e:
-            ctx.check_sum(1)
-        assert e.value.status == -6
-        assert ctx.check_sum(0) == 0.0   # context still usable
+        v[3, 1, 4, 4, 4] = 5000.0      # outside the fixed-point window:
+        ctx.upload(np.arange(8), v)    # the compensated FP64 sum instead
+        assert ctx.check_sum(1) == 5000.0
+        assert ctx.check_sum(0) == 0.0
         with pytest.raises(MamrError):
             ctx.comm(1, 5, 0)
+        assert ctx.check_sum(1) == 5000.0   # context still usable
 
 
 def test_batched_refuses_a_coarse_face_that_omits_the_block(gpu_lib):
@@ -339,3 +338,50 @@ def test_checksums_follow_every_change(gpu_lib, oracle_lib, dtype):
     assert np.array_equal(bits(outs[0]), bits(outs[1]))
     # the sums do move: not all rows alike
     assert len({tuple(r) for r in outs[0].tolist()}) > 5
+
+
+def _window_values(n, nxyz, V):
+    """Cells in and out of the FP32 checksum's fixed-point window (v == 0
+    or 2^-52 <= |v| < 2^10): variable 0 entirely inside, variable 1 with
+    one cell too large for the accumulator, variable 2 with a block of
+    cells too small to register, variable 3 with an infinite cell."""
+    rng = np.random.default_rng(3)
+    X = nxyz + 2
+    v = np.zeros((n, V, X, X, X))
+    v[:, :, 1:-1, 1:-1, 1:-1] = rng.uniform(0, 1, (n, V) + (nxyz,) * 3)
+    v[3, 1, 4, 4, 4] = 5000.0
+    v[5, 2, 1:-1, 1:-1, 1:-1] = 1e-20
+    v[6, 3, 2, 3, 4] = np.inf
+    return v
+
+
+@pytest.mark.parametrize("flags", [0, 1 | 2], ids=["plain", "batched_graph"])
+@pytest.mark.parametrize("stencil", [7, 27])
+@pytest.mark.parametrize("nxyz", [8, 16])
+def test_fp32_checksum_window_fallback(gpu_lib, oracle_lib, nxyz, stencil,
+                                       flags):
+    """FP32 checksums of variables with a cell outside the fixed-point
+    window take the reference's order in compensated FP64 instead of
+    failing: single check_sum calls and the checksums of plain and batched
+    runs (fused into the pencil, warp-per-block and generic stage kernels)
+    equal the oracle's bit for bit, and variables inside the window keep
+    the exact fixed-point sum."""
+    V, cap = 4, 80
+    cfg = Config.make(nxyz, nxyz, nxyz, V, cap, stencil=stencil, dtype=FP32)
+    init = _window_values(8, nxyz, V)
+    out = []
+    for lib in (gpu_lib, oracle_lib):
+        m = meshmod.initial_mesh(2, 2, 2, 1, cap)
+        with lib.context(cfg) as ctx:
+            ctx.upload(np.arange(8), init)
+            ctx.split(m.split_all())
+            ctx.set_mesh(m.blocks())
+            single = [ctx.check_sum(v) for v in range(V)]
+            sums = ctx.run_timesteps(2, 2, 1, flags=flags)
+            out.append((np.array(single), sums,
+                        ctx.download(m.sorted_slots())))
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(bits(a), bits(b))
+    single, sums, _ = out[0]
+    assert np.isfinite(single[:3]).all() and np.isinf(single[3])
+    assert np.isfinite(sums[:, :3]).all()
