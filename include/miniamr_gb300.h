@@ -121,7 +121,13 @@ typedef struct {
    int32_t uniform_refine;  /* --uniform_refine: every block below the
                                maximum level refines; no objects */
    int32_t mesh_size[3];    /* mesh_size[] (ref/init.c:430-437) */
-   int32_t reserved[10];    /* must be zero */
+   int32_t max_passes;      /* cap on the rule passes; 0 = the bound that
+                               always suffices, 2 * (blocks + parents).  A
+                               smaller cap the rules need more passes than
+                               ends the call with MAMR_EDEVICE (no
+                               counterpart in the reference: a test knob
+                               for the bounded device loop) */
+   int32_t reserved[9];     /* must be zero */
 } mamr_mark_params;
 
 /* One active block as the marking sees it (ref/block.h:36-53). */

@@ -59,7 +59,7 @@ class MarkParams(C.Structure):
     _fields_ = [
         ("num_refine", C.c_int32), ("refine_ghost", C.c_int32),
         ("uniform_refine", C.c_int32), ("mesh_size", C.c_int32 * 3),
-        ("reserved", C.c_int32 * 10),
+        ("max_passes", C.c_int32), ("reserved", C.c_int32 * 9),
     ]
 
     @classmethod

@@ -233,7 +233,9 @@ static inline const char *mamr_mark_validate(
    if (p->num_refine < 0 || p->num_refine > 29 || p->mesh_size[0] <= 0 ||
        p->mesh_size[1] <= 0 || p->mesh_size[2] <= 0)
       return "mark_refine: bad parameters";
-   for (k = 0; k < 10; k++)
+   if (p->max_passes < 0)
+      return "mark_refine: negative pass cap";
+   for (k = 0; k < 9; k++)
       if (p->reserved[k])
          return "mark_refine: reserved parameters must be zero";
    for (i = 0; i < nb; i++) {

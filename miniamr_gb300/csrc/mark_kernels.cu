@@ -252,6 +252,9 @@ int launch_mark_refine(const mamr_mark_params &p, int3 bsize,
       return -1;
    const long long bound = 2LL * ((long long) nb + np) + 2;
    int max_passes = (int) (bound < (1 << 30) ? bound : (1 << 30));
+   // a caller's cap (a test knob): running out sets ERR_MARK as above
+   if (p.max_passes > 0 && p.max_passes < max_passes)
+      max_passes = p.max_passes;
    int dev = 0, coop = 0, sms = 0, per_sm = 0;
    cudaGetDevice(&dev);
    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);

@@ -1170,7 +1170,7 @@ int mamr_mark_refine(mamr_ctx *c, const mamr_mark_params *p,
    unsigned char *listed;
    int32_t *ref, *pref, i, k;
    const char *msg;
-   int changed, uni, bsize[3];
+   int changed, uni, bsize[3], passes = 0;
    if (!c || (nb && !block_refine) || (np && !parent_refine))
       return fail(MAMR_EINVAL, "mark_refine: bad arguments");
    listed = (unsigned char *) calloc((size_t) cap + 1, 1);
@@ -1232,6 +1232,11 @@ int mamr_mark_refine(mamr_ctx *c, const mamr_mark_params *p,
                if (ch >= 0 && listed[ch])
                   mark_raise(&ref[ch], 0, &changed);
             }
+      /* the caller's pass cap, as the device applies it */
+      if (changed && p->max_passes > 0 && ++passes >= p->max_passes) {
+         free(listed); free(ref); free(pref);
+         return fail(MAMR_EDEVICE, "refinement marking did not settle");
+      }
    } while (changed);
    for (i = 0; i < nb; i++)
       block_refine[i] = ref[mb[i].slot];

@@ -94,3 +94,34 @@ def test_oracle_refuses_bad_marking_input(oracle_lib):
 @pytest.mark.gpu
 def test_gpu_refuses_bad_marking_input(gpu_lib):
     check_refusals(gpu_lib)
+
+
+def check_pass_cap(lib):
+    """The rule passes stop at params.max_passes: a cap below what a
+    recorded step needs ends the call with MAMR_EDEVICE (the device loop's
+    bound, not a hang), and the same context then gives the reference's
+    flags without the cap."""
+    from miniamr_gb300.abi import MamrError
+    steps = read_marks(mark_path("amr7_objects"))
+    st = steps[6]
+    cfg = Config.make(*st.block_size, 1, int(st.blocks["slot"].max()) + 1)
+    with lib.context(cfg) as ctx:
+        st.params.max_passes = 1
+        with pytest.raises(MamrError) as e:
+            ctx.mark_refine(st.params, st.objects, st.blocks, st.parents)
+        assert e.value.status == -6 and "settle" in str(e.value)
+        st.params.max_passes = 0
+        br, pr = ctx.mark_refine(st.params, st.objects, st.blocks,
+                                 st.parents)
+        act = st.parents["active"] == 1
+        assert np.array_equal(br, st.block_refine)
+        assert np.array_equal(pr[act], st.parent_refine[act])
+
+
+def test_oracle_marking_pass_cap(oracle_lib):
+    check_pass_cap(oracle_lib)
+
+
+@pytest.mark.gpu
+def test_gpu_marking_pass_cap(gpu_lib):
+    check_pass_cap(gpu_lib)
