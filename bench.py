@@ -208,25 +208,31 @@ def oracle_rate(steps, threads=None, stages=SPT, warm=1, init=INIT):
     return steps * stages * n0 * 8 * N ** 3 * V / dt, threads, dt
 
 
-def amr_plain(lib, dtype):
+def amr_sphere(lib, dtype, flags=0):
     """The AMR run with one moving sphere (4^3 blocks of 16^3, 40 vars,
     27-point, 4 levels, refine every 5 steps, 100 timesteps; up to 7429
-    blocks) replayed from the reference's recorded mesh sequence through
-    the plain path -- the drop-in's call sequence of comm, stencil and
-    check_sum, queued without host syncs.  FP64: every checksum compared
-    bit for bit with the reference's; FP32 pool (the drop-in with
-    MAMR_DTYPE=fp32): max and RMS relative error of every checksum against
-    the reference's FP64 checksums."""
+    blocks) replayed from the reference's recorded mesh sequence, each
+    stretch of stages between refinements as one run: through the plain
+    path (flags 0: the drop-in's call sequence of comm, stencil and
+    check_sum, queued without host syncs) or the batched path (one fused
+    launch per stage, edge and corner ghosts from their recipes, a CUDA
+    graph captured per stretch).  FP64: every checksum compared bit for bit
+    with the reference's; FP32 pool: max and RMS relative error of every
+    checksum against the reference's FP64 checksums.  For the batched path
+    a first replay lets the tuner time its launch shapes."""
     import torch
-    from miniamr_gb300.abi import FP64, RUN_PLAIN
+    from miniamr_gb300.abi import FP64
     from miniamr_gb300.trace import read_trace, replay_batched
     path = os.path.join(REPO, "tests", "golden", "config2.trace.xz")
     if not os.path.exists(path):
         return None
     recs = read_trace(path)
+    if flags:
+        _, ctx, _ = replay_batched(lib, recs, flags, dtype=dtype)
+        ctx.close()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    sums, ctx, timings = replay_batched(lib, recs, RUN_PLAIN, dtype=dtype)
+    sums, ctx, timings = replay_batched(lib, recs, flags, dtype=dtype)
     torch.cuda.synchronize()
     total = time.perf_counter() - t0
     ctx.close()
@@ -722,8 +728,10 @@ def main():
     if not args.no_configs:
         line["configs"] = {
             "uniform_fp64_7pt": uniform_fp64_7pt(lib, max(20, K)),
-            "amr_sphere_27pt_plain_fp64": amr_plain(lib, FP64),
-            "amr_sphere_27pt_plain_fp32": amr_plain(lib, FP32),
+            "amr_sphere_27pt_plain_fp64": amr_sphere(lib, FP64),
+            "amr_sphere_27pt_plain_fp32": amr_sphere(lib, FP32),
+            "amr_sphere_27pt_batched_fp64": amr_sphere(lib, FP64, flags),
+            "amr_sphere_27pt_batched_fp32": amr_sphere(lib, FP32, flags),
             "uniform_stencil0_fp64": uniform_stencil0(lib),
             "stress_multilevel_7pt_fp32": stress_multilevel(lib, FP32),
             "stress_multilevel_7pt_fp64": stress_multilevel(lib, FP64),

@@ -100,6 +100,9 @@ namespace mamr {
 struct BatchedState {
    DevBuf items, partials, sums, acc, chain, pencils, bad;
    DevBuf csflags;             // FP32: per checksum stage, 1 + V miss words
+   DevBuf recipes, keep;       // 27-point edge/corner recipes (multi-level)
+                               // and the blocks' keep masks
+   bool has_recipes = false;
    BItem *h_items = nullptr;   // pinned staging of the item upload
    size_t h_cap = 0;           // its capacity in items
    int n = 0;
@@ -114,7 +117,8 @@ void batched_destroy(BatchedState *b)
       return;
    b->items.release(); b->partials.release(); b->sums.release();
    b->acc.release(); b->chain.release(); b->pencils.release();
-   b->bad.release(); b->csflags.release();
+   b->bad.release(); b->csflags.release(); b->recipes.release();
+   b->keep.release();
    if (b->h_items)
       cudaFreeHost(b->h_items);
    delete b;
@@ -1094,7 +1098,45 @@ static int build_items_host(mamr_ctx *c)
 // 8^3 stress mesh, 24k blocks: about 1.6 ms on the host against tens of
 // microseconds).  A mesh the device build rejects is built again on the
 // host, which names what is wrong with it.
+static int build_items_only(mamr_ctx *c);
+
 static int build_items(mamr_ctx *c)
+{
+   BatchedState *B = c->batched;
+   B->has_recipes = false;
+   int r = build_items_only(c);
+   if (r != MAMR_OK || B->single_level || c->cfg.stencil != 27)
+      return r;
+   // multi-level 27-point: the edge and corner recipes, built on the
+   // device from the mesh copy (one thread per block and recipe)
+   const int n = B->n;
+   CUDA_TRY(B->recipes.ensure(sizeof(GhostRecipe) * kGhostRecipes *
+                              (size_t) std::max(1, n)));
+   CUDA_TRY(B->keep.ensure(sizeof(int) * (size_t) std::max(1, n)));
+   CUDA_TRY(B->bad.ensure(sizeof(int)));
+   CUDA_TRY(cudaMemsetAsync(B->bad.p, 0x7f, sizeof(int), c->stream));
+   if (launch_build_recipes((const mamr_block *) c->d_mesh.p, n,
+                            (const int32_t *) c->d_slot_pos.p, c->g,
+                            (GhostRecipe *) B->recipes.p, (int *) B->keep.p,
+                            (int *) B->bad.p, c->stream) < 0)
+      return fail(MAMR_ECUDA, "recipe build: %s",
+                  cudaGetErrorString(cudaGetLastError()));
+   c->launches++;
+   int bad = 0;
+   CUDA_TRY(cudaMemcpyAsync(&bad, B->bad.p, sizeof(int),
+                            cudaMemcpyDeviceToHost, c->stream));
+   CUDA_TRY(cudaStreamSynchronize(c->stream));
+   if (bad != 0x7f7f7f7f) {
+      B->valid = false;
+      return fail(MAMR_EMESH, "misconnected block (slot %d): an edge or "
+                  "corner ghost crosses a face whose neighbour does not "
+                  "list it", c->mesh[bad].slot);
+   }
+   B->has_recipes = true;
+   return MAMR_OK;
+}
+
+static int build_items_only(mamr_ctx *c)
 {
    BatchedState *B = c->batched;
    const int n = (int) c->mesh.size();
@@ -1236,10 +1278,12 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    if (c->cfg.code != 0)
       return fail(MAMR_EUNSUP, "the batched path gathers code-0 ghosts; "
                   "code %d runs on the plain path", c->cfg.code);
-   if (c->cfg.stencil == 27 && !B->single_level)
-      return fail(MAMR_EUNSUP, "batched 27-point stencil needs a "
-                  "single-level mesh (edge/corner ghosts at level jumps "
-                  "follow the per-call exchange only)");
+   if (c->cfg.stencil == 27 && c->cfg.permute)
+      return fail(MAMR_EUNSUP, "batched 27-point stencil with --permute: "
+                  "with the phases reordered, edge and corner ghosts take "
+                  "neighbours' ghost values of the previous stage, which "
+                  "one fused launch per stage does not keep; the plain "
+                  "path runs it");
    const int V = c->cfg.num_vars, nb = B->n;
    int per_ts = 0;
    if (freq)
@@ -1264,6 +1308,12 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    }
    const bool pencil = B->n_pencils > 0;
    const int np = B->n_pencils;
+   // stale edge/corner ghosts (multi-level 27-point) are read from the pool
+   // the run starts from: no stage before the last writes ghosts anywhere
+   const void *stale_pool = c->pool;
+   const GhostRecipe *recipes =
+      B->has_recipes ? (const GhostRecipe *) B->recipes.p : nullptr;
+   const int *keep = B->has_recipes ? (const int *) B->keep.p : nullptr;
    // one stage: cur -> oth with launch shape sh
    auto stage = [&](const void *cur, void *oth, const StageShape &sh,
                     int last, bool do_cs, int cnt) -> int {
@@ -1304,11 +1354,14 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       if (c->fp32)
          return fallback(launch_batched_stage(
             (const float *) cur, (float *) oth, c->g, c->cfg.stencil,
-            (const BItem *) B->items.p, nb, sh, last, do_cs, part, sums_at,
-            acc, flags, c->stream));
+            (const BItem *) B->items.p, recipes, keep,
+            (const float *) stale_pool,
+            nb, sh, last, do_cs, part, sums_at, acc, flags, c->stream));
       return launch_batched_stage((const double *) cur, (double *) oth, c->g,
                                   c->cfg.stencil, (const BItem *) B->items.p,
-                                  nb, sh, last, do_cs, part, sums_at, acc,
+                                  recipes, keep, (const double *) stale_pool,
+                                  nb,
+                                  sh, last, do_cs, part, sums_at, acc,
                                   c->d_err, c->stream);
    };
    std::vector<StageShape> cands;

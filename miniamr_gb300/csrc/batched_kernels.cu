@@ -44,13 +44,61 @@ __host__ __device__ inline size_t tile_bytes(const Geom &g)
 }
 
 
+// The value of an edge or corner ghost cell from its recipe (batched.h):
+// t is the cell's index along the edge (unused for corners).  Transforms
+// across a level jump are the face gathers' own (coarse/4, the 4-cell sum
+// in the reference's order); stale cells come from the pool the run
+// started from, which no stage before the last writes ghosts into.
+template <typename T, class DM>
+__device__ __forceinline__ T eval_recipe(const GhostRecipe &r, int t,
+                                         const T *__restrict__ src,
+                                         const T *__restrict__ stale,
+                                         const Geom &g, const DM &D, int var)
+{
+   int c[3] = {r.c[0], r.c[1], r.c[2]};
+   if (r.vax >= 0)
+      c[r.vax] = t;
+   // an interior cell now, or a ghost cell as the previous stage left it
+   // (the stage that wrote the source pool wrote it there)
+   if (r.kind == GR_INTERIOR || r.kind == GR_PREV)
+      return src[bv_offset(g, r.nb[0], var) + D.cell(c[0], c[1], c[2])];
+   if (r.kind == GR_STALE)
+      return stale[bv_offset(g, r.nb[0], var) + D.cell(c[0], c[1], c[2])];
+   const int dir = r.l >> 1;
+   const bool low = !(r.l & 1);
+   const int n = dir == 0 ? D.nx : (dir == 1 ? D.ny : D.nz);
+   const int na = dir == 0 ? D.ny : D.nx;
+   const int nbb = dir == 2 ? D.ny : D.nz;
+   const int ha = na / 2, hb = nbb / 2;
+   const int a = dir == 0 ? c[1] : c[0];
+   const int b = dir == 2 ? c[1] : c[2];
+   if (r.kind == GR_COARSE) {
+      const int iq = r.iqjq & 1, jq = r.iqjq >> 1;
+      return quarter(src[bv_offset(g, r.nb[0], var) +
+                         D.fcell(dir, low ? n : 1, (a + 1) / 2 + jq * ha,
+                                 (b + 1) / 2 + iq * hb)]);
+   }
+   const int jq = a > ha, iq = b > hb;
+   const int a2 = a - jq * ha, b2 = b - iq * hb;
+   const int p = low ? n : 1;
+   const T *f = src + bv_offset(g, r.nb[iq * 2 + jq], var);
+   T s = f[D.fcell(dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
+         f[D.fcell(dir, p, 2 * a2 - 1, 2 * b2)];
+   s = s + f[D.fcell(dir, p, 2 * a2, 2 * b2 - 1)];
+   s = s + f[D.fcell(dir, p, 2 * a2, 2 * b2)];
+   return s;
+}
+
 // A CTA takes the variables [vg * vpc, vg * vpc + vpc) of one block per
 // work item: blockDim.x / vpc threads (whole warps) and one shared tile
 // per variable, the block's neighbour record loaded once.
 template <typename T, int ST, int BX, int BY, int BZ>
 __global__ void __launch_bounds__(512)
 batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
-                     const BItem *__restrict__ items, int nb, int vpc,
+                     const BItem *__restrict__ items,
+                     const GhostRecipe *__restrict__ recipes,
+                     const int *__restrict__ keep,
+                     const T *__restrict__ stale, int nb, int vpc,
                      int write_ghosts, int do_cs,
                      unsigned long long *__restrict__ acc,
                      unsigned *__restrict__ err)
@@ -97,6 +145,8 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       __syncthreads();
       const T *s = src + bv_offset(g, sI.slot, active ? var : 0);
       T *d = dst + bv_offset(g, sI.slot, active ? var : 0);
+      // ghost cells the next stage reads as they stand after this one
+      const int kb = keep ? keep[b] : 0;
 
       if (active) {
          // interior rows, 16-byte vectors (rows start on a sector boundary)
@@ -157,36 +207,54 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                else if (dir == 1) { gi = a; gj = gn; gk = bq; }
                else { gi = a; gj = bq; gk = gn; }
                TS(gi, gj, gk) = v;
-               if (write_ghosts)
+               if (write_ghosts || (kb >> l & 1))
                   d[D.cell(gi, gj, gk)] = v;
             }
          }
 
          if (ST == 27) {
-            // 12 edges and 8 corners, resolved axis by axis
+            // 12 edges and 8 corners: on one level resolved axis by axis
+            // (nb27); across level jumps from the block's recipes
             const int ne = 4 * (nx + ny + nz) + 8;
             for (int e = gtid; e < ne; e += gthreads) {
-               int gi, gj, gk;
+               int gi, gj, gk, ri, t;
                if (e < 4 * nz) {
                   int q = e / nz;
                   gk = e - q * nz + 1;
                   gi = (q & 1) ? nx + 1 : 0;
                   gj = (q & 2) ? ny + 1 : 0;
+                  ri = q;
+                  t = gk;
                } else if (e < 4 * (nz + ny)) {
                   int e2 = e - 4 * nz, q = e2 / ny;
                   gj = e2 - q * ny + 1;
                   gi = (q & 1) ? nx + 1 : 0;
                   gk = (q & 2) ? nz + 1 : 0;
+                  ri = 4 + q;
+                  t = gj;
                } else if (e < 4 * (nz + ny + nx)) {
                   int e2 = e - 4 * (nz + ny), q = e2 / nx;
                   gi = e2 - q * nx + 1;
                   gj = (q & 1) ? ny + 1 : 0;
                   gk = (q & 2) ? nz + 1 : 0;
+                  ri = 8 + q;
+                  t = gi;
                } else {
                   int q = e - 4 * (nx + ny + nz);
                   gi = (q & 1) ? nx + 1 : 0;
                   gj = (q & 2) ? ny + 1 : 0;
                   gk = (q & 4) ? nz + 1 : 0;
+                  ri = 12 + q;
+                  t = 0;
+               }
+               if (recipes) {
+                  const T v = eval_recipe(recipes[(size_t) b * kGhostRecipes +
+                                                  ri],
+                                          t, src, stale, g, D, var);
+                  TS(gi, gj, gk) = v;
+                  if (write_ghosts || (ri < 12 && (kb >> (6 + ri) & 1)))
+                     d[D.cell(gi, gj, gk)] = v;
+                  continue;
                }
                int dx = gi == 0 ? -1 : (gi == nx + 1 ? 1 : 0);
                int dy = gj == 0 ? -1 : (gj == ny + 1 ? 1 : 0);
@@ -356,7 +424,8 @@ void batched_candidates(const Geom &g, int stencil, int n_blocks,
 
 template <typename T>
 int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
-                         const BItem *items, int n_blocks,
+                         const BItem *items, const GhostRecipe *recipes,
+                         const int *keep, const T *stale, int n_blocks,
                          const StageShape &sh, int write_ghosts, int do_cs,
                          double *partials, double *sums,
                          unsigned long long *acc, unsigned *err,
@@ -376,7 +445,8 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
    const int thr = sh.threads * sh.vpc;
 #define MAMR_GENERIC(ST, BX, BY, BZ)                                          \
    batched_stage_kernel<T, ST, BX, BY, BZ><<<sh.grid, thr, smem, s>>>(         \
-      src, dst, g, items, n_blocks, sh.vpc, write_ghosts,                     \
+      src, dst, g, items, recipes, keep, stale, n_blocks, sh.vpc,             \
+      write_ghosts,                                                           \
       sizeof(T) == 4 ? do_cs : 0, acc, err)
    const int kind = dims_kind(g);
    if (stencil == 7) {
@@ -416,43 +486,11 @@ __global__ void build_items_kernel(const mamr_block *__restrict__ mesh, int n,
    BItem it;
    it.slot = bp.slot;
    it.bmask = 0;
-#pragma unroll
    for (int l = 0; l < 6; l++) {
-      BFace &f = it.f[l];
-      f.nb[0] = f.nb[1] = f.nb[2] = f.nb[3] = 0;
-      f.iq = f.jq = 0;
-      const int nl = bp.nei_level[l];
-      if (nl == bp.level) {
-         f.type = FACE_SAME;
-         f.nb[0] = bp.nei[l][0][0];
-      } else if (nl == bp.level + 1) {
-         f.type = FACE_FINE;
-         for (int iq = 0; iq < 2; iq++)
-            for (int jq = 0; jq < 2; jq++)
-               f.nb[iq * 2 + jq] = bp.nei[l][iq][jq];
-      } else if (nl == -2) {
-         f.type = FACE_BC;
+      if (!face_desc(mesh, slot_pos, bp, l, it.f[l]))
+         atomicMin(bad, q);
+      if (bp.nei_level[l] == -2)
          it.bmask |= 1 << l;
-      } else {
-         const int m = bp.nei[l][0][0];
-         const int pm = slot_pos[m];
-         bool found = false;
-         if (pm >= 0)
-            for (int iq = 0; iq < 2 && !found; iq++)
-               for (int jq = 0; jq < 2 && !found; jq++)
-                  if (mesh[pm].nei[l ^ 1][iq][jq] == bp.slot) {
-                     f.iq = iq;
-                     f.jq = jq;
-                     found = true;
-                  }
-         if (found) {
-            f.type = FACE_COARSE;
-            f.nb[0] = m;
-         } else {
-            f.type = FACE_BC;
-            atomicMin(bad, q);
-         }
-      }
    }
    for (int d = 0; d < 27; d++) {
       int cur = bp.slot;
@@ -475,6 +513,49 @@ __global__ void build_items_kernel(const mamr_block *__restrict__ mesh, int n,
    items[q] = it;
 }
 
+// The edge and corner recipes of every block, one thread per (block,
+// recipe); a misconnected chain lowers *bad to the block's index and
+// leaves a recipe that reads the block's own cell.
+__global__ void build_recipes_kernel(const mamr_block *__restrict__ mesh,
+                                     int n, const int32_t *__restrict__ slot_pos,
+                                     int nx, int ny, int nz,
+                                     GhostRecipe *__restrict__ out,
+                                     int *__restrict__ keep,
+                                     int *__restrict__ bad)
+{
+   const long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+   if (t >= (long long) n * kGhostRecipes)
+      return;
+   const int q = (int) (t / kGhostRecipes), e = (int) (t % kGhostRecipes);
+   GhostRecipe r;
+   int kq, kbit;
+   if (!resolve_ghost(mesh, slot_pos, q, nx, ny, nz, e, r, kq, kbit)) {
+      r.kind = GR_INTERIOR;
+      r.vax = -1;
+      r.nb[0] = mesh[q].slot;
+      r.c[0] = r.c[1] = r.c[2] = 1;
+      atomicMin(bad, q);
+   } else if (kq >= 0) {
+      atomicOr(keep + kq, 1 << kbit);
+   }
+   out[t] = r;
+}
+
+int launch_build_recipes(const mamr_block *mesh, int n,
+                         const int32_t *slot_pos, const Geom &g,
+                         GhostRecipe *out, int *keep, int *bad,
+                         cudaStream_t s)
+{
+   if (n == 0)
+      return 0;
+   const long long items = (long long) n * kGhostRecipes;
+   if (cudaMemsetAsync(keep, 0, sizeof(int) * (size_t) n, s) != cudaSuccess)
+      return -1;
+   build_recipes_kernel<<<(unsigned) ((items + 127) / 128), 128, 0, s>>>(
+      mesh, n, slot_pos, g.nx, g.ny, g.nz, out, keep, bad);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
 int launch_build_items(const mamr_block *mesh, int n, const int32_t *slot_pos,
                        int single, BItem *items, int *bad, cudaStream_t s)
 {
@@ -490,13 +571,17 @@ template void batched_candidates<float>(const Geom &, int, int,
 template void batched_candidates<double>(const Geom &, int, int,
                                          std::vector<StageShape> &);
 template int launch_batched_stage<float>(const float *, float *, const Geom &,
-                                         int, const BItem *, int,
-                                         const StageShape &, int, int,
+                                         int, const BItem *,
+                                         const GhostRecipe *, const int *,
+                                         const float *,
+                                         int, const StageShape &, int, int,
                                          double *, double *,
                                          unsigned long long *, unsigned *,
                                          cudaStream_t);
 template int launch_batched_stage<double>(const double *, double *,
                                           const Geom &, int, const BItem *,
+                                          const GhostRecipe *, const int *,
+                                          const double *,
                                           int, const StageShape &, int, int,
                                           double *, double *,
                                           unsigned long long *, unsigned *,

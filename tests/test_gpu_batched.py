@@ -52,14 +52,16 @@ def test_batched_equals_plain_uniform(gpu_lib, case, dtype, flags):
         assert np.array_equal(bits(a), bits(b))
 
 
-@pytest.mark.parametrize("name", ["amr7", "amr7_objects"])
+@pytest.mark.parametrize("name", ["amr7", "amr7_objects", "amr27"])
 @pytest.mark.parametrize("dtype", [FP64, FP32])
-def test_batched_equals_plain_amr7(gpu_lib, name, dtype):
-    """7-point stencil on the reference's own multi-level meshes (states
-    reached by replaying its recorded runs): face ghosts across level jumps
-    (coarse/4 and 4-cell sums) gathered inside the fused kernel, by every
-    launch-shape candidate (amr7's 8^3 blocks include the warp-per-block
-    kernel's)."""
+def test_batched_equals_plain_multilevel(gpu_lib, name, dtype):
+    """The reference's own multi-level meshes (states reached by replaying
+    its recorded runs), every cell and checksum against the plain path, by
+    every launch-shape candidate: face ghosts across level jumps (coarse/4
+    and 4-cell sums) gathered inside the fused kernel (amr7's 8^3 blocks
+    include the warp-per-block kernel's); for the 27-point stencil also the
+    edge and corner ghosts -- chains of face exchanges, level-jump
+    transforms and cells no exchange writes -- from their recipes."""
     recs = read_trace(trace_path(name))
     res = replay(gpu_lib, recs, dtype=dtype)
     assert len(np.unique(res.mesh["level"])) > 1
@@ -164,10 +166,15 @@ def test_pencil_division_fixup(gpu_lib, dtype, stencil):
     assert np.signbit(outs[1][1][0, 0, 8, 8, 8])
 
 
-def test_batched_27_multilevel_is_refused(gpu_lib):
-    recs = read_trace(trace_path("amr27"))
+def test_batched_27_permute_is_refused(gpu_lib):
+    """With --permute the exchange phases run in a stage-dependent order,
+    and 27-point edge and corner ghosts then carry neighbours' ghost values
+    from the previous stage: the batched path refuses it (the plain path
+    runs it, tests/test_gpu_parity.py) and the context keeps working."""
+    recs = read_trace(trace_path("amr27_permute"))
     res = replay(gpu_lib, recs)
     with pytest.raises(MamrError) as e:
         res.ctx.run_timesteps(1, 1, 1, flags=RUN_BATCHED)
-    assert e.value.status == -5
+    assert e.value.status == -5 and "permute" in str(e.value)
+    res.ctx.run_timesteps(1, 1, 1)
     res.ctx.close()
