@@ -201,3 +201,39 @@ def test_cpu_port_keeps_up_with_the_reference_binary(tmp_path):
     print(f"reference {max(ref):.3e}, port {max(port):.3e} updates/s: the "
           f"port is {factor:.2f}x slower")
     assert factor <= 1.25, (ref, port)
+
+
+@pytest.mark.skipif(_reference_sources() is None,
+                    reason="reference sources absent")
+def test_dropin_links_against_the_gpu_library(tmp_path):
+    """The binding INTEGRATION.md gives: the reference's host files and the
+    drop-in units linked against libminiamr_gb300.so (oracle/Makefile
+    target gpu).  It links with every mamr_* symbol resolved from the GPU
+    library, and runs the reference's driver up to the first device call:
+    without a GPU that call fails and the drop-in stops in the reference's
+    error style; with one, the run equals the reference's log."""
+    import torch
+    from miniamr_gb300 import build
+    build.build_library()
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "gpu",
+                    "REF=" + _reference_sources()], check=True)
+    exe = os.path.join(REPO, "oracle", "_ref", "miniamr_gpu")
+    need = subprocess.run(["readelf", "-d", exe], capture_output=True,
+                          text=True, check=True).stdout
+    assert "libminiamr_gb300.so" in need
+    args = ["--init_x", "1", "--init_y", "1", "--init_z", "2", "--nx", "8",
+            "--ny", "8", "--nz", "8", "--num_vars", "2", "--stencil", "27",
+            "--num_tsteps", "2", "--checksum_freq", "1"]
+    log = tmp_path / "gpu.log"
+    r = subprocess.run([exe] + args, cwd=tmp_path, capture_output=True,
+                       text=True, timeout=300,
+                       env=dict(os.environ, MAMR_REF_LOG=str(log)))
+    if not torch.cuda.is_available():
+        assert "mamr_create" in r.stdout + r.stderr
+        return
+    assert r.returncode == 0, r.stdout[-1000:]
+    ref = tmp_path / "ref.log"
+    subprocess.run([os.path.join(REPO, "oracle", "_ref", "miniamr_ref")] +
+                   args, cwd=tmp_path, check=True, capture_output=True,
+                   env=dict(os.environ, MAMR_REF_LOG=str(ref)))
+    assert log.read_text() == ref.read_text()
