@@ -232,11 +232,11 @@ extern "C" int mamr_create(const mamr_config *cfg, mamr_ctx **out)
    g.koff = 0;
    g.kplane = (long long) g.X * g.Y * g.nz;
    g.bv = ((g.kplane + 2LL * g.X * g.Y + line - 1) / line) * line;
-   size_t tile = (size_t) g.X * g.Y * g.Z * elem_size(c);
-   if (tile > 200 * 1024) {
+   if (!plain_stencil_fits(g, elem_size(c))) {
       delete c;
-      return fail(MAMR_EUNSUP, "block of %zu bytes does not fit the on-chip "
-                  "stencil tile (200 KiB)", tile);
+      return fail(MAMR_EUNSUP, "blocks of %d x %d cells per i-plane do not "
+                  "fit the stencil's three-plane ring (%zu KiB)", g.Y, g.Z,
+                  kPlainRingBytes / 1024);
    }
    int dev = 0;
    cudaError_t e = cudaGetDevice(&dev);
@@ -1375,8 +1375,9 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       batched_candidates<double>(c->g, c->cfg.stencil, nb, cands);
    CUDA_TRY(cudaGetLastError());
    if (cands.empty())
-      return fail(MAMR_ECUDA, "no launch shape of the stage kernel fits "
-                  "this block size");
+      return fail(MAMR_EUNSUP, "no launch shape of the batched stage kernel "
+                  "fits blocks of %d x %d x %d cells; the plain path runs "
+                  "them", c->g.nx, c->g.ny, c->g.nz);
    int choice = 0;
    if (c->tune_force >= 0) {
       choice = std::min<int>(c->tune_force, (int) cands.size() - 1);

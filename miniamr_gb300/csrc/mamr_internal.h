@@ -96,6 +96,12 @@ int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil, int code,
 template <typename T>
 int launch_stencil(T *pool, const Geom &g, int stencil, const int32_t *slots,
                    int n, int var, cudaStream_t s);
+// The plain stencil stages a whole block-variable in shared memory up to
+// kPlainTileBytes and streams larger ones along i through a ring of three
+// planes, which must fit kPlainRingBytes (plain_stencil_fits).
+constexpr size_t kPlainTileBytes = 200 * 1024;
+constexpr size_t kPlainRingBytes = 200 * 1024;
+bool plain_stencil_fits(const Geom &g, size_t elem);
 // FP64: serial per-block sums in exact reference order, then a serial sum
 // over blocks; result in *d_out.
 int launch_checksum_fp64(const double *pool, const Geom &g,

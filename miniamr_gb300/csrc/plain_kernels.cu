@@ -389,6 +389,76 @@ stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
 #undef TL
 }
 
+// Blocks whose whole-block tile does not fit in shared memory (32^3 FP64
+// and up): one CTA per block-variable streams the block plane by plane
+// along i through a ring of three (ny+2) x (nz+2) planes.  Every read comes
+// from the ring, which holds planes i-1, i, i+1 as they were before the
+// stage, and plane i is written to the pool only after plane i+1 is in the
+// ring, so the in-place update is still the reference's work-array Jacobi
+// update (ref/stencil.c:82-99, 103-141) in its operation order.
+template <typename T, int ST>
+__global__ void __launch_bounds__(256)
+stencil_stream_kernel(T *__restrict__ pool, Geom g,
+                      const int32_t *__restrict__ slots, int var)
+{
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   T *ring = reinterpret_cast<T *>(smem_raw);
+   const int nx = g.nx, ny = g.ny, nz = g.nz, Z = nz + 2;
+   const int P = (ny + 2) * Z;
+   T *base = pool + bv_offset(g, slots[blockIdx.x], var);
+   auto load = [&](int i) {
+      T *pl = ring + (i % 3) * P;
+      for (int e = threadIdx.x; e < P; e += blockDim.x) {
+         const int j = e / Z, k = e - j * Z;
+         pl[e] = base[cell_offset(g, i, j, k)];
+      }
+   };
+   load(0);
+   load(1);
+   for (int i = 1; i <= nx; i++) {
+      load(i + 1);
+      __syncthreads();
+      const T *pm = ring + ((i - 1) % 3) * P, *pc = ring + (i % 3) * P,
+              *pp = ring + ((i + 1) % 3) * P;
+      for (int col = threadIdx.x; col < ny * nz; col += blockDim.x) {
+         const int j = col / nz + 1, k = col - (j - 1) * nz + 1;
+         const int e = j * Z + k;
+         T out;
+         if (ST == 7) {
+            T w = pm[e] + pc[e - Z];
+            w = w + pc[e - 1];
+            w = w + pc[e];
+            w = w + pc[e + 1];
+            w = w + pc[e + Z];
+            w = w + pp[e];
+            out = div7(w);
+         } else {
+            auto S = [&](const T *pl) -> T {
+               T s = pl[e - Z - 1] + pl[e - Z];
+               s = s + pl[e - Z + 1];
+               s = s + pl[e - 1];
+               s = s + pl[e];
+               s = s + pl[e + 1];
+               s = s + pl[e + Z - 1];
+               s = s + pl[e + Z];
+               s = s + pl[e + Z + 1];
+               return s;
+            };
+            out = div27((S(pm) + S(pc)) + S(pp));
+         }
+         base[cell_offset(g, i, j, k)] = out;
+      }
+      // the ring slot of plane i-1 is refilled with plane i+2 next
+      __syncthreads();
+   }
+}
+
+// The largest block the streaming kernel's ring fits (shared memory).
+bool plain_stencil_fits(const Geom &g, size_t elem)
+{
+   return 3 * (size_t) (g.ny + 2) * (g.nz + 2) * elem <= kPlainRingBytes;
+}
+
 template <typename T, int ST, int BX, int BY, int BZ>
 static void stencil_launch(T *pool, const Geom &g, const int32_t *slots,
                            int n, int var, int threads, size_t smem,
@@ -414,6 +484,16 @@ int launch_stencil(T *pool, const Geom &g, int stencil, const int32_t *slots,
    const size_t smem = (size_t) g.X * g.Y * plain_zs<T>(g.nz) * sizeof(T);
    int threads = g.ny * g.nz;
    threads = threads > 256 ? 256 : ((threads + 31) / 32) * 32;
+   if (smem > kPlainTileBytes) {
+      // too large to stage whole: stream the block through a plane ring
+      const size_t ring = 3 * (size_t) (g.ny + 2) * (g.nz + 2) * sizeof(T);
+      auto k7 = stencil_stream_kernel<T, 7>, k27 = stencil_stream_kernel<T, 27>;
+      auto kern = stencil == 7 ? k7 : k27;
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int) ring);
+      kern<<<n, threads, ring, s>>>(pool, g, slots, var);
+      return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+   }
    const int kind = dims_kind(g);
    // FP32 8^3 / 16^3: one thread per (4 i-planes, j-row, 4 k values)
    if (sizeof(T) == 4 && kind != 0)

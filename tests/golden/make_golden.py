@@ -191,6 +191,15 @@ CASES = {
                     "--uniform_refine", "1", "--num_tsteps", "2",
                     "--stages_per_ts", "4", "--checksum_freq", "1",
                     "--error_tol", "0", "--max_blocks", "600"],
+    # large blocks: 32^3 cells (a block-variable with ghosts is 308 KB in
+    # FP64, more than one CTA's shared memory), 27-point, refinement and
+    # coarsening around a moving sphere
+    "big32_amr27": ["--init_x", "1", "--init_y", "1", "--init_z", "2",
+                    "--nx", "32", "--ny", "32", "--nz", "32", "--num_vars",
+                    "2", "--stencil", "27", "--num_refine", "2",
+                    "--refine_freq", "2", "--num_tsteps", "6",
+                    "--stages_per_ts", "2", "--checksum_freq", "1",
+                    "--error_tol", "0", "--max_blocks", "400"] + SPHERE,
     "amr7_objects": ["--init_x", "2", "--init_y", "2", "--init_z", "2",
                      "--nx", "6", "--ny", "6", "--nz", "6", "--num_vars", "3",
                      "--stencil", "7", "--num_refine", "4", "--refine_freq",
