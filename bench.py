@@ -462,6 +462,10 @@ def profile_case(name):
         blocks, ~22k of them, 4 vars -- MAMR_PROFILE_VARS sets another
         count -- 7-point), replayed batched: 40 stages, one run per stretch
         between refinements, with its splits and consolidations;
+      amr27_fp32, amr27_fp64: the AMR sphere run (16^3 blocks, up to 7429,
+        4 levels, 27-point, 40 vars unless MAMR_PROFILE_VARS says
+        otherwise), replayed batched in the same way: 100 stages in 20
+        runs;
       plain_fp32_27, plain_fp64_27: the benchmark mesh (4096 blocks of
         16^3, 40 vars) through the plain path, the driver's call sequence:
         two timesteps of four stages."""
@@ -474,11 +478,12 @@ def profile_case(name):
     shape = int(os.environ.get("MAMR_PROFILE_SHAPE", "0"))
     build.build_library()
     lib = load()
-    if name.startswith("stress"):
+    if name.startswith("stress") or name.startswith("amr27"):
         from miniamr_gb300.trace import read_trace, replay_batched
-        import miniamr_gb300.trace as tr
-        recs = read_trace(os.path.join(REPO, "tests", "golden",
-                                       "config5.trace.xz"))
+        recs = read_trace(os.path.join(
+            REPO, "tests", "golden",
+            "config5.trace.xz" if name.startswith("stress")
+            else "config2.trace.xz"))
         orig = lib.context
 
         def forced(cfg):
@@ -587,8 +592,8 @@ def main():
                     help="timesteps of the FP64 comparison runs")
     ap.add_argument("--profile-case", default=None,
                     choices=["fp32_27", "fp32_7", "fp64_27", "fp64_7",
-                             "stress_fp32", "stress_fp64", "plain_fp32_27",
-                             "plain_fp64_27"],
+                             "stress_fp32", "stress_fp64", "amr27_fp32",
+                             "amr27_fp64", "plain_fp32_27", "plain_fp64_27"],
                     help="a small case for ncu (see profile_case)")
     args = ap.parse_args()
     if args.oracle_rate_steps:

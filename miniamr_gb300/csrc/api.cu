@@ -100,6 +100,7 @@ namespace mamr {
 struct BatchedState {
    DevBuf items, partials, sums, acc, chain, pencils, bad;
    DevBuf csflags;             // FP32: per checksum stage, 1 + V miss words
+                               // and the fallback's counter
    DevBuf recipes, keep;       // 27-point edge/corner recipes (multi-level)
                                // and the blocks' keep masks
    bool has_recipes = false;
@@ -661,11 +662,11 @@ static int checksum_queue(mamr_ctx *c, int32_t var, double *d_out,
 {
    const int n = (int) c->mesh.size();
    if (c->fp32) {
-      CUDA_TRY(c->d_csflags.ensure(2 * sizeof(unsigned)));
+      CUDA_TRY(c->d_csflags.ensure(3 * sizeof(unsigned)));
       unsigned *flags = (unsigned *) c->d_csflags.p;
       CUDA_TRY(cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long),
                                c->stream));
-      CUDA_TRY(cudaMemsetAsync(flags, 0, 2 * sizeof(unsigned), c->stream));
+      CUDA_TRY(cudaMemsetAsync(flags, 0, 3 * sizeof(unsigned), c->stream));
       LAUNCH_TRY(c, launch_checksum_fp32((const float *) c->pool, c->g,
                                          (const int32_t *) c->d_slots.p, n,
                                          var, acc, flags, c->stream));
@@ -882,7 +883,7 @@ static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
                                      : sizeof(double);
    CUDA_TRY(c->d_sums.ensure(std::max<size_t>(1, n_cs * V) * slot_bytes));
    if (c->fp32) {
-      const size_t fb = std::max<size_t>(1, n_cs) * (1 + V) * sizeof(unsigned);
+      const size_t fb = std::max<size_t>(1, n_cs) * (2 + V) * sizeof(unsigned);
       CUDA_TRY(c->d_csflags.ensure(fb));
       CUDA_TRY(cudaMemsetAsync(c->d_csflags.p, 0, fb, c->stream));
    }
@@ -905,7 +906,7 @@ static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
                                                 V,
                                      c->stream));
             unsigned *flags = (unsigned *) c->d_csflags.p +
-                              (size_t) cnt * (1 + V);
+                              (size_t) cnt * (2 + V);
             LAUNCH_TRY(c, launch_checksum_fp32_all(
                              (const float *) c->pool, c->g,
                              (const int32_t *) c->d_slots.p,
@@ -1300,7 +1301,7 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       CUDA_TRY(B->acc.ensure(std::max<size_t>(1, n_cs * V) * 16));
       CUDA_TRY(cudaMemsetAsync(B->acc.p, 0, std::max<size_t>(1, n_cs * V) * 16,
                                c->stream));
-      const size_t fb = std::max<size_t>(1, n_cs) * (1 + V) * sizeof(unsigned);
+      const size_t fb = std::max<size_t>(1, n_cs) * (2 + V) * sizeof(unsigned);
       CUDA_TRY(B->csflags.ensure(fb));
       CUDA_TRY(cudaMemsetAsync(B->csflags.p, 0, fb, c->stream));
    } else {
@@ -1327,7 +1328,7 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       // fixed-point window in the stage's miss word, and the fallback
       // (empty unless it was set) replaces those variables' sums
       unsigned *flags = c->fp32 && do_cs
-                           ? (unsigned *) B->csflags.p + (size_t) cnt * (1 + V)
+                           ? (unsigned *) B->csflags.p + (size_t) cnt * (2 + V)
                            : c->d_err;
       auto fallback = [&](int k) -> int {
          if (k < 0 || !c->fp32 || !do_cs)

@@ -299,6 +299,18 @@ template <typename T>
 void batched_candidates(const Geom &g, int stencil, int n_blocks,
                         std::vector<StageShape> &out);
 
+// Tile kernel for 8^3 and 16^3 blocks, 7 or 27 points, any mesh
+// (tile_kernels.cu): its launch shapes (kernel 2) and one stage.
+template <typename T>
+void tile_candidates(const Geom &g, int stencil, int n_blocks,
+                     std::vector<StageShape> &out);
+template <typename T>
+int launch_tile_stage(const T *src, T *dst, const Geom &g, int stencil,
+                      const BItem *items, const GhostRecipe *recipes,
+                      const int *keep, const T *stale, int n_blocks,
+                      const StageShape &sh, int write_ghosts, int do_cs,
+                      unsigned long long *acc, unsigned *err, cudaStream_t s);
+
 // Warp-per-item variant for 8^3 blocks and the 7-point stencil (any mesh):
 // its launch shapes, and one stage (FP32 checksums fused into acc).
 template <typename T>

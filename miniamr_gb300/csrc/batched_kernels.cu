@@ -22,6 +22,7 @@
 #include "batched.h"
 #include "arith.cuh"
 #include "dims.cuh"
+#include "ghost_eval.cuh"
 
 namespace mamr {
 
@@ -43,51 +44,6 @@ __host__ __device__ inline size_t tile_bytes(const Geom &g)
    return (size_t) g.X * g.Y * tile_zs(g.nz, vw) * sizeof(T);
 }
 
-
-// The value of an edge or corner ghost cell from its recipe (batched.h):
-// t is the cell's index along the edge (unused for corners).  Transforms
-// across a level jump are the face gathers' own (coarse/4, the 4-cell sum
-// in the reference's order); stale cells come from the pool the run
-// started from, which no stage before the last writes ghosts into.
-template <typename T, class DM>
-__device__ __forceinline__ T eval_recipe(const GhostRecipe &r, int t,
-                                         const T *__restrict__ src,
-                                         const T *__restrict__ stale,
-                                         const Geom &g, const DM &D, int var)
-{
-   int c[3] = {r.c[0], r.c[1], r.c[2]};
-   if (r.vax >= 0)
-      c[r.vax] = t;
-   // an interior cell now, or a ghost cell as the previous stage left it
-   // (the stage that wrote the source pool wrote it there)
-   if (r.kind == GR_INTERIOR || r.kind == GR_PREV)
-      return src[bv_offset(g, r.nb[0], var) + D.cell(c[0], c[1], c[2])];
-   if (r.kind == GR_STALE)
-      return stale[bv_offset(g, r.nb[0], var) + D.cell(c[0], c[1], c[2])];
-   const int dir = r.l >> 1;
-   const bool low = !(r.l & 1);
-   const int n = dir == 0 ? D.nx : (dir == 1 ? D.ny : D.nz);
-   const int na = dir == 0 ? D.ny : D.nx;
-   const int nbb = dir == 2 ? D.ny : D.nz;
-   const int ha = na / 2, hb = nbb / 2;
-   const int a = dir == 0 ? c[1] : c[0];
-   const int b = dir == 2 ? c[1] : c[2];
-   if (r.kind == GR_COARSE) {
-      const int iq = r.iqjq & 1, jq = r.iqjq >> 1;
-      return quarter(src[bv_offset(g, r.nb[0], var) +
-                         D.fcell(dir, low ? n : 1, (a + 1) / 2 + jq * ha,
-                                 (b + 1) / 2 + iq * hb)]);
-   }
-   const int jq = a > ha, iq = b > hb;
-   const int a2 = a - jq * ha, b2 = b - iq * hb;
-   const int p = low ? n : 1;
-   const T *f = src + bv_offset(g, r.nb[iq * 2 + jq], var);
-   T s = f[D.fcell(dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
-         f[D.fcell(dir, p, 2 * a2 - 1, 2 * b2)];
-   s = s + f[D.fcell(dir, p, 2 * a2, 2 * b2 - 1)];
-   s = s + f[D.fcell(dir, p, 2 * a2, 2 * b2)];
-   return s;
-}
 
 // A CTA takes the variables [vg * vpc, vg * vpc + vpc) of one block per
 // work item: blockDim.x / vpc threads (whole warps) and one shared tile
@@ -387,8 +343,10 @@ void batched_candidates(const Geom &g, int stencil, int n_blocks,
    cudaGetDevice(&dev);
    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
    out.clear();
-   // 8^3 blocks, 7-point: the warp-per-item kernel first
+   // 8^3 blocks, 7-point: the warp-per-item kernel first; 8^3 and 16^3
+   // blocks: the double-buffered tile kernel
    brick_candidates<T>(g, stencil, n_blocks, out);
+   tile_candidates<T>(g, stencil, n_blocks, out);
    const int cols = g.ny * g.nz;
    const int full = std::min(256, (cols + 31) / 32 * 32);
    for (int thr : {full, std::max(32, full / 2 / 32 * 32)}) {
@@ -433,6 +391,15 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
 {
    if (n_blocks == 0)
       return 0;
+   if (sh.kernel == 2) {
+      int launches = launch_tile_stage(src, dst, g, stencil, items, recipes,
+                                       keep, stale, n_blocks, sh,
+                                       write_ghosts, do_cs, acc, err, s);
+      if (launches >= 0 && do_cs && sizeof(T) == 8)
+         launches += launch_fp64_checksums((const double *) dst, g, items,
+                                           n_blocks, partials, sums, s);
+      return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
+   }
    if (sh.kernel == 1) {
       int launches = launch_brick_stage(src, dst, g, items, n_blocks, sh,
                                         write_ghosts, do_cs, acc, err, s);

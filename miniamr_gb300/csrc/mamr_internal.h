@@ -120,10 +120,10 @@ int launch_checksum_fp32_all(const float *pool, const Geom &g,
 // FP32 checksum fallback for the variables var0 .. var0+nvar-1 whose cells
 // leave the fixed-point window: flags[0] is the miss word the checksum set
 // (nothing runs while it is clear), flags[1 .. nvar] per-variable miss
-// words (zeroed first), partials n * nvar doubles, acc the checksum slots
-// of var0 .. (two words each), overwritten for the variables that missed
-// with the compensated FP64 sum under kChecksumFallbackMark.  Returns 2
-// (kernels launched) or -1.
+// words and flags[1 + nvar] a counter (all zeroed first), partials
+// n * nvar doubles, acc the checksum slots of var0 .. (two words each),
+// overwritten for the variables that missed with the compensated FP64 sum
+// under kChecksumFallbackMark.  Returns 1 (kernels launched) or -1.
 int launch_fp32_checksum_fallback(const float *pool, const Geom &g,
                                   const int32_t *slots, int n, int var0,
                                   int nvar, unsigned *flags,

@@ -761,56 +761,62 @@ int launch_checksum_fp32(const float *pool, const Geom &g,
 // window takes the reference's summation order in FP64 with Neumaier
 // compensation instead (ref/check_sum.c:44-53): each block's interior
 // serially (k fastest) into s + c, rounded once, then the block values
-// serially in sorted order, S + C rounded once.  flags[0] is the checksum's
-// miss word (the checksum or stage kernel sets it); while it is clear both
-// kernels return at once, so the common case costs two empty launches.
-
-// One thread per (block, variable): the block's compensated sum into
-// partials[v * n + b]; flags[1 + v] records whether variable var0 + v has a
-// cell outside the window.
-__global__ void fp32_fallback_blocks(const float *__restrict__ pool, Geom g,
-                                     const int32_t *__restrict__ slots, int n,
-                                     int var0, int nvar,
-                                     unsigned *__restrict__ flags,
-                                     double *__restrict__ partials)
+// serially in sorted order, S + C rounded once.  flags[0] is the
+// checksum's miss word (the checksum or stage kernel sets it); while it is
+// clear the kernel returns at once, so the common case costs one empty
+// launch.  One thread per (block, variable) forms the block's compensated
+// sum into partials[v * n + b] and records in flags[1 + v] whether variable
+// var0 + v has a cell outside the window; the CTA that finishes last (the
+// counter flags[1 + nvar]) then adds the block values of each variable that
+// missed and stores the result in its checksum slot under the fallback
+// mark.
+__global__ void __launch_bounds__(128)
+fp32_fallback_kernel(const float *__restrict__ pool, Geom g,
+                     const int32_t *__restrict__ slots, int n, int var0,
+                     int nvar, unsigned *__restrict__ flags,
+                     double *__restrict__ partials,
+                     unsigned long long *__restrict__ acc)
 {
-   if (flags[0] == 0)
+   __shared__ bool last;
+   if (*(volatile unsigned *) flags == 0)
       return;
-   const long long q = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-   if (q >= (long long) n * nvar)
+   const long long items = (long long) n * nvar;
+   for (long long q = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+        q < items; q += (long long) gridDim.x * blockDim.x) {
+      const int v = (int) (q / n), b = (int) (q - (long long) v * n);
+      const float *base = pool + bv_offset(g, slots[b], var0 + v);
+      double s = 0.0, c = 0.0;
+      bool miss = false;
+      for (int i = 1; i <= g.nx; i++)
+         for (int j = 1; j <= g.ny; j++)
+            for (int k = 1; k <= g.nz; k++) {
+               const float x = base[cell_offset(g, i, j, k)];
+               const float a = fabsf(x);
+               miss |= !(a < 1024.0f && (a >= 0x1p-52f || a == 0.0f));
+               neumaier_add(s, c, (double) x);
+            }
+      partials[q] = s + c;
+      if (miss)
+         atomicOr(flags + 1 + v, 1u);
+   }
+   __threadfence();
+   __syncthreads();
+   if (threadIdx.x == 0)
+      last = atomicAdd(flags + 1 + nvar, 1u) == gridDim.x - 1;
+   __syncthreads();
+   if (!last)
       return;
-   const int v = (int) (q / n), b = (int) (q - (long long) v * n);
-   const float *base = pool + bv_offset(g, slots[b], var0 + v);
-   double s = 0.0, c = 0.0;
-   bool miss = false;
-   for (int i = 1; i <= g.nx; i++)
-      for (int j = 1; j <= g.ny; j++)
-         for (int k = 1; k <= g.nz; k++) {
-            const float x = base[cell_offset(g, i, j, k)];
-            const float a = fabsf(x);
-            miss |= !(a < 1024.0f && (a >= 0x1p-52f || a == 0.0f));
-            neumaier_add(s, c, (double) x);
-         }
-   partials[q] = s + c;
-   if (miss)
-      atomicOr(flags + 1 + v, 1u);
-}
-
-// One thread per variable that missed: the serial compensated sum of its
-// block values, stored in its checksum slot under the fallback mark.
-__global__ void fp32_fallback_totals(int n, int nvar,
-                                     const unsigned *__restrict__ flags,
-                                     const double *__restrict__ partials,
-                                     unsigned long long *__restrict__ acc)
-{
-   const int v = blockIdx.x * blockDim.x + threadIdx.x;
-   if (flags[0] == 0 || v >= nvar || flags[1 + v] == 0)
-      return;
-   double s = 0.0, c = 0.0;
-   for (int b = 0; b < n; b++)
-      neumaier_add(s, c, partials[(long long) v * n + b]);
-   acc[2 * v] = (unsigned long long) __double_as_longlong(s + c);
-   acc[2 * v + 1] = kChecksumFallbackMark;
+   __threadfence();
+   for (int v = threadIdx.x; v < nvar; v += blockDim.x) {
+      if (((volatile unsigned *) flags)[1 + v] == 0)
+         continue;
+      double s = 0.0, c = 0.0;
+      for (int b = 0; b < n; b++)
+         neumaier_add(s, c, ((volatile double *) partials)[(long long) v * n +
+                                                           b]);
+      acc[2 * v] = (unsigned long long) __double_as_longlong(s + c);
+      acc[2 * v + 1] = kChecksumFallbackMark;
+   }
 }
 
 int launch_fp32_checksum_fallback(const float *pool, const Geom &g,
@@ -821,12 +827,17 @@ int launch_fp32_checksum_fallback(const float *pool, const Geom &g,
 {
    if (n == 0 || nvar == 0)
       return 0;
+   // one CTA per SM: the common case (nothing missed) is a single short
+   // wave; the rare recomputation strides over the items
+   int dev = 0, sms = 1;
+   cudaGetDevice(&dev);
+   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
    const long long items = (long long) n * nvar;
-   fp32_fallback_blocks<<<(unsigned) ((items + 127) / 128), 128, 0, s>>>(
-      pool, g, slots, n, var0, nvar, flags, partials);
-   fp32_fallback_totals<<<(nvar + 127) / 128, 128, 0, s>>>(n, nvar, flags,
-                                                           partials, acc);
-   return cudaPeekAtLastError() == cudaSuccess ? 2 : -1;
+   const unsigned grid = (unsigned) std::max<long long>(
+      1, std::min<long long>((items + 127) / 128, sms));
+   fp32_fallback_kernel<<<grid, 128, 0, s>>>(pool, g, slots, n, var0, nvar,
+                                             flags, partials, acc);
+   return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
 // ---------------------------------------------------------------------------

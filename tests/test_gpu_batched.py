@@ -52,7 +52,21 @@ def test_batched_equals_plain_uniform(gpu_lib, case, dtype, flags):
         assert np.array_equal(bits(a), bits(b))
 
 
-@pytest.mark.parametrize("name", ["amr7", "amr7_objects", "amr27"])
+def _multilevel_prefix(recs, n_meshes=2):
+    """The records of a run up to its n-th multi-level mesh (a state on
+    several levels without replaying the whole run)."""
+    from miniamr_gb300.trace import OP_SET_MESH
+    seen = 0
+    for q, r in enumerate(recs):
+        if r.op == OP_SET_MESH and len(set(r.args[0]["level"].tolist())) > 1:
+            seen += 1
+            if seen == n_meshes:
+                return recs[:q + 1]
+    return recs
+
+
+@pytest.mark.parametrize("name", ["amr7", "amr7_objects", "amr27",
+                                  "config2"])
 @pytest.mark.parametrize("dtype", [FP64, FP32])
 def test_batched_equals_plain_multilevel(gpu_lib, name, dtype):
     """The reference's own multi-level meshes (states reached by replaying
@@ -63,6 +77,8 @@ def test_batched_equals_plain_multilevel(gpu_lib, name, dtype):
     edge and corner ghosts -- chains of face exchanges, level-jump
     transforms and cells no exchange writes -- from their recipes."""
     recs = read_trace(trace_path(name))
+    if name == "config2":          # 16^3 blocks: the state after its 2nd
+        recs = _multilevel_prefix(recs)   # multi-level mesh
     res = replay(gpu_lib, recs, dtype=dtype)
     assert len(np.unique(res.mesh["level"])) > 1
     ctx = res.ctx
@@ -87,6 +103,9 @@ def test_batched_equals_plain_multilevel(gpu_lib, name, dtype):
             assert np.array_equal(bits(a), bits(b)), (k, got[2])
     if name == "amr7":
         assert kernels == {True, False}
+    if name in ("amr7", "amr27", "config2"):
+        # the double-buffered tile kernel is among the shapes tried
+        assert n >= 3
     ctx.close()
 
 
