@@ -18,23 +18,25 @@ __device__ __forceinline__ T eval_recipe(const GhostRecipe &r, int t,
                                          const T *__restrict__ stale,
                                          const Geom &g, const DM &D, int var)
 {
-   int c[3] = {r.c[0], r.c[1], r.c[2]};
-   if (r.vax >= 0)
-      c[r.vax] = t;
+   // the cell, with the edge index in place (selects, not an indexed
+   // array, so that nothing goes to local memory)
+   const int c0 = r.vax == 0 ? t : r.c[0];
+   const int c1 = r.vax == 1 ? t : r.c[1];
+   const int c2 = r.vax == 2 ? t : r.c[2];
    // an interior cell now, or a ghost cell as the previous stage left it
    // (the stage that wrote the source pool wrote it there)
    if (r.kind == GR_INTERIOR || r.kind == GR_PREV)
-      return src[bv_offset(g, r.nb[0], var) + D.cell(c[0], c[1], c[2])];
+      return src[bv_offset(g, r.nb[0], var) + D.cell(c0, c1, c2)];
    if (r.kind == GR_STALE)
-      return stale[bv_offset(g, r.nb[0], var) + D.cell(c[0], c[1], c[2])];
+      return stale[bv_offset(g, r.nb[0], var) + D.cell(c0, c1, c2)];
    const int dir = r.l >> 1;
    const bool low = !(r.l & 1);
    const int n = dir == 0 ? D.nx : (dir == 1 ? D.ny : D.nz);
    const int na = dir == 0 ? D.ny : D.nx;
    const int nbb = dir == 2 ? D.ny : D.nz;
    const int ha = na / 2, hb = nbb / 2;
-   const int a = dir == 0 ? c[1] : c[0];
-   const int b = dir == 2 ? c[1] : c[2];
+   const int a = dir == 0 ? c1 : c0;
+   const int b = dir == 2 ? c1 : c2;
    if (r.kind == GR_COARSE) {
       const int iq = r.iqjq & 1, jq = r.iqjq >> 1;
       return quarter(src[bv_offset(g, r.nb[0], var) +

@@ -158,12 +158,12 @@ __device__ __forceinline__ void tile_issue(const T *__restrict__ src,
             const GhostRecipe &r = rc[ri];
             if (r.kind == GR_COARSE || r.kind == GR_FINE)
                continue;                       // formed after the wait
-            int c[3] = {r.c[0], r.c[1], r.c[2]};
-            if (r.vax >= 0)
-               c[r.vax] = t;
+            const int c0 = r.vax == 0 ? t : r.c[0];
+            const int c1 = r.vax == 1 ? t : r.c[1];
+            const int c2 = r.vax == 2 ? t : r.c[2];
             const T *base = r.kind == GR_STALE ? stale : src;
             cp_async_elem(to, base + bv_offset(g, r.nb[0], var) +
-                                 D.cell(c[0], c[1], c[2]));
+                                 D.cell(c0, c1, c2));
          } else {
             // one level: the neighbour across each ghost axis, or the
             // block's own plane where that axis is a boundary
@@ -454,43 +454,56 @@ tile_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
    T *tiles = reinterpret_cast<T *>(smem_raw);
    BItem *sI = reinterpret_cast<BItem *>(tiles + 2 * K::TILE);
    const int tid = threadIdx.x;
-   const long long n_items = (long long) nb * g.V;
-   auto put_desc = [&](long long it, BItem &to) {
-      const int b = (int) (it % nb);
+   auto put_desc = [&](int b, BItem &to) {
       const int32_t *from = reinterpret_cast<const int32_t *>(items + b);
       int32_t *t = reinterpret_cast<int32_t *>(&to);
       for (int q = tid; q < (int) (sizeof(BItem) / 4); q += THREADS)
          t[q] = __ldg(from + q);
    };
+   // work items (block b, variable var), variable-major; CTA c takes
+   // items c, c + grid, ... tracked as (var, b) without divisions
+   struct Pos {
+      int var, b;
+   };
+   const int step_v = gridDim.x / nb, step_b = gridDim.x - step_v * nb;
+   auto advance = [&](Pos q) {
+      q.var += step_v;
+      q.b += step_b;
+      if (q.b >= nb) {
+         q.b -= nb;
+         q.var++;
+      }
+      return q;
+   };
+   auto recipes_of = [&](int b) {
+      return recipes ? recipes + (size_t) b * kGhostRecipes : nullptr;
+   };
    unsigned long long lo = 0, hi = 0;
    Fixed52 part;
    bool ok = true;
    int cs_var = -1;
-   long long it = blockIdx.x;
-   if (it >= n_items)
+   Pos cur_p{(int) (blockIdx.x / nb), (int) (blockIdx.x % nb)};
+   if (cur_p.var >= g.V)
       return;
-   put_desc(it, sI[0]);
+   put_desc(cur_p.b, sI[0]);
    __syncthreads();
-   tile_issue<T, ST, N>(src, stale, g, sI[0],
-                        recipes ? recipes + (size_t) (it % nb) * kGhostRecipes
-                                : nullptr,
-                        (int) (it / nb), tiles);
+   tile_issue<T, ST, N>(src, stale, g, sI[0], recipes_of(cur_p.b), cur_p.var,
+                        tiles);
    cp_async_commit();
    for (int n = 0;; n++) {
-      const int var = (int) (it / nb), b = (int) (it % nb);
-      const long long nx = it + gridDim.x;
+      const int var = cur_p.var, b = cur_p.b;
+      const Pos nx = advance(cur_p);
+      const bool more = nx.var < g.V;
       BItem &cur = sI[n % 3];
       T *tb = tiles + (n & 1) * K::TILE;
       // the next item: descriptor, then its copies into the other tile
       // (every thread finished reading that tile before this barrier)
-      if (nx < n_items)
-         put_desc(nx, sI[(n + 1) % 3]);
+      if (more)
+         put_desc(nx.b, sI[(n + 1) % 3]);
       __syncthreads();
-      if (nx < n_items)
-         tile_issue<T, ST, N>(
-            src, stale, g, sI[(n + 1) % 3],
-            recipes ? recipes + (size_t) (nx % nb) * kGhostRecipes : nullptr,
-            (int) (nx / nb), tiles + ((n + 1) & 1) * K::TILE);
+      if (more)
+         tile_issue<T, ST, N>(src, stale, g, sI[(n + 1) % 3], recipes_of(nx.b),
+                              nx.var, tiles + ((n + 1) & 1) * K::TILE);
       cp_async_commit();
       cp_async_wait_group<1>();
       __syncthreads();
@@ -512,9 +525,9 @@ tile_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       tile_update<T, ST, N>(tb, d, g, sizeof(T) == 4 ? do_cs : 0, part, ok);
       if (sizeof(T) == 4 && do_cs)
          fixed52_flush(part, lo, hi);
-      if (nx >= n_items)
+      if (!more)
          break;
-      it = nx;
+      cur_p = nx;
    }
    if (sizeof(T) == 4 && do_cs) {
       if (cs_var >= 0)
