@@ -101,6 +101,8 @@ struct BatchedState {
    DevBuf items, partials, sums, acc, chain, pencils, bad;
    DevBuf csflags;             // FP32: per checksum stage, 1 + V miss words
                                // and the fallback's counter
+   DevBuf zf[2];               // the warp-per-block kernel's z-face arrays
+                               // (stage q writes zf[q & 1])
    DevBuf recipes, keep;       // 27-point edge/corner recipes (multi-level)
                                // and the blocks' keep masks
    bool has_recipes = false;
@@ -119,6 +121,7 @@ void batched_destroy(BatchedState *b)
    b->items.release(); b->partials.release(); b->sums.release();
    b->acc.release(); b->chain.release(); b->pencils.release();
    b->bad.release(); b->csflags.release(); b->recipes.release();
+   b->zf[0].release(); b->zf[1].release();
    b->keep.release();
    if (b->h_items)
       cudaFreeHost(b->h_items);
@@ -1228,12 +1231,12 @@ static int tune_choice(mamr_ctx *c, const std::vector<StageShape> &cands,
    float best = 0.f;
    int status = MAMR_OK;
    for (size_t q = 0; q < cands.size() && status == MAMR_OK; q++) {
-      int k = stage(c->pool, c->pool_alt, cands[q], 0, false, 0);
+      int k = stage(c->pool, c->pool_alt, cands[q], 0, false, 0, -1);
       bool ok = k >= 0;
       c->launches += ok ? k : 0;
       ok = ok && cudaEventRecord(e0, c->stream) == cudaSuccess;
       for (int rep = 0; rep < 3 && ok; rep++) {
-         k = stage(c->pool, c->pool_alt, cands[q], 0, false, 0);
+         k = stage(c->pool, c->pool_alt, cands[q], 0, false, 0, -1);
          ok = k >= 0;
          c->launches += ok ? k : 0;
       }
@@ -1315,9 +1318,14 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    const GhostRecipe *recipes =
       B->has_recipes ? (const GhostRecipe *) B->recipes.p : nullptr;
    const int *keep = B->has_recipes ? (const int *) B->keep.p : nullptr;
-   // one stage: cur -> oth with launch shape sh
+   // one stage: cur -> oth with launch shape sh; q = the stage's index in
+   // the run (-1: a tuning stage).  The warp-per-block kernel writes the
+   // z-face array of stage q and reads that of stage q - 1.
    auto stage = [&](const void *cur, void *oth, const StageShape &sh,
-                    int last, bool do_cs, int cnt) -> int {
+                    int last, bool do_cs, int cnt, int q) -> int {
+      const bool zfs = sh.kernel == 1 && q >= 0;
+      void *zf_dst = zfs ? B->zf[q & 1].p : nullptr;
+      const void *zf_src = zfs && q > 0 ? B->zf[(q - 1) & 1].p : nullptr;
       unsigned long long *acc =
          c->fp32 ? (unsigned long long *) B->acc.p + (size_t) cnt * V * 2
                  : nullptr;
@@ -1357,13 +1365,15 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
             (const float *) cur, (float *) oth, c->g, c->cfg.stencil,
             (const BItem *) B->items.p, recipes, keep,
             (const float *) stale_pool,
-            nb, sh, last, do_cs, part, sums_at, acc, flags, c->stream));
+            nb, sh, last, do_cs, part, sums_at, acc, flags,
+            (const float *) zf_src, (float *) zf_dst, c->stream));
       return launch_batched_stage((const double *) cur, (double *) oth, c->g,
                                   c->cfg.stencil, (const BItem *) B->items.p,
                                   recipes, keep, (const double *) stale_pool,
                                   nb,
                                   sh, last, do_cs, part, sums_at, acc,
-                                  c->d_err, c->stream);
+                                  c->d_err, (const double *) zf_src,
+                                  (double *) zf_dst, c->stream);
    };
    std::vector<StageShape> cands;
    if (pencil && c->fp32)
@@ -1389,6 +1399,13 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    c->tune_last = choice;
    c->tune_n = (int) cands.size();
    c->tune_shape = sh;
+   if (sh.kernel == 1 && num_ts * spt > 1) {
+      // the warp-per-block kernel's z-face arrays (written by each stage,
+      // read by the next)
+      const size_t zb = brick_zface_elems(c->g, c->cfg.max_blocks) * es;
+      CUDA_TRY(B->zf[0].ensure(zb));
+      CUDA_TRY(B->zf[1].ensure(zb));
+   }
    // A run of an odd number of stages ends in the spare pool: it must then
    // hold what no stage writes (stale ghosts, free slots) as the current
    // pool does, so it starts as a copy.  With an even number the run ends
@@ -1412,7 +1429,7 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       for (int st = 0; st < spt; st++, q++) {
          const bool do_cs = freq && !(st % freq);
          const int last = (q == total - 1);
-         const int k = stage(cur, oth, sh, last, do_cs, cnt);
+         const int k = stage(cur, oth, sh, last, do_cs, cnt, q);
          if (k < 0) {
             status = fail(MAMR_ECUDA, "batched stage launch: %s",
                           cudaGetErrorString(cudaGetLastError()));

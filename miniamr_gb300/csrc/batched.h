@@ -285,7 +285,9 @@ struct StageShape {
 // recipes: the 27-point edge and corner recipes of a multi-level mesh
 // (n_blocks * kGhostRecipes, mesh order) and keep, the blocks' keep masks,
 // or null on one level; stale: the pool the run started from (recipes'
-// stale cells).
+// stale cells); zf_src / zf_dst: the warp-per-block kernel's z-face arrays
+// of the source (null when the previous stage wrote none) and the
+// destination (null: none written).
 template <typename T>
 int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
                          const BItem *items, const GhostRecipe *recipes,
@@ -293,7 +295,7 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
                          const StageShape &sh, int write_ghosts, int do_cs,
                          double *partials, double *sums,
                          unsigned long long *acc, unsigned *err,
-                         cudaStream_t s);
+                         const T *zf_src, T *zf_dst, cudaStream_t s);
 // The generic kernel's launch shapes for this geometry (first = default).
 template <typename T>
 void batched_candidates(const Geom &g, int stencil, int n_blocks,
@@ -320,7 +322,14 @@ template <typename T>
 int launch_brick_stage(const T *src, T *dst, const Geom &g,
                        const BItem *items, int n_blocks, const StageShape &sh,
                        int write_ghosts, int do_cs, unsigned long long *acc,
-                       unsigned *err, cudaStream_t s);
+                       unsigned *err, const T *zf_src, T *zf_dst,
+                       cudaStream_t s);
+// Elements of one z-face array (planes k = 1 and k = 8 of every slot and
+// variable) of the warp-per-block kernel.
+inline size_t brick_zface_elems(const Geom &g, int max_blocks)
+{
+   return (size_t) max_blocks * g.V * 2 * 64;
+}
 
 // Pencil variant for single-level meshes of 16^3 blocks: CTAs walk chains
 // of blocks along z (chain[pencils[p].x .. +pencils[p].y), bottom to

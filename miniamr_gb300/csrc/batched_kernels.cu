@@ -387,7 +387,7 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
                          const StageShape &sh, int write_ghosts, int do_cs,
                          double *partials, double *sums,
                          unsigned long long *acc, unsigned *err,
-                         cudaStream_t s)
+                         const T *zf_src, T *zf_dst, cudaStream_t s)
 {
    if (n_blocks == 0)
       return 0;
@@ -402,7 +402,8 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
    }
    if (sh.kernel == 1) {
       int launches = launch_brick_stage(src, dst, g, items, n_blocks, sh,
-                                        write_ghosts, do_cs, acc, err, s);
+                                        write_ghosts, do_cs, acc, err, zf_src,
+                                        zf_dst, s);
       if (launches >= 0 && do_cs && sizeof(T) == 8)
          launches += launch_fp64_checksums((const double *) dst, g, items,
                                            n_blocks, partials, sums, s);
@@ -544,6 +545,7 @@ template int launch_batched_stage<float>(const float *, float *, const Geom &,
                                          int, const StageShape &, int, int,
                                          double *, double *,
                                          unsigned long long *, unsigned *,
+                                         const float *, float *,
                                          cudaStream_t);
 template int launch_batched_stage<double>(const double *, double *,
                                           const Geom &, int, const BItem *,
@@ -552,6 +554,7 @@ template int launch_batched_stage<double>(const double *, double *,
                                           int, const StageShape &, int, int,
                                           double *, double *,
                                           unsigned long long *, unsigned *,
+                                          const double *, double *,
                                           cudaStream_t);
 
 }  // namespace mamr

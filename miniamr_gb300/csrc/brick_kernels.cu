@@ -5,7 +5,16 @@
 // ghosts that are copies (same-level neighbour, reflection) or single
 // values (coarser neighbour, scaled by 1/4 afterwards) -- with cp.async
 // while it computes the current item; ghosts from finer neighbours (sums of
-// four cells) are gathered after the wait.  The values and the operation
+// four cells) are gathered after the wait.
+//
+// z-face arrays.  The z ghosts of a block are one value from each of 64
+// rows of its neighbour -- a 32-byte sector per value.  So every stage also
+// stores each block-variable's k = 1 and k = 8 planes, 64 values each,
+// contiguously in a z-face array beside the destination pool, and the next
+// stage of the run fetches its z faces from there as 16-byte copies (the
+// first stage of a run, whose source has no such array yet, copies them
+// value by value).  A tile's z ghosts sit in two planes of 64 values after
+// the tile.  The values and the operation
 // order are those of the generic stage kernel (batched_kernels.cu): the
 // reference's face exchange (ref/comm.c:1465-1965) and 7-point update
 // (ref/stencil.c:82-101), with the FP32 fixed-point checksum of every
@@ -38,6 +47,8 @@ template <typename T> struct Brick {
    static constexpr int R = 8 / VW;                  // vectors per row
    static constexpr int S = sizeof(T) == 4 ? 12 : 10;
    static constexpr int TILE = 100 * S;
+   static constexpr int ZST = 128;   // z ghost planes k = 0, 9 after a tile
+   static constexpr int SLAB = TILE + ZST;
    static constexpr int DESC = 44;   // ints of a BItem read: slot .. f[5]
    __device__ static int at(int i, int j, int k)
    {
@@ -61,7 +72,14 @@ template <typename T> struct Brick {
    }
    static size_t smem_per_item()
    {
-      return 2 * (TILE * sizeof(T) + DESC * sizeof(int));
+      return 2 * (SLAB * sizeof(T) + DESC * sizeof(int));
+   }
+   // z-face array: planes k = 1 (side 0) and k = 8 (side 1) of a
+   // block-variable, 64 values each, at (i-1)*8 + (j-1)
+   __device__ static long long zf_at(const Geom &g, int slot, int var,
+                                     int side)
+   {
+      return (((long long) slot * g.V + var) * 2 + side) * 64;
    }
 };
 
@@ -97,12 +115,14 @@ __device__ __forceinline__ void st4(T *p, const T (&v)[4])
 // jump).
 template <typename T, int TPI>
 __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
+                                            const T *__restrict__ zf,
                                             const Geom &g, int var,
                                             const int *sd, T *tile, int lane)
 {
    bool fix = false;
    using B = Brick<T>;
    constexpr int VW = B::VW, R = B::R;
+   T *zst = tile + B::TILE;
    const T *own = src + bv_offset(g, sd[0], var);
 #pragma unroll
    for (int t = 0; t < 64 * R / TPI; t++) {
@@ -130,11 +150,17 @@ __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
                else
                   cp_async16(tile + B::at(a, gn, k), sb + B::gat(a, p, k));
             }
+         } else if (zf) {
+            // the plane from the z-face array: 64 values as 16-byte copies
+            const int slot = type == FACE_SAME ? f[1] : sd[0];
+            const T *pl = zf + B::zf_at(g, slot, var, p == 8);
+            if (lane < 64 / VW)
+               cp_async16(zst + (low ? 0 : 64) + lane * VW, pl + lane * VW);
          } else {
 #pragma unroll
             for (int u = 0; u < 64 / TPI; u++) {
                const int e = lane + TPI * u, i = (e >> 3) + 1, j = (e & 7) + 1;
-               cp_async_elem(tile + B::at(i, j, gn), sb + B::gat(i, j, p));
+               cp_async_elem(zst + (low ? 0 : 64) + e, sb + B::gat(i, j, p));
             }
          }
       } else if (type == FACE_COARSE) {
@@ -144,9 +170,17 @@ __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
 #pragma unroll
          for (int u = 0; u < 64 / TPI; u++) {
             const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
-            cp_async_elem(tile + B::ghost_at(dir, gn, a, b),
-                          sb + B::face_gat(dir, p, (a + 1) / 2 + 4 * jq,
-                                           (b + 1) / 2 + 4 * iq));
+            const int ca = (a + 1) / 2 + 4 * jq, cb = (b + 1) / 2 + 4 * iq;
+            if (dir < 2)
+               cp_async_elem(tile + B::ghost_at(dir, gn, a, b),
+                             sb + B::face_gat(dir, p, ca, cb));
+            else if (zf)
+               cp_async_elem(zst + (low ? 0 : 64) + e,
+                             zf + B::zf_at(g, f[1], var, p == 8) +
+                                (ca - 1) * 8 + (cb - 1));
+            else
+               cp_async_elem(zst + (low ? 0 : 64) + e,
+                             sb + B::face_gat(dir, p, ca, cb));
          }
       } else {
          fix = true;                   // finer neighbours: summed later
@@ -160,10 +194,12 @@ __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
 // neighbours' cells, in the reference's order.
 template <typename T, int TPI>
 __device__ __forceinline__ void brick_fix(const T *__restrict__ src,
+                                          const T *__restrict__ zf,
                                           const Geom &g, int var,
                                           const int *sd, T *tile, int lane)
 {
    using B = Brick<T>;
+   T *zst = tile + B::TILE;
 #pragma unroll
    for (int l = 0; l < 6; l++) {
       const int *f = sd + 2 + 7 * l;
@@ -176,17 +212,29 @@ __device__ __forceinline__ void brick_fix(const T *__restrict__ src,
 #pragma unroll
       for (int u = 0; u < 64 / TPI; u++) {
          const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
-         T &x = tile[B::ghost_at(dir, gn, a, b)];
+         T &x = dir < 2 ? tile[B::ghost_at(dir, gn, a, b)]
+                        : zst[(low ? 0 : 64) + e];
          if (type == FACE_COARSE) {
             x = quarter(x);
          } else {
             const int jq = a > 4, iq = b > 4;
             const int a2 = a - 4 * jq, b2 = b - 4 * iq;
-            const T *fb = src + bv_offset(g, f[1 + iq * 2 + jq], var);
-            T t = fb[B::face_gat(dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
-                  fb[B::face_gat(dir, p, 2 * a2 - 1, 2 * b2)];
-            t = t + fb[B::face_gat(dir, p, 2 * a2, 2 * b2 - 1)];
-            t = t + fb[B::face_gat(dir, p, 2 * a2, 2 * b2)];
+            const int nbs = f[1 + iq * 2 + jq];
+            T t;
+            if (dir == 2 && zf) {
+               // the fine block's plane p from its z-face array
+               const T *pl = zf + B::zf_at(g, nbs, var, p == 8);
+               t = pl[(2 * a2 - 2) * 8 + 2 * b2 - 2] +
+                   pl[(2 * a2 - 2) * 8 + 2 * b2 - 1];
+               t = t + pl[(2 * a2 - 1) * 8 + 2 * b2 - 2];
+               t = t + pl[(2 * a2 - 1) * 8 + 2 * b2 - 1];
+            } else {
+               const T *fb = src + bv_offset(g, nbs, var);
+               t = fb[B::face_gat(dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
+                   fb[B::face_gat(dir, p, 2 * a2 - 1, 2 * b2)];
+               t = t + fb[B::face_gat(dir, p, 2 * a2, 2 * b2 - 1)];
+               t = t + fb[B::face_gat(dir, p, 2 * a2, 2 * b2)];
+            }
             x = t;
          }
       }
@@ -218,7 +266,8 @@ __global__ void __launch_bounds__(BrickBounds<TPI, sizeof(T) == 4>::THREADS,
 brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                    const BItem *__restrict__ items, int nb, int write_ghosts,
                    int do_cs, unsigned long long *__restrict__ acc,
-                   unsigned *__restrict__ err)
+                   unsigned *__restrict__ err, const T *__restrict__ zf_src,
+                   T *__restrict__ zf_dst)
 {
    using B = Brick<T>;
    constexpr int DESC = B::DESC;
@@ -227,9 +276,9 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
    extern __shared__ __align__(16) unsigned char smem_raw[];
    const int lane = threadIdx.x % TPI, group = threadIdx.x / TPI;
    const int gpc = blockDim.x / TPI;
-   T *tiles = reinterpret_cast<T *>(smem_raw) + (size_t) group * 2 * B::TILE;
+   T *tiles = reinterpret_cast<T *>(smem_raw) + (size_t) group * 2 * B::SLAB;
    int *sdesc = reinterpret_cast<int *>(reinterpret_cast<T *>(smem_raw) +
-                                        (size_t) gpc * 2 * B::TILE) +
+                                        (size_t) gpc * 2 * B::SLAB) +
                 group * 2 * DESC;
    // work items (block b, variable var), variable-major; group w takes
    // items w, w + nw, w + 2 nw, ... tracked as (var, b) without divisions
@@ -272,7 +321,8 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
 
    load_desc(cur);
    put_desc(sdesc);
-   bool fix_cur = brick_issue<T, TPI>(src, g, cur.var, sdesc, tiles, lane);
+   bool fix_cur = brick_issue<T, TPI>(src, zf_src, g, cur.var, sdesc, tiles,
+                                      lane);
    cp_async_commit();
    Pos nxt = advance(cur);
    if (nxt.var < g.V)
@@ -284,15 +334,16 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
    int cs_var = -1;
    for (int n = 0;; n++) {
       const int cb = n & 1;
-      T *tile = tiles + cb * B::TILE;
+      T *tile = tiles + cb * B::SLAB;
+      const T *zst = tile + B::TILE;
       const int *sd = sdesc + cb * DESC;
       // the next item: descriptor into shared memory, copies in flight
       bool fix_next = false;
       if (nxt.var < g.V) {
          int *sdn = sdesc + (cb ^ 1) * DESC;
          put_desc(sdn);
-         fix_next = brick_issue<T, TPI>(src, g, nxt.var, sdn,
-                                        tiles + (cb ^ 1) * B::TILE, lane);
+         fix_next = brick_issue<T, TPI>(src, zf_src, g, nxt.var, sdn,
+                                        tiles + (cb ^ 1) * B::SLAB, lane);
          const Pos nn = advance(nxt);
          if (nn.var < g.V)
             load_desc(nn);
@@ -301,7 +352,7 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       cp_async_wait_group<1>();
       const int var = cur.var;
       if (fix_cur)
-         brick_fix<T, TPI>(src, g, var, sd, tile, lane);
+         brick_fix<T, TPI>(src, zf_src, g, var, sd, tile, lane);
       group_sync<TPI>(group);
       T *d = dst + bv_offset(g, sd[0], var);
       if (write_ghosts) {
@@ -315,7 +366,8 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                if (dir == 0) { gi = gn; gj = a; gk = b; }
                else if (dir == 1) { gi = a; gj = gn; gk = b; }
                else { gi = a; gj = b; gk = gn; }
-               d[D.cell(gi, gj, gk)] = tile[B::at(gi, gj, gk)];
+               d[D.cell(gi, gj, gk)] = dir < 2 ? tile[B::at(gi, gj, gk)]
+                                               : zst[(gn ? 64 : 0) + e];
             }
          }
       }
@@ -339,8 +391,10 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
             ld4(tile + B::at(i, j, k0), c);
             ld4(tile + B::at(i, j + 1, k0), jp);
             ld4(tile + B::at(i + 1, j, k0), bq);
-            const T cm = tile[B::at(i, j, k0 - 1)];
-            const T cp = tile[B::at(i, j, k0 + 4)];
+            // k = 0 and k = 9 from the tile's z ghost planes
+            const int zi = (i - 1) * 8 + (j - 1);
+            const T cm = h == 0 ? zst[zi] : tile[B::at(i, j, k0 - 1)];
+            const T cp = h == 1 ? zst[64 + zi] : tile[B::at(i, j, k0 + 4)];
             T w[4], q[4];
 #pragma unroll
             for (int t = 0; t < 4; t++) {
@@ -356,6 +410,11 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
             }
             div_const4<7>(w, q);
             st4(d + B::gat(i, j, k0), q);
+            if (zf_dst) {
+               // this block's k = 1 / k = 8 plane for the next stage
+               T *zp = zf_dst + B::zf_at(g, sd[0], var, h);
+               zp[zi] = h == 0 ? q[0] : q[3];
+            }
             if (sizeof(T) == 4 && do_cs) {
 #pragma unroll
                for (int t = 0; t < 4; t++)
@@ -435,7 +494,8 @@ template <typename T>
 int launch_brick_stage(const T *src, T *dst, const Geom &g,
                        const BItem *items, int n_blocks, const StageShape &sh,
                        int write_ghosts, int do_cs, unsigned long long *acc,
-                       unsigned *err, cudaStream_t s)
+                       unsigned *err, const T *zf_src, T *zf_dst,
+                       cudaStream_t s)
 {
    if (n_blocks == 0)
       return 0;
@@ -443,10 +503,12 @@ int launch_brick_stage(const T *src, T *dst, const Geom &g,
    const int cs = sizeof(T) == 4 ? do_cs : 0;
    if (sh.threads == 64)
       brick_stage_kernel<T, 64><<<sh.grid, 64 * sh.vpc, smem, s>>>(
-         src, dst, g, items, n_blocks, write_ghosts, cs, acc, err);
+         src, dst, g, items, n_blocks, write_ghosts, cs, acc, err, zf_src,
+         zf_dst);
    else
       brick_stage_kernel<T, 32><<<sh.grid, 32 * sh.vpc, smem, s>>>(
-         src, dst, g, items, n_blocks, write_ghosts, cs, acc, err);
+         src, dst, g, items, n_blocks, write_ghosts, cs, acc, err, zf_src,
+         zf_dst);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -457,11 +519,13 @@ template void brick_candidates<double>(const Geom &, int, int,
 template int launch_brick_stage<float>(const float *, float *, const Geom &,
                                        const BItem *, int, const StageShape &,
                                        int, int, unsigned long long *,
-                                       unsigned *, cudaStream_t);
+                                       unsigned *, const float *, float *,
+                                       cudaStream_t);
 template int launch_brick_stage<double>(const double *, double *,
                                         const Geom &, const BItem *, int,
                                         const StageShape &, int, int,
                                         unsigned long long *, unsigned *,
+                                        const double *, double *,
                                         cudaStream_t);
 
 }  // namespace mamr
