@@ -162,11 +162,15 @@ __device__ __forceinline__ float sum8(const float *t)
 struct Fixed52 {
    unsigned a1 = 0, a2 = 0, a3 = 0;   // sums of sign * bits(tk), mod 2^32
    int cnt = 0;                       // sum of the signs
+   // window statistics of the terms added: the largest bits(|v|) and the
+   // smallest bits(|v|) - 1 (a zero wraps to the top and counts as inside)
+   unsigned umax = 0u, umin1 = 0xffffffffu;
 };
 
-// Adds the term of v (negate: its opposite); returns whether v lies in the
-// exact window (v == 0 or 2^-52 <= |v| < 2^10).
-__device__ __forceinline__ bool fixed52_add(float v, Fixed52 &p,
+// Adds the term of v (negate: its opposite, a term taken back, which the
+// window statistics leave out).  Whether every term lay in the exact window
+// is asked once, of the statistics (fixed52_window), not per term.
+__device__ __forceinline__ void fixed52_add(float v, Fixed52 &p,
                                             bool negate = false)
 {
    const float x = fabsf(v);
@@ -182,7 +186,19 @@ __device__ __forceinline__ bool fixed52_add(float v, Fixed52 &p,
    p.a2 += (unsigned) s * __float_as_uint(t2);
    p.a3 += (unsigned) s * __float_as_uint(t3);
    p.cnt += s;
-   return x < 1024.0f && (x >= 0x1p-52f || x == 0.0f);
+   if (!negate) {
+      const unsigned u = __float_as_uint(x);
+      p.umax = max(p.umax, u);
+      p.umin1 = min(p.umin1, u - 1u);
+   }
+}
+
+// Whether every term added lay in the exact window: v == 0 or
+// 2^-52 <= |v| < 2^10 (NaN and infinities have larger bits than 2^10).
+__device__ __forceinline__ bool fixed52_window(const Fixed52 &p)
+{
+   return p.umax < __float_as_uint(1024.0f) &&
+          p.umin1 >= __float_as_uint(0x1p-52f) - 1u;
 }
 
 // The compensated (Neumaier) FP64 step the checksum fallback uses: adds x
@@ -229,7 +245,8 @@ __device__ __forceinline__ void fixed52_flush(Fixed52 &p,
        : "l"((unsigned long long) i1 << 40),
          "l"((unsigned long long) (i1 >> 24)));
    acc128_add(lo, hi, i2 * (1ll << 18) + i3);
-   p = Fixed52();
+   p.a1 = p.a2 = p.a3 = 0;     // the window statistics carry on
+   p.cnt = 0;
 }
 
 __device__ __forceinline__ void acc128_merge(unsigned long long &lo,

@@ -255,7 +255,7 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                   const T out = div7(w);
                   d[D.cell(i, j, k)] = out;
                   if (sizeof(T) == 4 && do_cs) {
-                     ok &= fixed52_add((float) out, part);
+                     fixed52_add((float) out, part);
                      if (nx > 256 && (i & 255) == 0)
                         fixed52_flush(part, lo, hi);
                   }
@@ -280,7 +280,7 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                   const T out = div27((s0 + s1) + s2);
                   d[D.cell(i, j, k)] = out;
                   if (sizeof(T) == 4 && do_cs) {
-                     ok &= fixed52_add((float) out, part);
+                     fixed52_add((float) out, part);
                      if (nx > 256 && (i & 255) == 0)
                         fixed52_flush(part, lo, hi);
                   }
@@ -296,7 +296,7 @@ batched_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
    if (sizeof(T) == 4 && do_cs) {
       if (cs_var >= 0)
          warp_acc128_flush(lo, hi, acc + 2 * cs_var);
-      if (!ok)
+      if (!ok || !fixed52_window(part))
          atomicOr(err, ERR_FIXED_RANGE);
    }
 #undef TS

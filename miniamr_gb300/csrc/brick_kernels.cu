@@ -418,7 +418,7 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
             if (sizeof(T) == 4 && do_cs) {
 #pragma unroll
                for (int t = 0; t < 4; t++)
-                  ok &= fixed52_add((float) q[t], part);
+                  fixed52_add((float) q[t], part);
             }
          }
       }
@@ -434,7 +434,7 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
    if (sizeof(T) == 4 && do_cs) {
       if (cs_var >= 0)
          warp_acc128_flush(lo, hi, acc + 2 * cs_var);
-      if (!ok)
+      if (!ok || !fixed52_window(part))
          atomicOr(err, ERR_FIXED_RANGE);
    }
 }

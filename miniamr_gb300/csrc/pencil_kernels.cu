@@ -186,7 +186,7 @@ __device__ __forceinline__ void checksum4(const T (&out)[4], bool &ok,
 {
 #pragma unroll
    for (int m = 0; m < 4; m++)
-      ok &= fixed52_add((float) out[m], part);
+      fixed52_add((float) out[m], part);
 }
 
 __device__ __forceinline__ float div_rn_inline(float x, float c)
@@ -232,7 +232,7 @@ __device__ __forceinline__ void emit4(const T (&w)[4], T *p, int do_cs,
             const T qc = div_rn_inline(w[m], (T) C);
             p[m] = qc;
             if (sizeof(T) == 4 && do_cs) {
-               st.ok &= fixed52_add((float) qc, st.part);
+               fixed52_add((float) qc, st.part);
                fixed52_add((float) qf, st.part, true);
             }
          }
@@ -483,7 +483,7 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
          }
       }
       if (sizeof(T) == 4 && do_cs) {
-         if (!st.ok)
+         if (!st.ok || !fixed52_window(st.part))
             atomicOr(err, ERR_FIXED_RANGE);
          block_acc128_flush(st.lo, st.hi, acc + 2 * var);
       }

@@ -654,10 +654,10 @@ __device__ __forceinline__ void interior_fixed52(const float *base,
          const int i = rr / BY + 1, j = rr % BY + 1;
          const float4 v = __ldg(
             reinterpret_cast<const float4 *>(base + (i * Y + j) * BZ) + q);
-         ok &= fixed52_add(v.x, part);
-         ok &= fixed52_add(v.y, part);
-         ok &= fixed52_add(v.z, part);
-         ok &= fixed52_add(v.w, part);
+         fixed52_add(v.x, part);
+         fixed52_add(v.y, part);
+         fixed52_add(v.z, part);
+         fixed52_add(v.w, part);
          if ((t & 63) == 0)                 // 256 terms
             fixed52_flush(part, lo, hi);
       }
@@ -666,11 +666,12 @@ __device__ __forceinline__ void interior_fixed52(const float *base,
       for (int e = threadIdx.x, t = 1; e < cells; e += blockDim.x, t++) {
          int i = e / (g.ny * g.nz) + 1, r = e % (g.ny * g.nz);
          int j = r / g.nz + 1, k = r % g.nz + 1;
-         ok &= fixed52_add(base[cell_offset(g, i, j, k)], part);
+         fixed52_add(base[cell_offset(g, i, j, k)], part);
          if ((t & 255) == 0)
             fixed52_flush(part, lo, hi);
       }
    }
+   ok &= fixed52_window(part);
    fixed52_flush(part, lo, hi);
 }
 

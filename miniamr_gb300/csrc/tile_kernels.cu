@@ -320,7 +320,7 @@ __device__ __forceinline__ void tile_update(const T *tb, T *d, const Geom &g,
          if (do_cs) {
 #pragma unroll
             for (int m = 0; m < 4; m++)
-               ok &= fixed52_add((float) q[m], part);
+               fixed52_add((float) q[m], part);
          }
       };
       if (ST == 7) {
@@ -532,7 +532,7 @@ tile_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
    if (sizeof(T) == 4 && do_cs) {
       if (cs_var >= 0)
          warp_acc128_flush(lo, hi, acc + 2 * cs_var);
-      if (!ok)
+      if (!ok || !fixed52_window(part))
          atomicOr(err, ERR_FIXED_RANGE);
    }
 }
