@@ -410,6 +410,69 @@ def stress_multilevel(lib, dtype):
                 for name, (t, n) in refine.items()}}
 
 
+def stress_driver(lib, dtype):
+    """The multi-level stress run at its full length through the AMR driver
+    (mamr_amr_run): 4^3 blocks of 8^3, 40 variables, 7-point, 5 levels,
+    four moving objects, refine every 2 steps, 300 timesteps x 2 stages,
+    checksum every stage -- 151 refinements, each the marking on the
+    device, the library's split/consolidation bookkeeping, the cell
+    movement on the device and a new mesh; every stretch of stages one
+    batched run under a freshly captured CUDA graph.  A 10-timestep run
+    first lets the tuner time its launch shapes.  Rates: updates over the
+    stretches' wall time (each stretch synchronised) and over the whole
+    call (initial values, upload and refinement included).  Checksums
+    against the reference's own log of the run: FP64 bit for bit, FP32 max
+    and RMS relative error."""
+    from miniamr_gb300 import run as runmod
+    meta = json.load(open(os.path.join(REPO, "tests", "golden",
+                                       "cases.json")))
+    if "config5_300" not in meta:
+        return None
+    spec = runmod.parse(meta["config5_300"]["args"])
+    spec.fp32 = dtype != 0
+    cfg = spec.config()
+    warm = spec.params()
+    warm.num_tsteps = 10
+    with lib.context(cfg) as ctx:
+        ctx.amr_run(warm, spec.objects)
+    with lib.context(cfg) as ctx:
+        sums, st, _ = ctx.amr_run(spec.params(), spec.objects)
+    out = {"timesteps": spec.opts["num_tsteps"],
+           "refinements": st["refinements"],
+           "max_blocks": st["max_active"], "final_blocks": st["final_active"],
+           "updates": st["updates"],
+           "updates_per_s": st["updates"] / st["stage_seconds"],
+           "updates_per_s_whole_run": st["updates"] / st["total_seconds"],
+           "stage_seconds": st["stage_seconds"],
+           "refine_seconds": st["refine_seconds"],
+           "total_seconds": st["total_seconds"], "checksums": sums.size}
+    path = os.path.join(REPO, "tests", "golden", "config5_300.reflog.xz")
+    if os.path.exists(path):
+        import lzma
+        import struct
+        ref = []
+        with lzma.open(path, "rt") as f:
+            for ln in f:
+                p = ln.split()
+                if p[0] == "cs":
+                    ref.append(struct.unpack(
+                        "<d", int(p[3], 16).to_bytes(8, "little"))[0])
+        ref = np.array(ref)
+        got = sums.reshape(-1)
+        if got.size == ref.size:
+            if dtype == 0:
+                out["checksums_bit_exact_vs_reference"] = bool(
+                    np.array_equal(got.view(np.uint64), ref.view(np.uint64)))
+            else:
+                rel = np.abs(got - ref) / np.abs(ref)
+                out["checksum_rel_error_vs_reference_fp64"] = {
+                    "max": float(rel.max()),
+                    "rms": float(np.sqrt(np.mean(rel ** 2)))}
+        else:
+            out["checksum_count_mismatch"] = [int(got.size), int(ref.size)]
+    return out
+
+
 def refine_marking(lib):
     """Refinement marking (mamr_mark_refine: reset_all, check_objects and
     refine_level of one rank) on the recorded steps of the multi-level
@@ -740,6 +803,8 @@ def main():
             "uniform_stencil0_fp64": uniform_stencil0(lib),
             "stress_multilevel_7pt_fp32": stress_multilevel(lib, FP32),
             "stress_multilevel_7pt_fp64": stress_multilevel(lib, FP64),
+            "stress_300ts_amr_driver_fp32": stress_driver(lib, FP32),
+            "stress_300ts_amr_driver_fp64": stress_driver(lib, FP64),
             "refine_marking_stress": refine_marking(lib),
         }
     # the figures the targets rest on last, where a truncated tail of the

@@ -279,6 +279,86 @@ int mamr_mark_refine(mamr_ctx *ctx, const mamr_mark_params *params,
                      const mamr_mark_parent *parents, int32_t n_parents,
                      int32_t *block_refine, int32_t *parent_refine);
 
+/* ---- a whole run: the driver, refinement and stage loop --------------- */
+
+/* The run parameters of the reference's command line that the AMR driver
+ * needs (ref/main.c:56-140, defaults ref/param.h); the block size,
+ * variable count, pool capacity, stencil, code, permute and precision come
+ * from the context's mamr_config. */
+typedef struct {
+   int32_t init_x, init_y, init_z;  /* --init_x/y/z: initial blocks (one rank) */
+   int32_t num_refine;              /* --num_refine: maximum level */
+   int32_t block_change;            /* --block_change (0: num_refine) */
+   int32_t refine_freq;             /* --refine_freq: timesteps between refines */
+   int32_t uniform_refine;          /* --uniform_refine */
+   int32_t refine_ghost;            /* --refine_ghost */
+   int32_t num_tsteps;              /* --num_tsteps */
+   int32_t stages_per_ts;           /* --stages_per_ts */
+   int32_t checksum_freq;           /* --checksum_freq */
+   int32_t run_flags;               /* MAMR_RUN_* of the stage stretches */
+   int32_t reserved[8];             /* must be zero */
+} mamr_amr_params;
+
+/* One --object of the command line (ref/main.c:118-137): type as in
+ * mamr_object, bounce (1: reflect off the unit cube's faces), centre,
+ * velocity per timestep, half-size, size change per timestep. */
+typedef struct {
+   int32_t type, bounce;
+   double cen[3], move[3], size[3], inc[3];
+} mamr_amr_object;
+
+/* What the driver reports as it goes (for checking it against recorded
+ * runs): kind 1 -- a split job list (data: mamr_split_job[n]); kind 2 -- a
+ * consolidation job list (mamr_consolidate_job[n]); kind 3 -- the mesh a
+ * refinement left (mamr_block[n] in sorted_list order, with numbers[n]
+ * the blocks' numbers and cen[3n] their integer centres).  ts is the
+ * timestep of the refinement (0: the initial one). */
+typedef void (*mamr_amr_event)(void *user, int32_t kind, int32_t ts,
+                               const void *data, int32_t n,
+                               const int64_t *numbers, const int32_t *cen);
+
+typedef struct {
+   double stage_seconds;    /* wall time of the stage stretches */
+   double refine_seconds;   /* marking, bookkeeping, data movement, mesh */
+   double total_seconds;    /* the whole call */
+   int64_t updates;         /* cell-variable updates of the stages (the
+                               reference's total_blocks x cells x vars) */
+   int32_t refinements;     /* refine() calls, the initial one included */
+   int32_t max_active;      /* most active blocks at any time */
+   int32_t final_active;    /* active blocks at the end */
+   int32_t stretches;       /* mamr_run_timesteps calls */
+   int32_t plain_stretches; /* of those, on the plain path because the
+                               batched path refused the configuration */
+   int32_t reserved[3];
+} mamr_amr_stats;
+
+/* A whole miniAMR run on one rank (ref/driver.c:36-140): the initial
+ * lattice of init() (ref/init.c:453-560) with its values (the reference's
+ * rand() stream, seed 1) and checksums; the initial refinement; then each
+ * timestep's stages, move() of the objects and, every refine_freq
+ * timesteps, refine() (ref/refine.c:38-210) -- the marking on the device
+ * (mamr_mark_refine), the split and consolidation bookkeeping of
+ * ref/block.c:41-608 in this library (slots, parent records, numbers,
+ * centres and neighbour tables exactly as the reference keeps them), the
+ * cell data movement on the device.  Each stretch of timesteps between two
+ * refinements is one mamr_run_timesteps call with params->run_flags; where
+ * those ask for the batched path and it refuses the configuration
+ * (MAMR_EUNSUP before any stage runs: stencil 0, code 1/2, a permuted
+ * 27-point stencil, blocks no launch shape fits) the stretch and the rest
+ * of the run take the plain path (stats->plain_stretches).
+ * cfg must be the context's configuration.  sums receives the initial
+ * checksums (num_vars) and then each checksum stage's num_vars sums, as
+ * the reference's check_sum calls produce them, up to max_sums values;
+ * *n_sums the count.  event (may be NULL) is called with user for each
+ * split and consolidation list and each mesh.  The tolerance check of
+ * ref/driver.c:96-101 is left to the caller.  Needs lb_method 0 (the
+ * reference's default) and one rank. */
+int mamr_amr_run(mamr_ctx *ctx, const mamr_config *cfg,
+                 const mamr_amr_params *params,
+                 const mamr_amr_object *objects, int32_t n_objects,
+                 double *sums, int64_t max_sums, int64_t *n_sums,
+                 mamr_amr_event event, void *user, mamr_amr_stats *stats);
+
 /* ---- launch-shape autotuner of the batched path ------------------------ */
 
 /* No counterpart in the reference (the batched path is this library's own).

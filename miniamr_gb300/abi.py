@@ -69,6 +69,53 @@ class MarkParams(C.Structure):
                    (C.c_int32 * 3)(*mesh_size))
 
 
+class AmrParams(C.Structure):
+    """struct mamr_amr_params: the command-line parameters of a whole run
+    (mamr_amr_run)."""
+
+    _fields_ = [
+        ("init_x", C.c_int32), ("init_y", C.c_int32), ("init_z", C.c_int32),
+        ("num_refine", C.c_int32), ("block_change", C.c_int32),
+        ("refine_freq", C.c_int32), ("uniform_refine", C.c_int32),
+        ("refine_ghost", C.c_int32), ("num_tsteps", C.c_int32),
+        ("stages_per_ts", C.c_int32), ("checksum_freq", C.c_int32),
+        ("run_flags", C.c_int32), ("reserved", C.c_int32 * 8),
+    ]
+
+    @classmethod
+    def make(cls, init=(1, 1, 1), num_refine=5, block_change=0,
+             refine_freq=5, uniform_refine=0, refine_ghost=0, num_tsteps=20,
+             stages_per_ts=20, checksum_freq=5, run_flags=0) -> "AmrParams":
+        """Defaults are the reference's (ref/param.h)."""
+        return cls(init[0], init[1], init[2], num_refine, block_change,
+                   refine_freq, uniform_refine, refine_ghost, num_tsteps,
+                   stages_per_ts, checksum_freq, run_flags)
+
+
+# struct mamr_amr_object: one --object (type, bounce, cen, move, size, inc)
+AMR_OBJECT_DTYPE = np.dtype([
+    ("type", "<i4"), ("bounce", "<i4"), ("cen", "<f8", (3,)),
+    ("move", "<f8", (3,)), ("size", "<f8", (3,)), ("inc", "<f8", (3,)),
+])
+
+
+class AmrStats(C.Structure):
+    """struct mamr_amr_stats."""
+
+    _fields_ = [
+        ("stage_seconds", C.c_double), ("refine_seconds", C.c_double),
+        ("total_seconds", C.c_double), ("updates", C.c_int64),
+        ("refinements", C.c_int32), ("max_active", C.c_int32),
+        ("final_active", C.c_int32), ("stretches", C.c_int32),
+        ("plain_stretches", C.c_int32), ("reserved", C.c_int32 * 3),
+    ]
+
+
+AMR_EVENT = C.CFUNCTYPE(None, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p,
+                        C.c_int32, C.c_void_p, C.c_void_p)
+EVENT_SPLIT, EVENT_CONSOLIDATE, EVENT_MESH = 1, 2, 3
+
+
 class MamrError(RuntimeError):
     """A mamr_* call returned a negative status."""
 
@@ -131,6 +178,9 @@ class Library:
                                 C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
             "mamr_mark_refine": [vp, C.POINTER(MarkParams), vp, i32, vp,
                                  i32, vp, i32, vp, vp],
+            "mamr_amr_run": [vp, C.POINTER(Config), C.POINTER(AmrParams),
+                             vp, i32, vp, C.c_int64, C.POINTER(C.c_int64),
+                             AMR_EVENT, vp, C.POINTER(AmrStats)],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -289,6 +339,54 @@ class Context:
                    checksum_freq, first_stage, flags,
                    _ptr(sums) if want_sums else None, C.byref(cnt))
         return sums[:cnt.value]
+
+    def amr_run(self, params: "AmrParams", objects=None, max_sums=None,
+                events: bool = False):
+        """A whole run (mamr_amr_run) on this context: returns (checksums
+        [n][num_vars], the initial ones first; stats dict; the event list --
+        ("split", ts, jobs), ("consolidate", ts, jobs), ("mesh", ts, blocks,
+        numbers, centres) -- when `events`)."""
+        if objects is None:
+            objects = np.zeros(0, dtype=AMR_OBJECT_DTYPE)
+        objects = np.ascontiguousarray(objects, dtype=AMR_OBJECT_DTYPE)
+        V = self.cfg.num_vars
+        if max_sums is None:
+            spt, cf = params.stages_per_ts, params.checksum_freq
+            per_ts = sum(1 for st in range(spt) if cf and st % cf == 0)
+            max_sums = V * (1 + per_ts * max(1, params.num_tsteps))
+        sums = np.zeros(max(max_sums, 1), dtype=np.float64)
+        n = C.c_int64()
+        stats = AmrStats()
+        got = []
+
+        def on_event(user, kind, ts, data, cnt, numbers, cen):
+            if kind == EVENT_SPLIT:
+                a = np.ctypeslib.as_array(
+                    C.cast(data, C.POINTER(C.c_int32)), (cnt * 9,))
+                got.append(("split", ts, a.view(SPLIT_DTYPE).copy()))
+            elif kind == EVENT_CONSOLIDATE:
+                a = np.ctypeslib.as_array(
+                    C.cast(data, C.POINTER(C.c_int32)), (cnt * 9,))
+                got.append(("consolidate", ts,
+                            a.view(CONSOLIDATE_DTYPE).copy()))
+            elif kind == EVENT_MESH:
+                per = BLOCK_DTYPE.itemsize // 4
+                a = np.ctypeslib.as_array(
+                    C.cast(data, C.POINTER(C.c_int32)), (cnt * per,))
+                num = np.ctypeslib.as_array(
+                    C.cast(numbers, C.POINTER(C.c_int64)), (cnt,)).copy()
+                c = np.ctypeslib.as_array(
+                    C.cast(cen, C.POINTER(C.c_int32)), (cnt * 3,))
+                got.append(("mesh", ts, a.view(BLOCK_DTYPE).copy(), num,
+                            c.reshape(cnt, 3).copy()))
+
+        cb = AMR_EVENT(on_event) if events else AMR_EVENT()
+        self._call("mamr_amr_run", C.byref(self.cfg), C.byref(params),
+                   _ptr(objects), len(objects), _ptr(sums), int(max_sums),
+                   C.byref(n), cb, None, C.byref(stats))
+        st = {f: getattr(stats, f) for f, _ in AmrStats._fields_
+              if f != "reserved"}
+        return sums[:n.value].reshape(-1, V), st, got
 
     def sync(self) -> None:
         self._call("mamr_sync")

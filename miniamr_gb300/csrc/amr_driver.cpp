@@ -1,0 +1,687 @@
+// The AMR driver: a whole miniAMR run on one rank through the mamr_* ABI
+// (mamr_amr_run, include/miniamr_gb300.h).
+//
+// The host side of refinement lives here, with its own data structures: the
+// per-slot block records, the parent records and the split and
+// consolidation bookkeeping of the reference (ref/block.c:41-608) --
+// slot allocation, parent records, block numbers, centres and the neighbour
+// tables, kept exactly as the reference keeps them, stale entries of a
+// reused slot included, because the next marking, the exchange and the
+// reference's own mesh hash read them.  The marking runs on the device
+// (mamr_mark_refine), the cell data movement too (mamr_split,
+// mamr_consolidate), and each stretch of timesteps between refinements is
+// one mamr_run_timesteps call.  Only public ABI calls are made, so the same
+// source runs over the GPU library and over the CPU oracle.
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "miniamr_gb300.h"
+
+extern "C" int mamr_driver_fail(int code, const char *msg);
+
+namespace {
+
+// Errors carry a message to mamr_last_error through a status the caller
+// turns into a return value.
+struct Fail {
+   int code;
+   std::string msg;
+};
+
+struct Blk {
+   long long number = -1;
+   int level = 0, refine = 0, parent = -1, child_number = 0;
+   int nei_level[6] = {0, 0, 0, 0, 0, 0};
+   int nei[6][2][2] = {};
+   int cen[3] = {0, 0, 0};
+};
+
+struct Par {
+   long long number = -1;
+   int level = 0, parent = -1, child_number = 0, refine = 0;
+   int child[8] = {};
+   int cen[3] = {0, 0, 0};
+};
+
+// Octant (i1 + 2*j1 + 4*k1) of the child that touches face c (W,E,S,N,D,U)
+// at tangential position (a, b) of nei[c][a][b]: for x faces a runs along z
+// and b along y; for y faces a along z, b along x; for z faces a along y,
+// b along x (the quarter offsets of ref/comm.c:1613-1614,1645-1646,1674).
+int face_child(int c, int a, int b)
+{
+   const int hi = c % 2;
+   int i1, j1, k1;
+   switch (c / 2) {
+   case 0: i1 = hi; j1 = b; k1 = a; break;
+   case 1: j1 = hi; i1 = b; k1 = a; break;
+   default: k1 = hi; i1 = b; j1 = a; break;
+   }
+   return i1 + 2 * j1 + 4 * k1;
+}
+
+class Mesh {
+ public:
+   Mesh(int ix, int iy, int iz, int num_refine, int max_blocks)
+      : ix_(ix), iy_(iy), iz_(iz), nr_(num_refine), cap_(max_blocks),
+        b_(max_blocks), p_(max_blocks), start_(num_refine + 2, 0),
+        count_(num_refine + 1, 0)
+   {
+      long long n = (long long) ix * iy * iz;
+      for (int l = 1; l <= num_refine + 1; l++) {
+         start_[l] = start_[l - 1] + n;
+         n *= 8;
+      }
+   }
+
+   // The initial lattice of init() on one rank (ref/init.c:453-560): slot
+   // == block number, x fastest, level 0, lattice neighbours, -2 on the
+   // domain boundary; centres i*size + size/2 with size = 2^(num_refine+1).
+   void init()
+   {
+      const int n0 = ix_ * iy_ * iz_;
+      if (n0 > cap_)
+         throw Fail{MAMR_EINVAL, "max_blocks is smaller than the initial "
+                                 "lattice"};
+      const int size = 1 << (nr_ + 1);
+      for (int k = 0, n = 0; k < iz_; k++)
+         for (int j = 0; j < iy_; j++)
+            for (int i = 0; i < ix_; i++, n++) {
+               Blk &bp = b_[n];
+               bp.number = n;
+               bp.level = 0;
+               bp.parent = -1;
+               bp.child_number = 0;
+               bp.refine = 0;
+               bp.cen[0] = i * size + size / 2;
+               bp.cen[1] = j * size + size / 2;
+               bp.cen[2] = k * size + size / 2;
+               const int pos[3] = {i, j, k}, dim[3] = {ix_, iy_, iz_};
+               const int step[3] = {1, ix_, ix_ * iy_};
+               for (int c = 0; c < 6; c++) {
+                  const int ax = c / 2, hi = c % 2;
+                  const bool edge = hi ? pos[ax] == dim[ax] - 1 : pos[ax] == 0;
+                  bp.nei_level[c] = edge ? -2 : 0;
+                  bp.nei[c][0][0] = edge ? 0 : n + (hi ? step[ax] : -step[ax]);
+               }
+            }
+      max_block_ = n0;
+      active_ = n0;
+      count_[0] = n0;
+   }
+
+   int cur_max_level() const
+   {
+      for (int l = nr_; l >= 0; l--)
+         if (count_[l])
+            return l;
+      return 0;
+   }
+   int active() const { return active_; }
+
+   // Active slots in sorted_list order: level ascending, block number
+   // descending (ref/block.c:610-625).
+   std::vector<int> sorted() const
+   {
+      std::vector<int> s;
+      s.reserve(active_);
+      for (int n = 0; n < max_block_; n++)
+         if (b_[n].number >= 0)
+            s.push_back(n);
+      std::sort(s.begin(), s.end(), [&](int x, int y) {
+         if (b_[x].level != b_[y].level)
+            return b_[x].level < b_[y].level;
+         return b_[x].number > b_[y].number;
+      });
+      return s;
+   }
+
+   void export_mesh(std::vector<mamr_block> &mesh,
+                    std::vector<int64_t> &numbers, std::vector<int32_t> &cen)
+      const
+   {
+      const std::vector<int> s = sorted();
+      mesh.resize(s.size());
+      numbers.resize(s.size());
+      cen.resize(3 * s.size());
+      for (size_t q = 0; q < s.size(); q++) {
+         const Blk &bp = b_[s[q]];
+         mamr_block &m = mesh[q];
+         m.slot = s[q];
+         m.level = bp.level;
+         for (int c = 0; c < 6; c++) {
+            m.nei_level[c] = bp.nei_level[c];
+            for (int a = 0; a < 2; a++)
+               for (int d = 0; d < 2; d++)
+                  m.nei[c][a][d] = bp.nei[c][a][d];
+         }
+         numbers[q] = bp.number;
+         for (int d = 0; d < 3; d++)
+            cen[3 * q + d] = bp.cen[d];
+      }
+   }
+
+   // The marking's inputs (ref/block.h: blocks in sorted order, parents
+   // [0, max_active_parent)) and, afterwards, its flags back.
+   void mark_lists(std::vector<mamr_mark_block> &mb,
+                   std::vector<mamr_mark_parent> &pa) const
+   {
+      const std::vector<int> s = sorted();
+      mb.resize(s.size());
+      for (size_t q = 0; q < s.size(); q++) {
+         const Blk &bp = b_[s[q]];
+         mamr_mark_block &m = mb[q];
+         m.slot = s[q];
+         m.level = bp.level;
+         m.parent = bp.parent;
+         for (int d = 0; d < 3; d++)
+            m.cen[d] = bp.cen[d];
+         for (int c = 0; c < 6; c++) {
+            m.nei_level[c] = bp.nei_level[c];
+            m.nei[c] = bp.nei[c][0][0];
+         }
+      }
+      pa.resize(max_parent_);
+      for (int p = 0; p < max_parent_; p++) {
+         pa[p].active = p_[p].number >= 0;
+         for (int o = 0; o < 8; o++)
+            pa[p].child[o] = p_[p].child[o];
+      }
+   }
+   void set_flags(const std::vector<mamr_mark_block> &mb,
+                  const std::vector<int32_t> &bref,
+                  const std::vector<int32_t> &pref)
+   {
+      for (size_t q = 0; q < mb.size(); q++)
+         b_[mb[q].slot].refine = bref[q];
+      for (int p = 0; p < max_parent_; p++)
+         if (p_[p].number >= 0)
+            p_[p].refine = pref[p];
+   }
+
+   // split_blocks() (ref/block.c:41-343) on one rank: levels ascending,
+   // blocks in slot order; each refined block gets a parent record (the
+   // first unused one) and eight children, each in the first free slot at
+   // or after a running index that also falls back to a freed parent's
+   // slot; numbers, centres and neighbour tables as the reference's.
+   void split(std::vector<mamr_split_job> &jobs)
+   {
+      jobs.clear();
+      const int top = cur_max_level();
+      int m = 0;
+      for (int level = 0; level <= top; level++) {
+         for (int n = 0; n < max_block_; n++) {
+            Blk &bp = b_[n];
+            if (bp.number < 0 || bp.level != level || bp.refine != 1)
+               continue;
+            const long long nl = bp.number - start_[level];
+            const long long lx = (long long) ix_ << level,
+                            ly = (long long) iy_ << level;
+            const long long zp = nl / (lx * ly), yp = (nl % (lx * ly)) / lx,
+                            xp = nl % lx;
+            if (active_ + 8 > cap_)
+               throw Fail{MAMR_ENOMEM, "split: more blocks needed than "
+                                       "max_blocks"};
+            active_ += 7;
+            count_[level]--;
+            count_[level + 1] += 8;
+            int p = 0;
+            while (p < max_parent_ && p_[p].number >= 0)
+               p++;
+            if (p == cap_)
+               throw Fail{MAMR_ENOMEM, "split: more parent records needed"};
+            if (p == max_parent_)
+               max_parent_++;
+            Par &pp = p_[p];
+            pp.number = bp.number;
+            pp.level = bp.level;
+            pp.parent = bp.parent;
+            pp.child_number = bp.child_number;
+            if (pp.parent >= 0)
+               p_[pp.parent].child[pp.child_number] = -1 - p;
+            pp.refine = 0;
+            for (int d = 0; d < 3; d++)
+               pp.cen[d] = bp.cen[d];
+            mamr_split_job job;
+            job.parent = n;
+            int sib[8];
+            const int half = 1 << (nr_ - level - 1);
+            const long long cx = (long long) ix_ << (level + 1),
+                            cy = (long long) iy_ << (level + 1);
+            for (int o = 0; o < 8; o++) {
+               while (m < cap_ && b_[m].number >= 0)
+                  m++;
+               if (m == cap_)
+                  throw Fail{MAMR_ENOMEM, "split: no inactive block slot"};
+               max_block_ = std::max(max_block_, m + 1);
+               Blk &c = b_[m];
+               sib[o] = m;
+               pp.child[o] = m;
+               job.child[o] = m;
+               c.refine = 0;
+               c.level = level + 1;
+               c.parent = p;
+               c.child_number = o;
+               const int i1 = o % 2, j1 = (o / 2) % 2, k1 = o / 4;
+               c.number = ((2 * zp + k1) * cy + (2 * yp + j1)) * cx +
+                          2 * xp + i1 + start_[level + 1];
+               c.cen[0] = bp.cen[0] + (2 * i1 - 1) * half;
+               c.cen[1] = bp.cen[1] + (2 * j1 - 1) * half;
+               c.cen[2] = bp.cen[2] + (2 * k1 - 1) * half;
+            }
+            jobs.push_back(job);
+            for (int c = 0; c < 6; c++) {
+               const int opp = c ^ 1, bit = 1 << (c / 2);
+               // siblings facing each other across the parent's mid-plane
+               for (int a = 0; a < 2; a++)
+                  for (int d = 0; d < 2; d++) {
+                     const int s = face_child(c, a, d);
+                     b_[sib[s ^ bit]].nei_level[c] = level + 1;
+                     b_[sib[s ^ bit]].nei[c][0][0] = sib[s];
+                  }
+               // the children on face c take over the parent's neighbour
+               const int nlv = bp.nei_level[c];
+               if (nlv == -2) {
+                  for (int a = 0; a < 2; a++)
+                     for (int d = 0; d < 2; d++) {
+                        Blk &ch = b_[sib[face_child(c, a, d)]];
+                        ch.nei_level[c] = -2;
+                        ch.nei[c][0][0] = 0;
+                     }
+               } else if (nlv == level) {
+                  const int other = bp.nei[c][0][0];
+                  b_[other].nei_level[opp] = level + 1;
+                  for (int a = 0; a < 2; a++)
+                     for (int d = 0; d < 2; d++) {
+                        const int ch = sib[face_child(c, a, d)];
+                        b_[ch].nei_level[c] = level;
+                        b_[ch].nei[c][0][0] = other;
+                        b_[other].nei[opp][a][d] = ch;
+                     }
+               } else if (nlv == level + 1) {
+                  for (int a = 0; a < 2; a++)
+                     for (int d = 0; d < 2; d++) {
+                        const int other = bp.nei[c][a][d];
+                        const int ch = sib[face_child(c, a, d)];
+                        b_[ch].nei_level[c] = level + 1;
+                        b_[ch].nei[c][0][0] = other;
+                        b_[other].nei_level[opp] = level + 1;
+                        b_[other].nei[opp][0][0] = ch;
+                     }
+               } else {
+                  // a coarser neighbour would have to split first: the
+                  // marking's rules exclude it on one rank
+                  throw Fail{MAMR_EMESH, "split: misconnected block"};
+               }
+            }
+            // the parent's slot is free again and may take a later child
+            bp.number = -1;
+            if (n < m)
+               m = n;
+         }
+      }
+   }
+
+   // consolidate_blocks() (ref/block.c:349-608) on one rank: levels
+   // descending, parent records in order; each parent marked -1 becomes a
+   // block again in the first free slot from 0, its eight children freed,
+   // the neighbour tables rewired as the reference's.
+   void consolidate(std::vector<mamr_consolidate_job> &jobs)
+   {
+      jobs.clear();
+      for (int level = cur_max_level(); level >= 0; level--)
+         for (int p = 0; p < max_parent_; p++) {
+            Par &pp = p_[p];
+            if (pp.number < 0 || pp.level != level || pp.refine != -1)
+               continue;
+            int n = 0;
+            while (n < cap_ && b_[n].number >= 0)
+               n++;
+            if (n == cap_)
+               throw Fail{MAMR_ENOMEM, "consolidate: no free block slot"};
+            max_block_ = std::max(max_block_, n + 1);
+            active_ -= 7;
+            count_[level]++;
+            count_[level + 1] -= 8;
+            Blk &bp = b_[n];
+            bp.number = pp.number;
+            pp.number = -1;
+            bp.level = pp.level;
+            bp.parent = pp.parent;
+            bp.child_number = pp.child_number;
+            if (bp.level)
+               p_[bp.parent].child[bp.child_number] = n;
+            bp.refine = 0;
+            for (int d = 0; d < 3; d++)
+               bp.cen[d] = pp.cen[d];
+            mamr_consolidate_job job;
+            job.target = n;
+            for (int o = 0; o < 8; o++) {
+               b_[pp.child[o]].number = -1;
+               job.child[o] = pp.child[o];
+            }
+            jobs.push_back(job);
+            for (int c = 0; c < 6; c++) {
+               const int opp = c ^ 1;
+               const Blk &first = b_[pp.child[face_child(c, 0, 0)]];
+               if (first.nei_level[c] == -2) {
+                  bp.nei_level[c] = -2;
+               } else if (first.nei_level[c] == level) {
+                  const int nb = first.nei[c][0][0];
+                  bp.nei[c][0][0] = nb;
+                  bp.nei_level[c] = level;
+                  b_[nb].nei[opp][0][0] = n;
+                  b_[nb].nei_level[opp] = level;
+               } else {
+                  for (int a = 0; a < 2; a++)
+                     for (int d = 0; d < 2; d++) {
+                        const Blk &ch = b_[pp.child[face_child(c, a, d)]];
+                        const int nb = ch.nei[c][0][0];
+                        if (ch.nei_level[c] == level + 2)
+                           throw Fail{MAMR_EMESH, "consolidate: neighbour "
+                                                  "two levels finer"};
+                        bp.nei[c][a][d] = nb;
+                        bp.nei_level[c] = level + 1;
+                        b_[nb].nei[opp][0][0] = n;
+                        b_[nb].nei_level[opp] = level;
+                     }
+               }
+            }
+         }
+   }
+
+ private:
+   int ix_, iy_, iz_, nr_, cap_;
+   std::vector<Blk> b_;
+   std::vector<Par> p_;
+   std::vector<long long> start_;
+   std::vector<long long> count_;
+   int max_block_ = 0, max_parent_ = 0, active_ = 0;
+};
+
+// move() (ref/move.c:37-63): position and size advance by delta; with
+// bounce 1 the centre reflects off the unit cube's faces and the motion
+// reverses.  The reference's bounce-2 branch hangs off the inner if-chain
+// of the bounce-1 branch (C's dangling else) and can never run, so any
+// other bounce value only moves the object.
+void move(std::vector<mamr_amr_object> &objs, double delta)
+{
+   for (mamr_amr_object &o : objs)
+      for (int d = 0; d < 3; d++) {
+         o.cen[d] += delta * o.move[d];
+         o.size[d] += delta * o.inc[d];
+         if (o.bounce != 1)
+            continue;
+         if (o.cen[d] >= 1.0) {
+            o.cen[d] = 2.0 - o.cen[d];
+            o.move[d] = -o.move[d];
+         } else if (o.cen[d] <= 0.0) {
+            o.cen[d] = 0.0 - o.cen[d];
+            o.move[d] = -o.move[d];
+         }
+      }
+}
+
+void check(int r, const char *what)
+{
+   if (r != MAMR_OK)
+      throw Fail{r, std::string(what) + ": " + mamr_last_error()};
+}
+
+double now()
+{
+   return std::chrono::duration<double>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+struct Run {
+   mamr_ctx *ctx;
+   const mamr_config &cfg;
+   const mamr_amr_params &prm;
+   std::vector<mamr_amr_object> objs;
+   double *sums;
+   int64_t max_sums, n_sums = 0;
+   mamr_amr_event event;
+   void *user;
+   mamr_amr_stats st{};
+   Mesh mesh;
+   int flags;   // the stretches' run flags (batched until it is refused)
+
+   Run(mamr_ctx *c, const mamr_config &cf, const mamr_amr_params &p)
+      : ctx(c), cfg(cf), prm(p), mesh(p.init_x, p.init_y, p.init_z,
+                                      p.num_refine, cf.max_blocks),
+        flags(p.run_flags)
+   {
+   }
+
+   void put_sums(const double *s, int64_t n)
+   {
+      for (int64_t q = 0; q < n && n_sums < max_sums; q++)
+         sums[n_sums++] = s[q];
+   }
+
+   void set_mesh(int ts, bool report)
+   {
+      std::vector<mamr_block> m;
+      std::vector<int64_t> numbers;
+      std::vector<int32_t> cen;
+      mesh.export_mesh(m, numbers, cen);
+      check(mamr_set_mesh(ctx, m.data(), (int32_t) m.size()),
+            "mamr_set_mesh");
+      if (event && report)
+         event(user, 3, ts, m.data(), (int32_t) m.size(), numbers.data(),
+               cen.data());
+      st.max_active = std::max(st.max_active, (int32_t) m.size());
+   }
+
+   // refine(ts) (ref/refine.c:38-210) on one rank: num_refine steps at
+   // ts 0, block_change steps after, each the marking, the splits and the
+   // consolidations.
+   void refine(int ts)
+   {
+      const double t0 = now();
+      const int steps = ts ? (prm.block_change ? prm.block_change
+                                               : prm.num_refine)
+                           : prm.num_refine;
+      std::vector<mamr_mark_block> mb;
+      std::vector<mamr_mark_parent> pa;
+      std::vector<int32_t> bref, pref;
+      std::vector<mamr_object> mo(objs.size());
+      std::vector<mamr_split_job> sj;
+      std::vector<mamr_consolidate_job> cj;
+      mamr_mark_params mp;
+      memset(&mp, 0, sizeof(mp));
+      mp.num_refine = prm.num_refine;
+      mp.refine_ghost = prm.refine_ghost;
+      mp.uniform_refine = prm.uniform_refine;
+      const int size = 1 << (prm.num_refine + 1);
+      mp.mesh_size[0] = prm.init_x * size;
+      mp.mesh_size[1] = prm.init_y * size;
+      mp.mesh_size[2] = prm.init_z * size;
+      for (int i = 0; i < steps; i++) {
+         for (size_t o = 0; o < objs.size(); o++) {
+            mo[o].type = objs[o].type;
+            mo[o].reserved = 0;
+            for (int d = 0; d < 3; d++) {
+               mo[o].cen[d] = objs[o].cen[d];
+               mo[o].size[d] = objs[o].size[d];
+            }
+         }
+         mesh.mark_lists(mb, pa);
+         bref.assign(mb.size() + 1, 0);
+         pref.assign(pa.size() + 1, 0);
+         check(mamr_mark_refine(ctx, &mp,
+                                prm.uniform_refine ? nullptr : mo.data(),
+                                prm.uniform_refine ? 0
+                                                   : (int32_t) mo.size(),
+                                mb.data(), (int32_t) mb.size(), pa.data(),
+                                (int32_t) pa.size(), bref.data(),
+                                pref.data()),
+               "mamr_mark_refine");
+         mesh.set_flags(mb, bref, pref);
+         mesh.split(sj);
+         if (!sj.empty()) {
+            check(mamr_split(ctx, sj.data(), (int32_t) sj.size()),
+                  "mamr_split");
+            if (event)
+               event(user, 1, ts, sj.data(), (int32_t) sj.size(), nullptr,
+                     nullptr);
+         }
+         mesh.consolidate(cj);
+         if (!cj.empty()) {
+            check(mamr_consolidate(ctx, cj.data(), (int32_t) cj.size()),
+                  "mamr_consolidate");
+            if (event)
+               event(user, 2, ts, cj.data(), (int32_t) cj.size(), nullptr,
+                     nullptr);
+         }
+      }
+      set_mesh(ts, true);
+      check(mamr_sync(ctx), "mamr_sync");
+      st.refinements++;
+      st.refine_seconds += now() - t0;
+   }
+
+   void stages(int n_ts, int first_stage)
+   {
+      if (n_ts <= 0)
+         return;
+      const int V = cfg.num_vars, spt = prm.stages_per_ts;
+      int per_ts = 0;
+      if (prm.checksum_freq)
+         for (int s = 0; s < spt; s++)
+            per_ts += !(s % prm.checksum_freq);
+      std::vector<double> s((size_t) std::max(1, per_ts * n_ts) * V);
+      int32_t got = 0;
+      const double t0 = now();
+      int r = mamr_run_timesteps(ctx, n_ts, spt, prm.checksum_freq,
+                                 first_stage, flags, s.data(), &got);
+      if (r == MAMR_EUNSUP && (flags & MAMR_RUN_BATCHED)) {
+         // refused before any stage ran: the plain path from here on
+         flags = MAMR_RUN_PLAIN;
+         r = mamr_run_timesteps(ctx, n_ts, spt, prm.checksum_freq,
+                                first_stage, flags, s.data(), &got);
+      }
+      check(r, "mamr_run_timesteps");
+      st.stretches++;
+      st.plain_stretches += (prm.run_flags & MAMR_RUN_BATCHED) &&
+                            !(flags & MAMR_RUN_BATCHED);
+      check(mamr_sync(ctx), "mamr_sync");
+      st.stage_seconds += now() - t0;
+      put_sums(s.data(), (int64_t) got * V);
+      st.updates += (int64_t) n_ts * spt * mesh.active() *
+                    ((int64_t) cfg.nx * cfg.ny * cfg.nz) * V;
+   }
+
+   void run()
+   {
+      const double t0 = now();
+      const int V = cfg.num_vars;
+      if (cfg.stencil == 0) {
+         double a1 = 0.0;
+         std::vector<double> a0((size_t) std::max(1, V / 4));
+         check(mamr_work_coefficients(V, &a1, a0.data()),
+               "mamr_work_coefficients");
+         check(mamr_set_work_params(ctx, a1, a0.data(), V / 4),
+               "mamr_set_work_params");
+      }
+      // init(): the lattice, its values (one rand() stream over all the
+      // initial blocks, so generated at once) and their checksums
+      mesh.init();
+      const int n0 = prm.init_x * prm.init_y * prm.init_z;
+      {
+         const size_t per = (size_t) V * (cfg.nx + 2) * (cfg.ny + 2) *
+                            (cfg.nz + 2);
+         std::vector<double> all((size_t) n0 * per);
+         check(mamr_initial_values(&cfg, n0, all.data()),
+               "mamr_initial_values");
+         std::vector<int32_t> slots(n0);
+         for (int q = 0; q < n0; q++)
+            slots[q] = q;
+         check(mamr_upload_blocks(ctx, slots.data(), n0, all.data()),
+               "mamr_upload_blocks");
+      }
+      set_mesh(0, false);
+      for (int var = 0; var < V; var++) {
+         double s = 0.0;
+         check(mamr_check_sum(ctx, var, &s), "mamr_check_sum");
+         put_sums(&s, 1);
+      }
+      if (prm.num_refine || prm.uniform_refine)
+         refine(0);
+      // ref/driver.c:66-140: stages, move, refine every refine_freq; the
+      // loop tests for the end after the first timestep, so it runs at
+      // least one
+      const bool moving = prm.num_refine && !prm.uniform_refine;
+      const int n_ts = std::max(1, prm.num_tsteps);
+      int pending = 0, first_ts = 1;
+      for (int ts = 1; ts <= n_ts; ts++) {
+         pending++;
+         const bool refine_now = moving && !(ts % prm.refine_freq);
+         if (refine_now || ts == n_ts) {
+            stages(pending, (first_ts - 1) * prm.stages_per_ts);
+            first_ts = ts + 1;
+            pending = 0;
+         }
+         if (moving) {
+            move(objs, 1.0);
+            if (refine_now)
+               refine(ts);
+         }
+      }
+      check(mamr_sync(ctx), "mamr_sync");
+      st.final_active = mesh.active();
+      st.total_seconds = now() - t0;
+   }
+};
+
+}  // namespace
+
+extern "C" int mamr_amr_run(mamr_ctx *ctx, const mamr_config *cfg,
+                            const mamr_amr_params *p,
+                            const mamr_amr_object *objects, int32_t n_objects,
+                            double *sums, int64_t max_sums, int64_t *n_sums,
+                            mamr_amr_event event, void *user,
+                            mamr_amr_stats *stats)
+{
+   if (!ctx || !cfg || !p || (n_objects && !objects) || n_objects < 0 ||
+       (max_sums && !sums) || max_sums < 0)
+      return mamr_driver_fail(MAMR_EINVAL, "mamr_amr_run: bad arguments");
+   if (p->init_x < 1 || p->init_y < 1 || p->init_z < 1 ||
+       p->num_refine < 0 || p->num_refine > 20 || p->block_change < 0 ||
+       p->refine_freq < 1 || p->num_tsteps < 0 || p->stages_per_ts < 1 ||
+       p->checksum_freq < 0)
+      return mamr_driver_fail(MAMR_EINVAL, "mamr_amr_run: bad parameters");
+   for (int r = 0; r < 8; r++)
+      if (p->reserved[r])
+         return mamr_driver_fail(MAMR_EINVAL, "mamr_amr_run: reserved "
+                                              "parameters must be zero");
+   Run run(ctx, *cfg, *p);
+   run.objs.assign(objects, objects + n_objects);
+   run.sums = sums;
+   run.max_sums = max_sums;
+   run.event = event;
+   run.user = user;
+   int status = MAMR_OK;
+   try {
+      run.run();
+   } catch (const Fail &f) {
+      status = f.code;
+      char buf[400];
+      snprintf(buf, sizeof(buf), "mamr_amr_run: %s", f.msg.c_str());
+      mamr_driver_fail(status, buf);
+   } catch (const std::bad_alloc &) {
+      status = MAMR_ENOMEM;
+      mamr_driver_fail(status, "mamr_amr_run: host allocation");
+   }
+   if (n_sums)
+      *n_sums = run.n_sums;
+   if (stats)
+      *stats = run.st;
+   return status;
+}

@@ -37,6 +37,12 @@ static int fail(int code, const char *fmt, ...)
 
 extern "C" const char *mamr_last_error(void) { return g_err; }
 
+// How the AMR driver (amr_driver.cpp) records its own failures.
+extern "C" int mamr_driver_fail(int code, const char *msg)
+{
+   return fail(code, "%s", msg);
+}
+
 int mamr::report_error(int code, const char *fmt, ...)
 {
    va_list ap;

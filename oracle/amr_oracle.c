@@ -57,6 +57,13 @@ static int fail(int code, const char *fmt, ...)
 
 const char *mamr_last_error(void) { return err_buf; }
 
+/* How the AMR driver (miniamr_gb300/csrc/amr_driver.cpp, linked into this
+ * library too) records its own failures. */
+int mamr_driver_fail(int code, const char *msg)
+{
+   return fail(code, "%s", msg);
+}
+
 /* Round to the pool's precision. */
 static inline double RF(const mamr_ctx *c, double x)
 {
@@ -1245,4 +1252,38 @@ int mamr_mark_refine(mamr_ctx *c, const mamr_mark_params *p,
          parent_refine[i] = pref[i];
    free(listed); free(ref); free(pref);
    return MAMR_OK;
+}
+
+/* Test helper, no counterpart in the ABI: the FNV-1a hash oracle/ref_hooks.c
+ * takes of the reference's mesh after each refine() -- per block in
+ * sorted_list order its number (8 bytes) and then slot, level,
+ * nei_level[6], nei[6][2][2] and cen[3] as 35 int32 values. */
+uint64_t mamr_oracle_mesh_hash(const mamr_block *b, const int64_t *numbers,
+                               const int32_t *cen, int32_t n)
+{
+   uint64_t h = 1469598103934665603ULL;
+   int32_t q, l, a, d;
+   for (q = 0; q < n; q++) {
+      int32_t rec[35];
+      const unsigned char *c;
+      size_t i;
+      rec[0] = b[q].slot;
+      rec[1] = b[q].level;
+      for (l = 0; l < 6; l++) {
+         rec[2 + l] = b[q].nei_level[l];
+         for (a = 0; a < 2; a++)
+            for (d = 0; d < 2; d++)
+               rec[8 + l*4 + a*2 + d] = b[q].nei[l][a][d];
+      }
+      rec[32] = cen[3*q];
+      rec[33] = cen[3*q + 1];
+      rec[34] = cen[3*q + 2];
+      c = (const unsigned char *) &numbers[q];
+      for (i = 0; i < sizeof(int64_t); i++)
+         h = (h ^ c[i]) * 1099511628211ULL;
+      c = (const unsigned char *) rec;
+      for (i = 0; i < sizeof(rec); i++)
+         h = (h ^ c[i]) * 1099511628211ULL;
+   }
+   return h;
 }

@@ -3,13 +3,14 @@ the CPU oracle, through the C ABI."""
 import numpy as np
 import pytest
 
-from golden_util import cases, hashed_stages, reflog, trace_path
+from golden_util import (cases, hashed_stages, reflog, trace_path,
+                         traced_cases)
 from miniamr_gb300 import mesh as meshmod
 from miniamr_gb300.abi import FP32, FP64, MamrError, Config
 from miniamr_gb300.trace import read_trace, replay
 
 pytestmark = pytest.mark.gpu
-CASES = sorted(cases())
+CASES = traced_cases()
 # the variable-work stencils (--stencil 0) run on FP64 pools only
 FP32_CASES = [c for c in CASES if "--stencil" not in cases()[c]["args"] or
               cases()[c]["args"][cases()[c]["args"].index("--stencil") + 1]

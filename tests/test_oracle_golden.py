@@ -9,12 +9,13 @@ initial values used by the benchmark to the reference's init()/refine().
 import numpy as np
 import pytest
 
-from golden_util import HEAVY, arg, cases, hashed_stages, reflog, trace_path
+from golden_util import (HEAVY, arg, cases, hashed_stages, reflog,
+                         trace_path, traced_cases)
 from miniamr_gb300 import mesh as meshmod
 from miniamr_gb300.abi import FP64, Config
 from miniamr_gb300.trace import read_trace, replay
 
-CASES = sorted(c for c in cases() if c not in HEAVY)
+CASES = [c for c in traced_cases() if c not in HEAVY]
 
 
 @pytest.mark.parametrize("name", CASES)
