@@ -319,17 +319,26 @@ typedef void (*mamr_amr_event)(void *user, int32_t kind, int32_t ts,
 
 typedef struct {
    double stage_seconds;    /* wall time of the stage stretches */
-   double refine_seconds;   /* marking, bookkeeping, data movement, mesh */
+   double refine_seconds;   /* refine() calls: the four parts below */
    double total_seconds;    /* the whole call */
+   double mark_seconds;     /* mamr_mark_refine calls (lists in, flags out) */
+   double bookkeeping_seconds; /* host: marking lists, split and
+                               consolidation records, job lists */
+   double data_seconds;     /* mamr_split / mamr_consolidate calls (the
+                               device work they queue overlaps the next
+                               step's host work and completes before the
+                               next marking returns) */
+   double mesh_seconds;     /* mesh export and mamr_set_mesh, completed */
    int64_t updates;         /* cell-variable updates of the stages (the
                                reference's total_blocks x cells x vars) */
    int32_t refinements;     /* refine() calls, the initial one included */
+   int32_t marking_steps;   /* refinement steps (block_change per call) */
    int32_t max_active;      /* most active blocks at any time */
    int32_t final_active;    /* active blocks at the end */
    int32_t stretches;       /* mamr_run_timesteps calls */
    int32_t plain_stretches; /* of those, on the plain path because the
                                batched path refused the configuration */
-   int32_t reserved[3];
+   int32_t reserved[2];
 } mamr_amr_stats;
 
 /* A whole miniAMR run on one rank (ref/driver.c:36-140): the initial

@@ -69,7 +69,7 @@ class Mesh {
    Mesh(int ix, int iy, int iz, int num_refine, int max_blocks)
       : ix_(ix), iy_(iy), iz_(iz), nr_(num_refine), cap_(max_blocks),
         b_(max_blocks), p_(max_blocks), start_(num_refine + 2, 0),
-        count_(num_refine + 1, 0)
+        count_(num_refine + 1, 0), used_(((size_t) max_blocks + 63) / 64, 0)
    {
       long long n = (long long) ix * iy * iz;
       for (int l = 1; l <= num_refine + 1; l++) {
@@ -93,6 +93,7 @@ class Mesh {
             for (int i = 0; i < ix_; i++, n++) {
                Blk &bp = b_[n];
                bp.number = n;
+               occupy(n);
                bp.level = 0;
                bp.parent = -1;
                bp.child_number = 0;
@@ -112,6 +113,7 @@ class Mesh {
       max_block_ = n0;
       active_ = n0;
       count_[0] = n0;
+      pfree_ = 0;
    }
 
    int cur_max_level() const
@@ -127,16 +129,22 @@ class Mesh {
    // descending (ref/block.c:610-625).
    std::vector<int> sorted() const
    {
-      std::vector<int> s;
-      s.reserve(active_);
+      // one key per block, level in the high bits and the complement of
+      // the number below it (numbers < 2^58: init blocks x 8^num_refine
+      // with num_refine <= 20 stays far below that for any lattice that
+      // fits a pool)
+      std::vector<std::pair<uint64_t, int>> k;
+      k.reserve(active_);
       for (int n = 0; n < max_block_; n++)
          if (b_[n].number >= 0)
-            s.push_back(n);
-      std::sort(s.begin(), s.end(), [&](int x, int y) {
-         if (b_[x].level != b_[y].level)
-            return b_[x].level < b_[y].level;
-         return b_[x].number > b_[y].number;
-      });
+            k.emplace_back(((uint64_t) b_[n].level << 58) |
+                              (((uint64_t) 1 << 58) - 1 -
+                               (uint64_t) b_[n].number),
+                           n);
+      std::sort(k.begin(), k.end());
+      std::vector<int> s(k.size());
+      for (size_t q = 0; q < k.size(); q++)
+         s[q] = k[q].second;
       return s;
    }
 
@@ -165,17 +173,20 @@ class Mesh {
       }
    }
 
-   // The marking's inputs (ref/block.h: blocks in sorted order, parents
-   // [0, max_active_parent)) and, afterwards, its flags back.
+   // The marking's inputs (ref/block.h: the active blocks -- in slot
+   // order, since the marking's result does not depend on the order --
+   // and parents [0, max_active_parent)) and, afterwards, its flags back.
    void mark_lists(std::vector<mamr_mark_block> &mb,
                    std::vector<mamr_mark_parent> &pa) const
    {
-      const std::vector<int> s = sorted();
-      mb.resize(s.size());
-      for (size_t q = 0; q < s.size(); q++) {
-         const Blk &bp = b_[s[q]];
-         mamr_mark_block &m = mb[q];
-         m.slot = s[q];
+      mb.resize(active_);
+      size_t q = 0;
+      for (int n = 0; n < max_block_; n++) {
+         const Blk &bp = b_[n];
+         if (bp.number < 0)
+            continue;
+         mamr_mark_block &m = mb[q++];
+         m.slot = n;
          m.level = bp.level;
          m.parent = bp.parent;
          for (int d = 0; d < 3; d++)
@@ -212,12 +223,17 @@ class Mesh {
    {
       jobs.clear();
       const int top = cur_max_level();
+      // the blocks marked to split, by level in slot order: splitting one
+      // level adds children with refine 0 in free slots and moves no other
+      // block, so the reference's slot scan of each level finds these
+      std::vector<std::vector<int>> marked(top + 1);
+      for (int n = 0; n < max_block_; n++)
+         if (b_[n].number >= 0 && b_[n].refine == 1 && b_[n].level <= top)
+            marked[b_[n].level].push_back(n);
       int m = 0;
       for (int level = 0; level <= top; level++) {
-         for (int n = 0; n < max_block_; n++) {
+         for (const int n : marked[level]) {
             Blk &bp = b_[n];
-            if (bp.number < 0 || bp.level != level || bp.refine != 1)
-               continue;
             const long long nl = bp.number - start_[level];
             const long long lx = (long long) ix_ << level,
                             ly = (long long) iy_ << level;
@@ -229,13 +245,16 @@ class Mesh {
             active_ += 7;
             count_[level]--;
             count_[level + 1] += 8;
-            int p = 0;
+            // the first unused parent record (every record below pfree_
+            // is in use)
+            int p = pfree_;
             while (p < max_parent_ && p_[p].number >= 0)
                p++;
             if (p == cap_)
                throw Fail{MAMR_ENOMEM, "split: more parent records needed"};
             if (p == max_parent_)
                max_parent_++;
+            pfree_ = p + 1;
             Par &pp = p_[p];
             pp.number = bp.number;
             pp.level = bp.level;
@@ -253,12 +272,12 @@ class Mesh {
             const long long cx = (long long) ix_ << (level + 1),
                             cy = (long long) iy_ << (level + 1);
             for (int o = 0; o < 8; o++) {
-               while (m < cap_ && b_[m].number >= 0)
-                  m++;
+               m = next_free(m);
                if (m == cap_)
                   throw Fail{MAMR_ENOMEM, "split: no inactive block slot"};
                max_block_ = std::max(max_block_, m + 1);
                Blk &c = b_[m];
+               occupy(m);
                sib[o] = m;
                pp.child[o] = m;
                job.child[o] = m;
@@ -320,6 +339,7 @@ class Mesh {
             }
             // the parent's slot is free again and may take a later child
             bp.number = -1;
+            release(n);
             if (n < m)
                m = n;
          }
@@ -338,9 +358,8 @@ class Mesh {
             Par &pp = p_[p];
             if (pp.number < 0 || pp.level != level || pp.refine != -1)
                continue;
-            int n = 0;
-            while (n < cap_ && b_[n].number >= 0)
-               n++;
+            // the first free slot
+            const int n = next_free(0);
             if (n == cap_)
                throw Fail{MAMR_ENOMEM, "consolidate: no free block slot"};
             max_block_ = std::max(max_block_, n + 1);
@@ -349,7 +368,9 @@ class Mesh {
             count_[level + 1] -= 8;
             Blk &bp = b_[n];
             bp.number = pp.number;
+            occupy(n);
             pp.number = -1;
+            pfree_ = std::min(pfree_, p);
             bp.level = pp.level;
             bp.parent = pp.parent;
             bp.child_number = pp.child_number;
@@ -362,6 +383,7 @@ class Mesh {
             job.target = n;
             for (int o = 0; o < 8; o++) {
                b_[pp.child[o]].number = -1;
+               release(pp.child[o]);
                job.child[o] = pp.child[o];
             }
             jobs.push_back(job);
@@ -401,6 +423,31 @@ class Mesh {
    std::vector<long long> start_;
    std::vector<long long> count_;
    int max_block_ = 0, max_parent_ = 0, active_ = 0;
+   // a lower bound of the first unused parent record: the search the
+   // reference starts from 0 starts here, with the same result
+   int pfree_ = 0;
+   // one bit per slot, set while the slot holds a block: the reference's
+   // scans for the next free slot (from a running index in split, from 0 in
+   // consolidate) skip 64 slots a word
+   std::vector<uint64_t> used_;
+
+   void occupy(int n) { used_[n >> 6] |= (uint64_t) 1 << (n & 63); }
+   void release(int n) { used_[n >> 6] &= ~((uint64_t) 1 << (n & 63)); }
+   // The first free slot at or after n, cap_ if none.
+   int next_free(int n) const
+   {
+      if (n >= cap_)
+         return cap_;
+      size_t w = (size_t) n >> 6;
+      uint64_t free_bits = ~used_[w] & (~(uint64_t) 0 << (n & 63));
+      while (!free_bits) {
+         if (++w == used_.size())
+            return cap_;
+         free_bits = ~used_[w];
+      }
+      const int f = (int) (w * 64) + __builtin_ctzll(free_bits);
+      return f < cap_ ? f : cap_;
+   }
 };
 
 // move() (ref/move.c:37-63): position and size advance by delta; with
@@ -437,6 +484,14 @@ double now()
    return std::chrono::duration<double>(
              std::chrono::steady_clock::now().time_since_epoch())
       .count();
+}
+
+// Seconds since t; t moves to now.
+double lap(double &t)
+{
+   const double n = now(), d = n - t;
+   t = n;
+   return d;
 }
 
 struct Run {
@@ -504,6 +559,7 @@ struct Run {
       mp.mesh_size[1] = prm.init_y * size;
       mp.mesh_size[2] = prm.init_z * size;
       for (int i = 0; i < steps; i++) {
+         double t = now();
          for (size_t o = 0; o < objs.size(); o++) {
             mo[o].type = objs[o].type;
             mo[o].reserved = 0;
@@ -515,6 +571,7 @@ struct Run {
          mesh.mark_lists(mb, pa);
          bref.assign(mb.size() + 1, 0);
          pref.assign(pa.size() + 1, 0);
+         st.bookkeeping_seconds += lap(t);
          check(mamr_mark_refine(ctx, &mp,
                                 prm.uniform_refine ? nullptr : mo.data(),
                                 prm.uniform_refine ? 0
@@ -523,26 +580,41 @@ struct Run {
                                 (int32_t) pa.size(), bref.data(),
                                 pref.data()),
                "mamr_mark_refine");
+         st.mark_seconds += lap(t);
+         st.marking_steps++;
          mesh.set_flags(mb, bref, pref);
          mesh.split(sj);
+         st.bookkeeping_seconds += lap(t);
          if (!sj.empty()) {
             check(mamr_split(ctx, sj.data(), (int32_t) sj.size()),
                   "mamr_split");
+            st.data_seconds += lap(t);
             if (event)
                event(user, 1, ts, sj.data(), (int32_t) sj.size(), nullptr,
                      nullptr);
          }
+         t = now();
          mesh.consolidate(cj);
+         st.bookkeeping_seconds += lap(t);
          if (!cj.empty()) {
             check(mamr_consolidate(ctx, cj.data(), (int32_t) cj.size()),
                   "mamr_consolidate");
+            st.data_seconds += lap(t);
             if (event)
                event(user, 2, ts, cj.data(), (int32_t) cj.size(), nullptr,
                      nullptr);
          }
+         // a step that changed nothing leaves the marking's inputs as they
+         // were (it starts from reset flags, and the objects move only
+         // between refinements), so the remaining steps change nothing
+         // either
+         if (sj.empty() && cj.empty())
+            break;
       }
+      double t = now();
       set_mesh(ts, true);
       check(mamr_sync(ctx), "mamr_sync");
+      st.mesh_seconds += lap(t);
       st.refinements++;
       st.refine_seconds += now() - t0;
    }
