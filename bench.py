@@ -410,25 +410,60 @@ def stress_multilevel(lib, dtype):
                 for name, (t, n) in refine.items()}}
 
 
-def stress_driver(lib, dtype):
+def _reflog_sums(name):
+    """Every checksum of a committed reference log, in call order."""
+    import lzma
+    import struct
+    path = os.path.join(REPO, "tests", "golden", name + ".reflog.xz")
+    if not os.path.exists(path):
+        return None
+    ref = []
+    with lzma.open(path, "rt") as f:
+        for ln in f:
+            p = ln.split()
+            if p[0] == "cs":
+                ref.append(struct.unpack(
+                    "<d", int(p[3], 16).to_bytes(8, "little"))[0])
+    return np.array(ref)
+
+
+def _reflog_meshes(name):
+    import lzma
+    path = os.path.join(REPO, "tests", "golden", name + ".reflog.xz")
+    if not os.path.exists(path):
+        return None
+    with lzma.open(path, "rt") as f:
+        return [(int(p[1]), int(p[2]), p[3]) for p in
+                (ln.split() for ln in f) if p[0] == "mesh"]
+
+
+def stress_driver(lib, dtype, case="config5_300", fp64_sums=None):
     """The multi-level stress run at its full length through the AMR driver
     (mamr_amr_run): 4^3 blocks of 8^3, 40 variables, 7-point, 5 levels,
     four moving objects, refine every 2 steps, 300 timesteps x 2 stages,
-    checksum every stage -- 151 refinements, each the marking on the
-    device, the library's split/consolidation bookkeeping, the cell
+    checksum every stage -- 151 refinements, each up to five marking steps
+    on the device, the library's split/consolidation bookkeeping, the cell
     movement on the device and a new mesh; every stretch of stages one
-    batched run under a freshly captured CUDA graph.  A 10-timestep run
-    first lets the tuner time its launch shapes.  Rates: updates over the
-    stretches' wall time (each stretch synchronised) and over the whole
-    call (initial values, upload and refinement included).  Checksums
-    against the reference's own log of the run: FP64 bit for bit, FP32 max
-    and RMS relative error."""
+    batched run under a freshly captured CUDA graph.  case "config5_300":
+    the objects of the recorded stress run (13k-24k blocks); case
+    "config5_named_mesh": the objects at the sizes the benchmark's
+    description names (spheres of radius 0.1, a cylinder of radius 0.05, a
+    box of side 0.2; 30k-53k blocks), run at 8^3 cells and 40 variables.
+    A 10-timestep run first lets the tuner time its launch shapes.  Rates:
+    updates over the stretches' wall time (each stretch synchronised) and
+    over the whole call (initial values, upload and refinement included);
+    the refinement time split into its parts.  Checksums against the
+    reference's own log of the run (FP64 bit for bit, FP32 max and RMS
+    relative error) or, for the named objects, the FP32 checksums against
+    fp64_sums (this path's FP64 run) and the meshes against the reference's
+    log of the meshes.  Returns (summary, checksums)."""
     from miniamr_gb300 import run as runmod
     meta = json.load(open(os.path.join(REPO, "tests", "golden",
                                        "cases.json")))
-    if "config5_300" not in meta:
-        return None
-    spec = runmod.parse(meta["config5_300"]["args"])
+    if case not in meta:
+        return None, None
+    spec = runmod.parse(meta[case]["args"])
+    spec.opts.update(nx=8, ny=8, nz=8, num_vars=V)
     spec.fp32 = dtype != 0
     cfg = spec.config()
     warm = spec.params()
@@ -436,41 +471,61 @@ def stress_driver(lib, dtype):
     with lib.context(cfg) as ctx:
         ctx.amr_run(warm, spec.objects)
     with lib.context(cfg) as ctx:
-        sums, st, _ = ctx.amr_run(spec.params(), spec.objects)
+        sums, st, ev = ctx.amr_run(spec.params(), spec.objects,
+                                   events=case != "config5_300")
     out = {"timesteps": spec.opts["num_tsteps"],
            "refinements": st["refinements"],
+           "marking_steps": st["marking_steps"],
            "max_blocks": st["max_active"], "final_blocks": st["final_active"],
            "updates": st["updates"],
            "updates_per_s": st["updates"] / st["stage_seconds"],
            "updates_per_s_whole_run": st["updates"] / st["total_seconds"],
            "stage_seconds": st["stage_seconds"],
            "refine_seconds": st["refine_seconds"],
-           "total_seconds": st["total_seconds"], "checksums": sums.size}
-    path = os.path.join(REPO, "tests", "golden", "config5_300.reflog.xz")
-    if os.path.exists(path):
-        import lzma
-        import struct
-        ref = []
-        with lzma.open(path, "rt") as f:
-            for ln in f:
-                p = ln.split()
-                if p[0] == "cs":
-                    ref.append(struct.unpack(
-                        "<d", int(p[3], 16).to_bytes(8, "little"))[0])
-        ref = np.array(ref)
-        got = sums.reshape(-1)
-        if got.size == ref.size:
-            if dtype == 0:
-                out["checksums_bit_exact_vs_reference"] = bool(
-                    np.array_equal(got.view(np.uint64), ref.view(np.uint64)))
-            else:
-                rel = np.abs(got - ref) / np.abs(ref)
-                out["checksum_rel_error_vs_reference_fp64"] = {
-                    "max": float(rel.max()),
-                    "rms": float(np.sqrt(np.mean(rel ** 2)))}
+           "refine_parts_seconds": {
+               k: st[k + "_seconds"]
+               for k in ("mark", "bookkeeping", "data", "mesh")},
+           "total_seconds": st["total_seconds"], "checksums": sums.size,
+           "timing": "host wall clock around each synchronised call"}
+    ref = _reflog_sums(case) if case == "config5_300" else None
+    got = sums.reshape(-1)
+    if ref is not None and got.size == ref.size:
+        if dtype == 0:
+            out["checksums_bit_exact_vs_reference"] = bool(
+                np.array_equal(got.view(np.uint64), ref.view(np.uint64)))
         else:
-            out["checksum_count_mismatch"] = [int(got.size), int(ref.size)]
-    return out
+            rel = np.abs(got - ref) / np.abs(ref)
+            out["checksum_rel_error_vs_reference_fp64"] = {
+                "max": float(rel.max()),
+                "rms": float(np.sqrt(np.mean(rel ** 2)))}
+    elif ref is not None:
+        out["checksum_count_mismatch"] = [int(got.size), int(ref.size)]
+    if fp64_sums is not None and fp64_sums.size == got.size:
+        rel = np.abs(got - fp64_sums.reshape(-1)) / np.abs(
+            fp64_sums.reshape(-1))
+        out["checksum_rel_error_vs_fp64_run"] = {
+            "max": float(rel.max()), "rms": float(np.sqrt(np.mean(rel ** 2)))}
+    meshes = _reflog_meshes(case) if case != "config5_300" else None
+    if meshes is not None:
+        from miniamr_gb300 import build
+        from miniamr_gb300.abi import Library
+        import ctypes as C
+        ol = Library(build.ORACLE_LIB if os.path.exists(build.ORACLE_LIB)
+                     else build.build_oracle())
+        f = ol.lib.mamr_oracle_mesh_hash
+        f.restype = C.c_uint64
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]
+        mine = []
+        for e in ev:
+            if e[0] == "mesh":
+                b, num, cen = (np.ascontiguousarray(e[2]),
+                               np.ascontiguousarray(e[3]),
+                               np.ascontiguousarray(e[4]))
+                mine.append((e[1], len(b), "%016x" % f(
+                    b.ctypes.data, num.ctypes.data, cen.ctypes.data,
+                    len(b))))
+        out["meshes_equal_reference"] = mine == meshes
+    return out, sums
 
 
 def refine_marking(lib):
@@ -803,8 +858,10 @@ def main():
             "uniform_stencil0_fp64": uniform_stencil0(lib),
             "stress_multilevel_7pt_fp32": stress_multilevel(lib, FP32),
             "stress_multilevel_7pt_fp64": stress_multilevel(lib, FP64),
-            "stress_300ts_amr_driver_fp32": stress_driver(lib, FP32),
-            "stress_300ts_amr_driver_fp64": stress_driver(lib, FP64),
+            "stress_300ts_amr_driver_fp32": stress_driver(lib, FP32)[0],
+            "stress_300ts_amr_driver_fp64": stress_driver(lib, FP64)[0],
+            "stress_named_objects_300ts_amr_driver_fp32": stress_driver(
+                lib, FP32, "config5_named_mesh")[0],
             "refine_marking_stress": refine_marking(lib),
         }
     # the figures the targets rest on last, where a truncated tail of the

@@ -320,7 +320,8 @@ typedef void (*mamr_amr_event)(void *user, int32_t kind, int32_t ts,
 typedef struct {
    double stage_seconds;    /* wall time of the stage stretches */
    double refine_seconds;   /* refine() calls: the four parts below */
-   double total_seconds;    /* the whole call */
+   double total_seconds;    /* the whole call (all times leave out the
+                               caller's event callback) */
    double mark_seconds;     /* mamr_mark_refine calls (lists in, flags out) */
    double bookkeeping_seconds; /* host: marking lists, split and
                                consolidation records, job lists */
@@ -388,7 +389,8 @@ int mamr_set_tuning(mamr_ctx *ctx, int32_t choice);
  * were, and its shape: shape[0..4] = threads per variable (generic
  * kernel) or per tile (pencil kernel), variables per CTA, j-rows and
  * i-planes per thread (pencil kernel), CTAs.  The warp-per-block kernel
- * reports (threads per (block, variable): 32 or 64, items per CTA, rows
+ * reports (threads per item -- a block and one or two of its variables:
+ * 32 or 64, variables per CTA (items per CTA x variables per item), rows
  * of 8 cells per thread: 2 or 1, 0, CTAs): i-planes 0 marks it. */
 int mamr_get_tuning(const mamr_ctx *ctx, int32_t *choice,
                     int32_t *n_candidates, int32_t *shape);

@@ -506,6 +506,18 @@ struct Run {
    mamr_amr_stats st{};
    Mesh mesh;
    int flags;   // the stretches' run flags (batched until it is refused)
+   double ev_s = 0.0;   // time spent in the caller's event callback, which
+                        // the stats leave out
+
+   void emit(int kind, int ts, const void *data, int32_t n,
+             const int64_t *numbers, const int32_t *cen)
+   {
+      if (!event)
+         return;
+      const double a = now();
+      event(user, kind, ts, data, n, numbers, cen);
+      ev_s += now() - a;
+   }
 
    Run(mamr_ctx *c, const mamr_config &cf, const mamr_amr_params &p)
       : ctx(c), cfg(cf), prm(p), mesh(p.init_x, p.init_y, p.init_z,
@@ -528,9 +540,9 @@ struct Run {
       mesh.export_mesh(m, numbers, cen);
       check(mamr_set_mesh(ctx, m.data(), (int32_t) m.size()),
             "mamr_set_mesh");
-      if (event && report)
-         event(user, 3, ts, m.data(), (int32_t) m.size(), numbers.data(),
-               cen.data());
+      if (report)
+         emit(3, ts, m.data(), (int32_t) m.size(), numbers.data(),
+              cen.data());
       st.max_active = std::max(st.max_active, (int32_t) m.size());
    }
 
@@ -539,7 +551,7 @@ struct Run {
    // consolidations.
    void refine(int ts)
    {
-      const double t0 = now();
+      const double t0 = now(), ev0 = ev_s;
       const int steps = ts ? (prm.block_change ? prm.block_change
                                                : prm.num_refine)
                            : prm.num_refine;
@@ -589,9 +601,7 @@ struct Run {
             check(mamr_split(ctx, sj.data(), (int32_t) sj.size()),
                   "mamr_split");
             st.data_seconds += lap(t);
-            if (event)
-               event(user, 1, ts, sj.data(), (int32_t) sj.size(), nullptr,
-                     nullptr);
+            emit(1, ts, sj.data(), (int32_t) sj.size(), nullptr, nullptr);
          }
          t = now();
          mesh.consolidate(cj);
@@ -600,9 +610,7 @@ struct Run {
             check(mamr_consolidate(ctx, cj.data(), (int32_t) cj.size()),
                   "mamr_consolidate");
             st.data_seconds += lap(t);
-            if (event)
-               event(user, 2, ts, cj.data(), (int32_t) cj.size(), nullptr,
-                     nullptr);
+            emit(2, ts, cj.data(), (int32_t) cj.size(), nullptr, nullptr);
          }
          // a step that changed nothing leaves the marking's inputs as they
          // were (it starts from reset flags, and the objects move only
@@ -612,11 +620,12 @@ struct Run {
             break;
       }
       double t = now();
+      const double ev_mesh = ev_s;
       set_mesh(ts, true);
       check(mamr_sync(ctx), "mamr_sync");
-      st.mesh_seconds += lap(t);
+      st.mesh_seconds += lap(t) - (ev_s - ev_mesh);
       st.refinements++;
-      st.refine_seconds += now() - t0;
+      st.refine_seconds += now() - t0 - (ev_s - ev0);
    }
 
    void stages(int n_ts, int first_stage)
@@ -708,7 +717,7 @@ struct Run {
       }
       check(mamr_sync(ctx), "mamr_sync");
       st.final_active = mesh.active();
-      st.total_seconds = now() - t0;
+      st.total_seconds = now() - t0 - ev_s;
    }
 };
 

@@ -1595,11 +1595,15 @@ extern "C" int mamr_get_tuning(const mamr_ctx *c, int32_t *choice,
    if (n_candidates)
       *n_candidates = c->tune_n;
    if (shape) {
-      shape[0] = c->tune_shape.threads;
-      shape[1] = c->tune_shape.vpc;
-      shape[2] = c->tune_shape.rows;
-      shape[3] = c->tune_shape.planes;
-      shape[4] = c->tune_shape.grid;
+      const StageShape &sh = c->tune_shape;
+      const bool brick = sh.kernel == 1;
+      shape[0] = sh.threads;
+      // the warp-per-block kernel: variables per CTA = items x variables
+      // per item, and i-planes 0
+      shape[1] = brick ? sh.vpc * std::max(1, sh.planes) : sh.vpc;
+      shape[2] = sh.rows;
+      shape[3] = brick ? 0 : sh.planes;
+      shape[4] = sh.grid;
    }
    return MAMR_OK;
 }

@@ -272,8 +272,9 @@ void batched_mesh_changed(BatchedState *b);
 //   pencil kernel:  `rows` j-rows and `planes` i-planes per thread
 //                   (threads = 1024 / (rows * planes))
 //   both:           `grid` CTAs
-//   warp-per-item kernel (8^3 blocks, 7-point; kernel = 1): threads = 32,
-//                   vpc = warps per CTA, rows = 2, planes = 0
+//   warp-per-item kernel (8^3 blocks, 7-point; kernel = 1): threads = 32
+//                   or 64 per item, vpc = items per CTA, rows = rows per
+//                   thread, planes = variables per item (1 or 2)
 struct StageShape {
    int threads = 0, vpc = 1, rows = 1, planes = 4, grid = 1;
    int kernel = 0;

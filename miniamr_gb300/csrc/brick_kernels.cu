@@ -1,11 +1,14 @@
 // Stage kernel for meshes of 8^3 blocks with the 7-point stencil: one or
-// two warps per work item (block, variable) and no CTA-wide barrier, so
-// that every item of an SM streams independently.  Each item's warps own
-// two tiles in shared memory and fill the next item's tile -- interior rows, and the face
-// ghosts that are copies (same-level neighbour, reflection) or single
-// values (coarser neighbour, scaled by 1/4 afterwards) -- with cp.async
-// while it computes the current item; ghosts from finer neighbours (sums of
-// four cells) are gathered after the wait.
+// two warps per work item -- a block and one or two of its variables -- and
+// no CTA-wide barrier, so that every item of an SM streams independently.
+// Each item's warps own two sets of tiles in shared memory and fill the
+// next item's tiles -- interior rows, and the face ghosts that are copies
+// (same-level neighbour, reflection) or single values (coarser neighbour,
+// scaled by 1/4 afterwards) -- with cp.async while they compute the current
+// item; ghosts from finer neighbours (sums of four cells) are gathered
+// after the wait.  With two variables per item the descriptor, the face
+// dispatch and the copy addresses serve both variables (their cells are one
+// block-variable stride apart), which halves that work per variable.
 //
 // z-face arrays.  The z ghosts of a block are one value from each of 64
 // rows of its neighbour -- a 32-byte sector per value.  So every stage also
@@ -35,23 +38,28 @@ template <typename T> struct Vec16;
 template <> struct Vec16<float> { using type = float4; };
 template <> struct Vec16<double> { using type = double2; };
 
-// Tile of one item: cell (i, j, k), 0 <= i, j, k <= 9, at
-// (i*10 + j)*S + k - 1.  A row (i, j) holds k = 1..8 in columns 0..7 (two
-// or four 16-byte vectors) and k = 9 in column 8; its k = 0 ghost sits in
-// the last column of the row before (only interior rows have one).  With
-// S = 12 (FP32) or 10 (FP64) the eight rows j = 1..8 of one plane start in
-// eight different 16-byte bank groups, so the vector loads of eight
-// consecutive lanes do not conflict.
+// Tile of one block-variable: row (i, j), 0 <= i, j <= 9, holds k = 1..8
+// (two or four 16-byte vectors); the z ghosts k = 0 and k = 9 sit in two
+// planes of 64 values after the rows.  FP32: rows of 8 values (S = 8),
+// with the two vectors of a row swapped when j = 4..7, so that the vector
+// loads of eight consecutive lanes -- rows j = 1..8, 0..7 or 2..9 of one
+// plane -- fall in eight different 16-byte bank groups.  FP64: rows padded
+// to S = 10 values, which spreads them the same way.
 template <typename T> struct Brick {
    static constexpr int VW = 16 / (int) sizeof(T);   // elements per vector
    static constexpr int R = 8 / VW;                  // vectors per row
-   static constexpr int S = sizeof(T) == 4 ? 12 : 10;
+   static constexpr bool SWZ = sizeof(T) == 4;
+   static constexpr int S = SWZ ? 8 : 10;
    static constexpr int TILE = 100 * S;
    static constexpr int ZST = 128;   // z ghost planes k = 0, 9 after a tile
    static constexpr int SLAB = TILE + ZST;
    static constexpr int DESC = 44;   // ints of a BItem read: slot .. f[5]
+   // element k (1 <= k <= 8) of row (i, j)
    __device__ static int at(int i, int j, int k)
    {
+      if (SWZ)
+         return (i * 10 + j) * 8 +
+                ((((k - 1) >> 2) ^ ((j >> 2) & 1)) << 2) + ((k - 1) & 3);
       return (i * 10 + j) * S + k - 1;
    }
    // pool offset of interior cell (i, j, k) (split layout, 1 <= k <= 8)
@@ -70,9 +78,9 @@ template <typename T> struct Brick {
       return dir == 0 ? at(gn, a, b) : (dir == 1 ? at(a, gn, b)
                                                  : at(a, b, gn));
    }
-   static size_t smem_per_item()
+   static size_t smem_per_item(int vpi)
    {
-      return 2 * (SLAB * sizeof(T) + DESC * sizeof(int));
+      return 2 * (vpi * SLAB * sizeof(T) + DESC * sizeof(int));
    }
    // z-face array: planes k = 1 (side 0) and k = 8 (side 1) of a
    // block-variable, 64 values each, at (i-1)*8 + (j-1)
@@ -108,27 +116,31 @@ __device__ __forceinline__ void st4(T *p, const T (&v)[4])
    }
 }
 
-// Queues the copies that fill the tile of item (block sd[0], var): the
-// interior rows, and the face ghosts of same-level, boundary and coarser
-// faces (the coarse values unscaled).  sd = the block's BItem, ints
-// 0..DESC-1.  Returns whether the tile needs brick_fix (a face at a level
-// jump).
-template <typename T, int TPI>
+// Queues the copies that fill the tiles of item (block sd[0], variables
+// var0 .. var0 + nv - 1; tile v at tile + v * SLAB): the interior rows, and
+// the face ghosts of same-level, boundary and coarser faces (the coarse
+// values unscaled).  sd = the block's BItem, ints 0..DESC-1.  Returns
+// whether the tiles need brick_fix (a face at a level jump).
+template <typename T, int TPI, int VPI>
 __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
                                             const T *__restrict__ zf,
-                                            const Geom &g, int var,
+                                            const Geom &g, int var0, int nv,
                                             const int *sd, T *tile, int lane)
 {
    bool fix = false;
    using B = Brick<T>;
    constexpr int VW = B::VW, R = B::R;
-   T *zst = tile + B::TILE;
-   const T *own = src + bv_offset(g, sd[0], var);
+   const long long bv = g.bv;           // stride of consecutive variables
+   const T *own = src + bv_offset(g, sd[0], var0);
 #pragma unroll
    for (int t = 0; t < 64 * R / TPI; t++) {
       const int c = lane + TPI * t, r = c / R, k = 1 + (c % R) * VW;
       const int i = (r >> 3) + 1, j = (r & 7) + 1;
-      cp_async16(tile + B::at(i, j, k), own + B::gat(i, j, k));
+#pragma unroll
+      for (int v = 0; v < VPI; v++)
+         if (v < nv)
+            cp_async16(tile + v * B::SLAB + B::at(i, j, k),
+                       own + v * bv + B::gat(i, j, k));
    }
 #pragma unroll
    for (int l = 0; l < 6; l++) {
@@ -137,50 +149,65 @@ __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
       const int dir = l >> 1;
       const bool low = !(l & 1);
       const int gn = low ? 0 : 9;
+      const int zo = B::TILE + (low ? 0 : 64);   // z ghost plane in a tile
       if (type == FACE_SAME || type == FACE_BC) {
-         const T *sb = type == FACE_SAME ? src + bv_offset(g, f[1], var)
+         const T *sb = type == FACE_SAME ? src + bv_offset(g, f[1], var0)
                                          : own;
          // same level: the neighbour's near plane; boundary: reflection
          const int p = (type == FACE_SAME) == low ? 8 : 1;
          if (dir < 2) {
             for (int c = lane; c < 8 * R; c += TPI) {
                const int a = c / R + 1, k = 1 + (c % R) * VW;
-               if (dir == 0)
-                  cp_async16(tile + B::at(gn, a, k), sb + B::gat(p, a, k));
-               else
-                  cp_async16(tile + B::at(a, gn, k), sb + B::gat(a, p, k));
+               const int to = dir == 0 ? B::at(gn, a, k) : B::at(a, gn, k);
+               const int from = dir == 0 ? B::gat(p, a, k) : B::gat(a, p, k);
+#pragma unroll
+               for (int v = 0; v < VPI; v++)
+                  if (v < nv)
+                     cp_async16(tile + v * B::SLAB + to, sb + v * bv + from);
             }
          } else if (zf) {
             // the plane from the z-face array: 64 values as 16-byte copies
             const int slot = type == FACE_SAME ? f[1] : sd[0];
-            const T *pl = zf + B::zf_at(g, slot, var, p == 8);
-            if (lane < 64 / VW)
-               cp_async16(zst + (low ? 0 : 64) + lane * VW, pl + lane * VW);
+            const T *pl = zf + B::zf_at(g, slot, var0, p == 8);
+            if (lane < 64 / VW) {
+#pragma unroll
+               for (int v = 0; v < VPI; v++)
+                  if (v < nv)
+                     cp_async16(tile + v * B::SLAB + zo + lane * VW,
+                                pl + v * 128 + lane * VW);
+            }
          } else {
 #pragma unroll
             for (int u = 0; u < 64 / TPI; u++) {
                const int e = lane + TPI * u, i = (e >> 3) + 1, j = (e & 7) + 1;
-               cp_async_elem(zst + (low ? 0 : 64) + e, sb + B::gat(i, j, p));
+#pragma unroll
+               for (int v = 0; v < VPI; v++)
+                  if (v < nv)
+                     cp_async_elem(tile + v * B::SLAB + zo + e,
+                                   sb + v * bv + B::gat(i, j, p));
             }
          }
       } else if (type == FACE_COARSE) {
          fix = true;
-         const T *sb = src + bv_offset(g, f[1], var);
+         const T *sb = src + bv_offset(g, f[1], var0);
          const int p = low ? 8 : 1, iq = f[5], jq = f[6];
 #pragma unroll
          for (int u = 0; u < 64 / TPI; u++) {
             const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
             const int ca = (a + 1) / 2 + 4 * jq, cb = (b + 1) / 2 + 4 * iq;
-            if (dir < 2)
-               cp_async_elem(tile + B::ghost_at(dir, gn, a, b),
-                             sb + B::face_gat(dir, p, ca, cb));
-            else if (zf)
-               cp_async_elem(zst + (low ? 0 : 64) + e,
-                             zf + B::zf_at(g, f[1], var, p == 8) +
-                                (ca - 1) * 8 + (cb - 1));
-            else
-               cp_async_elem(zst + (low ? 0 : 64) + e,
-                             sb + B::face_gat(dir, p, ca, cb));
+            const int to = dir < 2 ? B::ghost_at(dir, gn, a, b) : zo + e;
+            const T *from =
+               dir < 2 ? sb + B::face_gat(dir, p, ca, cb)
+                       : (zf ? zf + B::zf_at(g, f[1], var0, p == 8) +
+                                  (ca - 1) * 8 + (cb - 1)
+                             : sb + B::face_gat(dir, p, ca, cb));
+            // the variable stride of the source: the pool's, or the
+            // z-face array's 128 values per block-variable
+            const long long vs = dir == 2 && zf ? 128 : bv;
+#pragma unroll
+            for (int v = 0; v < VPI; v++)
+               if (v < nv)
+                  cp_async_elem(tile + v * B::SLAB + to, from + v * vs);
          }
       } else {
          fix = true;                   // finer neighbours: summed later
@@ -192,14 +219,14 @@ __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
 // After the copies landed: coarse ghosts scaled by 1/4 (each lane the
 // elements it copied) and fine ghosts summed from the four finer
 // neighbours' cells, in the reference's order.
-template <typename T, int TPI>
+template <typename T, int TPI, int VPI>
 __device__ __forceinline__ void brick_fix(const T *__restrict__ src,
                                           const T *__restrict__ zf,
-                                          const Geom &g, int var,
+                                          const Geom &g, int var0, int nv,
                                           const int *sd, T *tile, int lane)
 {
    using B = Brick<T>;
-   T *zst = tile + B::TILE;
+   const long long bv = g.bv;
 #pragma unroll
    for (int l = 0; l < 6; l++) {
       const int *f = sd + 2 + 7 * l;
@@ -212,41 +239,68 @@ __device__ __forceinline__ void brick_fix(const T *__restrict__ src,
 #pragma unroll
       for (int u = 0; u < 64 / TPI; u++) {
          const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
-         T &x = dir < 2 ? tile[B::ghost_at(dir, gn, a, b)]
-                        : zst[(low ? 0 : 64) + e];
+         const int to = dir < 2 ? B::ghost_at(dir, gn, a, b)
+                                : B::TILE + (low ? 0 : 64) + e;
          if (type == FACE_COARSE) {
-            x = quarter(x);
+#pragma unroll
+            for (int v = 0; v < VPI; v++)
+               if (v < nv) {
+                  T &x = tile[v * B::SLAB + to];
+                  x = quarter(x);
+               }
          } else {
             const int jq = a > 4, iq = b > 4;
             const int a2 = a - 4 * jq, b2 = b - 4 * iq;
             const int nbs = f[1 + iq * 2 + jq];
-            T t;
+            // the four fine cells: from the fine block's z-face array
+            // (plane p, 128 values per block-variable) or its pool cells
+            const T *q0;
+            int o[4];
+            long long vs;
             if (dir == 2 && zf) {
-               // the fine block's plane p from its z-face array
-               const T *pl = zf + B::zf_at(g, nbs, var, p == 8);
-               t = pl[(2 * a2 - 2) * 8 + 2 * b2 - 2] +
-                   pl[(2 * a2 - 2) * 8 + 2 * b2 - 1];
-               t = t + pl[(2 * a2 - 1) * 8 + 2 * b2 - 2];
-               t = t + pl[(2 * a2 - 1) * 8 + 2 * b2 - 1];
+               q0 = zf + B::zf_at(g, nbs, var0, p == 8);
+               o[0] = (2 * a2 - 2) * 8 + 2 * b2 - 2;
+               o[1] = o[0] + 1;
+               o[2] = o[0] + 8;
+               o[3] = o[0] + 9;
+               vs = 128;
             } else {
-               const T *fb = src + bv_offset(g, nbs, var);
-               t = fb[B::face_gat(dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
-                   fb[B::face_gat(dir, p, 2 * a2 - 1, 2 * b2)];
-               t = t + fb[B::face_gat(dir, p, 2 * a2, 2 * b2 - 1)];
-               t = t + fb[B::face_gat(dir, p, 2 * a2, 2 * b2)];
+               q0 = src + bv_offset(g, nbs, var0);
+               o[0] = B::face_gat(dir, p, 2 * a2 - 1, 2 * b2 - 1);
+               o[1] = B::face_gat(dir, p, 2 * a2 - 1, 2 * b2);
+               o[2] = B::face_gat(dir, p, 2 * a2, 2 * b2 - 1);
+               o[3] = B::face_gat(dir, p, 2 * a2, 2 * b2);
+               vs = bv;
             }
-            x = t;
+            T w[VPI][4];
+#pragma unroll
+            for (int v = 0; v < VPI; v++)
+               if (v < nv) {
+#pragma unroll
+                  for (int m = 0; m < 4; m++)
+                     w[v][m] = q0[v * vs + o[m]];
+               }
+#pragma unroll
+            for (int v = 0; v < VPI; v++)
+               if (v < nv) {
+                  T t = w[v][0] + w[v][1];
+                  t = t + w[v][2];
+                  t = t + w[v][3];
+                  tile[v * B::SLAB + to] = t;
+               }
          }
       }
    }
 }
 
-// TPI threads (one or two warps) per work item, at most 4 items per CTA.
-// Registers for the CTAs whose tiles fill the shared memory: 5 CTAs of
-// 4 one-warp items (FP32) or 3 (FP64); 4 CTAs of 4 two-warp items.
-template <int TPI, int FP32> struct BrickBounds {
+// TPI threads (one or two warps) per work item of VPI variables, at most
+// 4 items per CTA.  Registers for the CTAs whose tiles fill the shared
+// memory: one variable -- 5 CTAs of 4 one-warp items (FP32) or 3 (FP64), 4
+// CTAs of 4 two-warp items; two variables -- 3 CTAs.
+template <int TPI, int FP32, int VPI> struct BrickBounds {
    static constexpr int THREADS = 4 * TPI;
-   static constexpr int CTAS = TPI == 64 ? 4 : (FP32 ? 5 : 3);
+   static constexpr int CTAS =
+      VPI == 2 ? 3 : (TPI == 64 ? 4 : (FP32 ? 5 : 3));
 };
 
 // Barrier of the TPI threads that share an item: the warp itself, or a
@@ -260,9 +314,9 @@ template <int TPI> __device__ __forceinline__ void group_sync(int group)
                    : "memory");
 }
 
-template <typename T, int TPI>
-__global__ void __launch_bounds__(BrickBounds<TPI, sizeof(T) == 4>::THREADS,
-                                  BrickBounds<TPI, sizeof(T) == 4>::CTAS)
+template <typename T, int TPI, int VPI>
+__global__ void __launch_bounds__(BrickBounds<TPI, sizeof(T) == 4, VPI>::THREADS,
+                                  BrickBounds<TPI, sizeof(T) == 4, VPI>::CTAS)
 brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                    const BItem *__restrict__ items, int nb, int write_ghosts,
                    int do_cs, unsigned long long *__restrict__ acc,
@@ -273,33 +327,37 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
    constexpr int DESC = B::DESC;
    constexpr int ND = (DESC + TPI - 1) / TPI;     // descriptor ints a thread
    constexpr int RPT = 64 / TPI;                   // rows of 8 cells a thread
+   constexpr int SET = VPI * B::SLAB;              // one item's tiles
    extern __shared__ __align__(16) unsigned char smem_raw[];
    const int lane = threadIdx.x % TPI, group = threadIdx.x / TPI;
    const int gpc = blockDim.x / TPI;
-   T *tiles = reinterpret_cast<T *>(smem_raw) + (size_t) group * 2 * B::SLAB;
+   T *tiles = reinterpret_cast<T *>(smem_raw) + (size_t) group * 2 * SET;
    int *sdesc = reinterpret_cast<int *>(reinterpret_cast<T *>(smem_raw) +
-                                        (size_t) gpc * 2 * B::SLAB) +
+                                        (size_t) gpc * 2 * SET) +
                 group * 2 * DESC;
-   // work items (block b, variable var), variable-major; group w takes
-   // items w, w + nw, w + 2 nw, ... tracked as (var, b) without divisions
+   // work items (block b, variables VPI*pv ..), variable-major; group w
+   // takes items w, w + nw, w + 2 nw, ... tracked as (pv, b) without
+   // divisions
+   const int npv = (g.V + VPI - 1) / VPI;
    const int nw = gridDim.x * gpc;
    const int it0 = blockIdx.x * gpc + group;
    struct Pos {
-      int var, b;
+      int pv, b;
    };
    Pos cur{it0 / nb, it0 % nb};
-   if (cur.var >= g.V)
+   if (cur.pv >= npv)
       return;
    const int step_v = nw / nb, step_b = nw - step_v * nb;
    auto advance = [&](Pos q) {
-      q.var += step_v;
+      q.pv += step_v;
       q.b += step_b;
       if (q.b >= nb) {
          q.b -= nb;
-         q.var++;
+         q.pv++;
       }
       return q;
    };
+   auto nvars = [&](int pv) { return min(VPI, g.V - pv * VPI); };
    const Dims<8, 8, 8> D(g);
    // this thread's output rows (i0 + m, j), m < RPT
    const int j = (lane & 7) + 1, i0 = RPT * (lane >> 3) + 1;
@@ -321,146 +379,164 @@ brick_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
 
    load_desc(cur);
    put_desc(sdesc);
-   bool fix_cur = brick_issue<T, TPI>(src, zf_src, g, cur.var, sdesc, tiles,
-                                      lane);
+   bool fix_cur = brick_issue<T, TPI, VPI>(src, zf_src, g, cur.pv * VPI,
+                                           nvars(cur.pv), sdesc, tiles, lane);
    cp_async_commit();
    Pos nxt = advance(cur);
-   if (nxt.var < g.V)
+   if (nxt.pv < npv)
       load_desc(nxt);
 
-   unsigned long long lo = 0, hi = 0;
+   unsigned long long lo[VPI], hi[VPI];
+#pragma unroll
+   for (int v = 0; v < VPI; v++)
+      lo[v] = hi[v] = 0;
    Fixed52 part;
-   bool ok = true;
-   int cs_var = -1;
+   int cs_pv = -1;
    for (int n = 0;; n++) {
       const int cb = n & 1;
-      T *tile = tiles + cb * B::SLAB;
-      const T *zst = tile + B::TILE;
+      T *tile = tiles + cb * SET;
       const int *sd = sdesc + cb * DESC;
       // the next item: descriptor into shared memory, copies in flight
       bool fix_next = false;
-      if (nxt.var < g.V) {
+      if (nxt.pv < npv) {
          int *sdn = sdesc + (cb ^ 1) * DESC;
          put_desc(sdn);
-         fix_next = brick_issue<T, TPI>(src, zf_src, g, nxt.var, sdn,
-                                        tiles + (cb ^ 1) * B::SLAB, lane);
+         fix_next = brick_issue<T, TPI, VPI>(src, zf_src, g, nxt.pv * VPI,
+                                             nvars(nxt.pv), sdn,
+                                             tiles + (cb ^ 1) * SET, lane);
          const Pos nn = advance(nxt);
-         if (nn.var < g.V)
+         if (nn.pv < npv)
             load_desc(nn);
       }
       cp_async_commit();
       cp_async_wait_group<1>();
-      const int var = cur.var;
+      const int var0 = cur.pv * VPI, nv = nvars(cur.pv);
       if (fix_cur)
-         brick_fix<T, TPI>(src, zf_src, g, var, sd, tile, lane);
+         brick_fix<T, TPI, VPI>(src, zf_src, g, var0, nv, sd, tile, lane);
       group_sync<TPI>(group);
-      T *d = dst + bv_offset(g, sd[0], var);
-      if (write_ghosts) {
+      if (sizeof(T) == 4 && do_cs && cur.pv != cs_pv) {
+         if (cs_pv >= 0) {
 #pragma unroll
-         for (int l = 0; l < 6; l++) {
-            const int dir = l >> 1, gn = (l & 1) ? 9 : 0;
-#pragma unroll
-            for (int u = 0; u < 64 / TPI; u++) {
-               const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
-               int gi, gj, gk;
-               if (dir == 0) { gi = gn; gj = a; gk = b; }
-               else if (dir == 1) { gi = a; gj = gn; gk = b; }
-               else { gi = a; gj = b; gk = gn; }
-               d[D.cell(gi, gj, gk)] = dir < 2 ? tile[B::at(gi, gj, gk)]
-                                               : zst[(gn ? 64 : 0) + e];
+            for (int v = 0; v < VPI; v++) {
+               if (v < nvars(cs_pv))
+                  warp_acc128_flush(lo[v], hi[v], acc + 2 * (cs_pv * VPI + v));
+               lo[v] = hi[v] = 0;
             }
          }
+         cs_pv = cur.pv;
       }
-      if (sizeof(T) == 4 && do_cs && var != cs_var) {
-         if (cs_var >= 0) {
-            warp_acc128_flush(lo, hi, acc + 2 * cs_var);
-            lo = hi = 0;
-         }
-         cs_var = var;
-      }
-      // 7-point update of the thread's rows, four k at a time
 #pragma unroll
-      for (int m = 0; m < RPT; m++) {
-         const int i = i0 + m;
+      for (int v = 0; v < VPI; v++) {
+         if (v >= nv)
+            break;
+         const T *tv = tile + v * B::SLAB;
+         const T *zst = tv + B::TILE;
+         T *d = dst + bv_offset(g, sd[0], var0 + v);
+         if (write_ghosts) {
 #pragma unroll
-         for (int h = 0; h < 2; h++) {
-            const int k0 = 1 + 4 * h;
-            T a[4], jm[4], c[4], jp[4], bq[4];
-            ld4(tile + B::at(i - 1, j, k0), a);
-            ld4(tile + B::at(i, j - 1, k0), jm);
-            ld4(tile + B::at(i, j, k0), c);
-            ld4(tile + B::at(i, j + 1, k0), jp);
-            ld4(tile + B::at(i + 1, j, k0), bq);
-            // k = 0 and k = 9 from the tile's z ghost planes
-            const int zi = (i - 1) * 8 + (j - 1);
-            const T cm = h == 0 ? zst[zi] : tile[B::at(i, j, k0 - 1)];
-            const T cp = h == 1 ? zst[64 + zi] : tile[B::at(i, j, k0 + 4)];
-            T w[4], q[4];
+            for (int l = 0; l < 6; l++) {
+               const int dir = l >> 1, gn = (l & 1) ? 9 : 0;
 #pragma unroll
-            for (int t = 0; t < 4; t++) {
-               const T km = t == 0 ? cm : c[t - 1];
-               const T kp = t == 3 ? cp : c[t + 1];
-               T s = a[t] + jm[t];
-               s = s + km;
-               s = s + c[t];
-               s = s + kp;
-               s = s + jp[t];
-               s = s + bq[t];
-               w[t] = s;
-            }
-            div_const4<7>(w, q);
-            st4(d + B::gat(i, j, k0), q);
-            if (zf_dst) {
-               // this block's k = 1 / k = 8 plane for the next stage
-               T *zp = zf_dst + B::zf_at(g, sd[0], var, h);
-               zp[zi] = h == 0 ? q[0] : q[3];
-            }
-            if (sizeof(T) == 4 && do_cs) {
-#pragma unroll
-               for (int t = 0; t < 4; t++)
-                  fixed52_add((float) q[t], part);
+               for (int u = 0; u < 64 / TPI; u++) {
+                  const int e = lane + TPI * u, a = (e >> 3) + 1,
+                            b = (e & 7) + 1;
+                  int gi, gj, gk;
+                  if (dir == 0) { gi = gn; gj = a; gk = b; }
+                  else if (dir == 1) { gi = a; gj = gn; gk = b; }
+                  else { gi = a; gj = b; gk = gn; }
+                  d[D.cell(gi, gj, gk)] = dir < 2 ? tv[B::at(gi, gj, gk)]
+                                                  : zst[(gn ? 64 : 0) + e];
+               }
             }
          }
+         // 7-point update of the thread's rows, four k at a time
+#pragma unroll
+         for (int m = 0; m < RPT; m++) {
+            const int i = i0 + m;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+               const int k0 = 1 + 4 * h;
+               T a[4], jm[4], c[4], jp[4], bq[4];
+               ld4(tv + B::at(i - 1, j, k0), a);
+               ld4(tv + B::at(i, j - 1, k0), jm);
+               ld4(tv + B::at(i, j, k0), c);
+               ld4(tv + B::at(i, j + 1, k0), jp);
+               ld4(tv + B::at(i + 1, j, k0), bq);
+               // k = 0 and k = 9 from the tile's z ghost planes
+               const int zi = (i - 1) * 8 + (j - 1);
+               const T cm = h == 0 ? zst[zi] : tv[B::at(i, j, k0 - 1)];
+               const T cp = h == 1 ? zst[64 + zi] : tv[B::at(i, j, k0 + 4)];
+               T w[4], q[4];
+#pragma unroll
+               for (int t = 0; t < 4; t++) {
+                  const T km = t == 0 ? cm : c[t - 1];
+                  const T kp = t == 3 ? cp : c[t + 1];
+                  T s = a[t] + jm[t];
+                  s = s + km;
+                  s = s + c[t];
+                  s = s + kp;
+                  s = s + jp[t];
+                  s = s + bq[t];
+                  w[t] = s;
+               }
+               div_const4<7>(w, q);
+               st4(d + B::gat(i, j, k0), q);
+               if (zf_dst) {
+                  // this block's k = 1 / k = 8 plane for the next stage
+                  T *zp = zf_dst + B::zf_at(g, sd[0], var0 + v, h);
+                  zp[zi] = h == 0 ? q[0] : q[3];
+               }
+               if (sizeof(T) == 4 && do_cs) {
+#pragma unroll
+                  for (int t = 0; t < 4; t++)
+                     fixed52_add((float) q[t], part);
+               }
+            }
+         }
+         if (sizeof(T) == 4 && do_cs)
+            fixed52_flush(part, lo[v], hi[v]);
       }
-      if (sizeof(T) == 4 && do_cs)
-         fixed52_flush(part, lo, hi);
       group_sync<TPI>(group);
       cur = nxt;
       fix_cur = fix_next;
-      if (cur.var >= g.V)
+      if (cur.pv >= npv)
          break;
       nxt = advance(nxt);
    }
    if (sizeof(T) == 4 && do_cs) {
-      if (cs_var >= 0)
-         warp_acc128_flush(lo, hi, acc + 2 * cs_var);
-      if (!ok || !fixed52_window(part))
+      if (cs_pv >= 0) {
+#pragma unroll
+         for (int v = 0; v < VPI; v++)
+            if (v < nvars(cs_pv))
+               warp_acc128_flush(lo[v], hi[v], acc + 2 * (cs_pv * VPI + v));
+      }
+      if (!fixed52_window(part))
          atomicOr(err, ERR_FIXED_RANGE);
    }
 }
 
 }  // namespace
 
-// CTAs per SM with gpc items of TPI threads each; the kernel's dynamic
-// shared memory limit is raised once to what 4 items need.
-template <typename T, int TPI>
+// CTAs per SM with gpc items of TPI threads and VPI variables each; the
+// kernel's dynamic shared memory limit is raised once to what 4 items need.
+template <typename T, int TPI, int VPI>
 static int brick_per_sm(int gpc)
 {
    int per_sm = 0;
-   cudaFuncSetAttribute(brick_stage_kernel<T, TPI>,
+   cudaFuncSetAttribute(brick_stage_kernel<T, TPI, VPI>,
                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                        (int) (Brick<T>::smem_per_item() * 4));
+                        (int) (Brick<T>::smem_per_item(VPI) * 4));
    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, brick_stage_kernel<T, TPI>, TPI * gpc,
-      Brick<T>::smem_per_item() * gpc);
+      &per_sm, brick_stage_kernel<T, TPI, VPI>, TPI * gpc,
+      Brick<T>::smem_per_item(VPI) * gpc);
    return per_sm;
 }
 
 // Candidates: one warp per item (two rows of 8 cells a lane) or two warps
-// per item (one row a thread), 4 or 2 items per CTA, a persistent grid of
-// the CTAs one wave holds.  Shape fields: threads = threads per item,
-// vpc = items per CTA, rows = rows per thread, planes = 0 (marks this
-// kernel).
+// per item (one row a thread), 4 or 2 items per CTA; FP32 also two
+// variables per item with two warps; a persistent grid of the CTAs one
+// wave holds.  Shape fields: threads = threads per item, vpc = items per
+// CTA, rows = rows per thread, planes = variables per item.
 template <typename T>
 void brick_candidates(const Geom &g, int stencil, int n_blocks,
                       std::vector<StageShape> &out)
@@ -470,19 +546,31 @@ void brick_candidates(const Geom &g, int stencil, int n_blocks,
    int dev = 0, sms = 0;
    cudaGetDevice(&dev);
    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-   const long long items = (long long) n_blocks * g.V;
-   for (int tpi : {32, 64})
+   struct Form {
+      int tpi, vpi;
+   };
+   std::vector<Form> forms = {{32, 1}, {64, 1}};
+   if (sizeof(T) == 4 && g.V >= 2)
+      forms.push_back({64, 2});
+   for (const Form &fm : forms)
       for (int gpc : {4, 2}) {
-         const int per_sm = tpi == 32 ? brick_per_sm<T, 32>(gpc)
-                                      : brick_per_sm<T, 64>(gpc);
+         int per_sm = 0;
+         if (fm.vpi == 2) {
+            if constexpr (sizeof(T) == 4)
+               per_sm = brick_per_sm<T, 64, 2>(gpc);
+         } else
+            per_sm = fm.tpi == 32 ? brick_per_sm<T, 32, 1>(gpc)
+                                  : brick_per_sm<T, 64, 1>(gpc);
          if (per_sm <= 0)
             continue;
+         const long long items =
+            (long long) n_blocks * ((g.V + fm.vpi - 1) / fm.vpi);
          StageShape sh;
          sh.kernel = 1;
-         sh.threads = tpi;
+         sh.threads = fm.tpi;
          sh.vpc = gpc;
-         sh.rows = 64 / tpi;
-         sh.planes = 0;
+         sh.rows = 64 / fm.tpi;
+         sh.planes = fm.vpi;
          sh.grid = (int) std::max(1LL, std::min<long long>(
                                           (long long) per_sm * sms,
                                           (items + gpc - 1) / gpc));
@@ -499,14 +587,22 @@ int launch_brick_stage(const T *src, T *dst, const Geom &g,
 {
    if (n_blocks == 0)
       return 0;
-   const size_t smem = Brick<T>::smem_per_item() * sh.vpc;
+   const int vpi = sh.planes == 2 ? 2 : 1;
+   const size_t smem = Brick<T>::smem_per_item(vpi) * sh.vpc;
    const int cs = sizeof(T) == 4 ? do_cs : 0;
-   if (sh.threads == 64)
-      brick_stage_kernel<T, 64><<<sh.grid, 64 * sh.vpc, smem, s>>>(
+   if (vpi == 2) {
+      if constexpr (sizeof(T) == 4)
+         brick_stage_kernel<T, 64, 2><<<sh.grid, 64 * sh.vpc, smem, s>>>(
+            src, dst, g, items, n_blocks, write_ghosts, cs, acc, err, zf_src,
+            zf_dst);
+      else
+         return -1;
+   } else if (sh.threads == 64)
+      brick_stage_kernel<T, 64, 1><<<sh.grid, 64 * sh.vpc, smem, s>>>(
          src, dst, g, items, n_blocks, write_ghosts, cs, acc, err, zf_src,
          zf_dst);
    else
-      brick_stage_kernel<T, 32><<<sh.grid, 32 * sh.vpc, smem, s>>>(
+      brick_stage_kernel<T, 32, 1><<<sh.grid, 32 * sh.vpc, smem, s>>>(
          src, dst, g, items, n_blocks, write_ghosts, cs, acc, err, zf_src,
          zf_dst);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
