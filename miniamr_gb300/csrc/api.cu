@@ -1016,6 +1016,7 @@ static int build_items_host(mamr_ctx *c)
                            "coarser neighbour %d", bp.slot, m);
          }
       }
+      set_jump_bits(it);
       // neighbours across edges and corners, for single-level meshes only
       // (27-point edge/corner ghosts and the pencil kernel's in-plane
       // neighbours; neither applies to a multi-level mesh): hop x, then y,

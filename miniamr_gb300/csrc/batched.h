@@ -28,11 +28,23 @@ struct BFace {
 // Per active block, in sorted_list order.
 struct BItem {
    int32_t slot;
-   int32_t bmask;      // bit l: face l is a domain boundary
+   int32_t bmask;      // bit l: face l is a domain boundary; bit 8 + l:
+                       // f[l] is FACE_COARSE; bit 16 + l: FACE_FINE
    BFace f[6];
    int32_t nb27[27];   // neighbour at offset (dx,dy,dz), index
                        // (dx+1) + 3(dy+1) + 9(dz+1); single-level meshes
 };
+
+// Sets the level-jump bits of it.bmask from its faces' types.
+__host__ __device__ inline void set_jump_bits(BItem &it)
+{
+   for (int l = 0; l < 6; l++) {
+      if (it.f[l].type == FACE_COARSE)
+         it.bmask |= 1 << (8 + l);
+      else if (it.f[l].type == FACE_FINE)
+         it.bmask |= 1 << (16 + l);
+   }
+}
 
 // ---- 27-point edge and corner ghosts on multi-level meshes ---------------
 // comm() (code 0) runs its phases x, y, z in turn, each writing the ghost

@@ -460,6 +460,7 @@ __global__ void build_items_kernel(const mamr_block *__restrict__ mesh, int n,
       if (bp.nei_level[l] == -2)
          it.bmask |= 1 << l;
    }
+   set_jump_bits(it);
    for (int d = 0; d < 27; d++) {
       int cur = bp.slot;
       if (single) {

@@ -119,19 +119,23 @@ __device__ __forceinline__ void st4(T *p, const T (&v)[4])
 // Queues the copies that fill the tiles of item (block sd[0], variables
 // var0 .. var0 + nv - 1; tile v at tile + v * SLAB): the interior rows, and
 // the face ghosts of same-level, boundary and coarser faces (the coarse
-// values unscaled).  sd = the block's BItem, ints 0..DESC-1.  Returns
-// whether the tiles need brick_fix (a face at a level jump).
+// values unscaled).  sd = the block's BItem, ints 0..DESC-1; sd[1] = its
+// bmask, whose bits 8.. and 16.. mark the coarse and fine faces.  The four
+// x/y face planes are one pass of 16-byte copies over the item's lanes (a
+// lane's chunk decides its face), the two z planes another, so that no
+// lane idles through a face it has no chunk of.  Returns whether the tiles
+// need brick_fix (a face at a level jump).
 template <typename T, int TPI, int VPI>
 __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
                                             const T *__restrict__ zf,
                                             const Geom &g, int var0, int nv,
                                             const int *sd, T *tile, int lane)
 {
-   bool fix = false;
    using B = Brick<T>;
    constexpr int VW = B::VW, R = B::R;
    const long long bv = g.bv;           // stride of consecutive variables
    const T *own = src + bv_offset(g, sd[0], var0);
+   const int bmask = sd[1];
 #pragma unroll
    for (int t = 0; t < 64 * R / TPI; t++) {
       const int c = lane + TPI * t, r = c / R, k = 1 + (c % R) * VW;
@@ -142,78 +146,103 @@ __device__ __forceinline__ bool brick_issue(const T *__restrict__ src,
             cp_async16(tile + v * B::SLAB + B::at(i, j, k),
                        own + v * bv + B::gat(i, j, k));
    }
+   // x/y faces W, E, S, N: 8 rows of R chunks each
 #pragma unroll
-   for (int l = 0; l < 6; l++) {
-      const int *f = sd + 2 + 7 * l;
-      const int type = f[0];
-      const int dir = l >> 1;
-      const bool low = !(l & 1);
-      const int gn = low ? 0 : 9;
-      const int zo = B::TILE + (low ? 0 : 64);   // z ghost plane in a tile
+   for (int t = 0; t < (32 * R + TPI - 1) / TPI; t++) {
+      const int c = lane + TPI * t;
+      if (c >= 32 * R)
+         break;
+      const int l = c / (8 * R), cc = c % (8 * R);
+      const int a = cc / R + 1, k = 1 + (cc % R) * VW;
+      const int type = sd[2 + 7 * l];
       if (type == FACE_SAME || type == FACE_BC) {
-         const T *sb = type == FACE_SAME ? src + bv_offset(g, f[1], var0)
-                                         : own;
+         const bool low = !(l & 1);
+         const int gn = low ? 0 : 9;
          // same level: the neighbour's near plane; boundary: reflection
          const int p = (type == FACE_SAME) == low ? 8 : 1;
-         if (dir < 2) {
-            for (int c = lane; c < 8 * R; c += TPI) {
-               const int a = c / R + 1, k = 1 + (c % R) * VW;
-               const int to = dir == 0 ? B::at(gn, a, k) : B::at(a, gn, k);
-               const int from = dir == 0 ? B::gat(p, a, k) : B::gat(a, p, k);
+         const T *sb = type == FACE_SAME ? src + bv_offset(g, sd[3 + 7 * l], var0)
+                                         : own;
+         const int to = l < 2 ? B::at(gn, a, k) : B::at(a, gn, k);
+         const int from = l < 2 ? B::gat(p, a, k) : B::gat(a, p, k);
 #pragma unroll
-               for (int v = 0; v < VPI; v++)
-                  if (v < nv)
-                     cp_async16(tile + v * B::SLAB + to, sb + v * bv + from);
-            }
-         } else if (zf) {
-            // the plane from the z-face array: 64 values as 16-byte copies
-            const int slot = type == FACE_SAME ? f[1] : sd[0];
-            const T *pl = zf + B::zf_at(g, slot, var0, p == 8);
-            if (lane < 64 / VW) {
+         for (int v = 0; v < VPI; v++)
+            if (v < nv)
+               cp_async16(tile + v * B::SLAB + to, sb + v * bv + from);
+      }
+   }
+   // z faces D, U: 64 values each, from the z-face arrays as 16-byte copies
+   // or, without them, value by value from the pool
+   if (zf) {
 #pragma unroll
-               for (int v = 0; v < VPI; v++)
-                  if (v < nv)
-                     cp_async16(tile + v * B::SLAB + zo + lane * VW,
-                                pl + v * 128 + lane * VW);
-            }
-         } else {
-#pragma unroll
-            for (int u = 0; u < 64 / TPI; u++) {
-               const int e = lane + TPI * u, i = (e >> 3) + 1, j = (e & 7) + 1;
-#pragma unroll
-               for (int v = 0; v < VPI; v++)
-                  if (v < nv)
-                     cp_async_elem(tile + v * B::SLAB + zo + e,
-                                   sb + v * bv + B::gat(i, j, p));
-            }
-         }
-      } else if (type == FACE_COARSE) {
-         fix = true;
-         const T *sb = src + bv_offset(g, f[1], var0);
-         const int p = low ? 8 : 1, iq = f[5], jq = f[6];
-#pragma unroll
-         for (int u = 0; u < 64 / TPI; u++) {
-            const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
-            const int ca = (a + 1) / 2 + 4 * jq, cb = (b + 1) / 2 + 4 * iq;
-            const int to = dir < 2 ? B::ghost_at(dir, gn, a, b) : zo + e;
-            const T *from =
-               dir < 2 ? sb + B::face_gat(dir, p, ca, cb)
-                       : (zf ? zf + B::zf_at(g, f[1], var0, p == 8) +
-                                  (ca - 1) * 8 + (cb - 1)
-                             : sb + B::face_gat(dir, p, ca, cb));
-            // the variable stride of the source: the pool's, or the
-            // z-face array's 128 values per block-variable
-            const long long vs = dir == 2 && zf ? 128 : bv;
+      for (int t = 0; t < (2 * 64 / VW + TPI - 1) / TPI; t++) {
+         const int c = lane + TPI * t;
+         if (c >= 2 * 64 / VW)
+            break;
+         const int l = 4 + c / (64 / VW), cc = c % (64 / VW);
+         const int type = sd[2 + 7 * l];
+         if (type == FACE_SAME || type == FACE_BC) {
+            const bool low = l == 4;
+            const int p = (type == FACE_SAME) == low ? 8 : 1;
+            const int slot = type == FACE_SAME ? sd[3 + 7 * l] : sd[0];
+            const T *pl = zf + B::zf_at(g, slot, var0, p == 8) + cc * VW;
+            T *to = tile + B::TILE + (low ? 0 : 64) + cc * VW;
 #pragma unroll
             for (int v = 0; v < VPI; v++)
                if (v < nv)
-                  cp_async_elem(tile + v * B::SLAB + to, from + v * vs);
+                  cp_async16(to + v * B::SLAB, pl + v * 128);
          }
-      } else {
-         fix = true;                   // finer neighbours: summed later
+      }
+   } else {
+#pragma unroll
+      for (int t = 0; t < 128 / TPI; t++) {
+         const int c = lane + TPI * t, l = 4 + (c >> 6), e = c & 63;
+         const int type = sd[2 + 7 * l];
+         if (type == FACE_SAME || type == FACE_BC) {
+            const bool low = l == 4;
+            const int p = (type == FACE_SAME) == low ? 8 : 1;
+            const T *sb = type == FACE_SAME
+                             ? src + bv_offset(g, sd[3 + 7 * l], var0)
+                             : own;
+            const int i = (e >> 3) + 1, j = (e & 7) + 1;
+#pragma unroll
+            for (int v = 0; v < VPI; v++)
+               if (v < nv)
+                  cp_async_elem(tile + v * B::SLAB + B::TILE + (low ? 0 : 64) +
+                                   e,
+                                sb + v * bv + B::gat(i, j, p));
+         }
       }
    }
-   return fix;
+   // coarser neighbours: one value per ghost cell (each used by 2 x 2)
+   for (unsigned cm = (bmask >> 8) & 63; cm; cm &= cm - 1) {
+      const int l = __ffs(cm) - 1;
+      const int *f = sd + 2 + 7 * l;
+      const int dir = l >> 1;
+      const bool low = !(l & 1);
+      const int gn = low ? 0 : 9;
+      const int zo = B::TILE + (low ? 0 : 64);
+      const T *sb = src + bv_offset(g, f[1], var0);
+      const int p = low ? 8 : 1, iq = f[5], jq = f[6];
+#pragma unroll
+      for (int u = 0; u < 64 / TPI; u++) {
+         const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
+         const int ca = (a + 1) / 2 + 4 * jq, cb = (b + 1) / 2 + 4 * iq;
+         const int to = dir < 2 ? B::ghost_at(dir, gn, a, b) : zo + e;
+         const T *from =
+            dir < 2 ? sb + B::face_gat(dir, p, ca, cb)
+                    : (zf ? zf + B::zf_at(g, f[1], var0, p == 8) +
+                               (ca - 1) * 8 + (cb - 1)
+                          : sb + B::face_gat(dir, p, ca, cb));
+         // the variable stride of the source: the pool's, or the z-face
+         // array's 128 values per block-variable
+         const long long vs = dir == 2 && zf ? 128 : bv;
+#pragma unroll
+         for (int v = 0; v < VPI; v++)
+            if (v < nv)
+               cp_async_elem(tile + v * B::SLAB + to, from + v * vs);
+      }
+   }
+   return (bmask & 0x3f3f00) != 0;
 }
 
 // After the copies landed: coarse ghosts scaled by 1/4 (each lane the
@@ -227,12 +256,26 @@ __device__ __forceinline__ void brick_fix(const T *__restrict__ src,
 {
    using B = Brick<T>;
    const long long bv = g.bv;
+   const int bmask = sd[1];
+   for (unsigned cm = (bmask >> 8) & 63; cm; cm &= cm - 1) {
+      const int l = __ffs(cm) - 1;
+      const int dir = l >> 1, gn = (l & 1) ? 9 : 0;
 #pragma unroll
-   for (int l = 0; l < 6; l++) {
+      for (int u = 0; u < 64 / TPI; u++) {
+         const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
+         const int to = dir < 2 ? B::ghost_at(dir, gn, a, b)
+                                : B::TILE + (gn ? 64 : 0) + e;
+#pragma unroll
+         for (int v = 0; v < VPI; v++)
+            if (v < nv) {
+               T &x = tile[v * B::SLAB + to];
+               x = quarter(x);
+            }
+      }
+   }
+   for (unsigned fm = (bmask >> 16) & 63; fm; fm &= fm - 1) {
+      const int l = __ffs(fm) - 1;
       const int *f = sd + 2 + 7 * l;
-      const int type = f[0];
-      if (type != FACE_COARSE && type != FACE_FINE)
-         continue;
       const int dir = l >> 1;
       const bool low = !(l & 1);
       const int gn = low ? 0 : 9, p = low ? 8 : 1;
@@ -241,54 +284,45 @@ __device__ __forceinline__ void brick_fix(const T *__restrict__ src,
          const int e = lane + TPI * u, a = (e >> 3) + 1, b = (e & 7) + 1;
          const int to = dir < 2 ? B::ghost_at(dir, gn, a, b)
                                 : B::TILE + (low ? 0 : 64) + e;
-         if (type == FACE_COARSE) {
-#pragma unroll
-            for (int v = 0; v < VPI; v++)
-               if (v < nv) {
-                  T &x = tile[v * B::SLAB + to];
-                  x = quarter(x);
-               }
+         const int jq = a > 4, iq = b > 4;
+         const int a2 = a - 4 * jq, b2 = b - 4 * iq;
+         const int nbs = f[1 + iq * 2 + jq];
+         // the four fine cells: from the fine block's z-face array (plane
+         // p, 128 values per block-variable) or its pool cells
+         const T *q0;
+         int o[4];
+         long long vs;
+         if (dir == 2 && zf) {
+            q0 = zf + B::zf_at(g, nbs, var0, p == 8);
+            o[0] = (2 * a2 - 2) * 8 + 2 * b2 - 2;
+            o[1] = o[0] + 1;
+            o[2] = o[0] + 8;
+            o[3] = o[0] + 9;
+            vs = 128;
          } else {
-            const int jq = a > 4, iq = b > 4;
-            const int a2 = a - 4 * jq, b2 = b - 4 * iq;
-            const int nbs = f[1 + iq * 2 + jq];
-            // the four fine cells: from the fine block's z-face array
-            // (plane p, 128 values per block-variable) or its pool cells
-            const T *q0;
-            int o[4];
-            long long vs;
-            if (dir == 2 && zf) {
-               q0 = zf + B::zf_at(g, nbs, var0, p == 8);
-               o[0] = (2 * a2 - 2) * 8 + 2 * b2 - 2;
-               o[1] = o[0] + 1;
-               o[2] = o[0] + 8;
-               o[3] = o[0] + 9;
-               vs = 128;
-            } else {
-               q0 = src + bv_offset(g, nbs, var0);
-               o[0] = B::face_gat(dir, p, 2 * a2 - 1, 2 * b2 - 1);
-               o[1] = B::face_gat(dir, p, 2 * a2 - 1, 2 * b2);
-               o[2] = B::face_gat(dir, p, 2 * a2, 2 * b2 - 1);
-               o[3] = B::face_gat(dir, p, 2 * a2, 2 * b2);
-               vs = bv;
-            }
-            T w[VPI][4];
-#pragma unroll
-            for (int v = 0; v < VPI; v++)
-               if (v < nv) {
-#pragma unroll
-                  for (int m = 0; m < 4; m++)
-                     w[v][m] = q0[v * vs + o[m]];
-               }
-#pragma unroll
-            for (int v = 0; v < VPI; v++)
-               if (v < nv) {
-                  T t = w[v][0] + w[v][1];
-                  t = t + w[v][2];
-                  t = t + w[v][3];
-                  tile[v * B::SLAB + to] = t;
-               }
+            q0 = src + bv_offset(g, nbs, var0);
+            o[0] = B::face_gat(dir, p, 2 * a2 - 1, 2 * b2 - 1);
+            o[1] = B::face_gat(dir, p, 2 * a2 - 1, 2 * b2);
+            o[2] = B::face_gat(dir, p, 2 * a2, 2 * b2 - 1);
+            o[3] = B::face_gat(dir, p, 2 * a2, 2 * b2);
+            vs = bv;
          }
+         T w[VPI][4];
+#pragma unroll
+         for (int v = 0; v < VPI; v++)
+            if (v < nv) {
+#pragma unroll
+               for (int m = 0; m < 4; m++)
+                  w[v][m] = q0[v * vs + o[m]];
+            }
+#pragma unroll
+         for (int v = 0; v < VPI; v++)
+            if (v < nv) {
+               T t = w[v][0] + w[v][1];
+               t = t + w[v][2];
+               t = t + w[v][3];
+               tile[v * B::SLAB + to] = t;
+            }
       }
    }
 }

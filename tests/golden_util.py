@@ -53,7 +53,7 @@ def arg(args, flag, default=None):
 # Cases too large to replay through the CPU oracle inside the CPU suite;
 # they are pinned by make_golden.py (hybrid == reference) and replayed on
 # the GPU.
-HEAVY = {"config2", "config5", "config5_300"}
+HEAVY = {"config2", "config5", "config5_300", "config5_named_mesh"}
 
 
 def hashed_stages(hashes, V):

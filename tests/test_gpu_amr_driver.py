@@ -11,9 +11,12 @@ runs.
 * config 2 (the AMR sphere run, 16^3 blocks, 27-point, 100 timesteps) and
   config 5 (four moving objects, 8^3 blocks, up to ~23k blocks on six
   levels, 20 timesteps) at full size, the same checks;
-* config 5 at its full 40 variables and 300 timesteps (150 refinements):
+* config 5 at its full 40 variables and 300 timesteps (151 refinements):
   FP64 checksums bit-identical to the reference's own log, meshes equal,
-  and FP32 cells within 1e-6 relative of them at every checksum.
+  and FP32 cells within 1e-6 relative of them at every checksum;
+* config 5 with its objects at the sizes the benchmark's description names
+  (30k-53k blocks), 300 timesteps on 2^3-cell blocks: every mesh and
+  checksum the reference's.
 """
 import os
 
@@ -65,3 +68,17 @@ def test_config5_300_timesteps(gpu_lib, oracle_lib):
     _, s32, _, _ = run_case(gpu_lib, args, fp32=True)
     rel = np.abs(s32 - sums) / np.abs(sums)
     assert rel.max() <= 1e-6, rel.max()
+
+
+def test_command_line(gpu_lib, capsys):
+    """python -m miniamr_gb300.run with a recorded case's own options:
+    exits 0 (every checksum within the case's tolerance) and prints the
+    reference's final checksums."""
+    from miniamr_gb300 import run as runmod
+    args = cases()["amr7"]["args"]
+    assert runmod.main(args) == 0
+    out = capsys.readouterr().out
+    ref, _, _ = reflog("amr7")
+    V = int(args[args.index("--num_vars") + 1])
+    assert f"{ref[-V][1]:.15e}" in out
+    assert runmod.main(args + ["--fp32"]) == 0
