@@ -272,7 +272,8 @@ int mamr_launch_count(mamr_ctx *ctx, int64_t *count);
  * changes.  blocks[] lists the active blocks (any order); block_refine[i]
  * receives blocks[i]'s flag and parent_refine[p] parents[p]'s for the
  * active entries.  The cell block size is the context's.  Returns
- * MAMR_EINVAL for indices out of range. */
+ * MAMR_EINVAL for indices out of range.  May be called from any host
+ * thread (it makes the context's device current on that thread). */
 int mamr_mark_refine(mamr_ctx *ctx, const mamr_mark_params *params,
                      const mamr_object *objects, int32_t n_objects,
                      const mamr_mark_block *blocks, int32_t n_blocks,
@@ -318,18 +319,21 @@ typedef void (*mamr_amr_event)(void *user, int32_t kind, int32_t ts,
                                const int64_t *numbers, const int32_t *cen);
 
 typedef struct {
+   /* The refinement bookkeeping and marking depend on no cell value, so
+    * they run on a second host thread (with a marking context of their
+    * own) ahead of the stages; the stage side applies each refinement's
+    * job lists and mesh in order.  All times leave out the caller's event
+    * callback. */
    double stage_seconds;    /* wall time of the stage stretches */
-   double refine_seconds;   /* refine() calls: the four parts below */
-   double total_seconds;    /* the whole call (all times leave out the
-                               caller's event callback) */
-   double mark_seconds;     /* mamr_mark_refine calls (lists in, flags out) */
-   double bookkeeping_seconds; /* host: marking lists, split and
-                               consolidation records, job lists */
-   double data_seconds;     /* mamr_split / mamr_consolidate calls (the
-                               device work they queue overlaps the next
-                               step's host work and completes before the
-                               next marking returns) */
-   double mesh_seconds;     /* mesh export and mamr_set_mesh, completed */
+   double refine_seconds;   /* stage side's refinements: waiting for the
+                               planning thread, data movement, mesh */
+   double total_seconds;    /* the whole call */
+   double mark_seconds;     /* planning thread: mamr_mark_refine calls */
+   double bookkeeping_seconds; /* planning thread: marking lists, split
+                               and consolidation records, meshes */
+   double data_seconds;     /* mamr_split / mamr_consolidate calls */
+   double mesh_seconds;     /* mamr_set_mesh, completed */
+   double wait_seconds;     /* stage side waiting for the planning thread */
    int64_t updates;         /* cell-variable updates of the stages (the
                                reference's total_blocks x cells x vars) */
    int32_t refinements;     /* refine() calls, the initial one included */
@@ -360,7 +364,11 @@ typedef struct {
  * checksums (num_vars) and then each checksum stage's num_vars sums, as
  * the reference's check_sum calls produce them, up to max_sums values;
  * *n_sums the count.  event (may be NULL) is called with user for each
- * split and consolidation list and each mesh.  The tolerance check of
+ * split and consolidation list and each mesh, in the reference's order, on
+ * the calling thread.  The refinement bookkeeping and marking run ahead of
+ * the stages on a second host thread, through a marking context of their
+ * own (the same block shape, one variable, max_blocks slots: one more
+ * single-variable pool for the call's duration).  The tolerance check of
  * ref/driver.c:96-101 is left to the caller.  Needs lb_method 0 (the
  * reference's default) and one rank. */
 int mamr_amr_run(mamr_ctx *ctx, const mamr_config *cfg,

@@ -106,7 +106,8 @@ class AmrStats(C.Structure):
         ("stage_seconds", C.c_double), ("refine_seconds", C.c_double),
         ("total_seconds", C.c_double), ("mark_seconds", C.c_double),
         ("bookkeeping_seconds", C.c_double), ("data_seconds", C.c_double),
-        ("mesh_seconds", C.c_double), ("updates", C.c_int64),
+        ("mesh_seconds", C.c_double), ("wait_seconds", C.c_double),
+        ("updates", C.c_int64),
         ("refinements", C.c_int32), ("marking_steps", C.c_int32),
         ("max_active", C.c_int32), ("final_active", C.c_int32),
         ("stretches", C.c_int32), ("plain_stretches", C.c_int32),

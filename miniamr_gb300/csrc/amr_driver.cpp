@@ -14,10 +14,14 @@
 // source runs over the GPU library and over the CPU oracle.
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "miniamr_gb300.h"
@@ -494,6 +498,204 @@ double lap(double &t)
    return d;
 }
 
+// One refinement as the stages see it: the split and consolidation job
+// lists of its steps in order, then the mesh it leaves.
+struct Plan {
+   int ts = 0;
+   std::vector<std::vector<mamr_split_job>> split;
+   std::vector<std::vector<mamr_consolidate_job>> cons;
+   std::vector<mamr_block> mesh;
+   std::vector<int64_t> numbers;
+   std::vector<int32_t> cen;
+   int active = 0;
+};
+
+// The refinement side of the run: the octree bookkeeping and the marking,
+// on a thread of its own.  Nothing it computes depends on cell values --
+// the marking reads the mesh and the objects, the objects move by their
+// own arithmetic -- so it runs ahead of the stages and hands each
+// refinement over as a Plan through a short queue; the stage side applies
+// them in order.  The marking goes through a context of its own (one
+// variable), so that its device work does not wait behind the stages.
+class Planner {
+ public:
+   Planner(mamr_ctx *mctx, const mamr_amr_params &p,
+           const std::vector<mamr_amr_object> &objs, int cap)
+      : mctx_(mctx), prm_(p), objs_(objs),
+        mesh_(p.init_x, p.init_y, p.init_z, p.num_refine, cap)
+   {
+      mesh_.init();
+   }
+   ~Planner() { stop(); }
+
+   // The initial lattice's mesh (before the thread starts).
+   void initial(Plan &out) const
+   {
+      mesh_.export_mesh(out.mesh, out.numbers, out.cen);
+      out.active = mesh_.active();
+   }
+
+   void start()
+   {
+      th_ = std::thread([this] { body(); });
+   }
+
+   // The next refinement, in order; false once the planner has none left.
+   bool pop(Plan &out)
+   {
+      std::unique_lock<std::mutex> lk(mu_);
+      cv_.wait(lk, [this] { return !q_.empty() || done_; });
+      if (q_.empty()) {
+         if (err_)
+            throw Fail{err_, err_msg_};
+         return false;
+      }
+      out = std::move(q_.front());
+      q_.pop_front();
+      cv_.notify_all();
+      return true;
+   }
+
+   void stop()
+   {
+      {
+         std::lock_guard<std::mutex> lk(mu_);
+         stop_ = true;
+      }
+      cv_.notify_all();
+      if (th_.joinable())
+         th_.join();
+   }
+
+   double mark_s = 0.0, book_s = 0.0;
+   int marking_steps = 0;
+
+ private:
+   static constexpr size_t kAhead = 3;   // refinements planned ahead
+
+   void push(Plan &&p)
+   {
+      std::unique_lock<std::mutex> lk(mu_);
+      cv_.wait(lk, [this] { return q_.size() < kAhead || stop_; });
+      if (stop_)
+         throw Fail{MAMR_OK, ""};
+      q_.push_back(std::move(p));
+      cv_.notify_all();
+   }
+
+   void body()
+   {
+      try {
+         if (prm_.num_refine || prm_.uniform_refine)
+            refine(0);
+         // ref/driver.c:110-117: move() every timestep, refine() every
+         // refine_freq timesteps
+         if (prm_.num_refine && !prm_.uniform_refine) {
+            const int n_ts = std::max(1, prm_.num_tsteps);
+            for (int ts = 1; ts <= n_ts; ts++) {
+               move(objs_, 1.0);
+               if (!(ts % prm_.refine_freq))
+                  refine(ts);
+            }
+         }
+      } catch (const Fail &f) {
+         std::lock_guard<std::mutex> lk(mu_);
+         if (f.code != MAMR_OK) {
+            err_ = f.code;
+            err_msg_ = f.msg;
+         }
+      } catch (const std::bad_alloc &) {
+         std::lock_guard<std::mutex> lk(mu_);
+         err_ = MAMR_ENOMEM;
+         err_msg_ = "host allocation";
+      }
+      std::lock_guard<std::mutex> lk(mu_);
+      done_ = true;
+      cv_.notify_all();
+   }
+
+   // refine(ts) (ref/refine.c:38-210) on one rank: num_refine steps at
+   // ts 0, block_change steps after, each the marking, the splits and the
+   // consolidations.
+   void refine(int ts)
+   {
+      Plan plan;
+      plan.ts = ts;
+      const int steps = ts ? (prm_.block_change ? prm_.block_change
+                                                : prm_.num_refine)
+                           : prm_.num_refine;
+      std::vector<mamr_mark_block> mb;
+      std::vector<mamr_mark_parent> pa;
+      std::vector<int32_t> bref, pref;
+      std::vector<mamr_object> mo(objs_.size());
+      mamr_mark_params mp;
+      memset(&mp, 0, sizeof(mp));
+      mp.num_refine = prm_.num_refine;
+      mp.refine_ghost = prm_.refine_ghost;
+      mp.uniform_refine = prm_.uniform_refine;
+      const int size = 1 << (prm_.num_refine + 1);
+      mp.mesh_size[0] = prm_.init_x * size;
+      mp.mesh_size[1] = prm_.init_y * size;
+      mp.mesh_size[2] = prm_.init_z * size;
+      for (int i = 0; i < steps; i++) {
+         double t = now();
+         for (size_t o = 0; o < objs_.size(); o++) {
+            mo[o].type = objs_[o].type;
+            mo[o].reserved = 0;
+            for (int d = 0; d < 3; d++) {
+               mo[o].cen[d] = objs_[o].cen[d];
+               mo[o].size[d] = objs_[o].size[d];
+            }
+         }
+         mesh_.mark_lists(mb, pa);
+         bref.assign(mb.size() + 1, 0);
+         pref.assign(pa.size() + 1, 0);
+         book_s += lap(t);
+         check(mamr_mark_refine(mctx_, &mp,
+                                prm_.uniform_refine ? nullptr : mo.data(),
+                                prm_.uniform_refine ? 0
+                                                    : (int32_t) mo.size(),
+                                mb.data(), (int32_t) mb.size(), pa.data(),
+                                (int32_t) pa.size(), bref.data(),
+                                pref.data()),
+               "mamr_mark_refine");
+         mark_s += lap(t);
+         marking_steps++;
+         mesh_.set_flags(mb, bref, pref);
+         plan.split.emplace_back();
+         plan.cons.emplace_back();
+         mesh_.split(plan.split.back());
+         mesh_.consolidate(plan.cons.back());
+         book_s += lap(t);
+         // a step that changed nothing leaves the marking's inputs as they
+         // were (it starts from reset flags, and the objects move only
+         // between refinements), so the remaining steps change nothing
+         // either
+         if (plan.split.back().empty() && plan.cons.back().empty())
+            break;
+      }
+      double t = now();
+      mesh_.export_mesh(plan.mesh, plan.numbers, plan.cen);
+      plan.active = mesh_.active();
+      book_s += lap(t);
+      push(std::move(plan));
+   }
+
+   mamr_ctx *mctx_;
+   const mamr_amr_params &prm_;
+   std::vector<mamr_amr_object> objs_;
+   Mesh mesh_;
+   std::thread th_;
+   std::mutex mu_;
+   std::condition_variable cv_;
+   std::deque<Plan> q_;
+   bool done_ = false, stop_ = false;
+   int err_ = MAMR_OK;
+   std::string err_msg_;
+};
+
+// The stage side: the cell data, the stages and each refinement's data
+// movement and mesh, in the reference driver's order.
 struct Run {
    mamr_ctx *ctx;
    const mamr_config &cfg;
@@ -504,8 +706,8 @@ struct Run {
    mamr_amr_event event;
    void *user;
    mamr_amr_stats st{};
-   Mesh mesh;
-   int flags;   // the stretches' run flags (batched until it is refused)
+   int flags;    // the stretches' run flags (batched until it is refused)
+   int active = 0;
    double ev_s = 0.0;   // time spent in the caller's event callback, which
                         // the stats leave out
 
@@ -520,9 +722,7 @@ struct Run {
    }
 
    Run(mamr_ctx *c, const mamr_config &cf, const mamr_amr_params &p)
-      : ctx(c), cfg(cf), prm(p), mesh(p.init_x, p.init_y, p.init_z,
-                                      p.num_refine, cf.max_blocks),
-        flags(p.run_flags)
+      : ctx(c), cfg(cf), prm(p), flags(p.run_flags)
    {
    }
 
@@ -532,98 +732,48 @@ struct Run {
          sums[n_sums++] = s[q];
    }
 
-   void set_mesh(int ts, bool report)
+   void set_mesh(const Plan &p)
    {
-      std::vector<mamr_block> m;
-      std::vector<int64_t> numbers;
-      std::vector<int32_t> cen;
-      mesh.export_mesh(m, numbers, cen);
-      check(mamr_set_mesh(ctx, m.data(), (int32_t) m.size()),
+      check(mamr_set_mesh(ctx, p.mesh.data(), (int32_t) p.mesh.size()),
             "mamr_set_mesh");
-      if (report)
-         emit(3, ts, m.data(), (int32_t) m.size(), numbers.data(),
-              cen.data());
-      st.max_active = std::max(st.max_active, (int32_t) m.size());
+      active = p.active;
+      st.max_active = std::max(st.max_active, (int32_t) p.mesh.size());
    }
 
-   // refine(ts) (ref/refine.c:38-210) on one rank: num_refine steps at
-   // ts 0, block_change steps after, each the marking, the splits and the
-   // consolidations.
-   void refine(int ts)
+   // One refinement from the planner: its job lists, then its mesh.
+   void apply(Planner &pl)
    {
       const double t0 = now(), ev0 = ev_s;
-      const int steps = ts ? (prm.block_change ? prm.block_change
-                                               : prm.num_refine)
-                           : prm.num_refine;
-      std::vector<mamr_mark_block> mb;
-      std::vector<mamr_mark_parent> pa;
-      std::vector<int32_t> bref, pref;
-      std::vector<mamr_object> mo(objs.size());
-      std::vector<mamr_split_job> sj;
-      std::vector<mamr_consolidate_job> cj;
-      mamr_mark_params mp;
-      memset(&mp, 0, sizeof(mp));
-      mp.num_refine = prm.num_refine;
-      mp.refine_ghost = prm.refine_ghost;
-      mp.uniform_refine = prm.uniform_refine;
-      const int size = 1 << (prm.num_refine + 1);
-      mp.mesh_size[0] = prm.init_x * size;
-      mp.mesh_size[1] = prm.init_y * size;
-      mp.mesh_size[2] = prm.init_z * size;
-      for (int i = 0; i < steps; i++) {
-         double t = now();
-         for (size_t o = 0; o < objs.size(); o++) {
-            mo[o].type = objs[o].type;
-            mo[o].reserved = 0;
-            for (int d = 0; d < 3; d++) {
-               mo[o].cen[d] = objs[o].cen[d];
-               mo[o].size[d] = objs[o].size[d];
-            }
-         }
-         mesh.mark_lists(mb, pa);
-         bref.assign(mb.size() + 1, 0);
-         pref.assign(pa.size() + 1, 0);
-         st.bookkeeping_seconds += lap(t);
-         check(mamr_mark_refine(ctx, &mp,
-                                prm.uniform_refine ? nullptr : mo.data(),
-                                prm.uniform_refine ? 0
-                                                   : (int32_t) mo.size(),
-                                mb.data(), (int32_t) mb.size(), pa.data(),
-                                (int32_t) pa.size(), bref.data(),
-                                pref.data()),
-               "mamr_mark_refine");
-         st.mark_seconds += lap(t);
-         st.marking_steps++;
-         mesh.set_flags(mb, bref, pref);
-         mesh.split(sj);
-         st.bookkeeping_seconds += lap(t);
-         if (!sj.empty()) {
-            check(mamr_split(ctx, sj.data(), (int32_t) sj.size()),
+      Plan p;
+      if (!pl.pop(p))
+         throw Fail{MAMR_EINVAL, "refinement plan missing"};
+      double t = now();
+      st.wait_seconds += t - t0;
+      for (size_t i = 0; i < p.split.size(); i++) {
+         if (!p.split[i].empty()) {
+            check(mamr_split(ctx, p.split[i].data(),
+                             (int32_t) p.split[i].size()),
                   "mamr_split");
             st.data_seconds += lap(t);
-            emit(1, ts, sj.data(), (int32_t) sj.size(), nullptr, nullptr);
+            emit(1, p.ts, p.split[i].data(), (int32_t) p.split[i].size(),
+                 nullptr, nullptr);
+            t = now();
          }
-         t = now();
-         mesh.consolidate(cj);
-         st.bookkeeping_seconds += lap(t);
-         if (!cj.empty()) {
-            check(mamr_consolidate(ctx, cj.data(), (int32_t) cj.size()),
+         if (!p.cons[i].empty()) {
+            check(mamr_consolidate(ctx, p.cons[i].data(),
+                                   (int32_t) p.cons[i].size()),
                   "mamr_consolidate");
             st.data_seconds += lap(t);
-            emit(2, ts, cj.data(), (int32_t) cj.size(), nullptr, nullptr);
+            emit(2, p.ts, p.cons[i].data(), (int32_t) p.cons[i].size(),
+                 nullptr, nullptr);
+            t = now();
          }
-         // a step that changed nothing leaves the marking's inputs as they
-         // were (it starts from reset flags, and the objects move only
-         // between refinements), so the remaining steps change nothing
-         // either
-         if (sj.empty() && cj.empty())
-            break;
       }
-      double t = now();
-      const double ev_mesh = ev_s;
-      set_mesh(ts, true);
+      set_mesh(p);
       check(mamr_sync(ctx), "mamr_sync");
-      st.mesh_seconds += lap(t) - (ev_s - ev_mesh);
+      st.mesh_seconds += lap(t);
+      emit(3, p.ts, p.mesh.data(), (int32_t) p.mesh.size(), p.numbers.data(),
+           p.cen.data());
       st.refinements++;
       st.refine_seconds += now() - t0 - (ev_s - ev0);
    }
@@ -655,11 +805,11 @@ struct Run {
       check(mamr_sync(ctx), "mamr_sync");
       st.stage_seconds += now() - t0;
       put_sums(s.data(), (int64_t) got * V);
-      st.updates += (int64_t) n_ts * spt * mesh.active() *
+      st.updates += (int64_t) n_ts * spt * active *
                     ((int64_t) cfg.nx * cfg.ny * cfg.nz) * V;
    }
 
-   void run()
+   void run(mamr_ctx *mctx)
    {
       const double t0 = now();
       const int V = cfg.num_vars;
@@ -671,9 +821,9 @@ struct Run {
          check(mamr_set_work_params(ctx, a1, a0.data(), V / 4),
                "mamr_set_work_params");
       }
+      Planner pl(mctx, prm, objs, cfg.max_blocks);
       // init(): the lattice, its values (one rand() stream over all the
       // initial blocks, so generated at once) and their checksums
-      mesh.init();
       const int n0 = prm.init_x * prm.init_y * prm.init_z;
       {
          const size_t per = (size_t) V * (cfg.nx + 2) * (cfg.ny + 2) *
@@ -687,14 +837,19 @@ struct Run {
          check(mamr_upload_blocks(ctx, slots.data(), n0, all.data()),
                "mamr_upload_blocks");
       }
-      set_mesh(0, false);
+      {
+         Plan init;
+         pl.initial(init);
+         set_mesh(init);
+      }
+      pl.start();
       for (int var = 0; var < V; var++) {
          double s = 0.0;
          check(mamr_check_sum(ctx, var, &s), "mamr_check_sum");
          put_sums(&s, 1);
       }
       if (prm.num_refine || prm.uniform_refine)
-         refine(0);
+         apply(pl);
       // ref/driver.c:66-140: stages, move, refine every refine_freq; the
       // loop tests for the end after the first timestep, so it runs at
       // least one
@@ -709,14 +864,15 @@ struct Run {
             first_ts = ts + 1;
             pending = 0;
          }
-         if (moving) {
-            move(objs, 1.0);
-            if (refine_now)
-               refine(ts);
-         }
+         if (refine_now)
+            apply(pl);
       }
+      pl.stop();
+      st.mark_seconds = pl.mark_s;
+      st.bookkeeping_seconds = pl.book_s;
+      st.marking_steps = pl.marking_steps;
       check(mamr_sync(ctx), "mamr_sync");
-      st.final_active = mesh.active();
+      st.final_active = active;
       st.total_seconds = now() - t0 - ev_s;
    }
 };
@@ -748,9 +904,18 @@ extern "C" int mamr_amr_run(mamr_ctx *ctx, const mamr_config *cfg,
    run.max_sums = max_sums;
    run.event = event;
    run.user = user;
-   int status = MAMR_OK;
+   // the marking's own context: the block shape, one variable
+   mamr_config mc = *cfg;
+   mc.num_vars = 1;
+   mc.stencil = cfg->stencil == 27 ? 27 : 7;
+   mc.code = 0;
+   mc.permute = 0;
+   mamr_ctx *mctx = nullptr;
+   int status = mamr_create(&mc, &mctx);
+   if (status != MAMR_OK)
+      return status;
    try {
-      run.run();
+      run.run(mctx);
    } catch (const Fail &f) {
       status = f.code;
       char buf[400];
@@ -760,6 +925,7 @@ extern "C" int mamr_amr_run(mamr_ctx *ctx, const mamr_config *cfg,
       status = MAMR_ENOMEM;
       mamr_driver_fail(status, "mamr_amr_run: host allocation");
    }
+   mamr_destroy(mctx);
    if (n_sums)
       *n_sums = run.n_sums;
    if (stats)

@@ -1522,6 +1522,10 @@ extern "C" int mamr_mark_refine(mamr_ctx *c, const mamr_mark_params *p,
 {
    if (!c || (nb && !block_refine) || (np && !parent_refine))
       return fail(MAMR_EINVAL, "mark_refine: bad arguments");
+   // callable from any host thread: the context's device
+   int cur_dev = -1;
+   if (cudaGetDevice(&cur_dev) == cudaSuccess && cur_dev != c->device)
+      CUDA_TRY(cudaSetDevice(c->device));
    const int32_t cap = c->cfg.max_blocks;
    std::vector<unsigned char> listed((size_t) cap + 1, 0);
    if (const char *msg = mamr_mark_validate(p, objs, n_objs, mb, nb, pa, np,
