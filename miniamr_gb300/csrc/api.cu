@@ -195,6 +195,9 @@ static int check_error_word(mamr_ctx *c)
                      "fixed-point range (|v| < 1024, finite)");
       if (h & ERR_MARK)
          return fail(MAMR_EDEVICE, "refinement marking did not settle");
+      if (h & ERR_WAIT)
+         return fail(MAMR_EDEVICE, "a stage kernel's wait for its tensor "
+                     "copies ran out (results of the run are invalid)");
       return fail(MAMR_EDEVICE, "device error word 0x%x", h);
    }
    return MAMR_OK;
@@ -1353,12 +1356,13 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
             V, flags, (double *) B->partials.p, acc, c->stream);
          return f < 0 ? -1 : k + f;
       };
+      const long long n_bv = (long long) c->cfg.max_blocks * V;
       if (pencil && c->fp32)
          return fallback(launch_pencil_stage(
             (const float *) cur, (float *) oth, c->g, c->cfg.stencil,
             (const BItem *) B->items.p, nb, (const TileDesc *) B->chain.p,
             (const int2 *) B->pencils.p, np, sh, last, do_cs, part, sums_at,
-            acc, flags, c->stream));
+            acc, flags, c->d_err, n_bv, c->stream));
       if (pencil)
          return launch_pencil_stage((const double *) cur, (double *) oth,
                                     c->g, c->cfg.stencil,
@@ -1366,7 +1370,7 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
                                     (const TileDesc *) B->chain.p,
                                     (const int2 *) B->pencils.p, np, sh, last,
                                     do_cs, part, sums_at, acc, c->d_err,
-                                    c->stream);
+                                    c->d_err, n_bv, c->stream);
       if (c->fp32)
          return fallback(launch_batched_stage(
             (const float *) cur, (float *) oth, c->g, c->cfg.stencil,

@@ -284,6 +284,8 @@ void batched_mesh_changed(BatchedState *b);
 //   pencil kernel:  `rows` j-rows and `planes` i-planes per thread
 //                   (threads = 1024 / (rows * planes))
 //   both:           `grid` CTAs
+//   pencil kernel with tensor copies (FP32; kernel = 3): the interior and
+//                   x-face planes of each tile arrive by bulk tensor copy
 //   warp-per-item kernel (8^3 blocks, 7-point; kernel = 1): threads = 32
 //                   or 64 per item, vpc = items per CTA, rows = rows per
 //                   thread, planes = variables per item (1 or 2)
@@ -355,7 +357,7 @@ int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
                         int n_pencils, const StageShape &sh, int write_ghosts,
                         int do_cs, double *partials, double *sums,
                         unsigned long long *acc, unsigned *err,
-                        cudaStream_t s);
+                        unsigned *ctx_err, long long n_bv, cudaStream_t s);
 // FP64 checksums of every (block, variable) of a pool in the reference's
 // order: per-block serial sums into partials[var][block] (one thread per
 // block-variable), then sums[var] serially over blocks.  Returns the

@@ -74,7 +74,8 @@ constexpr unsigned long long kChecksumFallbackMark = 0x8000000000000000ull;
 enum : unsigned {
    ERR_FIXED_RANGE = 1u,   // a cell outside the fixed-point checksum range
    ERR_TASK = 2u,          // a task that does not fit the geometry
-   ERR_MARK = 4u           // refinement marking did not settle
+   ERR_MARK = 4u,          // refinement marking did not settle
+   ERR_WAIT = 8u           // a bounded wait for a bulk copy ran out
 };
 
 // --stencil 0: the variable-work kernel of calc_stage % 6 and

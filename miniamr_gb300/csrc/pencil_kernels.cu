@@ -26,6 +26,9 @@
 #include <algorithm>
 #include <vector>
 
+#include <cuda.h>
+#include <mutex>
+
 #include "batched.h"
 #include "arith.cuh"
 #include "cp_async.cuh"
@@ -39,15 +42,22 @@ constexpr int G = NB + 2;           // with ghosts
 constexpr int RS = NB;              // shared row: the 16 interior k values
 constexpr int KC = G * G;           // rows of a tile (i, j incl. ghosts)
 
-// Tile geometry in elements of T: row (i, j) starts at i * PW + j * RS.
-template <typename T> struct TileGeom {
-   static constexpr int PW = G * RS + 16 / (int) sizeof(T);   // plane
+// Tile geometry in elements of T: row (i, j) starts at joff() + i * PW +
+// j * RS.  TM = 0 (rows filled by cp.async): planes padded by 16 bytes.
+// TM = 1 (interior planes filled by the tensor engine, FP32): planes of 20
+// row slots (1280 bytes, a multiple of 128) with row j in slot j + 1, so
+// that each plane's 16 interior rows start on a 128-byte boundary, as a
+// bulk tensor copy's shared-memory destination must.
+template <typename T, int TM = 0> struct TileGeom {
+   static constexpr int PW = TM ? 20 * RS : G * RS + 16 / (int) sizeof(T);
    static constexpr int TILE = G * PW;
+   __host__ __device__ static constexpr int joff() { return TM ? RS : 0; }
 };
-template <typename T>
+// Offset of row (i, j) from row (0, 0).
+template <typename T, int TM = 0>
 __device__ __forceinline__ int trow(int i, int j)
 {
-   return i * TileGeom<T>::PW + j * RS;
+   return i * TileGeom<T, TM>::PW + j * RS;
 }
 
 // Work split: JP j-rows and IH i-planes per thread (JP x IH = 1x4, 2x4 or
@@ -90,10 +100,12 @@ template <> struct Quad<double> {
 // one upper column, one element per row; the upper column sits an odd
 // number of words after the lower ones so that the two read in one
 // instruction use disjoint banks.  After a 128-byte alignment pad.
-template <typename T>
+template <typename T, int TM = 0>
 constexpr size_t pencil_smem_bytes()
 {
-   return (size_t) (3 * TileGeom<T>::TILE + 3 * KC + 1) * sizeof(T) + 128;
+   // + the ring's three 8-byte barriers of the tensor-copy form
+   return (size_t) (3 * TileGeom<T, TM>::TILE + 3 * KC + 1) * sizeof(T) +
+          128 + (TM ? 32 : 0);
 }
 
 constexpr int DESC = sizeof(TileDesc) / sizeof(int32_t);
@@ -166,12 +178,12 @@ __device__ __forceinline__ void issue_tile(const T *__restrict__ src,
 // Every lane of the warp must call this together.
 // `tq` is the thread's quad in tile t (row 0 of plane 0 plus 4*kq) and
 // `eg` its ghost column (the lower column for kq < 3, the upper for kq = 3).
-template <typename T>
+template <typename T, int TM>
 __device__ __forceinline__ void row6(const T *tq, const T *eg, int i, int j,
                                      int kq, T (&r)[6])
 {
    T v[4];
-   Quad<T>::ld(tq + trow<T>(i, j), v);
+   Quad<T>::ld(tq + trow<T, TM>(i, j), v);
    const T left = __shfl_up_sync(0xffffffffu, v[3], 1);
    const T right = __shfl_down_sync(0xffffffffu, v[0], 1);
    const T edge = eg[i * G + j];
@@ -243,7 +255,7 @@ __device__ __forceinline__ void emit4(const T (&w)[4], T *p, int do_cs,
 // k values on planes 4*ih+1 .. 4*ih+4.  `tq` is the thread's quad of row
 // (4*ih, jrow) in the tile, `eg` its ghost column from the same row, `d`
 // the matching global position.  Every lane of the warp runs it together.
-template <typename T, int ST, int JP, int IH, bool FIX>
+template <typename T, int ST, int JP, int IH, bool FIX, int TM>
 __device__ __forceinline__ void tile_pass(const T *tq, const T *eg, T *d,
                                           int kq, int do_cs, PassState &st)
 {
@@ -252,17 +264,17 @@ __device__ __forceinline__ void tile_pass(const T *tq, const T *eg, T *d,
       T am[JP][4], r[JP][6];
 #pragma unroll
       for (int jj = 0; jj < JP; jj++) {
-         Quad<T>::ld(tq + trow<T>(0, jj), am[jj]);
-         row6(tq, eg, 1, jj, kq, r[jj]);
+         Quad<T>::ld(tq + trow<T, TM>(0, jj), am[jj]);
+         row6<T, TM>(tq, eg, 1, jj, kq, r[jj]);
       }
 #pragma unroll
       for (int ii = 1; ii <= IH; ii++) {
          T qm[4], qp[4], c[JP][6];
-         Quad<T>::ld(tq + trow<T>(ii, -1), qm);
-         Quad<T>::ld(tq + trow<T>(ii, JP), qp);
+         Quad<T>::ld(tq + trow<T, TM>(ii, -1), qm);
+         Quad<T>::ld(tq + trow<T, TM>(ii, JP), qp);
 #pragma unroll
          for (int jj = 0; jj < JP; jj++)
-            row6(tq, eg, ii + 1, jj, kq, c[jj]);
+            row6<T, TM>(tq, eg, ii + 1, jj, kq, c[jj]);
 #pragma unroll
          for (int jj = 0; jj < JP; jj++) {
             T w[4];
@@ -298,7 +310,7 @@ __device__ __forceinline__ void tile_pass(const T *tq, const T *eg, T *d,
          T rw[JP + 2][6];
 #pragma unroll
          for (int dd = 0; dd < JP + 2; dd++)
-            row6(tq, eg, pl, dd - 1, kq, rw[dd]);
+            row6<T, TM>(tq, eg, pl, dd - 1, kq, rw[dd]);
 #pragma unroll
          for (int jj = 0; jj < JP; jj++)
 #pragma unroll
@@ -342,11 +354,11 @@ __device__ __forceinline__ void tile_pass(const T *tq, const T *eg, T *d,
 
 // The fix-up pass out of line, so that its registers do not weigh on the
 // fast pass; called only when a warp met a sum outside the window.
-template <typename T, int ST, int JP, int IH>
+template <typename T, int ST, int JP, int IH, int TM>
 __device__ __noinline__ PassState tile_fix(const T *tq, const T *eg, T *d,
                                            int kq, int do_cs, PassState st)
 {
-   tile_pass<T, ST, JP, IH, true>(tq, eg, d, kq, do_cs, st);
+   tile_pass<T, ST, JP, IH, true, TM>(tq, eg, d, kq, do_cs, st);
    return st;
 }
 
@@ -440,9 +452,9 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
          const int slot = s_desc[s].slot;
          T *d = dst + bv_offset(g, slot, var) + grow(IH * ih, jrow) + 4 * kq;
          st.slow = false;
-         tile_pass<T, ST, JP, IH, false>(tq, eg, d, kq, do_cs, st);
+         tile_pass<T, ST, JP, IH, false, 0>(tq, eg, d, kq, do_cs, st);
          if (__any_sync(0xffffffffu, st.slow))
-            st = tile_fix<T, ST, JP, IH>(tq, eg, d, kq, do_cs, st);
+            st = tile_fix<T, ST, JP, IH, 0>(tq, eg, d, kq, do_cs, st);
          if (sizeof(T) == 4 && do_cs)
             fixed52_flush(st.part, st.lo, st.hi);
          if (write_ghosts) {
@@ -489,6 +501,257 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       }
       __syncthreads();
    }
+}
+
+// ---- the tensor-copy form (FP32, one j-row per thread) -------------------
+//
+// The same walk, update and ghost handling; only the filling of a tile
+// differs: its 16 interior planes and the two x-face planes (each 16 rows
+// of 64 bytes, contiguous in the pool and in the tile) arrive by bulk
+// tensor copies (cp.async.bulk.tensor, 18 per tile, issued by one warp)
+// that complete on the ring slot's mbarrier, and only the y-face rows and
+// the 27-point z-running edge rows remain per-thread 16-byte copies.  The
+// pool is the 4-d tensor (k: 16, j: 18, i: 18, block-variable) of the
+// split layout (rows of 64 bytes, planes of 1152 bytes, block-variables bv
+// elements apart); a box is one plane's 16 interior rows.
+
+// Waits for phase `parity` of the mbarrier at shared address bar; false if
+// it has not completed after 64 tries.  Each try suspends the thread until
+// the phase completes or a time hint of 10 ms runs out, so a waiting warp
+// takes no issue slots from the warps that compute.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+{
+   for (int it = 0; it < 64; it++) {
+      unsigned ok;
+      asm volatile("{\n\t.reg .pred p;\n\t"
+                   "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, "
+                   "%3;\n\t"
+                   "selp.u32 %0, 1, 0, p;\n\t}"
+                   : "=r"(ok)
+                   : "r"(bar), "r"(parity), "r"(10000000u)
+                   : "memory");
+      if (ok)
+         return true;
+   }
+   return false;
+}
+
+__device__ __forceinline__ void tma_plane(float *dst, const CUtensorMap *tm,
+                                          int i, int bvi, unsigned bar)
+{
+   const unsigned d = (unsigned) __cvta_generic_to_shared(dst);
+   asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile"
+                ".mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+                "[%6];"
+                ::"r"(d), "l"(reinterpret_cast<unsigned long long>(tm)),
+                "r"(0), "r"(1), "r"(i), "r"(bvi), "r"(bar)
+                : "memory");
+}
+
+// Bytes one tile's tensor copies deliver: 18 planes of 16 rows x 64 bytes.
+constexpr unsigned kTmaTileBytes = 18u * NB * NB * 4u;
+
+template <int ST, int THREADS>
+__device__ __forceinline__ void issue_tile_tma(const CUtensorMap *tm,
+                                               const float *__restrict__ src,
+                                               const Geom &g,
+                                               const TileDesc *it, int var,
+                                               float *t, unsigned bar)
+{
+   using TG = TileGeom<float, 1>;
+   constexpr int VW = 4, CPR = NB / VW;
+   const int tid = threadIdx.x;
+   const int slot = it->slot, bmask = it->bmask;
+   if (tid < 32) {
+      if (tid == 0)
+         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], "
+                      "%1;" ::"r"(bar), "r"(kTmaTileBytes)
+                      : "memory");
+      __syncwarp();
+      if (tid < NB) {
+         tma_plane(t + TG::joff() + trow<float, 1>(tid + 1, 1), tm, tid + 1,
+                   slot * g.V + var, bar);
+      } else if (tid < NB + 2) {
+         // x faces: the W / E neighbour's near plane, or (boundary) this
+         // block's own first / last plane
+         const int f = tid - NB;
+         const bool low = f == 0, bnd = (bmask >> f) & 1;
+         const int sp = bnd ? (low ? 1 : NB) : (low ? NB : 1);
+         const int nb = bnd ? slot : it->nb9[low ? 3 : 5];
+         tma_plane(t + TG::joff() + trow<float, 1>(low ? 0 : G - 1, 1), tm, sp,
+                   nb * g.V + var, bar);
+      }
+   }
+   // y faces S, N: 16 rows each, as 16-byte copies
+   const float *own = src + bv_offset(g, slot, var);
+   for (int c = tid; c < 2 * NB * CPR; c += THREADS) {
+      const int f = 2 + c / (NB * CPR), r = c % (NB * CPR);
+      const int a = r / CPR + 1, q = r % CPR;
+      const bool low = f == 2, bnd = (bmask >> f) & 1;
+      const float *blk = bnd ? own
+                             : src + bv_offset(g, it->nb9[low ? 1 : 7], var);
+      const int sp = bnd ? (low ? 1 : NB) : (low ? NB : 1);
+      cp_async16(t + TG::joff() + trow<float, 1>(a, low ? 0 : G - 1) + q * VW,
+                 blk + grow(a, sp) + q * VW);
+   }
+   if (ST == 27 && tid < 4 * CPR) {
+      const int e = tid / CPR, q = tid % CPR;
+      const int gi = (e & 1) ? G - 1 : 0, gj = (e & 2) ? G - 1 : 0;
+      int dx = (e & 1) ? 1 : -1, dy = (e & 2) ? 1 : -1, si, sj;
+      if (bmask & (1 << ((e & 1) ? 1 : 0))) { si = (e & 1) ? NB : 1; dx = 0; }
+      else si = (e & 1) ? 1 : NB;
+      if (bmask & (1 << ((e & 2) ? 3 : 2))) { sj = (e & 2) ? NB : 1; dy = 0; }
+      else sj = (e & 2) ? 1 : NB;
+      const int nb = it->nb9[(dx + 1) + 3 * (dy + 1)];
+      cp_async16(t + TG::joff() + trow<float, 1>(gi, gj) + q * VW,
+                 src + bv_offset(g, nb, var) + grow(si, sj) + q * VW);
+   }
+   cp_async_commit();
+}
+
+template <int ST, int IH>
+__global__ void __launch_bounds__(1024 / IH, 3)
+pencil_tma_kernel(const __grid_constant__ CUtensorMap tm,
+                  const float *__restrict__ src, float *__restrict__ dst,
+                  Geom g, const TileDesc *__restrict__ chain,
+                  const int2 *__restrict__ pencils, int n_pencils,
+                  int write_ghosts, int do_cs,
+                  unsigned long long *__restrict__ acc,
+                  unsigned *__restrict__ err, unsigned *__restrict__ ctx_err)
+{
+   using T = float;
+   constexpr int JP = 1, THREADS = 1024 / IH;
+   using TG = TileGeom<float, 1>;
+   constexpr int TILE = TG::TILE, JO = TG::joff();
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   __shared__ TileDesc s_desc[PENCIL_MAX];
+   T *tiles = reinterpret_cast<T *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t) 127);
+   T *klos = tiles + 3 * TILE;          // lower columns of tiles s, s+1
+   T *khi = klos + 2 * KC + 1;          // upper column of tile s
+   unsigned long long *bars = reinterpret_cast<unsigned long long *>(
+      (reinterpret_cast<uintptr_t>(khi + KC) + 7) & ~(uintptr_t) 7);
+   const unsigned bar0 = (unsigned) __cvta_generic_to_shared(bars);
+   const int tid = threadIdx.x;
+   const int kq = tid & 3, jrow = ((tid >> 2) & 15) + 1, ih = tid >> 6;
+   if (tid == 0) {
+      for (int b = 0; b < 3; b++)
+         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
+                         bar0 + 8 * b)
+                      : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+   }
+   __syncthreads();
+   unsigned phase = 0;                  // bit b: parity slot b waits for
+   bool timed_out = false;
+
+   constexpr int NFILL = (KC + THREADS - 1) / THREADS;
+   int fill[NFILL];
+#pragma unroll
+   for (int m = 0; m < NFILL; m++) {
+      const int q = tid + m * THREADS, i = q % G, j = q / G;
+      fill[m] = q < KC ? ((JO + trow<T, 1>(i, j)) << 9) | (i * G + j) : -1;
+   }
+
+   for (int w = blockIdx.x; w < n_pencils * g.V; w += gridDim.x) {
+      const int var = w / n_pencils, p = w - var * n_pencils;
+      const int2 pc = pencils[p];
+      const int len = pc.y;
+      {
+         const int32_t *from = reinterpret_cast<const int32_t *>(chain + pc.x);
+         int32_t *to = reinterpret_cast<int32_t *>(s_desc);
+         for (int q = tid; q < len * DESC; q += THREADS)
+            to[q] = from[q];
+      }
+      __syncthreads();
+      issue_tile_tma<ST, THREADS>(&tm, src, g, s_desc, var, tiles, bar0);
+      if (len > 1)
+         issue_tile_tma<ST, THREADS>(&tm, src, g, s_desc + 1, var,
+                                     tiles + TILE, bar0 + 8);
+      PassState st;
+      st.ok = true;
+      st.lo = st.hi = 0;
+      for (int s = 0; s < len; s++) {
+         const int sl = s % 3;
+         const T *t = tiles + sl * TILE;
+         const T *tn = tiles + ((s + 1) % 3) * TILE;
+         T *kcur = klos + (s & 1) * KC;
+         T *knext = klos + ((s + 1) & 1) * KC;
+         if (!mbar_wait(bar0 + 8 * sl, (phase >> sl) & 1))
+            timed_out = true;
+         phase ^= 1u << sl;
+         cp_async_wait_all();
+         __syncthreads();
+#pragma unroll
+         for (int m = 0; m < NFILL; m++) {
+            if (fill[m] < 0)
+               continue;
+            const int r = fill[m] >> 9, e = fill[m] & 511;
+            const T top = t[r + NB - 1];
+            khi[e] = s + 1 < len ? tn[r] : top;
+            if (s + 1 < len)
+               knext[e] = top;
+            if (s == 0)
+               kcur[e] = t[r];
+         }
+         __syncthreads();
+         if (s + 2 < len) {
+            const int sl2 = (s + 2) % 3;
+            issue_tile_tma<ST, THREADS>(&tm, src, g, s_desc + s + 2, var,
+                                        tiles + sl2 * TILE, bar0 + 8 * sl2);
+         }
+         const T *tq = t + JO + trow<T, 1>(IH * ih, jrow) + 4 * kq;
+         const T *eg = (kq == 3 ? khi : kcur) + IH * ih * G + jrow;
+         const int slot = s_desc[s].slot;
+         T *d = dst + bv_offset(g, slot, var) + grow(IH * ih, jrow) + 4 * kq;
+         st.slow = false;
+         tile_pass<T, ST, JP, IH, false, 1>(tq, eg, d, kq, do_cs, st);
+         if (__any_sync(0xffffffffu, st.slow))
+            st = tile_fix<T, ST, JP, IH, 1>(tq, eg, d, kq, do_cs, st);
+         if (do_cs)
+            fixed52_flush(st.part, st.lo, st.hi);
+         if (write_ghosts) {
+            T *base = dst + bv_offset(g, slot, var);
+            const int n_shell = G * G * G - NB * NB * NB;
+            for (int e = tid; e < n_shell; e += THREADS) {
+               int gi, gj, gk;
+               if (e < 2 * G * G) {
+                  gi = e < G * G ? 0 : G - 1;
+                  const int r = e % (G * G);
+                  gj = r / G; gk = r % G;
+               } else if (e < 2 * G * G + 2 * NB * G) {
+                  const int r = e - 2 * G * G;
+                  gj = r < NB * G ? 0 : G - 1;
+                  const int r2 = r % (NB * G);
+                  gi = r2 / G + 1; gk = r2 % G;
+               } else {
+                  const int r = e - 2 * G * G - 2 * NB * G;
+                  gk = r < NB * NB ? 0 : G - 1;
+                  const int r2 = r % (NB * NB);
+                  gi = r2 / NB + 1; gj = r2 % NB + 1;
+               }
+               const int outside = (gi == 0 || gi == G - 1) +
+                                   (gj == 0 || gj == G - 1) +
+                                   (gk == 0 || gk == G - 1);
+               if (ST == 7 && outside != 1)
+                  continue;
+               const int ee = gi * G + gj;
+               const T v = gk == 0 ? kcur[ee]
+                         : (gk == G - 1 ? khi[ee]
+                                        : t[JO + trow<T, 1>(gi, gj) + gk - 1]);
+               base[cell_offset(g, gi, gj, gk)] = v;
+            }
+         }
+      }
+      if (do_cs) {
+         if (!st.ok || !fixed52_window(st.part))
+            atomicOr(err, ERR_FIXED_RANGE);
+         block_acc128_flush(st.lo, st.hi, acc + 2 * var);
+      }
+      __syncthreads();
+   }
+   if (timed_out)
+      atomicOr(ctx_err, ERR_WAIT);
 }
 
 // FP64 checksum of every (block, variable) of the pool in the reference's
@@ -542,6 +805,65 @@ int launch_fp64_checksums(const double *pool, const Geom &g,
    return 2;
 }
 
+// cuTensorMapEncodeTiled, from the driver through the runtime (no link
+// against the driver library); null if unavailable.
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType,
+                                   cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                   CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled()
+{
+   static std::once_flag once;
+   static EncodeTiledFn fn = nullptr;
+   std::call_once(once, [] {
+      void *p = nullptr;
+      cudaDriverEntryPointQueryResult q;
+      if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p,
+                                           12000, cudaEnableDefault,
+                                           &q) == cudaSuccess &&
+          q == cudaDriverEntryPointSuccess)
+         fn = reinterpret_cast<EncodeTiledFn>(p);
+   });
+   return fn;
+}
+
+// The tensor map of an FP32 pool of 16^3 blocks in the split layout:
+// (k: 16, j: 18, i: 18, block-variable: n_bv), boxes of one plane's 16
+// interior rows.
+static bool pool_tensor_map(const float *pool, const Geom &g, long long n_bv,
+                            CUtensorMap *tm)
+{
+   EncodeTiledFn enc = encode_tiled();
+   if (!enc || g.kplane < 0 || n_bv < 1 || n_bv > (1ll << 31))
+      return false;
+   const cuuint64_t dims[4] = {(cuuint64_t) NB, (cuuint64_t) G,
+                               (cuuint64_t) G, (cuuint64_t) n_bv};
+   const cuuint64_t strides[3] = {NB * 4u, (cuuint64_t) G * NB * 4u,
+                                  (cuuint64_t) g.bv * 4u};
+   const cuuint32_t box[4] = {NB, NB, 1, 1};
+   const cuuint32_t estr[4] = {1, 1, 1, 1};
+   return enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+              const_cast<float *>(pool), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int ST, int IH>
+static int pencil_tma_per_sm()
+{
+   int per_sm = 0;
+   cudaFuncSetAttribute(pencil_tma_kernel<ST, IH>,
+                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                        (int) pencil_smem_bytes<float, 1>());
+   cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, pencil_tma_kernel<ST, IH>, 1024 / IH,
+      pencil_smem_bytes<float, 1>());
+   return per_sm;
+}
+
 template <typename T, int ST, int JP, int IH>
 static int pencil_per_sm()
 {
@@ -590,6 +912,29 @@ void pencil_candidates(int stencil, int n_work, std::vector<StageShape> &out)
          out.push_back(a);
       }
    }
+   // FP32: the tensor-copy form, one j-row and 8 planes per thread (with
+   // 4 planes it measured 8-10 % slower still, and is not offered)
+   if (sizeof(T) == 4 && encode_tiled()) {
+      for (int ih : {8}) {
+         const int per_sm = stencil == 7 ? pencil_tma_per_sm<7, 8>()
+                                         : pencil_tma_per_sm<27, 8>();
+         if (per_sm <= 0)
+            continue;
+         const long long wave = (long long) per_sm * sms;
+         StageShape a;
+         a.kernel = 3;
+         a.rows = 1;
+         a.planes = ih;
+         a.vpc = 1;
+         a.threads = 1024 / ih;
+         a.grid = (int) std::max(1LL, std::min<long long>(wave, n_work));
+         out.push_back(a);
+         if (n_work > wave) {
+            a.grid = n_work;
+            out.push_back(a);
+         }
+      }
+   }
 }
 
 template <typename T>
@@ -599,10 +944,32 @@ int launch_pencil_stage(const T *src, T *dst, const Geom &g, int stencil,
                         int n_pencils, const StageShape &sh, int write_ghosts,
                         int do_cs, double *partials, double *sums,
                         unsigned long long *acc, unsigned *err,
-                        cudaStream_t s)
+                        unsigned *ctx_err, long long n_bv, cudaStream_t s)
 {
    if (n_pencils == 0)
       return 0;
+   if (sh.kernel == 3) {
+      if constexpr (sizeof(T) == 4) {
+         CUtensorMap tm;
+         if (!pool_tensor_map(src, g, n_bv, &tm))
+            return -1;
+         const size_t smem = pencil_smem_bytes<float, 1>();
+#define MAMR_PENCIL_TMA(ST, IH)                                               \
+   pencil_tma_kernel<ST, IH><<<sh.grid, 1024 / IH, smem, s>>>(                \
+      tm, src, dst, g, chain, pencils, n_pencils, write_ghosts, do_cs, acc,   \
+      err, ctx_err)
+         if (sh.planes != 8)
+            return -1;
+         if (stencil == 7)
+            MAMR_PENCIL_TMA(7, 8);
+         else
+            MAMR_PENCIL_TMA(27, 8);
+#undef MAMR_PENCIL_TMA
+         return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+      } else {
+         return -1;
+      }
+   }
    const size_t smem = pencil_smem_bytes<T>();
    const int fused_cs = (sizeof(T) == 4) ? do_cs : 0;
    const int grid = sh.grid;
@@ -635,13 +1002,14 @@ template int launch_pencil_stage<float>(const float *, float *, const Geom &,
                                         const TileDesc *, const int2 *, int,
                                         const StageShape &, int, int, double *,
                                         double *, unsigned long long *,
-                                        unsigned *, cudaStream_t);
+                                        unsigned *, unsigned *, long long,
+                                        cudaStream_t);
 template int launch_pencil_stage<double>(const double *, double *,
                                          const Geom &, int, const BItem *,
                                          int, const TileDesc *, const int2 *,
                                          int, const StageShape &, int, int,
                                          double *, double *,
                                          unsigned long long *, unsigned *,
-                                         cudaStream_t);
+                                         unsigned *, long long, cudaStream_t);
 
 }  // namespace mamr
