@@ -338,14 +338,30 @@ template <int TPI, int FP32, int VPI> struct BrickBounds {
 };
 
 // Barrier of the TPI threads that share an item: the warp itself, or a
-// named barrier (id 1 + group) over the group's two warps.
+// named barrier (id 1 + group, at most 4 groups a CTA) over the group's two
+// warps.  The ids are immediates: with an id in a register the compiler
+// reserves all 16 barriers for the kernel, which caps an SM at 4 of its
+// CTAs.
 template <int TPI> __device__ __forceinline__ void group_sync(int group)
 {
-   if (TPI == 32)
+   if (TPI == 32) {
       __syncwarp();
-   else
-      asm volatile("bar.sync %0, %1;\n" ::"r"(group + 1), "n"(TPI)
-                   : "memory");
+      return;
+   }
+   switch (group) {
+   case 0:
+      asm volatile("bar.sync 1, %0;\n" ::"n"(TPI) : "memory");
+      break;
+   case 1:
+      asm volatile("bar.sync 2, %0;\n" ::"n"(TPI) : "memory");
+      break;
+   case 2:
+      asm volatile("bar.sync 3, %0;\n" ::"n"(TPI) : "memory");
+      break;
+   default:
+      asm volatile("bar.sync 4, %0;\n" ::"n"(TPI) : "memory");
+      break;
+   }
 }
 
 template <typename T, int TPI, int VPI>
