@@ -207,12 +207,18 @@ class Mesh {
             pa[p].child[o] = p_[p].child[o];
       }
    }
+   // The marking's flags: the blocks to split (by level, in slot order --
+   // mb lists the blocks in slot order) and the parents' flags.
    void set_flags(const std::vector<mamr_mark_block> &mb,
                   const std::vector<int32_t> &bref,
                   const std::vector<int32_t> &pref)
    {
+      marked_.resize(nr_ + 1);
+      for (std::vector<int> &m : marked_)
+         m.clear();
       for (size_t q = 0; q < mb.size(); q++)
-         b_[mb[q].slot].refine = bref[q];
+         if (bref[q] == 1 && mb[q].level <= nr_)
+            marked_[mb[q].level].push_back(mb[q].slot);
       for (int p = 0; p < max_parent_; p++)
          if (p_[p].number >= 0)
             p_[p].refine = pref[p];
@@ -227,16 +233,13 @@ class Mesh {
    {
       jobs.clear();
       const int top = cur_max_level();
-      // the blocks marked to split, by level in slot order: splitting one
-      // level adds children with refine 0 in free slots and moves no other
+      // the blocks marked to split, by level in slot order (set_flags):
+      // splitting one level adds children in free slots and moves no other
       // block, so the reference's slot scan of each level finds these
-      std::vector<std::vector<int>> marked(top + 1);
-      for (int n = 0; n < max_block_; n++)
-         if (b_[n].number >= 0 && b_[n].refine == 1 && b_[n].level <= top)
-            marked[b_[n].level].push_back(n);
       int m = 0;
-      for (int level = 0; level <= top; level++) {
-         for (const int n : marked[level]) {
+      for (int level = 0; level <= top && level < (int) marked_.size();
+           level++) {
+         for (const int n : marked_[level]) {
             Blk &bp = b_[n];
             const long long nl = bp.number - start_[level];
             const long long lx = (long long) ix_ << level,
@@ -434,6 +437,7 @@ class Mesh {
    // scans for the next free slot (from a running index in split, from 0 in
    // consolidate) skip 64 slots a word
    std::vector<uint64_t> used_;
+   std::vector<std::vector<int>> marked_;   // slots to split, by level
 
    void occupy(int n) { used_[n >> 6] |= (uint64_t) 1 << (n & 63); }
    void release(int n) { used_[n >> 6] &= ~((uint64_t) 1 << (n & 63)); }
@@ -619,14 +623,16 @@ class Planner {
    // consolidations.
    void refine(int ts)
    {
-      Plan plan;
+      Plan plan = recycled();
       plan.ts = ts;
+      plan.split.clear();
+      plan.cons.clear();
       const int steps = ts ? (prm_.block_change ? prm_.block_change
                                                 : prm_.num_refine)
                            : prm_.num_refine;
-      std::vector<mamr_mark_block> mb;
-      std::vector<mamr_mark_parent> pa;
-      std::vector<int32_t> bref, pref;
+      std::vector<mamr_mark_block> &mb = mb_;
+      std::vector<mamr_mark_parent> &pa = pa_;
+      std::vector<int32_t> &bref = bref_, &pref = pref_;
       std::vector<mamr_object> mo(objs_.size());
       mamr_mark_params mp;
       memset(&mp, 0, sizeof(mp));
@@ -681,10 +687,36 @@ class Planner {
       push(std::move(plan));
    }
 
+   // A used plan back from the stage side (its buffers keep their
+   // capacity), or a new one.
+   Plan recycled()
+   {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (free_.empty())
+         return Plan();
+      Plan p = std::move(free_.back());
+      free_.pop_back();
+      return p;
+   }
+
+ public:
+   // The stage side hands an applied plan back for reuse.
+   void give_back(Plan &&p)
+   {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (free_.size() < kAhead + 1)
+         free_.push_back(std::move(p));
+   }
+
+ private:
    mamr_ctx *mctx_;
    const mamr_amr_params &prm_;
    std::vector<mamr_amr_object> objs_;
    Mesh mesh_;
+   std::vector<mamr_mark_block> mb_;
+   std::vector<mamr_mark_parent> pa_;
+   std::vector<int32_t> bref_, pref_;
+   std::vector<Plan> free_;
    std::thread th_;
    std::mutex mu_;
    std::condition_variable cv_;
@@ -775,6 +807,7 @@ struct Run {
       emit(3, p.ts, p.mesh.data(), (int32_t) p.mesh.size(), p.numbers.data(),
            p.cen.data());
       st.refinements++;
+      pl.give_back(std::move(p));
       st.refine_seconds += now() - t0 - (ev_s - ev0);
    }
 
