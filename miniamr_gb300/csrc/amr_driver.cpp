@@ -39,7 +39,7 @@ struct Fail {
 
 struct Blk {
    long long number = -1;
-   int level = 0, refine = 0, parent = -1, child_number = 0;
+   int level = 0, parent = -1, child_number = 0;
    int nei_level[6] = {0, 0, 0, 0, 0, 0};
    int nei[6][2][2] = {};
    int cen[3] = {0, 0, 0};
@@ -101,7 +101,6 @@ class Mesh {
                bp.level = 0;
                bp.parent = -1;
                bp.child_number = 0;
-               bp.refine = 0;
                bp.cen[0] = i * size + size / 2;
                bp.cen[1] = j * size + size / 2;
                bp.cen[2] = k * size + size / 2;
@@ -288,7 +287,6 @@ class Mesh {
                sib[o] = m;
                pp.child[o] = m;
                job.child[o] = m;
-               c.refine = 0;
                c.level = level + 1;
                c.parent = p;
                c.child_number = o;
@@ -383,7 +381,6 @@ class Mesh {
             bp.child_number = pp.child_number;
             if (bp.level)
                p_[bp.parent].child[bp.child_number] = n;
-            bp.refine = 0;
             for (int d = 0; d < 3; d++)
                bp.cen[d] = pp.cen[d];
             mamr_consolidate_job job;
