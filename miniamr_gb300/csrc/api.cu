@@ -169,6 +169,12 @@ struct mamr_ctx {
    bool work_set = false;
    DevBuf d_work;                   // --stencil 0 work values
    DevBuf d_mark;                   // refinement marking lists and flags
+   // the plain path's z-face cache (mamr_internal.h: zcache_at) and, per
+   // variable, whether it holds what the pool holds: set by a plain
+   // stencil of the variable, cleared by anything else that changes
+   // interior cells or the mesh
+   DevBuf d_zc;
+   std::vector<char> zc_ok;
    // FP64 checksums of every variable, computed together on the first
    // mamr_check_sum after the pool or the mesh last changed (gen counts
    // those changes)
@@ -181,6 +187,30 @@ struct mamr_ctx {
 };
 
 static size_t elem_size(const mamr_ctx *c) { return c->fp32 ? 4 : 8; }
+
+// The z-face cache: dropped whenever interior cells or the mesh change
+// other than through a plain stencil; the buffer a plain stencil writes
+// (allocated on first use; null if it cannot be, and the stencil then
+// writes none).
+static void zcache_drop(mamr_ctx *c)
+{
+   std::fill(c->zc_ok.begin(), c->zc_ok.end(), 0);
+}
+static void *zcache_for_stencil(mamr_ctx *c)
+{
+   if (!c->d_zc.p) {
+      const size_t bytes =
+         zcache_elems(c->g, c->cfg.max_blocks) * elem_size(c);
+      if (c->d_zc.ensure(bytes) != cudaSuccess) {
+         cudaGetLastError();
+         c->d_zc.release();
+         return nullptr;
+      }
+      c->zc_ok.assign(c->cfg.num_vars, 0);
+   }
+   return c->d_zc.p;
+}
+
 
 static int check_error_word(mamr_ctx *c)
 {
@@ -297,7 +327,7 @@ extern "C" int mamr_destroy(mamr_ctx *c)
    c->d_slots.release(); c->d_partials.release(); c->d_jobs.release();
    c->d_stage.release(); c->d_stage_slots.release(); c->d_sums.release();
    c->d_xfer.release(); c->d_xfer_slots.release(); c->d_work.release();
-   c->d_mark.release(); c->d_cs.release();
+   c->d_mark.release(); c->d_cs.release(); c->d_zc.release();
    c->d_mesh.release(); c->d_slot_pos.release(); c->d_csflags.release();
    if (c->d_acc) cudaFree(c->d_acc);
    if (c->d_sum) cudaFree(c->d_sum);
@@ -404,6 +434,7 @@ extern "C" int mamr_upload_blocks(mamr_ctx *c, const int32_t *slots,
    if (!c)
       return fail(MAMR_EINVAL, "null context");
    c->gen++;
+   zcache_drop(c);
    return transfer(c, slots, n, const_cast<double *>(host), true);
 }
 
@@ -425,6 +456,7 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
    if (n > c->cfg.max_blocks)
       return fail(MAMR_EINVAL, "%d blocks exceed max_blocks", n);
    c->gen++;
+   zcache_drop(c);
    std::vector<int32_t> pos(c->cfg.max_blocks, -1);
    for (int32_t b = 0; b < n; b++) {
       const mamr_block &bp = blocks[b];
@@ -547,16 +579,26 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
 
 static int comm_impl(mamr_ctx *c, int32_t start, int32_t num, int32_t stage)
 {
+   // the cache serves the z exchange when it holds every variable of it
+   bool zc = c->d_zc.p != nullptr && num > 0;
+   for (int v = start; zc && v < start + num; v++)
+      zc = c->zc_ok[v] != 0;
    for (int o = 0; o < 3; o++) {
       int dir = c->cfg.permute ? kPerm[((stage % 6) + 6) % 6][o] : o;
       if (c->fp32)
          LAUNCH_TRY(c, launch_comm_dir((float *) c->pool, c->g, dir,
                                        c->cfg.stencil, c->cfg.code,
-                                       c->tasks[dir], start, num, c->stream));
+                                       c->tasks[dir], start, num,
+                                       zc ? (const float *) c->d_zc.p
+                                          : nullptr,
+                                       c->stream));
       else
          LAUNCH_TRY(c, launch_comm_dir((double *) c->pool, c->g, dir,
                                        c->cfg.stencil, c->cfg.code,
-                                       c->tasks[dir], start, num, c->stream));
+                                       c->tasks[dir], start, num,
+                                       zc ? (const double *) c->d_zc.p
+                                          : nullptr,
+                                       c->stream));
    }
    return MAMR_OK;
 }
@@ -587,39 +629,46 @@ static int stencil_impl(mamr_ctx *c, int32_t var, int32_t calc_stage,
                         "before the first stencil");
          CUDA_TRY(c->d_work.ensure(sizeof(double) * std::max(1, n) *
                                    c->cfg.nx * c->cfg.ny * c->cfg.nz));
+         if (!c->zc_ok.empty())
+            c->zc_ok[var] = 0;
          LAUNCH_TRY(c, launch_work_stencil(
                           (double *) c->pool, c->g,
                           (const int32_t *) c->d_slots.p, n, var, calc_stage,
                           c->work, (double *) c->d_work.p, c->stream));
          return MAMR_OK;
       }
+      double *zc = (double *) zcache_for_stencil(c);
       LAUNCH_TRY(c, launch_stencil((double *) c->pool, c->g, 7,
-                                   (const int32_t *) c->d_slots.p, n, var,
+                                   (const int32_t *) c->d_slots.p, n, var, zc,
                                    c->stream));
+      if (zc)
+         c->zc_ok[var] = 1;
       return MAMR_OK;
    }
+   void *zc = zcache_for_stencil(c);
    if (per_block) {
       for (int b = 0; b < n; b++) {
          const int32_t *one = (const int32_t *) c->d_slots.p + b;
          if (c->fp32)
             LAUNCH_TRY(c, launch_stencil((float *) c->pool, c->g,
                                          c->cfg.stencil, one, 1, var,
-                                         c->stream));
+                                         (float *) zc, c->stream));
          else
             LAUNCH_TRY(c, launch_stencil((double *) c->pool, c->g,
                                          c->cfg.stencil, one, 1, var,
-                                         c->stream));
+                                         (double *) zc, c->stream));
       }
-      return MAMR_OK;
-   }
-   if (c->fp32)
+   } else if (c->fp32) {
       LAUNCH_TRY(c, launch_stencil((float *) c->pool, c->g, c->cfg.stencil,
                                    (const int32_t *) c->d_slots.p, n, var,
-                                   c->stream));
-   else
+                                   (float *) zc, c->stream));
+   } else {
       LAUNCH_TRY(c, launch_stencil((double *) c->pool, c->g, c->cfg.stencil,
                                    (const int32_t *) c->d_slots.p, n, var,
-                                   c->stream));
+                                   (double *) zc, c->stream));
+   }
+   if (zc)
+      c->zc_ok[var] = 1;
    return MAMR_OK;
 }
 
@@ -806,6 +855,7 @@ extern "C" int mamr_split(mamr_ctx *c, const mamr_split_job *jobs, int32_t n)
    if (!c || n < 0 || (n && !jobs))
       return fail(MAMR_EINVAL, "bad split arguments");
    c->gen++;
+   zcache_drop(c);
    for (int32_t t = 0; t < n; t++) {
       if (!slot_ok(c, jobs[t].parent))
          return fail(MAMR_EINVAL, "split parent slot %d out of range",
@@ -845,6 +895,7 @@ extern "C" int mamr_consolidate(mamr_ctx *c, const mamr_consolidate_job *jobs,
    if (!c || n < 0 || (n && !jobs))
       return fail(MAMR_EINVAL, "bad consolidate arguments");
    c->gen++;
+   zcache_drop(c);
    for (int32_t t = 0; t < n; t++) {
       if (!slot_ok(c, jobs[t].target))
          return fail(MAMR_EINVAL, "consolidate target slot %d out of range",
@@ -1278,6 +1329,7 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
                        int32_t *n_sums)
 {
    int r;
+   zcache_drop(c);
    if (!c->batched) {
       c->batched = new (std::nothrow) BatchedState();
       if (!c->batched)

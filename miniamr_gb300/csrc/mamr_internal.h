@@ -93,10 +93,28 @@ int report_error(int code, const char *fmt, ...);
 // (>= 0) or -1 after a launch error (cudaGetLastError is left set).
 template <typename T>
 int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil, int code,
-                    const DirTasks &t, int var0, int nvar, cudaStream_t s);
+                    const DirTasks &t, int var0, int nvar, const T *zc,
+                    cudaStream_t s);
 template <typename T>
 int launch_stencil(T *pool, const Geom &g, int stencil, const int32_t *slots,
-                   int n, int var, cudaStream_t s);
+                   int n, int var, T *zc, cudaStream_t s);
+// The plain path's z-face cache: for every block-variable its interior
+// planes k = 1 (side 0) and k = nz (side 1), nx*ny values each at
+// (i-1)*ny + (j-1), as the last stencil left them.  The stencil writes it
+// (zc non-null) beside the pool; the z-direction face exchange reads the
+// interior rows' k = 1 / k = nz values from it (zc non-null) instead of
+// one value per 32-byte sector of the pool.
+__host__ __device__ inline long long zcache_at(const Geom &g, int slot,
+                                               int var, int side, int i,
+                                               int j)
+{
+   return (((long long) slot * g.V + var) * 2 + side) * (g.nx * g.ny) +
+          (long long) (i - 1) * g.ny + (j - 1);
+}
+inline size_t zcache_elems(const Geom &g, int max_blocks)
+{
+   return (size_t) max_blocks * g.V * 2 * g.nx * g.ny;
+}
 // The plain stencil stages a whole block-variable in shared memory up to
 // kPlainTileBytes and streams larger ones along i through a ring of three
 // planes, which must fit kPlainRingBytes (plain_stencil_fits).

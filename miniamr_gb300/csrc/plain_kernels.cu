@@ -28,7 +28,7 @@ __device__ __forceinline__ long long face_cell(const Geom &g, int dir, int nc,
 template <typename T, int DIR, int BX, int BY, int BZ>
 __global__ void __launch_bounds__(128)
 comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
-                DirTasks t, int var0)
+                DirTasks t, int var0, const T *__restrict__ zc)
 {
    const Dims<BX, BY, BZ> D(g);
    constexpr int dir = DIR;
@@ -38,6 +38,14 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
    const int nb = dir == 2 ? D.ny : D.nz;
    auto face_cell = [&](const Geom &, int, int nc, int a, int b) {
       return D.fcell(DIR, nc, a, b);
+   };
+   // interior plane nc (1 or n) of block `slot`, cell (a, b): from the
+   // z-face cache for the interior rows when there is one (z only),
+   // else from the pool
+   auto plane = [&](const T *blk, int slot, int nc, int a, int b) -> T {
+      if (DIR == 2 && zc && a >= 1 && a <= na && b >= 1 && b <= nb)
+         return zc[zcache_at(g, slot, var, nc == n ? 1 : 0, a, b)];
+      return blk[face_cell(g, dir, nc, a, b)];
    };
 
    if (task < t.n_same) {
@@ -56,8 +64,8 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
       const int cb = b1 - b0 + 1, cnt = (a1 - a0 + 1) * cb;
       for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
          int a = a0 + e / cb, b = b0 + e % cb;
-         lo[face_cell(g, dir, n + 1, a, b)] = hi[face_cell(g, dir, 1, a, b)];
-         hi[face_cell(g, dir, 0, a, b)] = lo[face_cell(g, dir, n, a, b)];
+         lo[face_cell(g, dir, n + 1, a, b)] = plane(hi, st.hi, 1, a, b);
+         hi[face_cell(g, dir, 0, a, b)] = plane(lo, st.lo, n, a, b);
       }
       return;
    }
@@ -114,15 +122,15 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
       }
       for (int e = threadIdx.x; e < ha * hb; e += blockDim.x) {
          int a = 1 + e / hb, b = 1 + e % hb;
-         T q = quarter(C[face_cell(g, dir, c1, a + oa, b + ob)]);
+         T q = quarter(plane(C, dt.coarse, c1, a + oa, b + ob));
          F[face_cell(g, dir, f2, 2*a - 1, 2*b - 1)] = q;
          F[face_cell(g, dir, f2, 2*a - 1, 2*b)] = q;
          F[face_cell(g, dir, f2, 2*a, 2*b - 1)] = q;
          F[face_cell(g, dir, f2, 2*a, 2*b)] = q;
-         T s = F[face_cell(g, dir, f3, 2*a - 1, 2*b - 1)] +
-               F[face_cell(g, dir, f3, 2*a - 1, 2*b)];
-         s = s + F[face_cell(g, dir, f3, 2*a, 2*b - 1)];
-         s = s + F[face_cell(g, dir, f3, 2*a, 2*b)];
+         T s = plane(F, dt.fine, f3, 2*a - 1, 2*b - 1) +
+               plane(F, dt.fine, f3, 2*a - 1, 2*b);
+         s = s + plane(F, dt.fine, f3, 2*a, 2*b - 1);
+         s = s + plane(F, dt.fine, f3, 2*a, 2*b);
          C[face_cell(g, dir, c0, a + oa, b + ob)] = s;
       }
       return;
@@ -140,7 +148,7 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
       const int cb = b1 - b0 + 1, cnt = (a1 - a0 + 1) * cb;
       for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
          int a = a0 + e / cb, b = b0 + e % cb;
-         B[face_cell(g, dir, tp, a, b)] = B[face_cell(g, dir, fp, a, b)];
+         B[face_cell(g, dir, tp, a, b)] = plane(B, bt.slot, fp, a, b);
       }
    }
 }
@@ -148,37 +156,42 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
 template <typename T, int DIR>
 static void comm_dir_launch(T *pool, const Geom &g, int stencil, int code,
                             const DirTasks &t, int var0, dim3 grid,
-                            cudaStream_t s)
+                            const T *zc, cudaStream_t s)
 {
    switch (dims_kind(g)) {
    case 1:
-      comm_dir_kernel<T, DIR, 8, 8, 8><<<grid, 128, 0, s>>>(pool, g, stencil,
-                                                            code, t, var0);
+      comm_dir_kernel<T, DIR, 8, 8, 8><<<grid, 128, 0, s>>>(
+         pool, g, stencil, code, t, var0, zc);
       break;
    case 2:
       comm_dir_kernel<T, DIR, 16, 16, 16><<<grid, 128, 0, s>>>(
-         pool, g, stencil, code, t, var0);
+         pool, g, stencil, code, t, var0, zc);
       break;
    default:
-      comm_dir_kernel<T, DIR, 0, 0, 0><<<grid, 128, 0, s>>>(pool, g, stencil,
-                                                            code, t, var0);
+      comm_dir_kernel<T, DIR, 0, 0, 0><<<grid, 128, 0, s>>>(
+         pool, g, stencil, code, t, var0, zc);
    }
 }
 
 template <typename T>
 int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil, int code,
-                    const DirTasks &t, int var0, int nvar, cudaStream_t s)
+                    const DirTasks &t, int var0, int nvar, const T *zc,
+                    cudaStream_t s)
 {
    int n = t.n_same + t.n_diff + t.n_bc;
    if (n == 0 || nvar == 0)
       return 0;
    const dim3 grid(n, nvar);
+   // the cache serves the code-0 exchange only
+   const T *z = code == 0 ? zc : nullptr;
    if (dir == 0)
-      comm_dir_launch<T, 0>(pool, g, stencil, code, t, var0, grid, s);
+      comm_dir_launch<T, 0>(pool, g, stencil, code, t, var0, grid, nullptr,
+                            s);
    else if (dir == 1)
-      comm_dir_launch<T, 1>(pool, g, stencil, code, t, var0, grid, s);
+      comm_dir_launch<T, 1>(pool, g, stencil, code, t, var0, grid, nullptr,
+                            s);
    else
-      comm_dir_launch<T, 2>(pool, g, stencil, code, t, var0, grid, s);
+      comm_dir_launch<T, 2>(pool, g, stencil, code, t, var0, grid, z, s);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -206,7 +219,7 @@ __host__ __device__ inline int plain_zs(int nz)
 template <typename T, int ST, int BX, int BY, int BZ>
 __global__ void __launch_bounds__(256)
 stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
-               int var)
+               int var, T *__restrict__ zc)
 {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    T *tile = reinterpret_cast<T *>(smem_raw);
@@ -214,7 +227,8 @@ stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
    const Dims<BX, BY, BZ> D(g);
    const int nx = D.nx, ny = D.ny, nz = D.nz, X = D.X, Y = D.Y;
    const int Zs = plain_zs<T>(nz);
-   T *base = pool + bv_offset(g, slots[blockIdx.x], var);
+   const int slot = slots[blockIdx.x];
+   T *base = pool + bv_offset(g, slot, var);
 #define TL(i, j, k) tile[((i) * Y + (j)) * Zs + KO + (k)]
    // interior rows (k = 1..nz) of all X*Y rows, then the k ghost planes
    if (nz % VW == 0) {
@@ -274,6 +288,13 @@ stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
          div4(w, q);
          *reinterpret_cast<float4 *>(base + D.cell(i, j, k)) =
             make_float4(q[0], q[1], q[2], q[3]);
+         if (zc) {
+            // the planes k = 1 and k = nz for the next z exchange
+            if (k == 1)
+               zc[zcache_at(g, slot, var, 0, i, j)] = q[0];
+            if (k + 3 == nz)
+               zc[zcache_at(g, slot, var, 1, i, j)] = q[3];
+         }
       };
       if (ST == 7) {
          T a[4], c[6];
@@ -359,7 +380,10 @@ stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
             w = w + TL(i, j, k + 1);
             w = w + TL(i, j + 1, k);
             w = w + TL(i + 1, j, k);
-            base[D.cell(i, j, k)] = div7(w);
+            const T out = div7(w);
+            base[D.cell(i, j, k)] = out;
+            if (zc && (k == 1 || k == nz))
+               zc[zcache_at(g, slot, var, k == nz ? 1 : 0, i, j)] = out;
          }
       } else {
          // S(p) = the 9-point left-to-right sum on plane p around (j, k):
@@ -380,7 +404,10 @@ stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
          T s0 = S(0), s1 = S(1);
          for (int i = 1; i <= nx; i++) {
             T s2 = S(i + 1);
-            base[D.cell(i, j, k)] = div27((s0 + s1) + s2);
+            const T out = div27((s0 + s1) + s2);
+            base[D.cell(i, j, k)] = out;
+            if (zc && (k == 1 || k == nz))
+               zc[zcache_at(g, slot, var, k == nz ? 1 : 0, i, j)] = out;
             s0 = s1;
             s1 = s2;
          }
@@ -399,13 +426,15 @@ stencil_kernel(T *__restrict__ pool, Geom g, const int32_t *__restrict__ slots,
 template <typename T, int ST>
 __global__ void __launch_bounds__(256)
 stencil_stream_kernel(T *__restrict__ pool, Geom g,
-                      const int32_t *__restrict__ slots, int var)
+                      const int32_t *__restrict__ slots, int var,
+                      T *__restrict__ zc)
 {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    T *ring = reinterpret_cast<T *>(smem_raw);
    const int nx = g.nx, ny = g.ny, nz = g.nz, Z = nz + 2;
    const int P = (ny + 2) * Z;
-   T *base = pool + bv_offset(g, slots[blockIdx.x], var);
+   const int slot = slots[blockIdx.x];
+   T *base = pool + bv_offset(g, slot, var);
    auto load = [&](int i) {
       T *pl = ring + (i % 3) * P;
       for (int e = threadIdx.x; e < P; e += blockDim.x) {
@@ -447,6 +476,8 @@ stencil_stream_kernel(T *__restrict__ pool, Geom g,
             out = div27((S(pm) + S(pc)) + S(pp));
          }
          base[cell_offset(g, i, j, k)] = out;
+         if (zc && (k == 1 || k == nz))
+            zc[zcache_at(g, slot, var, k == nz ? 1 : 0, i, j)] = out;
       }
       // the ring slot of plane i-1 is refilled with plane i+2 next
       __syncthreads();
@@ -461,7 +492,7 @@ bool plain_stencil_fits(const Geom &g, size_t elem)
 
 template <typename T, int ST, int BX, int BY, int BZ>
 static void stencil_launch(T *pool, const Geom &g, const int32_t *slots,
-                           int n, int var, int threads, size_t smem,
+                           int n, int var, int threads, size_t smem, T *zc,
                            cudaStream_t s)
 {
    cudaFuncAttributes fa;
@@ -472,12 +503,12 @@ static void stencil_launch(T *pool, const Geom &g, const int32_t *slots,
                            cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int) smem);
    stencil_kernel<T, ST, BX, BY, BZ><<<n, threads, smem, s>>>(pool, g, slots,
-                                                              var);
+                                                              var, zc);
 }
 
 template <typename T>
 int launch_stencil(T *pool, const Geom &g, int stencil, const int32_t *slots,
-                   int n, int var, cudaStream_t s)
+                   int n, int var, T *zc, cudaStream_t s)
 {
    if (n == 0)
       return 0;
@@ -491,7 +522,7 @@ int launch_stencil(T *pool, const Geom &g, int stencil, const int32_t *slots,
       auto kern = stencil == 7 ? k7 : k27;
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int) ring);
-      kern<<<n, threads, ring, s>>>(pool, g, slots, var);
+      kern<<<n, threads, ring, s>>>(pool, g, slots, var, zc);
       return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
    }
    const int kind = dims_kind(g);
@@ -501,12 +532,13 @@ int launch_stencil(T *pool, const Geom &g, int stencil, const int32_t *slots,
 #define MAMR_PLAIN_ST(ST)                                                     \
    if (kind == 1)                                                             \
       stencil_launch<T, ST, 8, 8, 8>(pool, g, slots, n, var, threads, smem,   \
-                                     s);                                      \
+                                     zc, s);                                  \
    else if (kind == 2)                                                        \
       stencil_launch<T, ST, 16, 16, 16>(pool, g, slots, n, var, threads,      \
-                                        smem, s);                             \
+                                        smem, zc, s);                         \
    else                                                                       \
-      stencil_launch<T, ST, 0, 0, 0>(pool, g, slots, n, var, threads, smem, s)
+      stencil_launch<T, ST, 0, 0, 0>(pool, g, slots, n, var, threads, smem,   \
+                                     zc, s)
    if (stencil == 7) {
       MAMR_PLAIN_ST(7);
    } else {
@@ -943,9 +975,10 @@ int launch_download(const T *pool, const Geom &g, const int32_t *slots,
 
 #define INSTANTIATE(T)                                                        \
    template int launch_comm_dir<T>(T *, const Geom &, int, int, int,          \
-                                   const DirTasks &, int, int, cudaStream_t); \
+                                   const DirTasks &, int, int, const T *,     \
+                                   cudaStream_t);                             \
    template int launch_stencil<T>(T *, const Geom &, int, const int32_t *,    \
-                                  int, int, cudaStream_t);                    \
+                                  int, int, T *, cudaStream_t);               \
    template int launch_stage_blocks<T>(T *, const T *, const Geom &,          \
                                        const int32_t *, int, cudaStream_t);   \
    template int launch_upload<T>(T *, const Geom &, const int32_t *, int,     \
