@@ -26,13 +26,22 @@ __device__ __forceinline__ long long face_cell(const Geom &g, int dir, int nc,
 // direction and, for 8^3 and 16^3 blocks, the block size are compile-time
 // constants, so face addressing folds to a few multiply-adds.
 template <typename T, int DIR, int BX, int BY, int BZ>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
-                DirTasks t, int var0, const T *__restrict__ zc)
+                DirTasks t, int var0, int nvar, const T *__restrict__ zc)
 {
    const Dims<BX, BY, BZ> D(g);
    constexpr int dir = DIR;
-   int task = blockIdx.x, var = var0 + blockIdx.y;
+   // one warp per (task, variable): a face is a few hundred cells, so a
+   // CTA per task spent more on its own launch than on the copies
+   const int lane = threadIdx.x & 31;
+   const int n_tasks = t.n_same + t.n_diff + t.n_bc;
+   const long long gw =
+      (long long) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+   if (gw >= (long long) n_tasks * nvar)
+      return;
+   int task = (int) (gw % n_tasks);
+   const int var = var0 + (int) (gw / n_tasks);
    const int n = dir == 0 ? D.nx : (dir == 1 ? D.ny : D.nz);
    const int na = dir == 0 ? D.ny : D.nx;
    const int nb = dir == 2 ? D.ny : D.nz;
@@ -62,7 +71,7 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
          if (dir == 2) { b0 = 0; b1 = nb + 1; }
       }
       const int cb = b1 - b0 + 1, cnt = (a1 - a0 + 1) * cb;
-      for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      for (int e = lane; e < cnt; e += 32) {
          int a = a0 + e / cb, b = b0 + e % cb;
          lo[face_cell(g, dir, n + 1, a, b)] = plane(hi, st.hi, 1, a, b);
          hi[face_cell(g, dir, 0, a, b)] = plane(lo, st.lo, n, a, b);
@@ -89,7 +98,7 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
          // sides and one corner.  Thread (p, q) of (ha+1) x (hb+1) writes
          // coarse cell (p ? p+oa : edge row, q ? q+ob : edge column).
          const int cnt = (na + 2) * (nb + 2);
-         for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+         for (int e = lane; e < cnt; e += 32) {
             const int A = e / (nb + 2), B = e % (nb + 2);
             const int ca = A == 0 ? oa
                          : (A == na + 1 ? ha + 1 + oa : (A + 1) / 2 + oa);
@@ -99,7 +108,7 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
                quarter(C[face_cell(g, dir, c1, ca, cb)]);
          }
          const int ae = dt.jq ? na + 1 : 0, be = dt.iq ? nb + 1 : 0;
-         for (int e = threadIdx.x; e < (ha + 1) * (hb + 1); e += blockDim.x) {
+         for (int e = lane; e < (ha + 1) * (hb + 1); e += 32) {
             const int p = e / (hb + 1), q = e % (hb + 1);
             T v;
             if (p && q) {
@@ -120,7 +129,7 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
          }
          return;
       }
-      for (int e = threadIdx.x; e < ha * hb; e += blockDim.x) {
+      for (int e = lane; e < ha * hb; e += 32) {
          int a = 1 + e / hb, b = 1 + e % hb;
          T q = quarter(plane(C, dt.coarse, c1, a + oa, b + ob));
          F[face_cell(g, dir, f2, 2*a - 1, 2*b - 1)] = q;
@@ -146,7 +155,7 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
       const int a0 = full ? 0 : 1, a1 = full ? na + 1 : na;
       const int b0 = full ? 0 : 1, b1 = full ? nb + 1 : nb;
       const int cb = b1 - b0 + 1, cnt = (a1 - a0 + 1) * cb;
-      for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      for (int e = lane; e < cnt; e += 32) {
          int a = a0 + e / cb, b = b0 + e % cb;
          B[face_cell(g, dir, tp, a, b)] = plane(B, bt.slot, fp, a, b);
       }
@@ -155,21 +164,21 @@ comm_dir_kernel(T *__restrict__ pool, Geom g, int stencil, int code,
 
 template <typename T, int DIR>
 static void comm_dir_launch(T *pool, const Geom &g, int stencil, int code,
-                            const DirTasks &t, int var0, dim3 grid,
-                            const T *zc, cudaStream_t s)
+                            const DirTasks &t, int var0, int nvar,
+                            unsigned grid, const T *zc, cudaStream_t s)
 {
    switch (dims_kind(g)) {
    case 1:
-      comm_dir_kernel<T, DIR, 8, 8, 8><<<grid, 128, 0, s>>>(
-         pool, g, stencil, code, t, var0, zc);
+      comm_dir_kernel<T, DIR, 8, 8, 8><<<grid, 256, 0, s>>>(
+         pool, g, stencil, code, t, var0, nvar, zc);
       break;
    case 2:
-      comm_dir_kernel<T, DIR, 16, 16, 16><<<grid, 128, 0, s>>>(
-         pool, g, stencil, code, t, var0, zc);
+      comm_dir_kernel<T, DIR, 16, 16, 16><<<grid, 256, 0, s>>>(
+         pool, g, stencil, code, t, var0, nvar, zc);
       break;
    default:
-      comm_dir_kernel<T, DIR, 0, 0, 0><<<grid, 128, 0, s>>>(
-         pool, g, stencil, code, t, var0, zc);
+      comm_dir_kernel<T, DIR, 0, 0, 0><<<grid, 256, 0, s>>>(
+         pool, g, stencil, code, t, var0, nvar, zc);
    }
 }
 
@@ -181,17 +190,19 @@ int launch_comm_dir(T *pool, const Geom &g, int dir, int stencil, int code,
    int n = t.n_same + t.n_diff + t.n_bc;
    if (n == 0 || nvar == 0)
       return 0;
-   const dim3 grid(n, nvar);
+   // 8 warps a CTA, one (task, variable) a warp
+   const unsigned grid = (unsigned) (((long long) n * nvar + 7) / 8);
    // the cache serves the code-0 exchange only
    const T *z = code == 0 ? zc : nullptr;
    if (dir == 0)
-      comm_dir_launch<T, 0>(pool, g, stencil, code, t, var0, grid, nullptr,
-                            s);
+      comm_dir_launch<T, 0>(pool, g, stencil, code, t, var0, nvar, grid,
+                            nullptr, s);
    else if (dir == 1)
-      comm_dir_launch<T, 1>(pool, g, stencil, code, t, var0, grid, nullptr,
-                            s);
+      comm_dir_launch<T, 1>(pool, g, stencil, code, t, var0, nvar, grid,
+                            nullptr, s);
    else
-      comm_dir_launch<T, 2>(pool, g, stencil, code, t, var0, grid, z, s);
+      comm_dir_launch<T, 2>(pool, g, stencil, code, t, var0, nvar, grid, z,
+                            s);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
