@@ -155,6 +155,7 @@ struct mamr_ctx {
    DevBuf d_mesh, d_slot_pos;       // device copies of mesh and slot_pos
    DevBuf d_tasks[3];
    DirTasks tasks[3];
+   bool tasks_dirty = true;         // tasks[] not built for the mesh yet
    DevBuf d_partials, d_jobs, d_stage, d_stage_slots, d_sums;
    DevBuf d_xfer, d_xfer_slots;      // staging copies for split/consolidate
    DevBuf d_csflags;                // FP32 checksum miss words (plain path)
@@ -446,8 +447,9 @@ extern "C" int mamr_download_blocks(mamr_ctx *c, const int32_t *slots,
    return transfer(c, slots, n, host, false);
 }
 
-// ref/comm.c:162-203 turned into per-direction task lists: the same faces,
-// in the same pairing, that the reference's on-rank loop visits.
+// The mesh: checked (the reference's misconnected-block errors,
+// ref/comm.c:198-201), its sorted slots and device copies uploaded; the
+// face exchange's task lists follow on its first call (build_tasks).
 extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
                              int32_t n)
 {
@@ -481,6 +483,61 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
                               "%d nei %d)", bp.slot, l, bp.nei[l][i][j]);
       }
    }
+   // every listed neighbour must be active, whichever of the pair visits
+   // the face (the batched path reads each block's own list)
+   for (int32_t in = 0; in < n; in++) {
+      const mamr_block &bp = blocks[in];
+      for (int l = 0; l < 6; l++) {
+         const int nl = bp.nei_level[l];
+         if (nl == -2)
+            continue;
+         const int cnt = nl == bp.level + 1 ? 4 : 1;
+         for (int q = 0; q < cnt; q++) {
+            const int m = bp.nei[l][q >> 1][q & 1];
+            if (pos[m] < 0)
+               return fail(MAMR_EMESH, "neighbour slot %d not active", m);
+         }
+      }
+   }
+   // sorted slots now; the face exchange's task lists when it first runs
+   // on this mesh (build_tasks), since a batched run never needs them
+   std::vector<int32_t> sorted(n);
+   for (int32_t b = 0; b < n; b++)
+      sorted[b] = blocks[b].slot;
+   CUDA_TRY(c->d_slots.ensure(sizeof(int32_t) * std::max(1, n)));
+   if (n)
+      CUDA_TRY(cudaMemcpyAsync(c->d_slots.p, sorted.data(),
+                               sizeof(int32_t) * n, cudaMemcpyHostToDevice,
+                               c->stream));
+   c->tasks_dirty = true;
+   CUDA_TRY(c->d_partials.ensure(sizeof(double) * std::max(1, n) *
+                                 c->cfg.num_vars));
+   // the mesh on the device, for the batched path's descriptor build
+   CUDA_TRY(c->d_mesh.ensure(sizeof(mamr_block) * std::max(1, n)));
+   if (n)
+      CUDA_TRY(cudaMemcpyAsync(c->d_mesh.p, blocks, sizeof(mamr_block) * n,
+                               cudaMemcpyHostToDevice, c->stream));
+   CUDA_TRY(c->d_slot_pos.ensure(sizeof(int32_t) * pos.size()));
+   CUDA_TRY(cudaMemcpyAsync(c->d_slot_pos.p, pos.data(),
+                            sizeof(int32_t) * pos.size(),
+                            cudaMemcpyHostToDevice, c->stream));
+   CUDA_TRY(cudaStreamSynchronize(c->stream));
+   c->mesh.assign(blocks, blocks + n);
+   c->slot_pos.swap(pos);
+   for (int32_t b = 0; b < n; b++)
+      c->hw_slots = std::max(c->hw_slots, blocks[b].slot + 1);
+   mamr::batched_mesh_changed(c->batched);
+   return MAMR_OK;
+}
+
+// ref/comm.c:162-203 turned into per-direction task lists for the current
+// mesh: the same faces, in the same pairing, that the reference's on-rank
+// loop visits (set_mesh has checked the mesh).
+static int build_tasks(mamr_ctx *c)
+{
+   const std::vector<mamr_block> &blocks = c->mesh;
+   const std::vector<int32_t> &pos = c->slot_pos;
+   const int32_t n = (int32_t) blocks.size();
    std::vector<SameTask> same[3];
    std::vector<DiffTask> diff[3];
    std::vector<BcTask> bc[3];
@@ -489,12 +546,8 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
       const int s = bp.slot;
       for (int l = 0; l < 6; l++) {
          const int dir = l / 2;
-         // every listed neighbour must be active, whichever of the pair
-         // visits the face (the batched path reads each block's own list)
          if (bp.nei_level[l] == bp.level) {
             int m = bp.nei[l][0][0];
-            if (pos[m] < 0)
-               return fail(MAMR_EMESH, "neighbour slot %d not active", m);
             if (m > s) {
                // l even: the neighbour is on the low side
                same[dir].push_back(l % 2 == 0 ? SameTask{m, s}
@@ -504,16 +557,11 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
             for (int i = 0; i < 2; i++)
                for (int j = 0; j < 2; j++) {
                   int m = bp.nei[l][i][j];
-                  if (pos[m] < 0)
-                     return fail(MAMR_EMESH, "neighbour slot %d not active",
-                                 m);
                   if (m > s)
                      diff[dir].push_back(DiffTask{s, m, l, i, j});
                }
          } else if (bp.nei_level[l] == bp.level - 1) {
             int m = bp.nei[l][0][0];
-            if (pos[m] < 0)
-               return fail(MAMR_EMESH, "neighbour slot %d not active", m);
             if (m > s) {
                const mamr_block &mb = blocks[pos[m]];
                int k = dir * 2 + 1 - l % 2;
@@ -527,15 +575,7 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
          }
       }
    }
-   // Upload: sorted slots, then per direction same | diff | bc.
-   std::vector<int32_t> sorted(n);
-   for (int32_t b = 0; b < n; b++)
-      sorted[b] = blocks[b].slot;
-   CUDA_TRY(c->d_slots.ensure(sizeof(int32_t) * std::max(1, n)));
-   if (n)
-      CUDA_TRY(cudaMemcpyAsync(c->d_slots.p, sorted.data(),
-                               sizeof(int32_t) * n, cudaMemcpyHostToDevice,
-                               c->stream));
+   // per direction: same | diff | bc
    for (int d = 0; d < 3; d++) {
       size_t b_same = same[d].size() * sizeof(SameTask);
       size_t b_diff = diff[d].size() * sizeof(DiffTask);
@@ -557,28 +597,20 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
       c->tasks[d].bc = (const BcTask *) (base + o_bc);
       c->tasks[d].n_bc = (int) bc[d].size();
    }
-   CUDA_TRY(c->d_partials.ensure(sizeof(double) * std::max(1, n) *
-                                 c->cfg.num_vars));
-   // the mesh on the device, for the batched path's descriptor build
-   CUDA_TRY(c->d_mesh.ensure(sizeof(mamr_block) * std::max(1, n)));
-   if (n)
-      CUDA_TRY(cudaMemcpyAsync(c->d_mesh.p, blocks, sizeof(mamr_block) * n,
-                               cudaMemcpyHostToDevice, c->stream));
-   CUDA_TRY(c->d_slot_pos.ensure(sizeof(int32_t) * pos.size()));
-   CUDA_TRY(cudaMemcpyAsync(c->d_slot_pos.p, pos.data(),
-                            sizeof(int32_t) * pos.size(),
-                            cudaMemcpyHostToDevice, c->stream));
+   // the blobs are pageable host memory: let the copies take them before
+   // they go
    CUDA_TRY(cudaStreamSynchronize(c->stream));
-   c->mesh.assign(blocks, blocks + n);
-   c->slot_pos.swap(pos);
-   for (int32_t b = 0; b < n; b++)
-      c->hw_slots = std::max(c->hw_slots, blocks[b].slot + 1);
-   mamr::batched_mesh_changed(c->batched);
+   c->tasks_dirty = false;
    return MAMR_OK;
 }
 
 static int comm_impl(mamr_ctx *c, int32_t start, int32_t num, int32_t stage)
 {
+   if (c->tasks_dirty) {
+      const int r = build_tasks(c);
+      if (r)
+         return r;
+   }
    // the cache serves the z exchange when it holds every variable of it
    bool zc = c->d_zc.p != nullptr && num > 0;
    for (int v = start; zc && v < start + num; v++)
