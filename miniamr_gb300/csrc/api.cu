@@ -149,6 +149,7 @@ struct mamr_ctx {
    void *pool;             // current pool
    size_t pool_bytes;
    void *pool_alt;         // second pool for the batched ping-pong (lazy)
+   size_t pool_shift;      // bytes both pools start past their allocations
    std::vector<mamr_block> mesh;
    std::vector<int32_t> slot_pos;   // slot -> index in mesh or -1
    DevBuf d_slots;                  // sorted slots
@@ -188,6 +189,44 @@ struct mamr_ctx {
 };
 
 static size_t elem_size(const mamr_ctx *c) { return c->fp32 ? 4 : 8; }
+
+// Where a pool starts past its (256-byte aligned) allocation: so that the
+// interior row (1, 1) of every block-variable -- each i-plane's interior
+// rows are one contiguous run -- starts a 128-byte line, which block-
+// variable strides of whole lines then keep for all of them (16^3 FP32:
+// 64 bytes, and every interior i-plane is 8 whole lines instead of 9
+// partial ones; 8^3 FP32: 32 bytes, every other plane whole; 8^3 FP64: 64;
+// 16^3 FP64: 0).  A multiple of 16 bytes, which every vector access and
+// tensor copy of the pool needs.
+static size_t pool_shift(const Geom &g, size_t es)
+{
+   const size_t off = ((size_t) g.Y + 1) * (size_t) g.nz * es;
+   return ((128 - off % 128) % 128) & ~(size_t) 15;
+}
+
+// A pool of c->pool_bytes past c->pool_shift bytes of its allocation, zero
+// filled (queued on the context's stream).
+static cudaError_t pool_alloc(mamr_ctx *c, void **pool)
+{
+   char *base = nullptr;
+   const size_t bytes = c->pool_bytes + c->pool_shift;
+   cudaError_t e = cudaMalloc((void **) &base, bytes);
+   if (e == cudaSuccess)
+      e = cudaMemsetAsync(base, 0, bytes, c->stream);
+   if (e != cudaSuccess) {
+      if (base)
+         cudaFree(base);
+      return e;
+   }
+   *pool = base + c->pool_shift;
+   return cudaSuccess;
+}
+
+static void pool_free(mamr_ctx *c, void *pool)
+{
+   if (pool)
+      cudaFree((char *) pool - c->pool_shift);
+}
 
 // The z-face cache: dropped whenever interior cells or the mesh change
 // other than through a plain stencil; the buffer a plain stencil writes
@@ -269,8 +308,9 @@ extern "C" int mamr_create(const mamr_config *cfg, mamr_ctx **out)
    Geom &g = c->g;
    g.nx = cfg->nx; g.ny = cfg->ny; g.nz = cfg->nz; g.V = cfg->num_vars;
    g.X = g.nx + 2; g.Y = g.ny + 2; g.Z = g.nz + 2;
-   // split layout: dense interior rows, then the two k-ghost planes; each
-   // block-variable starts a 128-byte line
+   // split layout: dense interior rows, then the two k-ghost planes; a
+   // block-variable takes whole 128-byte lines (and the pool's start,
+   // pool_shift, puts its interior rows on line boundaries)
    const int line = 128 / (int) elem_size(c);
    g.Zp = g.Z;
    g.koff = 0;
@@ -288,10 +328,9 @@ extern "C" int mamr_create(const mamr_config *cfg, mamr_ctx **out)
       e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
    c->device = dev;
    c->pool_bytes = (size_t) cfg->max_blocks * g.V * g.bv * elem_size(c);
+   c->pool_shift = pool_shift(g, elem_size(c));
    if (e == cudaSuccess)
-      e = cudaMalloc(&c->pool, c->pool_bytes);
-   if (e == cudaSuccess)
-      e = cudaMemsetAsync(c->pool, 0, c->pool_bytes, c->stream);
+      e = pool_alloc(c, &c->pool);
    if (e == cudaSuccess)
       e = cudaMalloc((void **) &c->d_acc, 64);
    if (e == cudaSuccess)
@@ -322,8 +361,8 @@ extern "C" int mamr_destroy(mamr_ctx *c)
    if (c->stream)
       cudaStreamSynchronize(c->stream);
    mamr::batched_destroy(c->batched);
-   if (c->pool) cudaFree(c->pool);
-   if (c->pool_alt) cudaFree(c->pool_alt);
+   pool_free(c, c->pool);
+   pool_free(c, c->pool_alt);
    for (auto &b : c->d_tasks) b.release();
    c->d_slots.release(); c->d_partials.release(); c->d_jobs.release();
    c->d_stage.release(); c->d_stage_slots.release(); c->d_sums.release();
@@ -1389,10 +1428,8 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
          per_ts += !(st % freq);
    const size_t n_cs = (size_t) per_ts * num_ts;
    const size_t es = elem_size(c);
-   if (!c->pool_alt) {
-      CUDA_TRY(cudaMalloc(&c->pool_alt, c->pool_bytes));
-      CUDA_TRY(cudaMemsetAsync(c->pool_alt, 0, c->pool_bytes, c->stream));
-   }
+   if (!c->pool_alt)
+      CUDA_TRY(pool_alloc(c, &c->pool_alt));
    CUDA_TRY(B->partials.ensure(sizeof(double) * std::max(1, nb) * V));
    if (c->fp32) {
       CUDA_TRY(B->acc.ensure(std::max<size_t>(1, n_cs * V) * 16));

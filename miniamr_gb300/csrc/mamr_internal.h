@@ -17,7 +17,8 @@ namespace mamr {
 //    128-byte lines DRAM delivers carry nothing but interior cells; the
 //    ghost values k = 0 and k = nz+1 of row (i, j) sit in two planes after
 //    the rows, at kplane + i*Y + j and kplane + X*Y + i*Y + j.  bv is
-//    rounded up to whole 128-byte lines.
+//    rounded up to whole 128-byte lines, and the device pools start where
+//    interior row (1, 1) of every block-variable begins a line.
 //  - inline (kplane < 0; host buffers): rows of Zp elements holding
 //    k = 0..nz+1 at columns koff .. koff+nz+1.
 struct Geom {
