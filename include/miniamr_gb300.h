@@ -399,7 +399,8 @@ int mamr_set_tuning(mamr_ctx *ctx, int32_t choice);
  * i-planes per thread (pencil kernel), CTAs.  The warp-per-block kernel
  * reports (threads per item -- a block and one or two of its variables:
  * 32 or 64, variables per CTA (items per CTA x variables per item), rows
- * of 8 cells per thread: 2 or 1, 0, CTAs): i-planes 0 marks it. */
+ * of 8 cells per thread: 2 or 1, 0, CTAs): i-planes 0 marks it, -1 its
+ * form whose tiles arrive by tensor copies. */
 int mamr_get_tuning(const mamr_ctx *ctx, int32_t *choice,
                     int32_t *n_candidates, int32_t *shape);
 

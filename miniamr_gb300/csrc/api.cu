@@ -1497,14 +1497,15 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
             (const float *) cur, (float *) oth, c->g, c->cfg.stencil,
             (const BItem *) B->items.p, recipes, keep,
             (const float *) stale_pool,
-            nb, sh, last, do_cs, part, sums_at, acc, flags,
+            nb, sh, last, do_cs, part, sums_at, acc, flags, c->d_err, n_bv,
             (const float *) zf_src, (float *) zf_dst, c->stream));
       return launch_batched_stage((const double *) cur, (double *) oth, c->g,
                                   c->cfg.stencil, (const BItem *) B->items.p,
                                   recipes, keep, (const double *) stale_pool,
                                   nb,
                                   sh, last, do_cs, part, sums_at, acc,
-                                  c->d_err, (const double *) zf_src,
+                                  c->d_err, c->d_err, n_bv,
+                                  (const double *) zf_src,
                                   (double *) zf_dst, c->stream);
    };
    std::vector<StageShape> cands;
@@ -1729,10 +1730,10 @@ extern "C" int mamr_get_tuning(const mamr_ctx *c, int32_t *choice,
       const bool brick = sh.kernel == 1;
       shape[0] = sh.threads;
       // the warp-per-block kernel: variables per CTA = items x variables
-      // per item, and i-planes 0
+      // per item, and i-planes 0 (-1: its tensor-copy form)
       shape[1] = brick ? sh.vpc * std::max(1, sh.planes) : sh.vpc;
       shape[2] = sh.rows;
-      shape[3] = brick ? 0 : sh.planes;
+      shape[3] = brick ? (sh.tma ? -1 : 0) : sh.planes;
       shape[4] = sh.grid;
    }
    return MAMR_OK;

@@ -288,10 +288,12 @@ void batched_mesh_changed(BatchedState *b);
 //                   x-face planes of each tile arrive by bulk tensor copy
 //   warp-per-item kernel (8^3 blocks, 7-point; kernel = 1): threads = 32
 //                   or 64 per item, vpc = items per CTA, rows = rows per
-//                   thread, planes = variables per item (1 or 2)
+//                   thread, planes = variables per item (1 or 2); tma = 1:
+//                   its tensor-copy form (FP32)
 struct StageShape {
    int threads = 0, vpc = 1, rows = 1, planes = 4, grid = 1;
    int kernel = 0;
+   int tma = 0;
 };
 
 // Launches one fused stage: src -> dst for every block and variable.
@@ -302,7 +304,8 @@ struct StageShape {
 // or null on one level; stale: the pool the run started from (recipes'
 // stale cells); zf_src / zf_dst: the warp-per-block kernel's z-face arrays
 // of the source (null when the previous stage wrote none) and the
-// destination (null: none written).
+// destination (null: none written); ctx_err: the context's error word (a
+// bounded wait that ran out); n_bv: block-variables the pools hold.
 template <typename T>
 int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
                          const BItem *items, const GhostRecipe *recipes,
@@ -310,6 +313,7 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
                          const StageShape &sh, int write_ghosts, int do_cs,
                          double *partials, double *sums,
                          unsigned long long *acc, unsigned *err,
+                         unsigned *ctx_err, long long n_bv,
                          const T *zf_src, T *zf_dst, cudaStream_t s);
 // The generic kernel's launch shapes for this geometry (first = default).
 template <typename T>
@@ -337,8 +341,8 @@ template <typename T>
 int launch_brick_stage(const T *src, T *dst, const Geom &g,
                        const BItem *items, int n_blocks, const StageShape &sh,
                        int write_ghosts, int do_cs, unsigned long long *acc,
-                       unsigned *err, const T *zf_src, T *zf_dst,
-                       cudaStream_t s);
+                       unsigned *err, unsigned *ctx_err, long long n_bv,
+                       const T *zf_src, T *zf_dst, cudaStream_t s);
 // Elements of one z-face array (planes k = 1 and k = 8 of every slot and
 // variable) of the warp-per-block kernel.
 inline size_t brick_zface_elems(const Geom &g, int max_blocks)

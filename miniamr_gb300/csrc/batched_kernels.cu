@@ -387,6 +387,7 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
                          const StageShape &sh, int write_ghosts, int do_cs,
                          double *partials, double *sums,
                          unsigned long long *acc, unsigned *err,
+                         unsigned *ctx_err, long long n_bv,
                          const T *zf_src, T *zf_dst, cudaStream_t s)
 {
    if (n_blocks == 0)
@@ -402,8 +403,8 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
    }
    if (sh.kernel == 1) {
       int launches = launch_brick_stage(src, dst, g, items, n_blocks, sh,
-                                        write_ghosts, do_cs, acc, err, zf_src,
-                                        zf_dst, s);
+                                        write_ghosts, do_cs, acc, err,
+                                        ctx_err, n_bv, zf_src, zf_dst, s);
       if (launches >= 0 && do_cs && sizeof(T) == 8)
          launches += launch_fp64_checksums((const double *) dst, g, items,
                                            n_blocks, partials, sums, s);
@@ -546,6 +547,7 @@ template int launch_batched_stage<float>(const float *, float *, const Geom &,
                                          int, const StageShape &, int, int,
                                          double *, double *,
                                          unsigned long long *, unsigned *,
+                                         unsigned *, long long,
                                          const float *, float *,
                                          cudaStream_t);
 template int launch_batched_stage<double>(const double *, double *,
@@ -555,6 +557,7 @@ template int launch_batched_stage<double>(const double *, double *,
                                           int, const StageShape &, int, int,
                                           double *, double *,
                                           unsigned long long *, unsigned *,
+                                          unsigned *, long long,
                                           const double *, double *,
                                           cudaStream_t);
 

@@ -32,6 +32,7 @@
 #include "batched.h"
 #include "arith.cuh"
 #include "cp_async.cuh"
+#include "tma.cuh"
 
 namespace mamr {
 
@@ -515,27 +516,6 @@ pencil_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
 // split layout (rows of 64 bytes, planes of 1152 bytes, block-variables bv
 // elements apart); a box is one plane's 16 interior rows.
 
-// Waits for phase `parity` of the mbarrier at shared address bar; false if
-// it has not completed after 64 tries.  Each try suspends the thread until
-// the phase completes or a time hint of 10 ms runs out, so a waiting warp
-// takes no issue slots from the warps that compute.
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
-{
-   for (int it = 0; it < 64; it++) {
-      unsigned ok;
-      asm volatile("{\n\t.reg .pred p;\n\t"
-                   "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, "
-                   "%3;\n\t"
-                   "selp.u32 %0, 1, 0, p;\n\t}"
-                   : "=r"(ok)
-                   : "r"(bar), "r"(parity), "r"(10000000u)
-                   : "memory");
-      if (ok)
-         return true;
-   }
-   return false;
-}
-
 __device__ __forceinline__ void tma_plane(float *dst, const CUtensorMap *tm,
                                           int i, int bvi, unsigned bar)
 {
@@ -805,15 +785,8 @@ int launch_fp64_checksums(const double *pool, const Geom &g,
    return 2;
 }
 
-// cuTensorMapEncodeTiled, from the driver through the runtime (no link
-// against the driver library); null if unavailable.
-using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType,
-                                   cuuint32_t, void *, const cuuint64_t *,
-                                   const cuuint64_t *, const cuuint32_t *,
-                                   const cuuint32_t *, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion,
-                                   CUtensorMapFloatOOBfill);
-static EncodeTiledFn encode_tiled()
+// cuTensorMapEncodeTiled through the runtime's driver entry point.
+EncodeTiledFn encode_tiled()
 {
    static std::once_flag once;
    static EncodeTiledFn fn = nullptr;
