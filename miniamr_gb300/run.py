@@ -20,8 +20,10 @@ Options this library does not run are refused: --morton, --hilbert and
 --trunc_hilbert (lb_method > 0 reorders the initial blocks and the
 children), --time (time-based stepping) and --plot_freq > 0.
 
-Two options are this library's own: --fp32 (cells in FP32,
-MAMR_FP32) and --plain (the per-call path instead of the batched one).
+Three options are this library's own: --fp32 (cells in FP32,
+MAMR_FP32), --plain (the per-call path instead of the batched one) and
+--tuning K (the batched path's launch-shape candidate K, mamr_set_tuning,
+instead of the tuner's choice).
 """
 from __future__ import annotations
 
@@ -67,6 +69,7 @@ class RunSpec:
     objects: np.ndarray
     fp32: bool = False
     plain: bool = False
+    tuning: int = -1
 
     @property
     def tol(self) -> float:
@@ -108,6 +111,7 @@ def parse(argv) -> RunSpec:
     o = dict(DEFAULTS)
     objs, n_objects = [], None
     fp32 = plain = False
+    tuning = -1
     argv = list(argv)
     i = 0
 
@@ -158,6 +162,11 @@ def parse(argv) -> RunSpec:
         elif a == "--plain":
             plain = True
             i += 1
+        elif a == "--tuning":
+            tuning = int(take(1)[0])
+            if tuning < 0:
+                raise ValueError("--tuning: a candidate index >= 0")
+            i += 2
         else:
             raise ValueError(f"Unknown input parameter {a}")
     if (n_objects or 0) != len(objs):
@@ -191,7 +200,7 @@ def parse(argv) -> RunSpec:
     objects = np.zeros(len(objs), dtype=AMR_OBJECT_DTYPE)
     for q, (t, b, c, m, s, inc) in enumerate(objs):
         objects[q] = (t, b, c, m, s, inc)
-    return RunSpec(o, objects, fp32=fp32, plain=plain)
+    return RunSpec(o, objects, fp32=fp32, plain=plain, tuning=tuning)
 
 
 def check_tolerance(spec: RunSpec, sums: np.ndarray):
@@ -217,7 +226,10 @@ def main(argv=None) -> int:
     lib = load()
     cfg = spec.config()
     with lib.context(cfg) as ctx:
+        if spec.tuning >= 0:
+            ctx.set_tuning(spec.tuning)
         sums, st, _ = ctx.amr_run(spec.params(), spec.objects)
+        tun = ctx.tuning()
     o = spec.opts
     print(f"miniAMR on one GB300: {o['nx']}x{o['ny']}x{o['nz']} cells, "
           f"{o['num_vars']} variables, stencil {o['stencil']}, "
@@ -236,6 +248,13 @@ def main(argv=None) -> int:
     print(f"time: total {st['total_seconds']:.3f} s, stages "
           f"{st['stage_seconds']:.3f} s ({rate:.3e} cell-var updates/s), "
           f"refinement {st['refine_seconds']:.3f} s")
+    if tun["choice"] >= 0:
+        print(f"launch shape: candidate {tun['choice']} of "
+              f"{tun['candidates']} ({tun['threads']} threads, "
+              f"{tun['vars_per_cta']} variables per CTA, "
+              f"{tun['rows_per_thread']} rows, "
+              f"{tun['planes_per_thread']} planes per thread, "
+              f"{tun['ctas']} CTAs)")
     return 1 if bad is not None else 0
 
 

@@ -65,12 +65,15 @@ def test_parse_defaults_and_refusals():
     assert spec.tol == 1e-8
     for bad in (["--hilbert"], ["--time", "1.0"], ["--nx", "3"],
                 ["--npx", "2"], ["--stencil", "9"], ["--bogus"],
-                ["--num_objects", "1"], ["--plot_freq", "2"]):
+                ["--num_objects", "1"], ["--plot_freq", "2"],
+                ["--tuning", "-1"], ["--tuning"]):
         with pytest.raises(ValueError):
             runmod.parse(bad)
     # one-rank no-ops are accepted
     runmod.parse(["--lb_opt", "2", "--send_faces", "--rcb", "--reorder",
                   "1", "--comm_vars", "5"])
+    assert spec.tuning == -1
+    assert runmod.parse(["--tuning", "3", "--fp32"]).tuning == 3
 
 
 def test_driver_errors(oracle_lib):
