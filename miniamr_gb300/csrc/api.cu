@@ -1450,11 +1450,11 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       B->has_recipes ? (const GhostRecipe *) B->recipes.p : nullptr;
    const int *keep = B->has_recipes ? (const int *) B->keep.p : nullptr;
    // one stage: cur -> oth with launch shape sh; q = the stage's index in
-   // the run (-1: a tuning stage).  The warp-per-block kernel writes the
-   // z-face array of stage q and reads that of stage q - 1.
+   // the run (-1: a tuning stage).  The warp-per-block and tile kernels
+   // write the z-face array of stage q and read that of stage q - 1.
    auto stage = [&](const void *cur, void *oth, const StageShape &sh,
                     int last, bool do_cs, int cnt, int q) -> int {
-      const bool zfs = sh.kernel == 1 && q >= 0;
+      const bool zfs = (sh.kernel == 1 || sh.kernel == 2) && q >= 0;
       void *zf_dst = zfs ? B->zf[q & 1].p : nullptr;
       const void *zf_src = zfs && q > 0 ? B->zf[(q - 1) & 1].p : nullptr;
       unsigned long long *acc =
@@ -1532,10 +1532,10 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    c->tune_last = choice;
    c->tune_n = (int) cands.size();
    c->tune_shape = sh;
-   if (sh.kernel == 1 && num_ts * spt > 1) {
-      // the warp-per-block kernel's z-face arrays (written by each stage,
-      // read by the next)
-      const size_t zb = brick_zface_elems(c->g, c->cfg.max_blocks) * es;
+   if ((sh.kernel == 1 || sh.kernel == 2) && num_ts * spt > 1) {
+      // the warp-per-block and tile kernels' z-face arrays (written by
+      // each stage, read by the next)
+      const size_t zb = zface_elems(c->g, c->cfg.max_blocks) * es;
       CUDA_TRY(B->zf[0].ensure(zb));
       CUDA_TRY(B->zf[1].ensure(zb));
    }

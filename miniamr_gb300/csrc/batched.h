@@ -330,7 +330,8 @@ int launch_tile_stage(const T *src, T *dst, const Geom &g, int stencil,
                       const BItem *items, const GhostRecipe *recipes,
                       const int *keep, const T *stale, int n_blocks,
                       const StageShape &sh, int write_ghosts, int do_cs,
-                      unsigned long long *acc, unsigned *err, cudaStream_t s);
+                      unsigned long long *acc, unsigned *err,
+                      const T *zf_src, T *zf_dst, cudaStream_t s);
 
 // Warp-per-item variant for 8^3 blocks and the 7-point stencil (any mesh):
 // its launch shapes, and one stage (FP32 checksums fused into acc).
@@ -343,11 +344,20 @@ int launch_brick_stage(const T *src, T *dst, const Geom &g,
                        int write_ghosts, int do_cs, unsigned long long *acc,
                        unsigned *err, unsigned *ctx_err, long long n_bv,
                        const T *zf_src, T *zf_dst, cudaStream_t s);
-// Elements of one z-face array (planes k = 1 and k = 8 of every slot and
-// variable) of the warp-per-block kernel.
-inline size_t brick_zface_elems(const Geom &g, int max_blocks)
+// z-face arrays of the warp-per-block and tile kernels: each stage of a
+// batched run also stores every block-variable's k = 1 and k = nz planes
+// (side 0 and 1, nx * ny values each at (i-1)*ny + (j-1)) contiguously,
+// and the next stage reads its z ghosts from there instead of one value
+// per row of the neighbour.  Elements of one array, and the offset of a
+// plane.
+inline size_t zface_elems(const Geom &g, int max_blocks)
 {
-   return (size_t) max_blocks * g.V * 2 * 64;
+   return (size_t) max_blocks * g.V * 2 * g.nx * g.ny;
+}
+__host__ __device__ inline long long zface_at(const Geom &g, int slot,
+                                              int var, int side)
+{
+   return (((long long) slot * g.V + var) * 2 + side) * g.nx * g.ny;
 }
 
 // Pencil variant for single-level meshes of 16^3 blocks: CTAs walk chains

@@ -395,7 +395,8 @@ int launch_batched_stage(const T *src, T *dst, const Geom &g, int stencil,
    if (sh.kernel == 2) {
       int launches = launch_tile_stage(src, dst, g, stencil, items, recipes,
                                        keep, stale, n_blocks, sh,
-                                       write_ghosts, do_cs, acc, err, s);
+                                       write_ghosts, do_cs, acc, err, zf_src,
+                                       zf_dst, s);
       if (launches >= 0 && do_cs && sizeof(T) == 8)
          launches += launch_fp64_checksums((const double *) dst, g, items,
                                            n_blocks, partials, sums, s);

@@ -13,7 +13,13 @@
 // i-planes (16-byte row loads, each 27-point plane sum formed once), FP64
 // threads one (j, k) column; the reference's operation order
 // (ref/stencil.c:82-144) and correctly rounded division throughout, the
-// FP32 fixed-point checksum fused.
+// FP32 fixed-point checksum fused.  During a run each stage also stores
+// the k = 1 and k = N planes of every block-variable it updates in a
+// z-face array (batched.h: zface_at), and the next stage takes its z faces
+// from there -- the same-level and boundary planes as 16-byte copies into
+// a staging area, scattered into the tile after the wait; coarse and fine
+// z faces as values of those planes -- instead of one value per 64-byte
+// row of the neighbour.
 #include <algorithm>
 #include <vector>
 
@@ -39,6 +45,7 @@ template <typename T, int N> struct TileK {
                                                  : N * N;
    static constexpr int MINB = sizeof(T) == 4 ? (N == 16 ? 3 : 16)
                                               : (N == 16 ? 2 : 8);
+   static constexpr int ZP = N * N;                  // z-plane elements
    __device__ static int at(int i, int j, int k)
    {
       return (i * Y + j) * ZS + KO + k;
@@ -48,9 +55,12 @@ template <typename T, int N> struct TileK {
       return dir == 0 ? at(gn, a, b) : (dir == 1 ? at(a, gn, b)
                                                  : at(a, b, gn));
    }
+   // two tiles, each with a staging area for its two z planes, and three
+   // descriptors
    static size_t smem_bytes()
    {
-      return 2 * (size_t) TILE * sizeof(T) + 3 * sizeof(BItem) + 16;
+      return 2 * (size_t) (TILE + 2 * ZP) * sizeof(T) + 3 * sizeof(BItem) +
+             16;
    }
 };
 
@@ -92,13 +102,16 @@ __device__ __forceinline__ void edge_cell(int e, int &gi, int &gj, int &gk,
    }
 }
 
-// Queues the copies that fill tile tb for item (block sd, var).
+// Queues the copies that fill tile tb for item (block sd, var); with the
+// source's z-face array zf, the same-level and boundary z planes go to the
+// staging area zs (plane of side 0, then side 1).
 template <typename T, int ST, int N>
 __device__ __forceinline__ void tile_issue(const T *__restrict__ src,
                                            const T *__restrict__ stale,
                                            const Geom &g, const BItem &sd,
                                            const GhostRecipe *__restrict__ rc,
-                                           int var, T *tb)
+                                           int var, T *tb,
+                                           const T *__restrict__ zf, T *zs)
 {
    using K = TileK<T, N>;
    constexpr int VW = K::VW, CPR = K::CPR, THREADS = K::THREADS;
@@ -131,6 +144,11 @@ __device__ __forceinline__ void tile_issue(const T *__restrict__ src,
                   cp_async16(tb + K::at(a, gn, 1 + q * VW),
                              sb + D.cell(a, p, 1) + q * VW);
             }
+         } else if (zf) {
+            const int nbs = f.type == FACE_SAME ? f.nb[0] : sd.slot;
+            const T *pl = zf + zface_at(g, nbs, var, p == N);
+            for (int c = tid; c < K::ZP / VW; c += THREADS)
+               cp_async16(zs + (low ? 0 : K::ZP) + c * VW, pl + c * VW);
          } else {
             for (int e = tid; e < N * N; e += THREADS) {
                const int i = e / N + 1, j = e - (i - 1) * N + 1;
@@ -138,14 +156,18 @@ __device__ __forceinline__ void tile_issue(const T *__restrict__ src,
             }
          }
       } else if (f.type == FACE_COARSE) {
-         // the coarse values, scaled by 1/4 once they have landed
+         // the coarse values, scaled by 1/4 once they have landed (z: from
+         // the coarse block's plane in the z-face array)
          const T *sb = src + bv_offset(g, f.nb[0], var);
          const int p = low ? N : 1, h = N / 2;
+         const T *pl = dir == 2 && zf ? zf + zface_at(g, f.nb[0], var, p == N)
+                                      : nullptr;
          for (int e = tid; e < N * N; e += THREADS) {
             const int a = e / N + 1, b = e - (a - 1) * N + 1;
+            const int ca = (a + 1) / 2 + f.jq * h, cb = (b + 1) / 2 + f.iq * h;
             cp_async_elem(tb + K::ghost_at(dir, gn, a, b),
-                          sb + D.fcell(dir, p, (a + 1) / 2 + f.jq * h,
-                                       (b + 1) / 2 + f.iq * h));
+                          pl ? pl + (ca - 1) * N + (cb - 1)
+                             : sb + D.fcell(dir, p, ca, cb));
          }
       }
    }
@@ -191,19 +213,36 @@ __device__ __forceinline__ void tile_issue(const T *__restrict__ src,
    }
 }
 
-// After the copies landed: coarse face values scaled, fine faces summed,
-// recipe transforms of the 27-point edges formed.
+// After the copies landed: staged z planes scattered into the tile,
+// coarse face values scaled, fine faces summed (z: from the finer blocks'
+// planes in the z-face array zf), recipe transforms of the 27-point edges
+// formed.
 template <typename T, int ST, int N>
 __device__ __forceinline__ void tile_fix(const T *__restrict__ src,
                                          const T *__restrict__ stale,
                                          const Geom &g, const BItem &sd,
                                          const GhostRecipe *__restrict__ rc,
-                                         int var, T *tb)
+                                         int var, T *tb,
+                                         const T *__restrict__ zf,
+                                         const T *zs)
 {
    using K = TileK<T, N>;
    constexpr int THREADS = K::THREADS;
    const Dims<N, N, N> D(g);
    const int tid = threadIdx.x;
+   if (zf) {
+#pragma unroll
+      for (int l = 4; l < 6; l++) {
+         const int type = sd.f[l].type;
+         if (type != FACE_SAME && type != FACE_BC)
+            continue;
+         const int gn = l == 4 ? 0 : N + 1;
+         for (int e = tid; e < N * N; e += THREADS) {
+            const int i = e / N + 1, j = e - (i - 1) * N + 1;
+            tb[K::at(i, j, gn)] = zs[(l - 4) * K::ZP + e];
+         }
+      }
+   }
 #pragma unroll
    for (int l = 0; l < 6; l++) {
       const BFace &f = sd.f[l];
@@ -220,11 +259,21 @@ __device__ __forceinline__ void tile_fix(const T *__restrict__ src,
          } else {
             const int jq = a > h, iq = b > h;
             const int a2 = a - jq * h, b2 = b - iq * h;
-            const T *fb = src + bv_offset(g, f.nb[iq * 2 + jq], var);
-            T s = fb[D.fcell(dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
-                  fb[D.fcell(dir, p, 2 * a2 - 1, 2 * b2)];
-            s = s + fb[D.fcell(dir, p, 2 * a2, 2 * b2 - 1)];
-            s = s + fb[D.fcell(dir, p, 2 * a2, 2 * b2)];
+            const int nbs = f.nb[iq * 2 + jq];
+            T s;
+            if (dir == 2 && zf) {
+               const T *pl = zf + zface_at(g, nbs, var, p == N) +
+                             (2 * a2 - 2) * N + 2 * b2 - 2;
+               s = pl[0] + pl[1];
+               s = s + pl[N];
+               s = s + pl[N + 1];
+            } else {
+               const T *fb = src + bv_offset(g, nbs, var);
+               s = fb[D.fcell(dir, p, 2 * a2 - 1, 2 * b2 - 1)] +
+                   fb[D.fcell(dir, p, 2 * a2 - 1, 2 * b2)];
+               s = s + fb[D.fcell(dir, p, 2 * a2, 2 * b2 - 1)];
+               s = s + fb[D.fcell(dir, p, 2 * a2, 2 * b2)];
+            }
             x = s;
          }
       }
@@ -277,11 +326,12 @@ __device__ __forceinline__ void tile_ghosts_out(const T *tb, T *d,
 }
 
 // The update of one tile into d (the item's destination block-variable),
-// FP32 checksum terms into part.
+// FP32 checksum terms into part; with zfd, its k = 1 and k = N planes also
+// into the z-face array (side 0 at zfd, side 1 at zfd + ZP).
 template <typename T, int ST, int N>
 __device__ __forceinline__ void tile_update(const T *tb, T *d, const Geom &g,
                                             int do_cs, Fixed52 &part,
-                                            bool &ok)
+                                            bool &ok, T *zfd)
 {
    using K = TileK<T, N>;
    const Dims<N, N, N> D(g);
@@ -317,6 +367,12 @@ __device__ __forceinline__ void tile_update(const T *tb, T *d, const Geom &g,
          div4(w, q);
          *reinterpret_cast<float4 *>(d + D.cell(i, j, k)) =
             make_float4(q[0], q[1], q[2], q[3]);
+         if (zfd) {
+            if (k == 1)
+               zfd[(i - 1) * N + j - 1] = q[0];
+            if (k + 3 == N)
+               zfd[K::ZP + (i - 1) * N + j - 1] = q[3];
+         }
          if (do_cs) {
 #pragma unroll
             for (int m = 0; m < 4; m++)
@@ -409,7 +465,10 @@ __device__ __forceinline__ void tile_update(const T *tb, T *d, const Geom &g,
             w = w + TL(i, j, k + 1);
             w = w + TL(i, j + 1, k);
             w = w + ap;
-            d[D.cell(i, j, k)] = div7(w);
+            const T q = div7(w);
+            d[D.cell(i, j, k)] = q;
+            if (zfd && (k == 1 || k == N))
+               zfd[(k == N ? K::ZP : 0) + (i - 1) * N + j - 1] = q;
             am = ac;
             ac = ap;
          }
@@ -429,7 +488,10 @@ __device__ __forceinline__ void tile_update(const T *tb, T *d, const Geom &g,
 #pragma unroll 4
          for (int i = 1; i <= N; i++) {
             const T s2 = S(i + 1);
-            d[D.cell(i, j, k)] = div27((s0 + s1) + s2);
+            const T q = div27((s0 + s1) + s2);
+            d[D.cell(i, j, k)] = q;
+            if (zfd && (k == 1 || k == N))
+               zfd[(k == N ? K::ZP : 0) + (i - 1) * N + j - 1] = q;
             s0 = s1;
             s1 = s2;
          }
@@ -446,13 +508,15 @@ tile_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
                   const int *__restrict__ keep, const T *__restrict__ stale,
                   int nb, int write_ghosts, int do_cs,
                   unsigned long long *__restrict__ acc,
-                  unsigned *__restrict__ err)
+                  unsigned *__restrict__ err, const T *__restrict__ zf_src,
+                  T *__restrict__ zf_dst)
 {
    using K = TileK<T, N>;
    constexpr int THREADS = K::THREADS;
    extern __shared__ __align__(16) unsigned char smem_raw[];
    T *tiles = reinterpret_cast<T *>(smem_raw);
-   BItem *sI = reinterpret_cast<BItem *>(tiles + 2 * K::TILE);
+   T *stg = tiles + 2 * K::TILE;        // z-plane staging of each tile
+   BItem *sI = reinterpret_cast<BItem *>(stg + 4 * K::ZP);
    const int tid = threadIdx.x;
    auto put_desc = [&](int b, BItem &to) {
       const int32_t *from = reinterpret_cast<const int32_t *>(items + b);
@@ -488,7 +552,7 @@ tile_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
    put_desc(cur_p.b, sI[0]);
    __syncthreads();
    tile_issue<T, ST, N>(src, stale, g, sI[0], recipes_of(cur_p.b), cur_p.var,
-                        tiles);
+                        tiles, zf_src, stg);
    cp_async_commit();
    for (int n = 0;; n++) {
       const int var = cur_p.var, b = cur_p.b;
@@ -496,6 +560,7 @@ tile_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       const bool more = nx.var < g.V;
       BItem &cur = sI[n % 3];
       T *tb = tiles + (n & 1) * K::TILE;
+      const T *zs = stg + (n & 1) * 2 * K::ZP;
       // the next item: descriptor, then its copies into the other tile
       // (every thread finished reading that tile before this barrier)
       if (more)
@@ -503,13 +568,14 @@ tile_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
       __syncthreads();
       if (more)
          tile_issue<T, ST, N>(src, stale, g, sI[(n + 1) % 3], recipes_of(nx.b),
-                              nx.var, tiles + ((n + 1) & 1) * K::TILE);
+                              nx.var, tiles + ((n + 1) & 1) * K::TILE, zf_src,
+                              stg + ((n + 1) & 1) * 2 * K::ZP);
       cp_async_commit();
       cp_async_wait_group<1>();
       __syncthreads();
       const GhostRecipe *rc =
          recipes ? recipes + (size_t) b * kGhostRecipes : nullptr;
-      tile_fix<T, ST, N>(src, stale, g, cur, rc, var, tb);
+      tile_fix<T, ST, N>(src, stale, g, cur, rc, var, tb, zf_src, zs);
       __syncthreads();
       T *d = dst + bv_offset(g, cur.slot, var);
       const int kb = keep ? keep[b] : 0;
@@ -522,7 +588,9 @@ tile_stage_kernel(const T *__restrict__ src, T *__restrict__ dst, Geom g,
          }
          cs_var = var;
       }
-      tile_update<T, ST, N>(tb, d, g, sizeof(T) == 4 ? do_cs : 0, part, ok);
+      tile_update<T, ST, N>(tb, d, g, sizeof(T) == 4 ? do_cs : 0, part, ok,
+                            zf_dst ? zf_dst + zface_at(g, cur.slot, var, 0)
+                                   : nullptr);
       if (sizeof(T) == 4 && do_cs)
          fixed52_flush(part, lo, hi);
       if (!more)
@@ -596,7 +664,8 @@ int launch_tile_stage(const T *src, T *dst, const Geom &g, int stencil,
                       const BItem *items, const GhostRecipe *recipes,
                       const int *keep, const T *stale, int n_blocks,
                       const StageShape &sh, int write_ghosts, int do_cs,
-                      unsigned long long *acc, unsigned *err, cudaStream_t s)
+                      unsigned long long *acc, unsigned *err,
+                      const T *zf_src, T *zf_dst, cudaStream_t s)
 {
    if (n_blocks == 0)
       return 0;
@@ -605,7 +674,7 @@ int launch_tile_stage(const T *src, T *dst, const Geom &g, int stencil,
    tile_stage_kernel<T, ST, N>                                               \
       <<<sh.grid, TileK<T, N>::THREADS, TileK<T, N>::smem_bytes(), s>>>(      \
          src, dst, g, items, recipes, keep, stale, n_blocks, write_ghosts,    \
-         cs, acc, err)
+         cs, acc, err, zf_src, zf_dst)
    const int kind = dims_kind(g);
    if (kind == 1) {
       if (stencil == 7) MAMR_TILE(7, 8);
@@ -627,13 +696,14 @@ template int launch_tile_stage<float>(const float *, float *, const Geom &,
                                       const int *, const float *, int,
                                       const StageShape &, int, int,
                                       unsigned long long *, unsigned *,
-                                      cudaStream_t);
+                                      const float *, float *, cudaStream_t);
 template int launch_tile_stage<double>(const double *, double *,
                                        const Geom &, int, const BItem *,
                                        const GhostRecipe *, const int *,
                                        const double *, int,
                                        const StageShape &, int, int,
                                        unsigned long long *, unsigned *,
+                                       const double *, double *,
                                        cudaStream_t);
 
 }  // namespace mamr
