@@ -386,9 +386,10 @@ int mamr_amr_run(mamr_ctx *ctx, const mamr_config *cfg,
  * for 8^3 blocks and the 7-point stencil, first one or two warps per
  * (block, variable) with 4 or 2 items per CTA; otherwise threads per variable and
  * variables per CTA (1, 2, 4).  choice < 0 (the default): the first batched
- * run for each (block shape, stencil, precision, kernel, work size) times
- * every candidate for a few stages into the spare pool and keeps the
- * fastest for the process (environment MAMR_TUNE=off keeps candidate 0).
+ * run for each (block shape, stencil, precision, kernel, work size,
+ * checksum frequency) times every candidate for a few stages into the
+ * spare pool, taking checksums as the run does, and keeps the fastest for
+ * the process (environment MAMR_TUNE=off keeps candidate 0).
  * choice >= 0 forces that candidate (clamped to the last) on this context.
  * Every candidate gives bit-identical results. */
 int mamr_set_tuning(mamr_ctx *ctx, int32_t choice);

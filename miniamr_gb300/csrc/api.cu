@@ -1305,19 +1305,24 @@ static int build_items_only(mamr_ctx *c)
 
 // The stage loop of ref/driver.c:73-108 as one fused launch per stage.
 // ---- launch-shape autotuner ----------------------------------------------
+// Stage indices of the tuner's stages (a run's stages count from 0).
+constexpr int kTunePrime = -2, kTuneTimed = -3;
 // The first batched run for each (block shape, stencil, precision, kernel,
-// work size) times every candidate shape of the stage kernel -- one
-// warm-up and three timed stages each, current pool into the spare pool,
-// no checksum, no ghost writes -- and keeps the fastest for the process.
+// work size, checksum frequency) times every candidate shape of the stage
+// kernel -- one warm-up and three timed stages each, current pool into the
+// spare pool, checksums as the run takes them, no ghost writes, z-face
+// arrays as after a run's first stage -- and keeps the fastest for the
+// process.
 // MAMR_TUNE=off in the environment keeps the first (default) candidate.
 namespace {
 struct TuneKey {
-   int nx, ny, nz, stencil, fp32, pencil, work_log2, n_cands;
+   int nx, ny, nz, stencil, fp32, pencil, work_log2, n_cands, freq;
    bool operator<(const TuneKey &o) const
    {
-      return std::tie(nx, ny, nz, stencil, fp32, pencil, work_log2, n_cands) <
+      return std::tie(nx, ny, nz, stencil, fp32, pencil, work_log2, n_cands,
+                      freq) <
              std::tie(o.nx, o.ny, o.nz, o.stencil, o.fp32, o.pencil,
-                      o.work_log2, o.n_cands);
+                      o.work_log2, o.n_cands, o.freq);
    }
 };
 std::mutex g_tune_mu;
@@ -1332,7 +1337,8 @@ bool tuning_disabled()
 
 template <typename Stage>
 static int tune_choice(mamr_ctx *c, const std::vector<StageShape> &cands,
-                       bool pencil, int nb, Stage &stage, int &choice)
+                       bool pencil, int nb, int freq, int scratch_cs,
+                       Stage &stage, int &choice)
 {
    choice = 0;
    if (cands.size() < 2 || tuning_disabled())
@@ -1345,7 +1351,7 @@ static int tune_choice(mamr_ctx *c, const std::vector<StageShape> &cands,
    }
    const TuneKey key{c->g.nx, c->g.ny, c->g.nz, c->cfg.stencil,
                      c->fp32 ? 1 : 0, pencil ? 1 : 0, lg,
-                     (int) cands.size()};
+                     (int) cands.size(), std::min(freq, 8)};
    {
       std::lock_guard<std::mutex> lk(g_tune_mu);
       auto it = g_tune_best.find(key);
@@ -1362,13 +1368,32 @@ static int tune_choice(mamr_ctx *c, const std::vector<StageShape> &cands,
    }
    float best = 0.f;
    int status = MAMR_OK;
+   // the kernels with z-face arrays are timed as the stages after a run's
+   // first run them, reading one array and writing the other: a priming
+   // stage of the first such candidate fills the array they read
+   for (size_t q = 0; q < cands.size(); q++)
+      if (cands[q].kernel == 1 || cands[q].kernel == 2) {
+         const int k = stage(c->pool, c->pool_alt, cands[q], 0, false, 0,
+                             kTunePrime);
+         if (k < 0) {
+            status = fail(MAMR_ECUDA, "priming stage: %s",
+                          cudaGetErrorString(cudaGetLastError()));
+            break;
+         }
+         c->launches += k;
+         break;
+      }
+   // the timed stages take checksums as the run's stages do (stage t of
+   // the three when t % freq == 0), into the scratch checksum slot
    for (size_t q = 0; q < cands.size() && status == MAMR_OK; q++) {
-      int k = stage(c->pool, c->pool_alt, cands[q], 0, false, 0, -1);
+      int k = stage(c->pool, c->pool_alt, cands[q], 0, false, scratch_cs,
+                    kTuneTimed);
       bool ok = k >= 0;
       c->launches += ok ? k : 0;
       ok = ok && cudaEventRecord(e0, c->stream) == cudaSuccess;
       for (int rep = 0; rep < 3 && ok; rep++) {
-         k = stage(c->pool, c->pool_alt, cands[q], 0, false, 0, -1);
+         k = stage(c->pool, c->pool_alt, cands[q], 0, freq && !(rep % freq),
+                   scratch_cs, kTuneTimed);
          ok = k >= 0;
          c->launches += ok ? k : 0;
       }
@@ -1431,15 +1456,16 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    if (!c->pool_alt)
       CUDA_TRY(pool_alloc(c, &c->pool_alt));
    CUDA_TRY(B->partials.ensure(sizeof(double) * std::max(1, nb) * V));
+   // checksum slots: one per checksum stage, and a scratch slot (n_cs) for
+   // the tuner's stages
    if (c->fp32) {
-      CUDA_TRY(B->acc.ensure(std::max<size_t>(1, n_cs * V) * 16));
-      CUDA_TRY(cudaMemsetAsync(B->acc.p, 0, std::max<size_t>(1, n_cs * V) * 16,
-                               c->stream));
-      const size_t fb = std::max<size_t>(1, n_cs) * (2 + V) * sizeof(unsigned);
+      CUDA_TRY(B->acc.ensure((n_cs + 1) * V * 16));
+      CUDA_TRY(cudaMemsetAsync(B->acc.p, 0, (n_cs + 1) * V * 16, c->stream));
+      const size_t fb = (n_cs + 1) * (2 + V) * sizeof(unsigned);
       CUDA_TRY(B->csflags.ensure(fb));
       CUDA_TRY(cudaMemsetAsync(B->csflags.p, 0, fb, c->stream));
    } else {
-      CUDA_TRY(B->sums.ensure(sizeof(double) * std::max<size_t>(1, n_cs * V)));
+      CUDA_TRY(B->sums.ensure(sizeof(double) * (n_cs + 1) * V));
    }
    const bool pencil = B->n_pencils > 0;
    const int np = B->n_pencils;
@@ -1450,13 +1476,25 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       B->has_recipes ? (const GhostRecipe *) B->recipes.p : nullptr;
    const int *keep = B->has_recipes ? (const int *) B->keep.p : nullptr;
    // one stage: cur -> oth with launch shape sh; q = the stage's index in
-   // the run (-1: a tuning stage).  The warp-per-block and tile kernels
-   // write the z-face array of stage q and read that of stage q - 1.
+   // the run, or a tuning stage (kTunePrime, kTuneTimed).  The
+   // warp-per-block and tile kernels write the z-face array of stage q and
+   // read that of stage q - 1; tuning stages write array 0 (priming) or
+   // read array 0 and write array 1 (timed).
    auto stage = [&](const void *cur, void *oth, const StageShape &sh,
                     int last, bool do_cs, int cnt, int q) -> int {
-      const bool zfs = (sh.kernel == 1 || sh.kernel == 2) && q >= 0;
-      void *zf_dst = zfs ? B->zf[q & 1].p : nullptr;
-      const void *zf_src = zfs && q > 0 ? B->zf[(q - 1) & 1].p : nullptr;
+      const bool zk = sh.kernel == 1 || sh.kernel == 2;
+      int zin = -1, zout = -1;
+      if (zk && q >= 0) {
+         zout = q & 1;
+         zin = q > 0 ? (q - 1) & 1 : -1;
+      } else if (zk && q == kTunePrime) {
+         zout = 0;
+      } else if (zk && q == kTuneTimed) {
+         zin = 0;
+         zout = 1;
+      }
+      void *zf_dst = zout >= 0 ? B->zf[zout].p : nullptr;
+      const void *zf_src = zin >= 0 ? B->zf[zin].p : nullptr;
       unsigned long long *acc =
          c->fp32 ? (unsigned long long *) B->acc.p + (size_t) cnt * V * 2
                  : nullptr;
@@ -1522,23 +1560,26 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
       return fail(MAMR_EUNSUP, "no launch shape of the batched stage kernel "
                   "fits blocks of %d x %d x %d cells; the plain path runs "
                   "them", c->g.nx, c->g.ny, c->g.nz);
+   // the warp-per-block and tile kernels' z-face arrays (written by each
+   // stage, read by the next; the tuner times those kernels with them)
+   for (const StageShape &cd : cands)
+      if (cd.kernel == 1 || cd.kernel == 2) {
+         const size_t zb = zface_elems(c->g, c->cfg.max_blocks) * es;
+         CUDA_TRY(B->zf[0].ensure(zb));
+         CUDA_TRY(B->zf[1].ensure(zb));
+         break;
+      }
    int choice = 0;
    if (c->tune_force >= 0) {
       choice = std::min<int>(c->tune_force, (int) cands.size() - 1);
-   } else if ((r = tune_choice(c, cands, pencil, nb, stage, choice))) {
+   } else if ((r = tune_choice(c, cands, pencil, nb, freq, (int) n_cs, stage,
+                               choice))) {
       return r;
    }
    const StageShape sh = cands[choice];
    c->tune_last = choice;
    c->tune_n = (int) cands.size();
    c->tune_shape = sh;
-   if ((sh.kernel == 1 || sh.kernel == 2) && num_ts * spt > 1) {
-      // the warp-per-block and tile kernels' z-face arrays (written by
-      // each stage, read by the next)
-      const size_t zb = zface_elems(c->g, c->cfg.max_blocks) * es;
-      CUDA_TRY(B->zf[0].ensure(zb));
-      CUDA_TRY(B->zf[1].ensure(zb));
-   }
    // A run of an odd number of stages ends in the spare pool: it must then
    // hold what no stage writes (stale ghosts, free slots) as the current
    // pool does, so it starts as a copy.  With an even number the run ends
