@@ -180,7 +180,10 @@ int mamr_sync(mamr_ctx *ctx);
 /* Copies n blocks from a host buffer laid out [n][num_vars][nx+2][ny+2]
  * [nz+2] (doubles) into pool slots slots[0..n).  FP32 pools round to
  * nearest.  Used once after the reference's init() has filled its host
- * arrays (ref/init.c:484-495). */
+ * arrays (ref/init.c:484-495).  A pinned buffer (cudaMallocHost,
+ * cudaHostAlloc) is read in place by one kernel over the host link; other
+ * buffers move through a device staging area.  Both directions return
+ * once the copy is complete. */
 int mamr_upload_blocks(mamr_ctx *ctx, const int32_t *slots, int32_t n,
                        const double *host);
 /* The reverse copy, for verification and dumps. */

@@ -407,7 +407,8 @@ static bool slot_ok(const mamr_ctx *c, int32_t s)
    return s >= 0 && s < c->cfg.max_blocks;
 }
 
-// Host buffers move through a bounded device staging area.
+// Host buffers that are not pinned move through a bounded device staging
+// area.
 static const size_t kStageBytes = 256u << 20;
 
 static int transfer(mamr_ctx *c, const int32_t *slots, int32_t n,
@@ -423,6 +424,33 @@ static int transfer(mamr_ctx *c, const int32_t *slots, int32_t n,
          c->hw_slots = std::max(c->hw_slots, slots[b] + 1);
    const Geom &g = c->g;
    const size_t per_block = (size_t) g.V * g.X * g.Y * g.Z;
+   // Pinned host memory the device can address: one launch reads (or
+   // writes) it in place over the host link -- no staging copy and no
+   // synchronisation per chunk.
+   cudaPointerAttributes pa;
+   if (n && cudaPointerGetAttributes(&pa, host) == cudaSuccess &&
+       pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+      double *dh = static_cast<double *>(pa.devicePointer);
+      CUDA_TRY(c->d_stage_slots.ensure(sizeof(int32_t) * n));
+      CUDA_TRY(cudaMemcpyAsync(c->d_stage_slots.p, slots, sizeof(int32_t) * n,
+                               cudaMemcpyHostToDevice, c->stream));
+      const int32_t *ds = (const int32_t *) c->d_stage_slots.p;
+      if (up && c->fp32)
+         LAUNCH_TRY(c, launch_upload((float *) c->pool, g, ds, n, dh,
+                                     c->stream));
+      else if (up)
+         LAUNCH_TRY(c, launch_upload((double *) c->pool, g, ds, n, dh,
+                                     c->stream));
+      else if (c->fp32)
+         LAUNCH_TRY(c, launch_download((const float *) c->pool, g, ds, n, dh,
+                                       c->stream));
+      else
+         LAUNCH_TRY(c, launch_download((const double *) c->pool, g, ds, n, dh,
+                                       c->stream));
+      CUDA_TRY(cudaStreamSynchronize(c->stream));
+      return MAMR_OK;
+   }
+   cudaGetLastError();
    int32_t chunk = (int32_t) std::max<size_t>(1, kStageBytes /
                                               (per_block * sizeof(double)));
    CUDA_TRY(c->d_stage.ensure(std::min<size_t>(n, chunk) * per_block *
