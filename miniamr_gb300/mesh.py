@@ -103,12 +103,15 @@ class UniformMesh:
     def split_all(self) -> np.ndarray:
         """Refines every active block once (one uniform-refine pass) and
         returns the split jobs in the reference's order.  Free slots are
-        kept in a sorted list, so "the first free slot at or after the
-        running index" is one bisection."""
+        kept negated in an ascending list -- the lowest slots last, where
+        the running index takes them and freed parents return -- so "the
+        first free slot at or after the running index" is one bisection and
+        taking or returning a slot moves few list entries."""
         import bisect
         number = self.number.tolist()
         level = self.level.tolist()
-        free = [q for q in range(self.max_blocks) if number[q] < 0]
+        neg = [-q for q in range(self.max_blocks - 1, -1, -1)
+               if number[q] < 0]
         jobs = []
         m = 0
         active = [q for q in range(self.max_blocks) if number[q] >= 0]
@@ -126,10 +129,10 @@ class UniformMesh:
                     x, y, z = nl % nx, (nl // nx) % ny, nl // (nx * ny)
                     child = [0] * 8
                     for o in range(8):
-                        i = bisect.bisect_left(free, m)
-                        if i == len(free):
+                        i = bisect.bisect_right(neg, -m) - 1
+                        if i < 0:
                             raise RuntimeError("No inactive blocks available")
-                        m = free.pop(i)
+                        m = -neg.pop(i)
                         max_active = max(max_active, m + 1)
                         i1, j1, k1 = o % 2, (o // 2) % 2, o // 4
                         number[m] = ((2 * z + k1) * cny + (2 * y + j1)) \
@@ -138,7 +141,7 @@ class UniformMesh:
                         child[o] = m
                     jobs.append((n, child))
                     number[n] = -1
-                    bisect.insort(free, n)
+                    bisect.insort(neg, -n)
                     if n < m:
                         m = n
                 n += 1
