@@ -429,7 +429,8 @@ static int transfer(mamr_ctx *c, const int32_t *slots, int32_t n,
    // synchronisation per chunk.
    cudaPointerAttributes pa;
    if (n && cudaPointerGetAttributes(&pa, host) == cudaSuccess &&
-       pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+       pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+       !(reinterpret_cast<uintptr_t>(pa.devicePointer) & 15)) {
       double *dh = static_cast<double *>(pa.devicePointer);
       CUDA_TRY(c->d_stage_slots.ensure(sizeof(int32_t) * n));
       CUDA_TRY(cudaMemcpyAsync(c->d_stage_slots.p, slots, sizeof(int32_t) * n,

@@ -922,21 +922,43 @@ int launch_stage_blocks(T *stage, const T *pool, const Geom &g,
 
 // ---------------------------------------------------------------------------
 // Host layout [n][V][X][Y][Z] doubles <-> pool slots.
+//
+// Upload: the values are read as 16-byte pairs (rows start on 16 bytes: Z
+// is even, so a pair never straddles two rows), consecutive threads taking
+// consecutive pairs and each thread four pairs a grid stride apart in
+// flight -- enough bytes moving when the values are read in place from
+// pinned host memory over the host link.
 template <typename T>
 __global__ void upload_kernel(T *__restrict__ pool, Geom g,
-                              const int32_t *__restrict__ slots, long long total,
+                              const int32_t *__restrict__ slots,
+                              long long n_pairs,
                               const double *__restrict__ dense)
 {
-   for (long long e = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-        e < total; e += (long long) gridDim.x * blockDim.x) {
-      long long row = e / g.Z;
-      int k = (int) (e - row * g.Z);
-      long long bvi = row / (g.X * g.Y);
-      int r = (int) (row - bvi * (g.X * g.Y));
-      int b = (int) (bvi / g.V), var = (int) (bvi - (long long) b * g.V);
-      int i = r / g.Y, j = r - i * g.Y;
-      pool[bv_offset(g, slots[b], var) + cell_offset(g, i, j, k)] =
-         (T) dense[e];
+   const int XY = g.X * g.Y, HZ = g.Z / 2;
+   const double2 *src = reinterpret_cast<const double2 *>(dense);
+   const long long stride = (long long) gridDim.x * blockDim.x;
+   auto put = [&](long long pr, double2 v) {
+      const long long row = pr / HZ;
+      const int k = 2 * (int) (pr - row * HZ);
+      const long long bvi = row / XY;
+      const int r = (int) (row - bvi * XY);
+      const int b = (int) (bvi / g.V), var = (int) (bvi - (long long) b * g.V);
+      const int i = r / g.Y, j = r - i * g.Y;
+      T *base = pool + bv_offset(g, slots[b], var);
+      base[cell_offset(g, i, j, k)] = (T) v.x;
+      base[cell_offset(g, i, j, k + 1)] = (T) v.y;
+   };
+   for (long long p = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+        p < n_pairs; p += 4 * stride) {
+      double2 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+         if (p + u * stride < n_pairs)
+            v[u] = src[p + u * stride];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+         if (p + u * stride < n_pairs)
+            put(p + u * stride, v[u]);
    }
 }
 
@@ -962,12 +984,14 @@ template <typename T>
 int launch_upload(T *pool, const Geom &g, const int32_t *slots, int n,
                   const double *dense, cudaStream_t s)
 {
-   long long total = (long long) n * g.V * g.X * g.Y * g.Z;
-   if (total == 0)
+   const long long pairs = (long long) n * g.V * g.X * g.Y * (g.Z / 2);
+   if (pairs == 0)
       return 0;
-   long long blocks = (total + 255) / 256;
-   upload_kernel<T><<<(int) (blocks < 152 * 64 ? blocks : 152 * 64), 256, 0,
-                      s>>>(pool, g, slots, total, dense);
+   if ((reinterpret_cast<uintptr_t>(dense) & 15) || (g.Z & 1))
+      return -1;   // the 16-byte pairs need both
+   long long blocks = (pairs + 1023) / 1024;
+   upload_kernel<T><<<(int) (blocks < 152 * 16 ? blocks : 152 * 16), 256, 0,
+                      s>>>(pool, g, slots, pairs, dense);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 

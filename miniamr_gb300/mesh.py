@@ -107,6 +107,9 @@ class UniformMesh:
         the running index takes them and freed parents return -- so "the
         first free slot at or after the running index" is one bisection and
         taking or returning a slot moves few list entries."""
+        fast = self._split_fresh_lattice()
+        if fast is not None:
+            return fast
         import bisect
         number = self.number.tolist()
         level = self.level.tolist()
@@ -151,6 +154,44 @@ class UniformMesh:
         for q, (p, ch) in enumerate(jobs):
             out["parent"][q] = p
             out["child"][q] = ch
+        return out
+
+
+    def _split_fresh_lattice(self):
+        """split_all when the active blocks are one level filling slots
+        0 .. A-1 and every later slot is free (the initial lattice): the
+        reference's slot walk then has a closed form -- job 0's children
+        take A .. A+7; job t >= 1's take the slot job t-1 freed, then the
+        next seven of A+8 ... -- computed without the walk; None otherwise."""
+        act = np.nonzero(self.number >= 0)[0]
+        a = len(act)
+        if a == 0 or act[-1] != a - 1:
+            return None
+        lev = int(self.level[0])
+        if not (self.level[:a] == lev).all() or self.max_blocks < 8 * a + 1:
+            return None
+        nx, ny, _ = self.dims(lev)
+        cnx, cny, _ = self.dims(lev + 1)
+        start, cstart = self.block_start(lev), self.block_start(lev + 1)
+        t = np.arange(a, dtype=np.int64)
+        child = np.empty((a, 8), dtype=np.int64)
+        child[0] = a + np.arange(8)
+        if a > 1:
+            child[1:, 0] = t[1:] - 1
+            child[1:, 1:] = (a + 8 + 7 * (t[1:, None] - 1) +
+                             np.arange(7)[None, :])
+        nl = self.number[:a] - start
+        x, y, z = nl % nx, (nl // nx) % ny, nl // (nx * ny)
+        o = np.arange(8)
+        i1, j1, k1 = o % 2, (o // 2) % 2, o // 4
+        cnum = (((2 * z[:, None] + k1) * cny + (2 * y[:, None] + j1)) * cnx +
+                2 * x[:, None] + i1 + cstart)
+        self.number[:a] = -1
+        self.number[child.ravel()] = cnum.ravel()
+        self.level[child.ravel()] = lev + 1
+        out = np.zeros(a, dtype=SPLIT_DTYPE)
+        out["parent"] = t
+        out["child"] = child
         return out
 
 
