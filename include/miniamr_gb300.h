@@ -155,9 +155,16 @@ enum {
    MAMR_RUN_BATCHED = 1,  /* one fused ghost+stencil(+checksum) launch per
                              stage over every block and variable */
    MAMR_RUN_GRAPH   = 2,  /* with BATCHED: replay the stages as a CUDA graph */
-   MAMR_RUN_PER_BLOCK = 4 /* with PLAIN: one stencil launch per (block,
+   MAMR_RUN_PER_BLOCK = 4, /* with PLAIN: one stencil launch per (block,
                              variable) -- the naive port, kept as a
                              baseline to measure the batched path against */
+   MAMR_RUN_NO_GHOSTS = 8 /* with BATCHED and the 7-point stencil: the
+                             run's last stage leaves the pool's ghost cells
+                             as they were instead of writing back the ghost
+                             layer it gathered -- for a caller whose next
+                             work (further batched stages, splits and
+                             consolidations) reads no ghost cell before a
+                             run without it writes them */
 };
 
 /* ---- lifetime --------------------------------------------------------- */
@@ -299,7 +306,10 @@ typedef struct {
    int32_t num_tsteps;              /* --num_tsteps */
    int32_t stages_per_ts;           /* --stages_per_ts */
    int32_t checksum_freq;           /* --checksum_freq */
-   int32_t run_flags;               /* MAMR_RUN_* of the stage stretches */
+   int32_t run_flags;               /* MAMR_RUN_* of the stage stretches
+                                       (NO_GHOSTS is the driver's own: it
+                                       sets it on the batched 7-point
+                                       stretches before the last) */
    int32_t reserved[8];             /* must be zero */
 } mamr_amr_params;
 

@@ -19,6 +19,7 @@ RUN_PLAIN = 0
 RUN_BATCHED = 1
 RUN_GRAPH = 2
 RUN_PER_BLOCK = 4
+RUN_NO_GHOSTS = 8
 
 STATUS = {
     0: "MAMR_OK",

@@ -751,7 +751,7 @@ struct Run {
    }
 
    Run(mamr_ctx *c, const mamr_config &cf, const mamr_amr_params &p)
-      : ctx(c), cfg(cf), prm(p), flags(p.run_flags)
+      : ctx(c), cfg(cf), prm(p), flags(p.run_flags & ~MAMR_RUN_NO_GHOSTS)
    {
    }
 
@@ -808,7 +808,13 @@ struct Run {
       st.refine_seconds += now() - t0 - (ev_s - ev0);
    }
 
-   void stages(int n_ts, int first_stage)
+   // A stretch of n_ts timesteps.  Batched 7-point stretches before the
+   // last leave the ghost cells in the pool as they were: the next
+   // stretch gathers its ghosts from the interiors, and splits and
+   // consolidations move interiors only, so only the last stretch's
+   // ghost layer (the one the reference's last exchange leaves) is
+   // written back.
+   void stages(int n_ts, int first_stage, bool final)
    {
       if (n_ts <= 0)
          return;
@@ -820,8 +826,11 @@ struct Run {
       std::vector<double> s((size_t) std::max(1, per_ts * n_ts) * V);
       int32_t got = 0;
       const double t0 = now();
+      const int fl = (flags & MAMR_RUN_BATCHED) && cfg.stencil == 7 && !final
+                        ? flags | MAMR_RUN_NO_GHOSTS
+                        : flags;
       int r = mamr_run_timesteps(ctx, n_ts, spt, prm.checksum_freq,
-                                 first_stage, flags, s.data(), &got);
+                                 first_stage, fl, s.data(), &got);
       if (r == MAMR_EUNSUP && (flags & MAMR_RUN_BATCHED)) {
          // refused before any stage ran: the plain path from here on
          flags = MAMR_RUN_PLAIN;
@@ -890,7 +899,7 @@ struct Run {
          pending++;
          const bool refine_now = moving && !(ts % prm.refine_freq);
          if (refine_now || ts == n_ts) {
-            stages(pending, (first_ts - 1) * prm.stages_per_ts);
+            stages(pending, (first_ts - 1) * prm.stages_per_ts, ts == n_ts);
             first_ts = ts + 1;
             pending = 0;
          }

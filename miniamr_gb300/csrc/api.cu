@@ -1450,8 +1450,8 @@ static int tune_choice(mamr_ctx *c, const std::vector<StageShape> &cands,
 }
 
 static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
-                       int32_t freq, bool graph, double *sums,
-                       int32_t *n_sums)
+                       int32_t freq, bool graph, bool ghosts_out,
+                       double *sums, int32_t *n_sums)
 {
    int r;
    zcache_drop(c);
@@ -1631,7 +1631,7 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    for (int ts = 0, q = 0; ts < num_ts && status == MAMR_OK; ts++)
       for (int st = 0; st < spt; st++, q++) {
          const bool do_cs = freq && !(st % freq);
-         const int last = (q == total - 1);
+         const int last = ghosts_out && q == total - 1;
          const int k = stage(cur, oth, sh, last, do_cs, cnt, q);
          if (k < 0) {
             status = fail(MAMR_ECUDA, "batched stage launch: %s",
@@ -1696,8 +1696,13 @@ extern "C" int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts,
    if (!c || num_ts < 0 || stages_per_ts < 1 || checksum_freq < 0)
       return fail(MAMR_EINVAL, "bad run arguments");
    c->gen++;
-   if (flags & ~(MAMR_RUN_BATCHED | MAMR_RUN_GRAPH | MAMR_RUN_PER_BLOCK))
+   if (flags & ~(MAMR_RUN_BATCHED | MAMR_RUN_GRAPH | MAMR_RUN_PER_BLOCK |
+                 MAMR_RUN_NO_GHOSTS))
       return fail(MAMR_EINVAL, "unknown run flags 0x%x", flags);
+   if ((flags & MAMR_RUN_NO_GHOSTS) &&
+       (!(flags & MAMR_RUN_BATCHED) || c->cfg.stencil != 7))
+      return fail(MAMR_EINVAL, "MAMR_RUN_NO_GHOSTS needs MAMR_RUN_BATCHED "
+                  "and the 7-point stencil");
    if (!(flags & MAMR_RUN_BATCHED)) {
       if (flags & MAMR_RUN_GRAPH)
          return fail(MAMR_EINVAL, "MAMR_RUN_GRAPH needs MAMR_RUN_BATCHED");
@@ -1707,7 +1712,8 @@ extern "C" int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts,
    if (flags & MAMR_RUN_PER_BLOCK)
       return fail(MAMR_EINVAL, "MAMR_RUN_PER_BLOCK applies to the plain path");
    return run_batched(c, num_ts, stages_per_ts, checksum_freq,
-                      (flags & MAMR_RUN_GRAPH) != 0, sums, n_sums);
+                      (flags & MAMR_RUN_GRAPH) != 0,
+                      (flags & MAMR_RUN_NO_GHOSTS) == 0, sums, n_sums);
 }
 
 extern "C" int mamr_mark_refine(mamr_ctx *c, const mamr_mark_params *p,

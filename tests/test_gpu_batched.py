@@ -7,7 +7,8 @@ import pytest
 from golden_util import trace_path
 from miniamr_gb300 import mesh as meshmod
 from miniamr_gb300.abi import (FP32, FP64, RUN_BATCHED, RUN_GRAPH,
-                               RUN_PER_BLOCK, Config, MamrError)
+                               RUN_NO_GHOSTS, RUN_PER_BLOCK, Config,
+                               MamrError)
 from miniamr_gb300.trace import read_trace, replay
 
 pytestmark = pytest.mark.gpu
@@ -197,3 +198,35 @@ def test_batched_27_permute_is_refused(gpu_lib):
     assert e.value.status == -5 and "permute" in str(e.value)
     res.ctx.run_timesteps(1, 1, 1)
     res.ctx.close()
+
+
+@pytest.mark.parametrize("dtype", [FP64, FP32])
+def test_no_ghosts_runs_then_a_full_run(gpu_lib, dtype):
+    """A batched 7-point run with MAMR_RUN_NO_GHOSTS (its last stage writes
+    no ghost layer back), then a run without the flag: every cell of the
+    pool -- ghosts included -- and every checksum as the plain path's, on
+    the reference's own multi-level mesh (the AMR driver's GPU tests cover
+    the flag with splits and consolidations between the runs).  The flag
+    is refused without the batched path and with the 27-point stencil."""
+    recs = _multilevel_prefix(read_trace(trace_path("amr7")))
+    res = replay(gpu_lib, recs, dtype=dtype)
+    ctx = res.ctx
+    cap = ctx.cfg.max_blocks
+    every = np.arange(cap)
+    state = ctx.download(every)
+    outs = []
+    for first in (0, RUN_BATCHED | RUN_GRAPH | RUN_NO_GHOSTS):
+        ctx.upload(every, state)
+        s1 = ctx.run_timesteps(1, 3, 1, flags=first)
+        s2 = ctx.run_timesteps(1, 2, 1, first_stage=3,
+                               flags=RUN_BATCHED if first else 0)
+        outs.append((s1, s2, ctx.download(every)))
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(bits(a), bits(b))
+    with pytest.raises(MamrError, match="NO_GHOSTS"):
+        ctx.run_timesteps(1, 1, 1, flags=RUN_NO_GHOSTS)
+    ctx.close()
+    cfg = Config.make(8, 8, 8, 2, 16, stencil=27, dtype=dtype)
+    with gpu_lib.context(cfg) as c27:
+        with pytest.raises(MamrError, match="NO_GHOSTS"):
+            c27.run_timesteps(1, 1, 1, flags=RUN_BATCHED | RUN_NO_GHOSTS)
