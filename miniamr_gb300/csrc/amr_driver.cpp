@@ -129,9 +129,48 @@ class Mesh {
    int active() const { return active_; }
 
    // Active slots in sorted_list order: level ascending, block number
-   // descending (ref/block.c:610-625).
+   // descending (ref/block.c:610-625).  Level l's numbers fill
+   // [start_[l], start_[l+1]), so start_[l] + start_[l+1] - 1 - number
+   // orders the blocks that way within [0, start_[num_refine+1]); while
+   // that range fits 32 bits the keys are radix-sorted (11 bits a pass),
+   // else sorted as (level, complement of the number) pairs.
    std::vector<int> sorted() const
    {
+      const long long total = start_[nr_ + 1];
+      if (total > 0 && total <= (1ll << 32)) {
+         std::vector<uint32_t> k, k2;
+         std::vector<int> v, v2;
+         k.reserve(active_);
+         v.reserve(active_);
+         for (int n = 0; n < max_block_; n++) {
+            const Blk &bp = b_[n];
+            if (bp.number < 0)
+               continue;
+            k.push_back((uint32_t) (start_[bp.level] + start_[bp.level + 1] -
+                                    1 - bp.number));
+            v.push_back(n);
+         }
+         k2.resize(k.size());
+         v2.resize(v.size());
+         int bits = 0;
+         while (bits < 33 && (1ll << bits) < total)
+            bits++;
+         for (int sh = 0; sh < bits; sh += 11) {
+            size_t cnt[2049] = {};
+            for (const uint32_t x : k)
+               cnt[((x >> sh) & 2047) + 1]++;
+            for (int d = 0; d < 2048; d++)
+               cnt[d + 1] += cnt[d];
+            for (size_t q = 0; q < k.size(); q++) {
+               const size_t to = cnt[(k[q] >> sh) & 2047]++;
+               k2[to] = k[q];
+               v2[to] = v[q];
+            }
+            k.swap(k2);
+            v.swap(v2);
+         }
+         return v;
+      }
       // one key per block, level in the high bits and the complement of
       // the number below it (numbers < 2^58: init blocks x 8^num_refine
       // with num_refine <= 20 stays far below that for any lattice that
@@ -218,9 +257,18 @@ class Mesh {
       for (size_t q = 0; q < mb.size(); q++)
          if (bref[q] == 1 && mb[q].level <= nr_)
             marked_[mb[q].level].push_back(mb[q].slot);
+      // and the parents to consolidate, by level in record order (split
+      // adds records with flag 0 and changes no other record's flag, level
+      // or activity, so consolidate's scan of the records finds these)
+      coarsen_.resize(nr_ + 1);
+      for (std::vector<int> &m : coarsen_)
+         m.clear();
       for (int p = 0; p < max_parent_; p++)
-         if (p_[p].number >= 0)
+         if (p_[p].number >= 0) {
             p_[p].refine = pref[p];
+            if (pref[p] == -1 && p_[p].level <= nr_)
+               coarsen_[p_[p].level].push_back(p);
+         }
    }
 
    // split_blocks() (ref/block.c:41-343) on one rank: levels ascending,
@@ -358,8 +406,9 @@ class Mesh {
    void consolidate(std::vector<mamr_consolidate_job> &jobs)
    {
       jobs.clear();
-      for (int level = cur_max_level(); level >= 0; level--)
-         for (int p = 0; p < max_parent_; p++) {
+      for (int level = std::min(cur_max_level(), (int) coarsen_.size() - 1);
+           level >= 0; level--)
+         for (const int p : coarsen_[level]) {
             Par &pp = p_[p];
             if (pp.number < 0 || pp.level != level || pp.refine != -1)
                continue;
@@ -435,6 +484,7 @@ class Mesh {
    // consolidate) skip 64 slots a word
    std::vector<uint64_t> used_;
    std::vector<std::vector<int>> marked_;   // slots to split, by level
+   std::vector<std::vector<int>> coarsen_;  // parents to consolidate
 
    void occupy(int n) { used_[n >> 6] |= (uint64_t) 1 << (n & 63); }
    void release(int n) { used_[n >> 6] &= ~((uint64_t) 1 << (n & 63)); }
