@@ -201,7 +201,10 @@ int mamr_download_blocks(mamr_ctx *ctx, const int32_t *slots, int32_t n,
 
 /* Replaces the active mesh: n blocks in sorted_list order.  Checks the
  * connectivity the exchange relies on and returns MAMR_EMESH where the
- * reference would print "misconnected block" (ref/comm.c:198-201). */
+ * reference would print "misconnected block" (ref/comm.c:198-201).  Returns
+ * once the mesh's device copies are queued on the context's stream (blocks
+ * may be reused at once); a device-side failure surfaces at the next call
+ * that synchronises. */
 int mamr_set_mesh(mamr_ctx *ctx, const mamr_block *blocks, int32_t n);
 
 /* ---- the hot path (reference entry point each one replaces) ----------- */
@@ -243,12 +246,15 @@ int mamr_check_sum(mamr_ctx *ctx, int32_t var, double *sum);
 
 /* split_blocks() cell data: ref/block.c:158-173.  Jobs run in the given
  * (reference) order semantics: a child may reuse a slot freed by an
- * earlier parent in the same call. */
+ * earlier parent in the same call.  Like mamr_consolidate, it returns once
+ * the work is queued on the context's stream (jobs may be reused at once);
+ * the calls that read cells or checksums back synchronise, and a
+ * device-side failure surfaces there. */
 int mamr_split(mamr_ctx *ctx, const mamr_split_job *jobs, int32_t n);
 
 /* consolidate_blocks() cell data: ref/block.c:411-431, same ordering
  * semantics (a later target may be an earlier job's freed child, and a
- * later job may read an earlier job's target). */
+ * later job may read an earlier job's target).  Queued as mamr_split. */
 int mamr_consolidate(mamr_ctx *ctx, const mamr_consolidate_job *jobs,
                      int32_t n);
 
@@ -337,15 +343,18 @@ typedef struct {
     * own) ahead of the stages; the stage side applies each refinement's
     * job lists and mesh in order.  All times leave out the caller's event
     * callback. */
-   double stage_seconds;    /* wall time of the stage stretches */
+   double stage_seconds;    /* wall time of the stage stretches (each
+                               completed, so it includes the device work
+                               queued before it) */
    double refine_seconds;   /* stage side's refinements: waiting for the
                                planning thread, data movement, mesh */
    double total_seconds;    /* the whole call */
    double mark_seconds;     /* planning thread: mamr_mark_refine calls */
    double bookkeeping_seconds; /* planning thread: marking lists, split
                                and consolidation records, meshes */
-   double data_seconds;     /* mamr_split / mamr_consolidate calls */
-   double mesh_seconds;     /* mamr_set_mesh, completed */
+   double data_seconds;     /* mamr_split / mamr_consolidate calls (their
+                               device work is queued and runs on) */
+   double mesh_seconds;     /* mamr_set_mesh calls (likewise) */
    double wait_seconds;     /* stage side waiting for the planning thread */
    int64_t updates;         /* cell-variable updates of the stages (the
                                reference's total_blocks x cells x vars) */

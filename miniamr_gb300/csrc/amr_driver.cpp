@@ -848,8 +848,9 @@ struct Run {
             t = now();
          }
       }
+      // queued behind the data movement; the next stretch's stages follow
+      // on the same stream
       set_mesh(p);
-      check(mamr_sync(ctx), "mamr_sync");
       st.mesh_seconds += lap(t);
       emit(3, p.ts, p.mesh.data(), (int32_t) p.mesh.size(), p.numbers.data(),
            p.cen.data());

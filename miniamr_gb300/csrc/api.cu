@@ -186,9 +186,62 @@ struct mamr_ctx {
    int tune_force = -1;             // forced launch-shape candidate
    int tune_last = -1, tune_n = 0;  // last batched run's choice / count
    mamr::StageShape tune_shape;
+   // pinned host staging of the copies mamr_split, mamr_consolidate and
+   // mamr_set_mesh queue without waiting for them: a ring whose slots are
+   // taken again once the copies from them have run (an event each)
+   struct HostStage {
+      void *p = nullptr;
+      size_t cap = 0;
+      cudaEvent_t ev = nullptr;
+      bool pending = false;
+   };
+   static constexpr int kHostStages = 8;
+   HostStage hstage[kHostStages];
+   int hstage_next = 0;
 };
 
 static size_t elem_size(const mamr_ctx *c) { return c->fp32 ? 4 : 8; }
+
+// The next slot of the host staging ring, at least `bytes` long, once the
+// copies queued from it before have run; null on a CUDA error (*e).
+static void *host_stage_take(mamr_ctx *c, size_t bytes, int *slot,
+                             cudaError_t *e)
+{
+   *slot = c->hstage_next;
+   c->hstage_next = (c->hstage_next + 1) % mamr_ctx::kHostStages;
+   mamr_ctx::HostStage &h = c->hstage[*slot];
+   *e = cudaSuccess;
+   if (h.pending) {
+      h.pending = false;
+      if ((*e = cudaEventSynchronize(h.ev)) != cudaSuccess)
+         return nullptr;
+   }
+   if (!h.ev &&
+       (*e = cudaEventCreateWithFlags(&h.ev, cudaEventDisableTiming)) !=
+          cudaSuccess)
+      return nullptr;
+   if (h.cap < bytes) {
+      if (h.p)
+         cudaFreeHost(h.p);
+      h.p = nullptr;
+      h.cap = 0;
+      const size_t want = bytes + bytes / 4 + 4096;
+      if ((*e = cudaMallocHost(&h.p, want)) != cudaSuccess)
+         return nullptr;
+      h.cap = want;
+   }
+   return h.p;
+}
+
+// The copies from ring slot `slot` are queued: the slot is taken again
+// after they have run.
+static cudaError_t host_stage_queued(mamr_ctx *c, int slot)
+{
+   mamr_ctx::HostStage &h = c->hstage[slot];
+   const cudaError_t e = cudaEventRecord(h.ev, c->stream);
+   h.pending = e == cudaSuccess;
+   return e;
+}
 
 // Where a pool starts past its (256-byte aligned) allocation: so that the
 // interior row (1, 1) of every block-variable -- each i-plane's interior
@@ -363,6 +416,12 @@ extern "C" int mamr_destroy(mamr_ctx *c)
    mamr::batched_destroy(c->batched);
    pool_free(c, c->pool);
    pool_free(c, c->pool_alt);
+   for (mamr_ctx::HostStage &h : c->hstage) {
+      if (h.ev)
+         cudaEventDestroy(h.ev);
+      if (h.p)
+         cudaFreeHost(h.p);
+   }
    for (auto &b : c->d_tasks) b.release();
    c->d_slots.release(); c->d_partials.release(); c->d_jobs.release();
    c->d_stage.release(); c->d_stage_slots.release(); c->d_sums.release();
@@ -569,27 +628,41 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
    }
    // sorted slots now; the face exchange's task lists when it first runs
    // on this mesh (build_tasks), since a batched run never needs them
-   std::vector<int32_t> sorted(n);
-   for (int32_t b = 0; b < n; b++)
-      sorted[b] = blocks[b].slot;
    CUDA_TRY(c->d_slots.ensure(sizeof(int32_t) * std::max(1, n)));
-   if (n)
-      CUDA_TRY(cudaMemcpyAsync(c->d_slots.p, sorted.data(),
-                               sizeof(int32_t) * n, cudaMemcpyHostToDevice,
-                               c->stream));
    c->tasks_dirty = true;
    CUDA_TRY(c->d_partials.ensure(sizeof(double) * std::max(1, n) *
                                  c->cfg.num_vars));
    // the mesh on the device, for the batched path's descriptor build
    CUDA_TRY(c->d_mesh.ensure(sizeof(mamr_block) * std::max(1, n)));
-   if (n)
-      CUDA_TRY(cudaMemcpyAsync(c->d_mesh.p, blocks, sizeof(mamr_block) * n,
-                               cudaMemcpyHostToDevice, c->stream));
    CUDA_TRY(c->d_slot_pos.ensure(sizeof(int32_t) * pos.size()));
-   CUDA_TRY(cudaMemcpyAsync(c->d_slot_pos.p, pos.data(),
-                            sizeof(int32_t) * pos.size(),
-                            cudaMemcpyHostToDevice, c->stream));
-   CUDA_TRY(cudaStreamSynchronize(c->stream));
+   // sorted slots, mesh and slot positions through the pinned ring: queued
+   {
+      const size_t bs = sizeof(int32_t) * (size_t) n;
+      const size_t bm = sizeof(mamr_block) * (size_t) n;
+      const size_t bp = sizeof(int32_t) * pos.size();
+      const size_t om = (bs + 15) & ~(size_t) 15;
+      const size_t op = (om + bm + 15) & ~(size_t) 15;
+      int slot = 0;
+      cudaError_t e;
+      char *h = (char *) host_stage_take(c, op + bp + 16, &slot, &e);
+      if (!h)
+         return fail(MAMR_ECUDA, "host staging: %s", cudaGetErrorString(e));
+      int32_t *hs = reinterpret_cast<int32_t *>(h);
+      for (int32_t b = 0; b < n; b++)
+         hs[b] = blocks[b].slot;
+      if (bm)
+         memcpy(h + om, blocks, bm);
+      memcpy(h + op, pos.data(), bp);
+      if (n) {
+         CUDA_TRY(cudaMemcpyAsync(c->d_slots.p, h, bs,
+                                  cudaMemcpyHostToDevice, c->stream));
+         CUDA_TRY(cudaMemcpyAsync(c->d_mesh.p, h + om, bm,
+                                  cudaMemcpyHostToDevice, c->stream));
+      }
+      CUDA_TRY(cudaMemcpyAsync(c->d_slot_pos.p, h + op, bp,
+                               cudaMemcpyHostToDevice, c->stream));
+      CUDA_TRY(host_stage_queued(c, slot));
+   }
    c->mesh.assign(blocks, blocks + n);
    c->slot_pos.swap(pos);
    for (int32_t b = 0; b < n; b++)
@@ -924,14 +997,29 @@ static int run_segments(mamr_ctx *c, const Job *jobs_in, int32_t n,
       max_stage = 8;
    }
    CUDA_TRY(c->d_jobs.ensure(sizeof(Job) * jobs.size()));
-   CUDA_TRY(cudaMemcpyAsync(c->d_jobs.p, jobs.data(), sizeof(Job) * n,
-                            cudaMemcpyHostToDevice, c->stream));
    CUDA_TRY(c->d_xfer_slots.ensure(sizeof(int32_t) *
                                    std::max<size_t>(1, staged.size())));
-   if (!staged.empty())
-      CUDA_TRY(cudaMemcpyAsync(c->d_xfer_slots.p, staged.data(),
-                               sizeof(int32_t) * staged.size(),
-                               cudaMemcpyHostToDevice, c->stream));
+   // the job list and the staged slots through the pinned ring: queued,
+   // the caller's arrays free on return
+   {
+      const size_t bj = sizeof(Job) * (size_t) n;
+      const size_t bs = sizeof(int32_t) * staged.size();
+      const size_t os = (bj + 15) & ~(size_t) 15;
+      int slot = 0;
+      cudaError_t e;
+      char *h = (char *) host_stage_take(c, os + bs + 16, &slot, &e);
+      if (!h)
+         return fail(MAMR_ECUDA, "host staging: %s", cudaGetErrorString(e));
+      memcpy(h, jobs.data(), bj);
+      if (bs)
+         memcpy(h + os, staged.data(), bs);
+      CUDA_TRY(cudaMemcpyAsync(c->d_jobs.p, h, bj, cudaMemcpyHostToDevice,
+                               c->stream));
+      if (bs)
+         CUDA_TRY(cudaMemcpyAsync(c->d_xfer_slots.p, h + os, bs,
+                                  cudaMemcpyHostToDevice, c->stream));
+      CUDA_TRY(host_stage_queued(c, slot));
+   }
    for (const Segment &sg : segs) {
       const int32_t *sl = (const int32_t *) c->d_xfer_slots.p + sg.stage_begin;
       const int ns = (int) (sg.stage_end - sg.stage_begin);
@@ -946,7 +1034,6 @@ static int run_segments(mamr_ctx *c, const Job *jobs_in, int32_t n,
       const Job *dj = (const Job *) c->d_jobs.p + sg.begin;
       LAUNCH_TRY(c, launch(dj, (int) (sg.end - sg.begin)));
    }
-   CUDA_TRY(cudaStreamSynchronize(c->stream));
    return MAMR_OK;
 }
 
