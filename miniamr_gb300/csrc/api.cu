@@ -198,6 +198,14 @@ struct mamr_ctx {
    static constexpr int kHostStages = 8;
    HostStage hstage[kHostStages];
    int hstage_next = 0;
+   // the batched path's z-face arrays across runs: zface_live is the array
+   // (0 or 1) that holds the k = 1 and k = nz planes of every slot
+   // zface_ok marks, as the pool holds them -- written by the last stage
+   // of a run with the warp-per-block or tile kernel and, while live, by
+   // splits and consolidations for the blocks they write -- or -1 when
+   // none does; a run's first stage then reads its z ghosts from there
+   int zface_live = -1;
+   std::vector<char> zface_ok;
 };
 
 static size_t elem_size(const mamr_ctx *c) { return c->fp32 ? 4 : 8; }
@@ -289,6 +297,15 @@ static void zcache_drop(mamr_ctx *c)
 {
    std::fill(c->zc_ok.begin(), c->zc_ok.end(), 0);
 }
+// The live z-face array (for splits and consolidations to store the
+// planes of the blocks they write), or null.
+static void *zface_live_array(mamr_ctx *c)
+{
+   if (c->zface_live < 0 || !c->batched)
+      return nullptr;
+   return c->batched->zf[c->zface_live].p;
+}
+
 static void *zcache_for_stencil(mamr_ctx *c)
 {
    if (!c->d_zc.p) {
@@ -403,6 +420,7 @@ extern "C" int mamr_create(const mamr_config *cfg, mamr_ctx **out)
       return fail(code, "mamr_create: %s", cudaGetErrorString(e));
    }
    c->slot_pos.assign(cfg->max_blocks, -1);
+   c->zface_ok.assign(cfg->max_blocks, 0);
    *out = c;
    return MAMR_OK;
 }
@@ -563,6 +581,7 @@ extern "C" int mamr_upload_blocks(mamr_ctx *c, const int32_t *slots,
       return fail(MAMR_EINVAL, "null context");
    c->gen++;
    zcache_drop(c);
+   c->zface_live = -1;
    return transfer(c, slots, n, const_cast<double *>(host), true);
 }
 
@@ -792,6 +811,7 @@ static int stencil_impl(mamr_ctx *c, int32_t var, int32_t calc_stage,
                         bool per_block = false)
 {
    const int n = (int) c->mesh.size();
+   c->zface_live = -1;
    if (c->cfg.stencil == 0) {
       // stencil_driver (ref/stencil.c:43-74): var 0 and var >= 4*mat take
       // the 7-point stencil, the others the variable-work kernels
@@ -1056,6 +1076,13 @@ extern "C" int mamr_split(mamr_ctx *c, const mamr_split_job *jobs, int32_t n)
    }
    if (n == 0)
       return MAMR_OK;
+   void *zf = zface_live_array(c);
+   if (zf)
+      for (int32_t t = 0; t < n; t++) {
+         c->zface_ok[jobs[t].parent] = 0;
+         for (int o = 0; o < 8; o++)
+            c->zface_ok[jobs[t].child[o]] = 1;
+      }
    return run_segments<1, 8>(
       c, jobs, n,
       [](mamr_split_job &j) { return std::array<int32_t *, 1>{&j.parent}; },
@@ -1069,10 +1096,10 @@ extern "C" int mamr_split(mamr_ctx *c, const mamr_split_job *jobs, int32_t n)
          return c->fp32
                    ? launch_split((float *) c->pool,
                                   (const float *) c->d_xfer.p, c->g, dj, m,
-                                  c->stream)
+                                  (float *) zf, c->stream)
                    : launch_split((double *) c->pool,
                                   (const double *) c->d_xfer.p, c->g, dj, m,
-                                  c->stream);
+                                  (double *) zf, c->stream);
       });
 }
 
@@ -1095,6 +1122,13 @@ extern "C" int mamr_consolidate(mamr_ctx *c, const mamr_consolidate_job *jobs,
    }
    if (n == 0)
       return MAMR_OK;
+   void *zf = zface_live_array(c);
+   if (zf)
+      for (int32_t t = 0; t < n; t++) {
+         for (int o = 0; o < 8; o++)
+            c->zface_ok[jobs[t].child[o]] = 0;
+         c->zface_ok[jobs[t].target] = 1;
+      }
    return run_segments<8, 1>(
       c, jobs, n,
       [](mamr_consolidate_job &j) {
@@ -1110,10 +1144,10 @@ extern "C" int mamr_consolidate(mamr_ctx *c, const mamr_consolidate_job *jobs,
          return c->fp32
                    ? launch_consolidate((float *) c->pool,
                                         (const float *) c->d_xfer.p, c->g, dj,
-                                        m, c->stream)
+                                        m, (float *) zf, c->stream)
                    : launch_consolidate((double *) c->pool,
                                         (const double *) c->d_xfer.p, c->g,
-                                        dj, m, c->stream);
+                                        dj, m, (double *) zf, c->stream);
       });
 }
 
@@ -1123,6 +1157,7 @@ static int run_plain(mamr_ctx *c, int32_t num_ts, int32_t spt, int32_t freq,
                      int32_t first_stage, bool per_block, double *sums,
                      int32_t *n_sums)
 {
+   c->zface_live = -1;
    const int V = c->cfg.num_vars;
    int per_ts = 0;
    if (freq)
@@ -1454,9 +1489,10 @@ bool tuning_disabled()
 template <typename Stage>
 static int tune_choice(mamr_ctx *c, const std::vector<StageShape> &cands,
                        bool pencil, int nb, int freq, int scratch_cs,
-                       Stage &stage, int &choice)
+                       Stage &stage, int &choice, bool *timed)
 {
    choice = 0;
+   *timed = false;
    if (cands.size() < 2 || tuning_disabled())
       return MAMR_OK;
    long long work = (long long) nb * c->cfg.num_vars;
@@ -1476,6 +1512,7 @@ static int tune_choice(mamr_ctx *c, const std::vector<StageShape> &cands,
          return MAMR_OK;
       }
    }
+   *timed = true;      // its stages write over both z-face arrays
    cudaEvent_t e0 = nullptr, e1 = nullptr;
    CUDA_TRY(cudaEventCreate(&e0));
    if (cudaEventCreate(&e1) != cudaSuccess) {
@@ -1548,6 +1585,10 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
          return fail(MAMR_ENOMEM, "host allocation");
    }
    BatchedState *B = c->batched;
+   // the z-face array the previous run left live (if any), and none live
+   // until this run completes
+   const int live0 = c->zface_live;
+   c->zface_live = -1;
    if (!B->valid && (r = build_items(c)))
       return r;
    if (c->cfg.stencil == 0)
@@ -1593,16 +1634,19 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    const int *keep = B->has_recipes ? (const int *) B->keep.p : nullptr;
    // one stage: cur -> oth with launch shape sh; q = the stage's index in
    // the run, or a tuning stage (kTunePrime, kTuneTimed).  The
-   // warp-per-block and tile kernels write the z-face array of stage q and
-   // read that of stage q - 1; tuning stages write array 0 (priming) or
-   // read array 0 and write array 1 (timed).
+   // warp-per-block and tile kernels write the z-face array (zb + q) & 1
+   // and read the one stage q - 1 wrote -- the first stage the array the
+   // previous run left live when it holds every active block (first_in);
+   // tuning stages write array 0 (priming) or read array 0 and write
+   // array 1 (timed).
+   int zb = 0, first_in = -1;
    auto stage = [&](const void *cur, void *oth, const StageShape &sh,
                     int last, bool do_cs, int cnt, int q) -> int {
       const bool zk = sh.kernel == 1 || sh.kernel == 2;
       int zin = -1, zout = -1;
       if (zk && q >= 0) {
-         zout = q & 1;
-         zin = q > 0 ? (q - 1) & 1 : -1;
+         zout = (zb + q) & 1;
+         zin = q > 0 ? (zb + q - 1) & 1 : first_in;
       } else if (zk && q == kTunePrime) {
          zout = 0;
       } else if (zk && q == kTuneTimed) {
@@ -1680,22 +1724,35 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    // stage, read by the next; the tuner times those kernels with them)
    for (const StageShape &cd : cands)
       if (cd.kernel == 1 || cd.kernel == 2) {
-         const size_t zb = zface_elems(c->g, c->cfg.max_blocks) * es;
-         CUDA_TRY(B->zf[0].ensure(zb));
-         CUDA_TRY(B->zf[1].ensure(zb));
+         const size_t zbytes = zface_elems(c->g, c->cfg.max_blocks) * es;
+         CUDA_TRY(B->zf[0].ensure(zbytes));
+         CUDA_TRY(B->zf[1].ensure(zbytes));
          break;
       }
    int choice = 0;
+   bool tuned_now = false;
    if (c->tune_force >= 0) {
       choice = std::min<int>(c->tune_force, (int) cands.size() - 1);
    } else if ((r = tune_choice(c, cands, pencil, nb, freq, (int) n_cs, stage,
-                               choice))) {
+                               choice, &tuned_now))) {
       return r;
    }
    const StageShape sh = cands[choice];
    c->tune_last = choice;
    c->tune_n = (int) cands.size();
    c->tune_shape = sh;
+   const bool zkern = sh.kernel == 1 || sh.kernel == 2;
+   // the first stage reads the z-face array the previous run left, if no
+   // tuning stage has written over it and it holds every active block
+   if (zkern && live0 >= 0 && !tuned_now && B->zf[live0].p) {
+      bool all = true;
+      for (const mamr_block &b : c->mesh)
+         all = all && c->zface_ok[b.slot];
+      if (all) {
+         first_in = live0;
+         zb = 1 - live0;
+      }
+   }
    // A run of an odd number of stages ends in the spare pool: it must then
    // hold what no stage writes (stale ghosts, free slots) as the current
    // pool does, so it starts as a copy.  With an even number the run ends
@@ -1754,6 +1811,13 @@ static int run_batched(mamr_ctx *c, int32_t num_ts, int32_t spt,
    c->launches += launches;
    if (cur != c->pool) {
       std::swap(c->pool, c->pool_alt);
+   }
+   if (zkern && total > 0 && B->zf[(zb + total - 1) & 1].p) {
+      // the last stage wrote every active block's planes
+      c->zface_live = (zb + total - 1) & 1;
+      std::fill(c->zface_ok.begin(), c->zface_ok.end(), 0);
+      for (const mamr_block &b : c->mesh)
+         c->zface_ok[b.slot] = 1;
    }
    if ((r = mamr_sync(c)))
       return r;

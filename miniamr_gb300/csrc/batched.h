@@ -344,21 +344,7 @@ int launch_brick_stage(const T *src, T *dst, const Geom &g,
                        int write_ghosts, int do_cs, unsigned long long *acc,
                        unsigned *err, unsigned *ctx_err, long long n_bv,
                        const T *zf_src, T *zf_dst, cudaStream_t s);
-// z-face arrays of the warp-per-block and tile kernels: each stage of a
-// batched run also stores every block-variable's k = 1 and k = nz planes
-// (side 0 and 1, nx * ny values each at (i-1)*ny + (j-1)) contiguously,
-// and the next stage reads its z ghosts from there instead of one value
-// per row of the neighbour.  Elements of one array, and the offset of a
-// plane.
-inline size_t zface_elems(const Geom &g, int max_blocks)
-{
-   return (size_t) max_blocks * g.V * 2 * g.nx * g.ny;
-}
-__host__ __device__ inline long long zface_at(const Geom &g, int slot,
-                                              int var, int side)
-{
-   return (((long long) slot * g.V + var) * 2 + side) * g.nx * g.ny;
-}
+// zface_elems / zface_at: mamr_internal.h.
 
 // Pencil variant for single-level meshes of 16^3 blocks: CTAs walk chains
 // of blocks along z (chain[pencils[p].x .. +pencils[p].y), bottom to

@@ -46,6 +46,23 @@ __host__ __device__ inline long long cell_offset(const Geom &g, int i, int j,
    return g.kplane + (k == 0 ? 0 : (long long) g.X * g.Y) + row;
 }
 
+// z-face arrays of the warp-per-block and tile kernels: each stage of a
+// batched run also stores every block-variable's k = 1 and k = nz planes
+// (side 0 and 1, nx * ny values each at (i-1)*ny + (j-1)) contiguously,
+// and the next stage reads its z ghosts from there instead of one value
+// per row of the neighbour; splits and consolidations store the planes of
+// the blocks they write while the arrays are live.  Elements of one
+// array, and the offset of a plane.
+inline size_t zface_elems(const Geom &g, int max_blocks)
+{
+   return (size_t) max_blocks * g.V * 2 * g.nx * g.ny;
+}
+__host__ __device__ inline long long zface_at(const Geom &g, int slot,
+                                              int var, int side)
+{
+   return (((long long) slot * g.V + var) * 2 + side) * g.nx * g.ny;
+}
+
 // Offset of interior row (i, j), k = 1, in the split layout.
 __host__ __device__ inline long long row_offset(const Geom &g, int i, int j)
 {
@@ -158,13 +175,15 @@ int launch_checksum_fp32(const float *pool, const Geom &g,
 template <typename T>
 int launch_stage_blocks(T *stage, const T *pool, const Geom &g,
                         const int32_t *slots, int n, cudaStream_t s);
-// Data-movement reads with a negative slot s come from staging entry -s-1.
+// Data-movement reads with a negative slot s come from staging entry -s-1;
+// zf (may be null): the live z-face array, into which the kernels also
+// store the k = 1 and k = nz planes of the blocks they write.
 template <typename T>
 int launch_split(T *pool, const T *stage, const Geom &g,
-                 const mamr_split_job *jobs, int n, cudaStream_t s);
+                 const mamr_split_job *jobs, int n, T *zf, cudaStream_t s);
 template <typename T>
 int launch_consolidate(T *pool, const T *stage, const Geom &g,
-                       const mamr_consolidate_job *jobs, int n,
+                       const mamr_consolidate_job *jobs, int n, T *zf,
                        cudaStream_t s);
 template <typename T>
 int launch_upload(T *pool, const Geom &g, const int32_t *slots, int n,

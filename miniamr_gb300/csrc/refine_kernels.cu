@@ -100,7 +100,7 @@ __device__ __forceinline__ double sum8_children(const double (&t)[8])
 template <typename T, int BX, int BY, int BZ>
 __global__ void __launch_bounds__(256)
 split_jobs_kernel(T *__restrict__ pool, const T *__restrict__ stage, Geom g,
-                  const mamr_split_job *__restrict__ jobs)
+                  const mamr_split_job *__restrict__ jobs, T *__restrict__ zf)
 {
    const Dims<BX, BY, BZ> D(g);
    const int job = blockIdx.x, var = blockIdx.y;
@@ -132,6 +132,13 @@ split_jobs_kernel(T *__restrict__ pool, const T *__restrict__ stage, Geom g,
          for (int ck = 1; ck <= D.nz; ck++)
             crow[ck - 1] = eighth(prow[(ck + 1) / 2 - 1]);
       }
+      if (zf) {
+         // the child's k = 1 and k = nz planes for the z-face array
+         T *z = zf + zface_at(g, jobs[job].child[o], var, 0) +
+                (ci - 1) * D.ny + (cj - 1);
+         z[0] = eighth(prow[0]);
+         z[D.nx * D.ny] = eighth(prow[D.nz / 2 - 1]);
+      }
    }
 }
 
@@ -142,7 +149,8 @@ split_jobs_kernel(T *__restrict__ pool, const T *__restrict__ stage, Geom g,
 template <typename T, int BX, int BY, int BZ>
 __global__ void __launch_bounds__(256)
 consolidate_jobs_kernel(T *__restrict__ pool, const T *__restrict__ stage,
-                        Geom g, const mamr_consolidate_job *__restrict__ jobs)
+                        Geom g, const mamr_consolidate_job *__restrict__ jobs,
+                        T *__restrict__ zf)
 {
    const Dims<BX, BY, BZ> D(g);
    const int job = blockIdx.x, var = blockIdx.y;
@@ -160,6 +168,7 @@ consolidate_jobs_kernel(T *__restrict__ pool, const T *__restrict__ stage,
       const T *f01 = C + D.cell(2 * i - 1, 2 * j, 1);
       const T *f11 = C + D.cell(2 * i, 2 * j, 1);
       T *prow = P + D.cell(i + i1, j + j1, 1 + k1);
+      T zv = 0;   // the target's k = 1 (k1 = 0) or k = nz value of the row
       if (BZ && (BZ / 2) % Vec<T>::W == 0) {
          constexpr int W = Vec<T>::W;
 #pragma unroll
@@ -177,15 +186,25 @@ consolidate_jobs_kernel(T *__restrict__ pool, const T *__restrict__ stage,
                out[m] = sum8_children(t);
             }
             Vec<T>::st(prow + q, out);
+            if (q == 0 && k1 == 0)
+               zv = out[0];
+            if (q + W == BZ / 2 && k1 != 0)
+               zv = out[W - 1];
          }
       } else {
          for (int k = 1; k <= hz; k++) {
             const int k2 = 2 * k - 1;
             const T t[8] = {f00[k2 - 1], f10[k2 - 1], f01[k2 - 1],
                             f11[k2 - 1], f00[k2], f10[k2], f01[k2], f11[k2]};
-            prow[k - 1] = sum8_children(t);
+            const T v = sum8_children(t);
+            prow[k - 1] = v;
+            if ((k == 1 && k1 == 0) || (k == hz && k1 != 0))
+               zv = v;
          }
       }
+      if (zf)
+         zf[zface_at(g, jobs[job].target, var, k1 != 0) +
+            (i + i1 - 1) * D.ny + (j + j1 - 1)] = zv;
    }
 }
 
@@ -193,28 +212,30 @@ consolidate_jobs_kernel(T *__restrict__ pool, const T *__restrict__ stage,
 
 template <typename T>
 int launch_split(T *pool, const T *stage, const Geom &g,
-                 const mamr_split_job *jobs, int n, cudaStream_t s)
+                 const mamr_split_job *jobs, int n, T *zf, cudaStream_t s)
 {
    if (n == 0)
       return 0;
    const dim3 grid(n, g.V);
    switch (dims_kind(g)) {
    case 1:
-      split_jobs_kernel<T, 8, 8, 8><<<grid, 128, 0, s>>>(pool, stage, g, jobs);
+      split_jobs_kernel<T, 8, 8, 8><<<grid, 128, 0, s>>>(pool, stage, g, jobs,
+                                                         zf);
       break;
    case 2:
       split_jobs_kernel<T, 16, 16, 16><<<grid, 256, 0, s>>>(pool, stage, g,
-                                                            jobs);
+                                                            jobs, zf);
       break;
    default:
-      split_jobs_kernel<T, 0, 0, 0><<<grid, 256, 0, s>>>(pool, stage, g, jobs);
+      split_jobs_kernel<T, 0, 0, 0><<<grid, 256, 0, s>>>(pool, stage, g, jobs,
+                                                         zf);
    }
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
 template <typename T>
 int launch_consolidate(T *pool, const T *stage, const Geom &g,
-                       const mamr_consolidate_job *jobs, int n,
+                       const mamr_consolidate_job *jobs, int n, T *zf,
                        cudaStream_t s)
 {
    if (n == 0)
@@ -223,29 +244,31 @@ int launch_consolidate(T *pool, const T *stage, const Geom &g,
    switch (dims_kind(g)) {
    case 1:
       consolidate_jobs_kernel<T, 8, 8, 8><<<grid, 128, 0, s>>>(pool, stage, g,
-                                                               jobs);
+                                                               jobs, zf);
       break;
    case 2:
       consolidate_jobs_kernel<T, 16, 16, 16><<<grid, 256, 0, s>>>(
-         pool, stage, g, jobs);
+         pool, stage, g, jobs, zf);
       break;
    default:
       consolidate_jobs_kernel<T, 0, 0, 0><<<grid, 256, 0, s>>>(pool, stage, g,
-                                                               jobs);
+                                                               jobs, zf);
    }
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
 template int launch_split<float>(float *, const float *, const Geom &,
-                                 const mamr_split_job *, int, cudaStream_t);
+                                 const mamr_split_job *, int, float *,
+                                 cudaStream_t);
 template int launch_split<double>(double *, const double *, const Geom &,
-                                  const mamr_split_job *, int, cudaStream_t);
+                                  const mamr_split_job *, int, double *,
+                                  cudaStream_t);
 template int launch_consolidate<float>(float *, const float *, const Geom &,
                                        const mamr_consolidate_job *, int,
-                                       cudaStream_t);
+                                       float *, cudaStream_t);
 template int launch_consolidate<double>(double *, const double *,
                                         const Geom &,
                                         const mamr_consolidate_job *, int,
-                                        cudaStream_t);
+                                        double *, cudaStream_t);
 
 }  // namespace mamr
