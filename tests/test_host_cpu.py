@@ -237,3 +237,45 @@ def test_dropin_links_against_the_gpu_library(tmp_path):
                    args, cwd=tmp_path, check=True, capture_output=True,
                    env=dict(os.environ, MAMR_REF_LOG=str(ref)))
     assert log.read_text() == ref.read_text()
+
+
+@pytest.mark.parametrize("init,passes,cap", [
+    ((8, 8, 8), 1, 4624), ((2, 2, 2), 2, 600), ((3, 1, 2), 1, 60),
+    ((1, 1, 1), 3, 600), ((4, 3, 2), 2, 1800)])
+def test_uniform_split_closed_form_equals_the_slot_walk(monkeypatch, init,
+                                                       passes, cap):
+    """The uniform-mesh helper's closed form for the initial lattice's
+    split gives the jobs, numbers, levels and meshes of the reference's
+    slot walk (the helper's general path)."""
+    from miniamr_gb300 import mesh as meshmod
+
+    def run():
+        m = meshmod.initial_mesh(*init, passes, cap)
+        out = [m.split_all().tobytes() for _ in range(passes)]
+        return out + [m.blocks().tobytes(), m.number.tobytes()]
+
+    fast = run()
+    monkeypatch.setattr(meshmod.UniformMesh, "_split_fresh_lattice",
+                        lambda self: None)
+    assert run() == fast
+
+
+def test_no_ghosts_flag_is_accepted_by_the_oracle(oracle_lib):
+    """MAMR_RUN_NO_GHOSTS is part of the ABI: the oracle (which always
+    writes ghost layers back) accepts it and gives the same cells and
+    checksums as without it."""
+    from miniamr_gb300 import mesh as meshmod
+    from miniamr_gb300.abi import RUN_BATCHED, RUN_NO_GHOSTS, Config
+    cfg = Config.make(4, 4, 4, 2, 40, stencil=7)
+    init = oracle_lib.initial_values(cfg, 4)
+    outs = []
+    for fl in (RUN_BATCHED, RUN_BATCHED | RUN_NO_GHOSTS):
+        m = meshmod.initial_mesh(2, 2, 1, 1, 40)
+        with oracle_lib.context(cfg) as ctx:
+            ctx.upload(np.arange(4), init)
+            ctx.split(m.split_all())
+            ctx.set_mesh(m.blocks())
+            s = ctx.run_timesteps(2, 2, 1, flags=fl)
+            outs.append((s, ctx.download(np.arange(40))))
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
