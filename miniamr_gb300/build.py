@@ -29,7 +29,8 @@ ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "libmamr_oracle.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17",
-                  "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
+                  "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp",
+                  "-I" + INCLUDE, "-I" + CSRC]
 
 
 def _sources():
@@ -74,7 +75,8 @@ def build_library(verbose: bool = False) -> str:
                 if verbose and (r.stdout or r.stderr):
                     print(r.stdout + r.stderr)
     if jobs or _newer(LIB, objs):
-        _run([NVCC] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", LIB] +
+        _run([NVCC] + ARCH + ["-shared", "-Xcompiler", "-fPIC",
+                              "-Xcompiler", "-fopenmp", "-o", LIB] +
              objs + ["-cudart", "static"])
     return LIB
 

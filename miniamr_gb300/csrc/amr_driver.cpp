@@ -68,6 +68,9 @@ int face_child(int c, int a, int b)
    return i1 + 2 * j1 + 4 * k1;
 }
 
+// Threads of the bookkeeping's list building (marking lists, meshes).
+constexpr int kBookThreads = 4;
+
 class Mesh {
  public:
    Mesh(int ix, int iy, int iz, int num_refine, int max_blocks)
@@ -138,17 +141,24 @@ class Mesh {
    {
       const long long total = start_[nr_ + 1];
       if (total > 0 && total <= (1ll << 32)) {
-         std::vector<uint32_t> k, k2;
-         std::vector<int> v, v2;
-         k.reserve(active_);
-         v.reserve(active_);
-         for (int n = 0; n < max_block_; n++) {
-            const Blk &bp = b_[n];
-            if (bp.number < 0)
-               continue;
-            k.push_back((uint32_t) (start_[bp.level] + start_[bp.level + 1] -
-                                    1 - bp.number));
-            v.push_back(n);
+         // the keys of the active slots, word by word as mark_lists
+         const int nw = (max_block_ + 63) / 64;
+         std::vector<int> at(nw + 1, 0);
+         for (int w = 0; w < nw; w++)
+            at[w + 1] = at[w] + __builtin_popcountll(used_[w]);
+         std::vector<uint32_t> k(at[nw]), k2;
+         std::vector<int> v(at[nw]), v2;
+#pragma omp parallel for num_threads(kBookThreads) schedule(static) \
+   if (nw >= 256)
+         for (int w = 0; w < nw; w++) {
+            int q = at[w];
+            for (uint64_t bits = used_[w]; bits; bits &= bits - 1) {
+               const int n = w * 64 + __builtin_ctzll(bits);
+               const Blk &bp = b_[n];
+               k[q] = (uint32_t) (start_[bp.level] + start_[bp.level + 1] -
+                                  1 - bp.number);
+               v[q++] = n;
+            }
          }
          k2.resize(k.size());
          v2.resize(v.size());
@@ -198,7 +208,10 @@ class Mesh {
       mesh.resize(s.size());
       numbers.resize(s.size());
       cen.resize(3 * s.size());
-      for (size_t q = 0; q < s.size(); q++) {
+      const long long ns = (long long) s.size();
+#pragma omp parallel for num_threads(kBookThreads) schedule(static) \
+   if (ns >= 16384)
+      for (long long q = 0; q < ns; q++) {
          const Blk &bp = b_[s[q]];
          mamr_block &m = mesh[q];
          m.slot = s[q];
@@ -221,24 +234,36 @@ class Mesh {
    void mark_lists(std::vector<mamr_mark_block> &mb,
                    std::vector<mamr_mark_parent> &pa) const
    {
-      mb.resize(active_);
-      size_t q = 0;
-      for (int n = 0; n < max_block_; n++) {
-         const Blk &bp = b_[n];
-         if (bp.number < 0)
-            continue;
-         mamr_mark_block &m = mb[q++];
-         m.slot = n;
-         m.level = bp.level;
-         m.parent = bp.parent;
-         for (int d = 0; d < 3; d++)
-            m.cen[d] = bp.cen[d];
-         for (int c = 0; c < 6; c++) {
-            m.nei_level[c] = bp.nei_level[c];
-            m.nei[c] = bp.nei[c][0][0];
+      // the active slots word by word (the occupancy bitmap), each word's
+      // first list position from the counts before it, so that the words
+      // fill their stretches of the list on several threads
+      const int nw = (max_block_ + 63) / 64;
+      std::vector<int> at(nw + 1, 0);
+      for (int w = 0; w < nw; w++)
+         at[w + 1] = at[w] + __builtin_popcountll(used_[w]);
+      mb.resize(at[nw]);
+#pragma omp parallel for num_threads(kBookThreads) schedule(static) \
+   if (nw >= 256)
+      for (int w = 0; w < nw; w++) {
+         int q = at[w];
+         for (uint64_t bits = used_[w]; bits; bits &= bits - 1) {
+            const int n = w * 64 + __builtin_ctzll(bits);
+            const Blk &bp = b_[n];
+            mamr_mark_block &m = mb[q++];
+            m.slot = n;
+            m.level = bp.level;
+            m.parent = bp.parent;
+            for (int d = 0; d < 3; d++)
+               m.cen[d] = bp.cen[d];
+            for (int c = 0; c < 6; c++) {
+               m.nei_level[c] = bp.nei_level[c];
+               m.nei[c] = bp.nei[c][0][0];
+            }
          }
       }
       pa.resize(max_parent_);
+#pragma omp parallel for num_threads(kBookThreads) schedule(static) \
+   if (max_parent_ >= 4096)
       for (int p = 0; p < max_parent_; p++) {
          pa[p].active = p_[p].number >= 0;
          for (int o = 0; o < 8; o++)
