@@ -344,8 +344,8 @@ typedef struct {
     * job lists and mesh in order.  All times leave out the caller's event
     * callback. */
    double stage_seconds;    /* wall time of the stage stretches (each
-                               completed, so it includes the device work
-                               queued before it) */
+                               completed; each refinement's device work
+                               is done before the next stretch starts) */
    double refine_seconds;   /* stage side's refinements: waiting for the
                                planning thread, data movement, mesh */
    double total_seconds;    /* the whole call */
@@ -353,8 +353,10 @@ typedef struct {
    double bookkeeping_seconds; /* planning thread: marking lists, split
                                and consolidation records, meshes */
    double data_seconds;     /* mamr_split / mamr_consolidate calls (their
-                               device work is queued and runs on) */
-   double mesh_seconds;     /* mamr_set_mesh calls (likewise) */
+                               device work is queued) and the wait for
+                               the refinement's device work (cell
+                               movement, mesh upload) after its mesh */
+   double mesh_seconds;     /* mamr_set_mesh calls (queued uploads) */
    double wait_seconds;     /* stage side waiting for the planning thread */
    int64_t updates;         /* cell-variable updates of the stages (the
                                reference's total_blocks x cells x vars) */

@@ -873,10 +873,13 @@ struct Run {
             t = now();
          }
       }
-      // queued behind the data movement; the next stretch's stages follow
-      // on the same stream
+      // queued behind the data movement on the same stream
       set_mesh(p);
       st.mesh_seconds += lap(t);
+      // the refinement's device work (cell movement, mesh upload) done
+      // here, so that the stage stretches' time holds only stages
+      check(mamr_sync(ctx), "mamr_sync");
+      st.data_seconds += lap(t);
       emit(3, p.ts, p.mesh.data(), (int32_t) p.mesh.size(), p.numbers.data(),
            p.cen.data());
       st.refinements++;

@@ -150,7 +150,26 @@ struct mamr_ctx {
    size_t pool_bytes;
    void *pool_alt;         // second pool for the batched ping-pong (lazy)
    size_t pool_shift;      // bytes both pools start past their allocations
-   std::vector<mamr_block> mesh;
+   // The mesh as mamr_set_mesh last took it: a view of one of two pinned
+   // host buffers, which the mesh's upload to d_mesh reads; the next mesh
+   // goes into the other one (once that one's upload has run).
+   struct MeshView {
+      const mamr_block *p = nullptr;
+      size_t n = 0;
+      size_t size() const { return n; }
+      const mamr_block &operator[](size_t i) const { return p[i]; }
+      const mamr_block *begin() const { return p; }
+      const mamr_block *end() const { return p + n; }
+   };
+   MeshView mesh;
+   struct MeshBuf {
+      mamr_block *p = nullptr;
+      size_t cap = 0;
+      cudaEvent_t ev = nullptr;
+      bool pending = false;
+   };
+   MeshBuf hmesh[2];
+   int hmesh_cur = 0;
    std::vector<int32_t> slot_pos;   // slot -> index in mesh or -1
    DevBuf d_slots;                  // sorted slots
    DevBuf d_mesh, d_slot_pos;       // device copies of mesh and slot_pos
@@ -209,6 +228,9 @@ struct mamr_ctx {
 };
 
 static size_t elem_size(const mamr_ctx *c) { return c->fp32 ? 4 : 8; }
+
+// Host threads (OpenMP) of the checks and copies over long block lists.
+constexpr int kHostThreads = 4;
 
 // The next slot of the host staging ring, at least `bytes` long, once the
 // copies queued from it before have run; null on a CUDA error (*e).
@@ -434,6 +456,12 @@ extern "C" int mamr_destroy(mamr_ctx *c)
    mamr::batched_destroy(c->batched);
    pool_free(c, c->pool);
    pool_free(c, c->pool_alt);
+   for (mamr_ctx::MeshBuf &h : c->hmesh) {
+      if (h.ev)
+         cudaEventDestroy(h.ev);
+      if (h.p)
+         cudaFreeHost(h.p);
+   }
    for (mamr_ctx::HostStage &h : c->hstage) {
       if (h.ev)
          cudaEventDestroy(h.ev);
@@ -593,9 +621,79 @@ extern "C" int mamr_download_blocks(mamr_ctx *c, const int32_t *slots,
    return transfer(c, slots, n, host, false);
 }
 
+// Per-block checks of mamr_set_mesh that need no other block: the slot
+// and, on every face, the neighbour level and the neighbour slots the face
+// uses.
+static bool mesh_block_ok(const mamr_ctx *c, const mamr_block &bp)
+{
+   if (!slot_ok(c, bp.slot))
+      return false;
+   for (int l = 0; l < 6; l++) {
+      const int nl = bp.nei_level[l];
+      if (nl == -2)
+         continue;
+      if (nl != bp.level && nl != bp.level + 1 && nl != bp.level - 1)
+         return false;
+      const int cnt = nl == bp.level + 1 ? 4 : 1;
+      for (int q = 0; q < cnt; q++)
+         if (!slot_ok(c, bp.nei[l][q >> 1][q & 1]))
+            return false;
+   }
+   return true;
+}
+
+// mamr_set_mesh's checks and copies for a long mesh on kHostThreads
+// threads: each slot's position claimed by an atomic exchange (a slot
+// listed twice finds it taken), the blocks copied into dst and their slots
+// into hs.  False on any failure, after which the serial checks name it.
+static bool set_mesh_parallel(const mamr_ctx *c, const mamr_block *blocks,
+                              int32_t n, int32_t *pos, mamr_block *dst,
+                              int32_t *hs, int *hw)
+{
+   const int32_t cap = c->cfg.max_blocks;
+   int bad = 0, top = 0;
+#pragma omp parallel num_threads(kHostThreads) reduction(| : bad) \
+   reduction(max : top)
+   {
+#pragma omp for schedule(static)
+      for (int32_t b = 0; b < n; b++) {
+         const mamr_block &bp = blocks[b];
+         dst[b] = bp;
+         hs[b] = bp.slot;
+         int32_t none = -1;
+         if (!mesh_block_ok(c, bp) ||
+             !__atomic_compare_exchange_n(&pos[bp.slot], &none, b, false,
+                                          __ATOMIC_RELAXED, __ATOMIC_RELAXED))
+            bad = 1;
+         else
+            top = std::max(top, bp.slot + 1);
+      }
+      // every listed neighbour active (slots checked again: a block that
+      // failed above may list any value)
+#pragma omp for schedule(static)
+      for (int32_t b = 0; b < n; b++) {
+         const mamr_block &bp = blocks[b];
+         for (int l = 0; l < 6; l++) {
+            const int nl = bp.nei_level[l];
+            if (nl == -2)
+               continue;
+            const int cnt = nl == bp.level + 1 ? 4 : 1;
+            for (int q = 0; q < cnt; q++) {
+               const int m = bp.nei[l][q >> 1][q & 1];
+               if (m < 0 || m >= cap || pos[m] < 0)
+                  bad = 1;
+            }
+         }
+      }
+   }
+   *hw = top;
+   return !bad;
+}
+
 // The mesh: checked (the reference's misconnected-block errors,
-// ref/comm.c:198-201), its sorted slots and device copies uploaded; the
-// face exchange's task lists follow on its first call (build_tasks).
+// ref/comm.c:198-201), its slots, blocks and slot positions uploaded
+// (queued); the face exchange's task lists follow on its first call
+// (build_tasks).  The blocks are kept in the pinned buffer the upload reads.
 extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
                              int32_t n)
 {
@@ -603,48 +701,92 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
       return fail(MAMR_EINVAL, "bad mesh arguments");
    if (n > c->cfg.max_blocks)
       return fail(MAMR_EINVAL, "%d blocks exceed max_blocks", n);
-   c->gen++;
-   zcache_drop(c);
-   std::vector<int32_t> pos(c->cfg.max_blocks, -1);
-   for (int32_t b = 0; b < n; b++) {
-      const mamr_block &bp = blocks[b];
-      if (!slot_ok(c, bp.slot))
-         return fail(MAMR_EINVAL, "block %d: slot %d out of range", b,
-                     bp.slot);
-      if (pos[bp.slot] >= 0)
-         return fail(MAMR_EINVAL, "slot %d listed twice", bp.slot);
-      pos[bp.slot] = b;
-      for (int l = 0; l < 6; l++) {
-         int nl = bp.nei_level[l];
-         if (nl == -2)
-            continue;
-         if (nl != bp.level && nl != bp.level + 1 && nl != bp.level - 1)
-            return fail(MAMR_EMESH, "misconnected block (slot %d face %d)",
-                        bp.slot, l);
-         for (int i = 0; i < 2; i++)
-            for (int j = 0; j < 2; j++)
-               if ((nl == bp.level + 1 || (i == 0 && j == 0)) &&
-                   !slot_ok(c, bp.nei[l][i][j]))
-                  return fail(MAMR_EMESH, "misconnected block (slot %d face "
-                              "%d nei %d)", bp.slot, l, bp.nei[l][i][j]);
-      }
+   // the pinned buffer the current mesh is not in, once its last upload
+   // has run
+   const int k = 1 - c->hmesh_cur;
+   mamr_ctx::MeshBuf &hm = c->hmesh[k];
+   if (hm.pending) {
+      hm.pending = false;
+      CUDA_TRY(cudaEventSynchronize(hm.ev));
    }
-   // every listed neighbour must be active, whichever of the pair visits
-   // the face (the batched path reads each block's own list)
-   for (int32_t in = 0; in < n; in++) {
-      const mamr_block &bp = blocks[in];
-      for (int l = 0; l < 6; l++) {
-         const int nl = bp.nei_level[l];
-         if (nl == -2)
-            continue;
-         const int cnt = nl == bp.level + 1 ? 4 : 1;
-         for (int q = 0; q < cnt; q++) {
-            const int m = bp.nei[l][q >> 1][q & 1];
-            if (pos[m] < 0)
-               return fail(MAMR_EMESH, "neighbour slot %d not active", m);
+   if (!hm.ev)
+      CUDA_TRY(cudaEventCreateWithFlags(&hm.ev, cudaEventDisableTiming));
+   if (hm.cap < (size_t) std::max(1, n)) {
+      if (hm.p)
+         cudaFreeHost(hm.p);
+      hm.p = nullptr;
+      hm.cap = 0;
+      const size_t want = std::min<size_t>(
+         (size_t) std::max(1, n) * 5 / 4 + 64, c->cfg.max_blocks + (size_t) 1);
+      CUDA_TRY(cudaMallocHost((void **) &hm.p, sizeof(mamr_block) * want));
+      hm.cap = want;
+   }
+   // slots and slot positions through the pinned ring
+   const size_t bs = sizeof(int32_t) * (size_t) n;
+   const size_t bp = sizeof(int32_t) * (size_t) c->cfg.max_blocks;
+   const size_t op = (bs + 15) & ~(size_t) 15;
+   int slot = 0;
+   cudaError_t e;
+   char *h = (char *) host_stage_take(c, op + bp + 16, &slot, &e);
+   if (!h)
+      return fail(MAMR_ECUDA, "host staging: %s", cudaGetErrorString(e));
+   int32_t *hs = reinterpret_cast<int32_t *>(h);
+   std::vector<int32_t> pos(c->cfg.max_blocks, -1);
+   int hw = 0;
+   bool done = n >= 4096 &&
+               set_mesh_parallel(c, blocks, n, pos.data(), hm.p, hs, &hw);
+   if (!done) {
+      std::fill(pos.begin(), pos.end(), -1);
+      for (int32_t b = 0; b < n; b++) {
+         const mamr_block &bp = blocks[b];
+         if (!slot_ok(c, bp.slot))
+            return fail(MAMR_EINVAL, "block %d: slot %d out of range", b,
+                        bp.slot);
+         if (pos[bp.slot] >= 0)
+            return fail(MAMR_EINVAL, "slot %d listed twice", bp.slot);
+         pos[bp.slot] = b;
+         for (int l = 0; l < 6; l++) {
+            int nl = bp.nei_level[l];
+            if (nl == -2)
+               continue;
+            if (nl != bp.level && nl != bp.level + 1 && nl != bp.level - 1)
+               return fail(MAMR_EMESH, "misconnected block (slot %d face %d)",
+                           bp.slot, l);
+            for (int i = 0; i < 2; i++)
+               for (int j = 0; j < 2; j++)
+                  if ((nl == bp.level + 1 || (i == 0 && j == 0)) &&
+                      !slot_ok(c, bp.nei[l][i][j]))
+                     return fail(MAMR_EMESH, "misconnected block (slot %d "
+                                 "face %d nei %d)", bp.slot, l,
+                                 bp.nei[l][i][j]);
          }
       }
+      // every listed neighbour must be active, whichever of the pair
+      // visits the face (the batched path reads each block's own list)
+      for (int32_t in = 0; in < n; in++) {
+         const mamr_block &bp = blocks[in];
+         for (int l = 0; l < 6; l++) {
+            const int nl = bp.nei_level[l];
+            if (nl == -2)
+               continue;
+            const int cnt = nl == bp.level + 1 ? 4 : 1;
+            for (int q = 0; q < cnt; q++) {
+               const int m = bp.nei[l][q >> 1][q & 1];
+               if (pos[m] < 0)
+                  return fail(MAMR_EMESH, "neighbour slot %d not active", m);
+            }
+         }
+      }
+      for (int32_t b = 0; b < n; b++) {
+         hs[b] = blocks[b].slot;
+         hw = std::max(hw, blocks[b].slot + 1);
+      }
+      if (n)
+         memcpy(hm.p, blocks, sizeof(mamr_block) * n);
    }
+   c->gen++;
+   zcache_drop(c);
+   memcpy(h + op, pos.data(), bp);
    // sorted slots now; the face exchange's task lists when it first runs
    // on this mesh (build_tasks), since a batched run never needs them
    CUDA_TRY(c->d_slots.ensure(sizeof(int32_t) * std::max(1, n)));
@@ -653,39 +795,23 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
                                  c->cfg.num_vars));
    // the mesh on the device, for the batched path's descriptor build
    CUDA_TRY(c->d_mesh.ensure(sizeof(mamr_block) * std::max(1, n)));
-   CUDA_TRY(c->d_slot_pos.ensure(sizeof(int32_t) * pos.size()));
-   // sorted slots, mesh and slot positions through the pinned ring: queued
-   {
-      const size_t bs = sizeof(int32_t) * (size_t) n;
-      const size_t bm = sizeof(mamr_block) * (size_t) n;
-      const size_t bp = sizeof(int32_t) * pos.size();
-      const size_t om = (bs + 15) & ~(size_t) 15;
-      const size_t op = (om + bm + 15) & ~(size_t) 15;
-      int slot = 0;
-      cudaError_t e;
-      char *h = (char *) host_stage_take(c, op + bp + 16, &slot, &e);
-      if (!h)
-         return fail(MAMR_ECUDA, "host staging: %s", cudaGetErrorString(e));
-      int32_t *hs = reinterpret_cast<int32_t *>(h);
-      for (int32_t b = 0; b < n; b++)
-         hs[b] = blocks[b].slot;
-      if (bm)
-         memcpy(h + om, blocks, bm);
-      memcpy(h + op, pos.data(), bp);
-      if (n) {
-         CUDA_TRY(cudaMemcpyAsync(c->d_slots.p, h, bs,
-                                  cudaMemcpyHostToDevice, c->stream));
-         CUDA_TRY(cudaMemcpyAsync(c->d_mesh.p, h + om, bm,
-                                  cudaMemcpyHostToDevice, c->stream));
-      }
-      CUDA_TRY(cudaMemcpyAsync(c->d_slot_pos.p, h + op, bp,
+   CUDA_TRY(c->d_slot_pos.ensure(bp));
+   if (n) {
+      CUDA_TRY(cudaMemcpyAsync(c->d_slots.p, h, bs, cudaMemcpyHostToDevice,
+                               c->stream));
+      CUDA_TRY(cudaMemcpyAsync(c->d_mesh.p, hm.p, sizeof(mamr_block) * n,
                                cudaMemcpyHostToDevice, c->stream));
-      CUDA_TRY(host_stage_queued(c, slot));
+      CUDA_TRY(cudaEventRecord(hm.ev, c->stream));
+      hm.pending = true;
    }
-   c->mesh.assign(blocks, blocks + n);
+   CUDA_TRY(cudaMemcpyAsync(c->d_slot_pos.p, h + op, bp,
+                            cudaMemcpyHostToDevice, c->stream));
+   CUDA_TRY(host_stage_queued(c, slot));
+   c->mesh.p = hm.p;
+   c->mesh.n = (size_t) n;
+   c->hmesh_cur = k;
    c->slot_pos.swap(pos);
-   for (int32_t b = 0; b < n; b++)
-      c->hw_slots = std::max(c->hw_slots, blocks[b].slot + 1);
+   c->hw_slots = std::max(c->hw_slots, hw);
    mamr::batched_mesh_changed(c->batched);
    return MAMR_OK;
 }
@@ -695,7 +821,7 @@ extern "C" int mamr_set_mesh(mamr_ctx *c, const mamr_block *blocks,
 // loop visits (set_mesh has checked the mesh).
 static int build_tasks(mamr_ctx *c)
 {
-   const std::vector<mamr_block> &blocks = c->mesh;
+   const mamr_ctx::MeshView &blocks = c->mesh;
    const std::vector<int32_t> &pos = c->slot_pos;
    const int32_t n = (int32_t) blocks.size();
    std::vector<SameTask> same[3];
@@ -1867,6 +1993,52 @@ extern "C" int mamr_run_timesteps(mamr_ctx *c, int32_t num_ts,
                       (flags & MAMR_RUN_NO_GHOSTS) == 0, sums, n_sums);
 }
 
+// mamr_mark_validate for long block lists: the per-block checks spread
+// over kHostThreads threads, each slot's mark set by an atomic exchange (a
+// slot listed twice finds its mark already set).  On any failure the
+// serial check runs again on a cleared mark array, so that the message is
+// the one it returns.
+static const char *mark_validate(const mamr_mark_params *p,
+                                 const mamr_object *objs, int32_t n_objs,
+                                 const mamr_mark_block *mb, int32_t nb,
+                                 const mamr_mark_parent *pa, int32_t np,
+                                 int32_t cap, unsigned char *listed)
+{
+   if (nb < 4096 || !mb)
+      return mamr_mark_validate(p, objs, n_objs, mb, nb, pa, np, cap, listed);
+   // parameters and parents (nothing listed yet)
+   int bad = mamr_mark_validate(p, objs, n_objs, mb, 0, pa, np, cap,
+                                listed) != nullptr;
+   if (!bad) {
+#pragma omp parallel for num_threads(kHostThreads) schedule(static) \
+   reduction(| : bad)
+      for (int32_t i = 0; i < nb; i++) {
+         const mamr_mark_block &b = mb[i];
+         if (b.slot < 0 || b.slot >= cap || b.level < 0 ||
+             b.level > p->num_refine || b.parent < -1 || b.parent >= np)
+            bad = 1;
+         else if (__atomic_exchange_n(&listed[b.slot], (unsigned char) 1,
+                                      __ATOMIC_RELAXED))
+            bad = 1;
+      }
+   }
+   if (!bad) {
+#pragma omp parallel for num_threads(kHostThreads) schedule(static) \
+   reduction(| : bad)
+      for (int32_t i = 0; i < nb; i++)
+         for (int l = 0; l < 6; l++) {
+            const int nl = mb[i].nei_level[l], n = mb[i].nei[l];
+            if ((nl == mb[i].level || nl == mb[i].level - 1) &&
+                (n < 0 || n >= cap || !listed[n]))
+               bad = 1;
+         }
+   }
+   if (!bad)
+      return nullptr;
+   std::memset(listed, 0, (size_t) cap + 1);
+   return mamr_mark_validate(p, objs, n_objs, mb, nb, pa, np, cap, listed);
+}
+
 extern "C" int mamr_mark_refine(mamr_ctx *c, const mamr_mark_params *p,
                                 const mamr_object *objs, int32_t n_objs,
                                 const mamr_mark_block *mb, int32_t nb,
@@ -1881,8 +2053,8 @@ extern "C" int mamr_mark_refine(mamr_ctx *c, const mamr_mark_params *p,
       CUDA_TRY(cudaSetDevice(c->device));
    const int32_t cap = c->cfg.max_blocks;
    std::vector<unsigned char> listed((size_t) cap + 1, 0);
-   if (const char *msg = mamr_mark_validate(p, objs, n_objs, mb, nb, pa, np,
-                                            cap, listed.data()))
+   if (const char *msg = mark_validate(p, objs, n_objs, mb, nb, pa, np, cap,
+                                       listed.data()))
       return fail(MAMR_EINVAL, "%s", msg);
    // one device allocation: objects, blocks, parents, flags by slot,
    // parent flags, output, each 256-byte aligned

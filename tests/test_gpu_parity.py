@@ -142,6 +142,49 @@ def test_errors_are_reported_and_context_survives(gpu_lib):
         assert ctx.check_sum(1) == 5000.0   # context still usable
 
 
+def test_long_mesh_refusals_keep_the_last_mesh(gpu_lib):
+    """Mistakes planted in a 4913-block mesh (long enough that the library
+    checks it on several threads) are refused with the status and message
+    of the first mistake in list order; the context keeps the last mesh it
+    took: a batched run after the refusals equals one without them."""
+    from miniamr_gb300.abi import RUN_BATCHED
+    cap = 5000
+    cfg = Config.make(8, 8, 8, 1, cap, stencil=7, dtype=FP32)
+    good = meshmod.initial_mesh(17, 17, 17, 0, cap).blocks()
+    n, s = len(good), good["slot"]
+    assert n >= 4096 and s.max() < cap - 1
+    q = int(np.flatnonzero(good["nei_level"][:, 1] == 0)[n // 3])
+    plants = []
+    b = good.copy(); b["slot"][n - 1] = s[5]
+    plants.append((b, -1, f"slot {s[5]} listed twice"))
+    b = good.copy(); b["slot"][n // 2] = cap
+    plants.append((b, -1, f"block {n // 2}: slot {cap} out of range"))
+    b = good.copy(); b["nei_level"][n - 3, 2] = 3
+    plants.append((b, -4, f"misconnected block (slot {s[n - 3]} face 2)"))
+    b = good.copy(); b["nei"][q, 1, 0, 0] = -7
+    plants.append((b, -4, f"misconnected block (slot {s[q]} face 1 nei -7)"))
+    b = good.copy(); b["nei"][q, 1, 0, 0] = cap - 1
+    plants.append((b, -4, f"neighbour slot {cap - 1} not active"))
+    b = good.copy(); b["nei_level"][10, 0] = 4; b["slot"][n - 1] = s[0]
+    plants.append((b, -4, f"misconnected block (slot {s[10]} face 0)"))
+    rng = np.random.default_rng(11)
+    vals = rng.uniform(-1, 1, size=(n, 1, 10, 10, 10))
+    outs = []
+    for refuse in (True, False):
+        with gpu_lib.context(cfg) as ctx:
+            ctx.upload(np.arange(n), vals)
+            ctx.set_mesh(good)
+            if refuse:
+                for blk, status, msg in plants:
+                    with pytest.raises(MamrError) as e:
+                        ctx.set_mesh(blk)
+                    assert e.value.status == status
+                    assert str(e.value).endswith(msg), (str(e.value), msg)
+            ctx.run_timesteps(2, 2, 1, flags=RUN_BATCHED)
+            outs.append(ctx.download(np.arange(n)))
+    assert np.array_equal(bits(outs[0]), bits(outs[1]))
+
+
 def test_batched_refuses_a_coarse_face_that_omits_the_block(gpu_lib):
     """The batched descriptors of a multi-level mesh are built on the
     device; a fine block whose coarser neighbour does not list it on the

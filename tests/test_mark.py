@@ -125,3 +125,57 @@ def test_oracle_marking_pass_cap(oracle_lib):
 @pytest.mark.gpu
 def test_gpu_marking_pass_cap(gpu_lib):
     check_pass_cap(gpu_lib)
+
+
+def long_list_refusals(lib):
+    """Mistakes planted in the stress mesh's longest block list (about 20k
+    blocks, where the library checks the list on several threads): each is
+    refused with MAMR_EINVAL and its message; with two mistakes the one the
+    serial check meets first is named.  The context then gives the
+    reference's flags for the untouched list."""
+    steps = read_marks(mark_path("config5"))
+    st = max(steps, key=lambda s: len(s.blocks))
+    n = len(st.blocks)
+    assert n >= 4096
+    cap = int(st.blocks["slot"].max()) + 1
+    plants = []
+    b = st.blocks.copy(); b["slot"][n - 1] = b["slot"][3]
+    plants.append(b)
+    b = st.blocks.copy(); b["slot"][n // 2] = cap
+    plants.append(b)
+    b = st.blocks.copy(); b["level"][n - 2] = st.params.num_refine + 1
+    b["slot"][n - 1] = b["slot"][0]
+    plants.append(b)
+    b = st.blocks.copy()
+    i = int(np.flatnonzero(b["nei_level"][:, 0] == b["level"])[-1])
+    b["nei"][i, 0] = -1
+    plants.append(b)
+    b = st.blocks.copy(); b["parent"][7] = len(st.parents)
+    b["slot"][n - 1] = cap + 5
+    plants.append(b)
+    msgs = []
+    cfg = Config.make(*st.block_size, 1, cap)
+    with lib.context(cfg) as ctx:
+        for blk in plants:
+            with pytest.raises(MamrError) as e:
+                ctx.mark_refine(st.params, st.objects, blk, st.parents)
+            assert e.value.status == -1
+            msgs.append(str(e.value).rsplit(": ", 1)[-1])
+        br, pr = ctx.mark_refine(st.params, st.objects, st.blocks,
+                                 st.parents)
+    act = st.parents["active"] == 1
+    assert np.array_equal(br, st.block_refine)
+    assert np.array_equal(pr[act], st.parent_refine[act])
+    assert "listed twice" in msgs[0] and "out of range" in msgs[1]
+    assert "level or parent" in msgs[2] and "neighbour" in msgs[3]
+    assert "level or parent" in msgs[4]
+    return msgs
+
+
+def test_oracle_refuses_long_bad_lists(oracle_lib):
+    long_list_refusals(oracle_lib)
+
+
+@pytest.mark.gpu
+def test_gpu_refuses_long_bad_lists_like_oracle(gpu_lib, oracle_lib):
+    assert long_list_refusals(gpu_lib) == long_list_refusals(oracle_lib)
