@@ -107,6 +107,57 @@ split_jobs_kernel(T *__restrict__ pool, const T *__restrict__ stage, Geom g,
    const T *P = read_base(pool, stage, g, jobs[job].parent, var);
    const int hx = D.nx / 2, hy = D.ny / 2, hz = D.nz / 2;
    const int per_child = D.nx * D.ny;
+   if constexpr (BX > 0 && (BZ / 2) % Vec<T>::W == 0) {
+      // 8^3 and 16^3: the thread's rows r = threadIdx.x + u * NT in groups
+      // of G, each group's parent half-rows loaded before any of its child
+      // rows is stored (no row a segment's jobs read is written in it), so
+      // that G loads are in flight instead of one
+      constexpr int W = Vec<T>::W, H = BZ / 2;
+      constexpr int NT = BX == 8 ? 128 : 256;   // launch_split's CTA size
+      constexpr int RPT = 8 * BX * BY / NT, G = RPT < 4 ? RPT : 4;
+      static_assert((BX == 8 || BX == 16) && RPT * NT == 8 * BX * BY &&
+                    RPT % G == 0, "split rows per thread");
+      const int32_t *ch = jobs[job].child;
+#pragma unroll 1
+      for (int u0 = 0; u0 < RPT; u0 += G) {
+         T p[G][H];
+#pragma unroll
+         for (int u = 0; u < G; u++) {
+            const int r = threadIdx.x + (u0 + u) * NT;
+            const int o = r / per_child, rr = r - o * per_child;
+            const int ci = rr / D.ny + 1, cj = rr - (ci - 1) * D.ny + 1;
+            const T *prow = P + D.cell((ci + 1) / 2 + (o & 1) * hx,
+                                       (cj + 1) / 2 + ((o >> 1) & 1) * hy,
+                                       1 + (o >> 2) * hz);
+#pragma unroll
+            for (int q = 0; q < H; q += W)
+               Vec<T>::ld(prow + q, p[u] + q);
+         }
+#pragma unroll
+         for (int u = 0; u < G; u++) {
+            const int r = threadIdx.x + (u0 + u) * NT;
+            const int o = r / per_child, rr = r - o * per_child;
+            const int ci = rr / D.ny + 1, cj = rr - (ci - 1) * D.ny + 1;
+            T *crow = pool + bv_offset(g, ch[o], var) + D.cell(ci, cj, 1);
+#pragma unroll
+            for (int q = 0; q < H; q += W) {
+               T c[2 * W];
+#pragma unroll
+               for (int m = 0; m < W; m++)
+                  c[2 * m] = c[2 * m + 1] = eighth(p[u][q + m]);
+               Vec<T>::st(crow + 2 * q, c);
+               Vec<T>::st(crow + 2 * q + W, c + W);
+            }
+            if (zf) {
+               T *z = zf + zface_at(g, ch[o], var, 0) + (ci - 1) * D.ny +
+                      (cj - 1);
+               z[0] = eighth(p[u][0]);
+               z[D.nx * D.ny] = eighth(p[u][H - 1]);
+            }
+         }
+      }
+      return;
+   }
    for (int r = threadIdx.x; r < 8 * per_child; r += blockDim.x) {
       const int o = r / per_child, rr = r - o * per_child;
       const int ci = rr / D.ny + 1, cj = rr - (ci - 1) * D.ny + 1;
