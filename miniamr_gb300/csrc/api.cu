@@ -230,7 +230,7 @@ struct mamr_ctx {
 static size_t elem_size(const mamr_ctx *c) { return c->fp32 ? 4 : 8; }
 
 // Host threads (OpenMP) of the checks and copies over long block lists.
-constexpr int kHostThreads = 4;
+[[maybe_unused]] constexpr int kHostThreads = 4;
 
 // The next slot of the host staging ring, at least `bytes` long, once the
 // copies queued from it before have run; null on a CUDA error (*e).
