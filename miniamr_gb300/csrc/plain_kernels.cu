@@ -885,26 +885,42 @@ int launch_fp32_checksum_fallback(const float *pool, const Geom &g,
 }
 
 // ---------------------------------------------------------------------------
-// Copies whole blocks (all variables, ghosts included) from pool slots to
-// consecutive staging entries; one CTA row per block, 16-byte vectors when
-// the block size allows.
+// Copies the interior cells of whole blocks (all variables) from pool slots
+// to consecutive staging entries, at the same offsets: the split and
+// consolidation kernels read nothing else from a staged block.  In the
+// device layout the interior rows j = 1..ny of i-plane i are one run of
+// ny*nz values from row_offset(i, 1), so a block-variable is nx runs.  One
+// CTA row per block, 16-byte vectors when nz values fill whole vectors.
 template <typename T>
 __global__ void __launch_bounds__(256)
 stage_blocks_kernel(T *__restrict__ stage, const T *__restrict__ pool, Geom g,
                     const int32_t *__restrict__ slots)
 {
-   const long long words = (long long) g.V * g.bv;
    const T *src = pool + bv_offset(g, slots[blockIdx.y], 0);
    T *dst = stage + bv_offset(g, blockIdx.y, 0);
    const long long step = (long long) gridDim.x * blockDim.x;
    const long long t0 = (long long) blockIdx.x * blockDim.x + threadIdx.x;
-   if ((words * sizeof(T)) % 16 == 0) {
-      const long long vec = words * sizeof(T) / 16;
-      for (long long e = t0; e < vec; e += step)
-         ((uint4 *) dst)[e] = __ldg((const uint4 *) src + e);
+   const long long run = (long long) g.ny * g.nz;
+   const long long runs = (long long) g.V * g.nx;
+   if ((g.nz * sizeof(T)) % 16 == 0) {
+      const long long rv = run * (long long) sizeof(T) / 16;   // vectors
+      constexpr int VW = 16 / sizeof(T);
+      for (long long e = t0; e < runs * rv; e += step) {
+         const long long q = e / rv, w = e - q * rv;
+         const int var = (int) (q / g.nx), i = (int) (q - (long long) var *
+                                                      g.nx) + 1;
+         const long long off = var * g.bv + row_offset(g, i, 1) + w * VW;
+         *reinterpret_cast<uint4 *>(dst + off) =
+            __ldg(reinterpret_cast<const uint4 *>(src + off));
+      }
    } else {
-      for (long long e = t0; e < words; e += step)
-         dst[e] = src[e];
+      for (long long e = t0; e < runs * run; e += step) {
+         const long long q = e / run, w = e - q * run;
+         const int var = (int) (q / g.nx), i = (int) (q - (long long) var *
+                                                      g.nx) + 1;
+         const long long off = var * g.bv + row_offset(g, i, 1) + w;
+         dst[off] = src[off];
+      }
    }
 }
 
@@ -914,7 +930,8 @@ int launch_stage_blocks(T *stage, const T *pool, const Geom &g,
 {
    if (n == 0)
       return 0;
-   long long vec = ((long long) g.V * g.bv * sizeof(T) + 15) / 16;
+   long long vec = ((long long) g.V * g.nx * g.ny * g.nz * sizeof(T) + 15) /
+                   16;
    int gx = (int) std::min<long long>((vec + 255) / 256, 64);
    stage_blocks_kernel<T><<<dim3(gx, n), 256, 0, s>>>(stage, pool, g, slots);
    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
